@@ -1,0 +1,193 @@
+/*
+ * tnalg_gb300 — C ABI of the GB300-native finite-size DMRG sweep.
+ *
+ * The reference (T-Nalg) is pure Python/numpy and has no FFI layer; its hot path
+ * is MpsOpenBoundaryClass (MPSClass.py:26-1098) driven by dmrg_finite_size
+ * (DMRG_anyH.py:18-101). Each entry point below replaces a numpy/scipy step of
+ * that path, cited as file:line. The Python host (tnalg_gb300/MPSClass.py) binds
+ * these functions with ctypes; INTEGRATION.md shows the binding.
+ *
+ * Conventions
+ *  - All pointers except descriptor/option structs are DEVICE pointers owned by the
+ *    caller (plain cudaMalloc or torch storage). Descriptor and option structs and
+ *    result structs live in HOST memory.
+ *  - Every function returns an int status (TN_OK == 0); nothing throws across the
+ *    ABI. tn_last_error() returns a thread-local message for the last failure.
+ *  - `stream` is a cudaStream_t passed as void*; every kernel of a call is queued
+ *    on it. Calls are not re-entrant on one stream with one workspace.
+ *  - Tensors are row-major FP64. An MPS site tensor is (chi_l, d, chi_r); an
+ *    environment is (chi, chi) indexed [bra, ket] (TensorBasicModule.py:530-619).
+ *  - Strides are in elements.
+ */
+#ifndef TNALG_GB300_H
+#define TNALG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  TN_OK = 0,
+  TN_ERR_ARG = 1,        /* invalid argument / unsupported shape */
+  TN_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+  TN_ERR_WORKSPACE = 3,  /* workspace missing or too small */
+  TN_ERR_NOCONV = 4,     /* eigensolver hit its iteration limit (result still usable) */
+  TN_ERR_NUMERIC = 5,    /* NaN/Inf detected */
+  TN_ERR_TIMEOUT = 6     /* a bounded device-side wait gave up */
+};
+
+enum { TN_PREC_FP64 = 0, TN_PREC_TF32X3 = 1 };
+
+/* ---- library --------------------------------------------------------------- */
+const char* tn_last_error(void);
+int tn_version(void);
+/* SM count and compute capability of the current device. */
+int tn_device_info(int* sm_count, int* cc_major, int* cc_minor);
+
+/* ---- contraction primitive -------------------------------------------------- */
+/*
+ * C[b] = alpha * sum_r A[b,r] . B[b,r] + beta * Cin[b]
+ * A[b,r](m,k) = A[b*sAb + r*sAr + m*sAm + k*sAk], same pattern for B(k,n), C(m,n).
+ * Cin may equal C or be NULL (then beta multiplies C itself).
+ * Replaces the np.dot calls inside absorb_matrix2tensor / bound_vec_operator_*
+ * (TensorBasicModule.py:387-424, 530-619).
+ * precision: TN_PREC_FP64 (CUDA-core FP64) or TN_PREC_TF32X3 (tcgen05 tensor cores,
+ * split-TF32 products with FP32 accumulation, FP64 in/out).
+ * ws may be NULL; with ws the FP64 path splits K across CTAs for small outputs.
+ */
+int tn_gemm(int precision, int64_t M, int64_t N, int64_t K,
+            const double* A, int64_t sAm, int64_t sAk,
+            const double* B, int64_t sBk, int64_t sBn,
+            double* C, int64_t sCm, int64_t sCn, const double* Cin,
+            int64_t batch, int64_t sAb, int64_t sBb, int64_t sCb,
+            int64_t nred, int64_t sAr, int64_t sBr,
+            double alpha, double beta, void* ws, size_t ws_bytes, void* stream);
+size_t tn_gemm_workspace_bytes(int precision, int64_t M, int64_t N, int64_t K, int64_t batch);
+
+/* ---- effective-operator building blocks ------------------------------------ */
+/* One term of a block operator: coeff * E[slot] (x) ops[op]; slot < 0 -> identity,
+ * op < 0 -> identity. */
+typedef struct {
+  int32_t slot;
+  int32_t op;
+  double coeff;
+} tn_block_term;
+
+/*
+ * Dense block operator of an enlarged block (classify_and_update_env buckets,
+ * MPSClass.py:684-733, summed into one matrix):
+ *   side == 0 (left):  W[(a',s'),(a,s)] = sum_t c_t E_t[a',a] O_t[s',s]   (chi*d)^2
+ *   side == 1 (right): W[(s',b'),(s,b)] = sum_t c_t O_t[s',s] E_t[b',b]   (d*chi)^2
+ * env: nslots x chi x chi (slot stride chi*chi); ops: nops x d x d; terms: DEVICE array.
+ */
+int tn_assemble_block(int side, int64_t chi, int64_t d, const double* env, const double* ops,
+                      const tn_block_term* terms, int64_t nterms, double* w, void* stream);
+
+/* out[g] = sum over terms t with group g of coeff_t * env[slot_t]; groups listed as a
+ * DEVICE array of (group, slot, coeff) triples encoded as tn_block_term{slot, op=group}. */
+int tn_combine_slots(int64_t chi, const double* env, const tn_block_term* terms, int64_t nterms,
+                     int64_t ngroups, double* out, void* stream);
+
+/* out[k][a,s',b] = sum_s ops[opidx[k]][s',s] in[a,s,b]   (absorb_matrix2tensor on the
+ * physical bond, TensorBasicModule.py:414-421). opidx: DEVICE int32 array (-1 = identity). */
+int tn_apply_site_ops(int64_t chil, int64_t d, int64_t chir, const double* in, const double* ops,
+                      const int32_t* opidx, int64_t nout, double* out, int64_t out_stride, void* stream);
+
+/* out[s',s] += alpha * sum_{x,z} M[x,s',z] T[x,s,z]   (d <= 4): the local reduced density
+ * matrix used by observation_s1 / observation_s1_s2 (MPSClass.py:857-909). out: d*d DEVICE. */
+int tn_pair_contract(int64_t chil, int64_t d, int64_t chir, const double* m, const double* t,
+                     double alpha, double* out, void* stream);
+
+/* ---- effective Hamiltonian matvec (K1) ------------------------------------------ */
+typedef struct {
+  int64_t chil, d, chir;
+  const double* wl;   /* (chil*d)^2 left block incl. on-site terms, or NULL */
+  const double* wr;   /* (d*chir)^2 right block, or NULL */
+  int64_t nstr;       /* straddling pairs: sum_k SL[k] (x) 1 (x) SR[k] */
+  const double* sl;   /* nstr x chil x chil (coefficients folded in) */
+  const double* sr;   /* nstr x chir x chir */
+} tn_site_desc;
+
+/*
+ * y = beta * psi + alpha * H_eff psi  with H_eff = WL (x) 1 + 1 (x) WR + sum_k SL_k (x) 1 (x) SR_k.
+ * Replaces update_tensor_eigs_f_handle_optimized (MPSClass.py:755-776), which is the
+ * case alpha = -tau, beta = 1.
+ */
+int tn_matvec(const tn_site_desc* desc, const double* psi, double* y, double alpha, double beta,
+              int precision, void* ws, size_t ws_bytes, void* stream);
+size_t tn_matvec_workspace_bytes(const tn_site_desc* desc, int precision);
+
+/* ---- local eigensolver (K2) ----------------------------------------------------- */
+typedef struct {
+  double eigs_tol;      /* tolerance as passed to the reference's eigsh */
+  double tau;           /* the reference's shift; tol on ||Hx - t x|| = eigs_tol/tau*|1-tau*t| */
+  double tol_cap;       /* if > 0: residual tol = min(above, tol_cap * max(1, |t|)) */
+  double mixed_floor;   /* TF32X3: residual floor relative to |t| (precision limit) */
+  int32_t max_krylov;   /* Lanczos vectors per restart */
+  int32_t max_restarts;
+  int32_t check_every;  /* steps between host convergence checks */
+  int32_t precision;    /* matvec precision */
+  int32_t refine;       /* 1: FP64 residual + Rayleigh quotient of the final vector */
+  int32_t reserved;
+} tn_lanczos_opts;
+
+typedef struct {
+  double energy;        /* Ritz value of H_eff */
+  double residual;      /* ||H x - energy x|| (estimate, or FP64 value when refined) */
+  double energy_fp64;   /* FP64 Rayleigh quotient x.Hx (refine == 1) */
+  int32_t matvecs;
+  int32_t restarts;
+  int32_t converged;
+  int32_t reserved;
+} tn_lanczos_result;
+
+/*
+ * Lowest eigenpair of H_eff by Lanczos with full (classical Gram-Schmidt, twice)
+ * reorthogonalisation; Krylov basis, dot products and the tridiagonal problem in
+ * FP64. psi_inout: start vector in, unit eigenvector out.
+ * Replaces eigsh(LinearOperator(I - tau*H_eff), k=1, which='LM', v0=psi, tol)
+ * (MPSClass.py:800-807; same eigenvector, eigenvalue reported for H_eff).
+ */
+int tn_lanczos(const tn_site_desc* desc, double* psi_inout, const tn_lanczos_opts* opts,
+               void* ws, size_t ws_bytes, tn_lanczos_result* result, void* stream);
+size_t tn_lanczos_workspace_bytes(const tn_site_desc* desc, const tn_lanczos_opts* opts);
+
+/* ---- gauge move (K4) ------------------------------------------------------------- */
+/*
+ * Thin Householder QR in FP64 of the m x n matrix A (general strides):
+ * A = Q R, Q: m x k with orthonormal columns, R: k x n upper trapezoidal, k = min(m, n).
+ * Replaces np.linalg.qr in left2right_decompose_tensor / right2left_decompose_tensor
+ * (TensorBasicModule.py:314-384). Columns of Q are those of LAPACK up to sign.
+ */
+int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn,
+          double* q, int64_t sQm, int64_t sQn, double* r, int64_t sRm, int64_t sRn,
+          void* ws, size_t ws_bytes, void* stream);
+size_t tn_qr_workspace_bytes(int64_t m, int64_t n);
+
+/* ---- entanglement spectrum (K5) ----------------------------------------------------- */
+/*
+ * Singular values of the k x n matrix X (general strides) by parallel one-sided
+ * Jacobi in FP64; s_out (DEVICE, k values, unsorted). Replaces np.linalg.svd in the
+ * SVD moves of calculate_entanglement_spectrum (MPSClass.py:812-832,
+ * TensorBasicModule.py:338-342,374-377). tol: relative off-diagonal threshold.
+ */
+int tn_singular_values(int64_t k, int64_t n, const double* x, int64_t sXr, int64_t sXc, double* s_out,
+                       double tol, int max_sweeps, void* ws, size_t ws_bytes, void* stream);
+size_t tn_singular_values_workspace_bytes(int64_t k, int64_t n);
+
+/* ---- small vector helpers ------------------------------------------------------- */
+/* out[0] = sum x[i]*y[i] (FP64, deterministic two-stage reduction). */
+int tn_dot(int64_t n, const double* x, const double* y, double* out, void* ws, size_t ws_bytes,
+           void* stream);
+/* x[i] *= alpha / sqrt(nrm2[0]) when nrm2 != NULL, else x[i] *= alpha. */
+int tn_scale(int64_t n, double* x, double alpha, const double* nrm2, void* stream);
+/* eye: n x n identity into a (row stride lda). */
+int tn_set_identity(int64_t n, double* a, int64_t lda, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TNALG_GB300_H */

@@ -1,0 +1,238 @@
+"""numpy test double of libtnalg_gb300's C ABI, operating on HOST pointers.
+
+Used only by the CPU tests to exercise the host orchestration (layouts, strides,
+environment bookkeeping, sweep logic) of tnalg_gb300 without a GPU. Each function
+implements the documented semantics of the matching entry point in
+include/tnalg_gb300.h with plain numpy; the CUDA kernels themselves are checked
+on the GPU by the `gpu`-marked tests.
+"""
+import ctypes
+
+import numpy as np
+from scipy.sparse.linalg import LinearOperator, eigsh
+
+OK, ERR_ARG, ERR_NOCONV = 0, 1, 4
+
+
+def _addr(p):
+    if p is None:
+        return None
+    if isinstance(p, ctypes.c_void_p):
+        return p.value
+    return int(p)
+
+
+def _view(p, n, dtype=np.float64):
+    a = _addr(p)
+    if a is None or n <= 0:
+        return np.zeros(0, dtype=dtype)
+    ct = {np.float64: ctypes.c_double, np.int32: ctypes.c_int32}[dtype]
+    return np.ctypeslib.as_array((ct * int(n)).from_address(a))
+
+
+def _struct(ref):
+    return ref._obj if hasattr(ref, "_obj") else ref
+
+
+def _extent(*pairs):
+    return 1 + sum((int(n) - 1) * abs(int(s)) for n, s in pairs if n > 0)
+
+
+def _strided(p, shape, strides):
+    n = _extent(*zip(shape, strides))
+    base = _view(p, n)
+    return np.lib.stride_tricks.as_strided(base, shape=shape, strides=[8 * s for s in strides])
+
+
+def _terms(p, n):
+    raw = _view(p, 2 * n) if n else np.zeros(0)
+    out = []
+    for k in range(n):
+        slot_op = np.frombuffer(raw[2 * k:2 * k + 1].tobytes(), dtype=np.int32)
+        out.append((int(slot_op[0]), int(slot_op[1]), float(raw[2 * k + 1])))
+    return out
+
+
+class FakeLib:
+    def __init__(self):
+        self.err = b""
+        self.calls = {}
+
+    def _count(self, name):
+        self.calls[name] = self.calls.get(name, 0) + 1
+
+    def tn_last_error(self):
+        return self.err
+
+    def tn_version(self):
+        return 100
+
+    # -- GEMM ----------------------------------------------------------------------
+    def tn_gemm_workspace_bytes(self, prec, M, N, K, batch):
+        return 0
+
+    def tn_gemm(self, prec, M, N, K, A, sAm, sAk, B, sBk, sBn, C, sCm, sCn, Cin, batch, sAb, sBb, sCb, nred, sAr,
+                sBr, alpha, beta, ws, wsb, stream):
+        self._count("tn_gemm")
+        M, N, K = int(M), int(N), int(K)
+        if M == 0 or N == 0 or batch == 0:
+            return OK
+        Cv = _strided(C, (batch, M, N), (sCb, sCm, sCn))
+        Ci = _strided(Cin, (batch, M, N), (sCb, sCm, sCn)).copy() if _addr(Cin) else Cv.copy()
+        acc = np.zeros((batch, M, N))
+        if K > 0 and nred > 0:
+            Av = _strided(A, (batch, nred, M, K), (sAb, sAr, sAm, sAk))
+            Bv = _strided(B, (batch, nred, K, N), (sBb, sBr, sBk, sBn))
+            acc = np.einsum("brmk,brkn->bmn", Av, Bv)
+        res = alpha * acc + (beta * Ci if beta != 0 else 0.0)
+        Cv[...] = res
+        return OK
+
+    # -- building blocks -------------------------------------------------------------
+    def tn_assemble_block(self, side, chi, d, env, ops, terms, nterms, w, stream):
+        self._count("tn_assemble_block")
+        chi, d = int(chi), int(d)
+        tl = _terms(terms, int(nterms))
+        nslot = 1 + max([s for s, _, _ in tl] + [0])
+        E = _view(env, nslot * chi * chi).reshape(nslot, chi, chi)
+        nop = 1 + max([o for _, o, _ in tl] + [0])
+        O = _view(ops, nop * d * d).reshape(nop, d, d) if nop > 0 else None
+        W = np.zeros((chi * d, chi * d))
+        for slot, op, c in tl:
+            e = np.eye(chi) if slot < 0 else E[slot]
+            o = np.eye(d) if op < 0 else O[op]
+            W += c * (np.kron(e, o) if side == 0 else np.kron(o, e))
+        _view(w, W.size)[:] = W.reshape(-1)
+        return OK
+
+    def tn_combine_slots(self, chi, env, terms, nterms, ngroups, out, stream):
+        self._count("tn_combine_slots")
+        chi = int(chi)
+        tl = _terms(terms, int(nterms))
+        nslot = 1 + max([s for s, _, _ in tl] + [0])
+        E = _view(env, nslot * chi * chi).reshape(nslot, chi, chi)
+        res = np.zeros((int(ngroups), chi, chi))
+        for slot, g, c in tl:
+            res[g] += c * (np.eye(chi) if slot < 0 else E[slot])
+        _view(out, res.size)[:] = res.reshape(-1)
+        return OK
+
+    def tn_apply_site_ops(self, chil, d, chir, inp, ops, opidx, nout, out, out_stride, stream):
+        self._count("tn_apply_site_ops")
+        chil, d, chir, nout = int(chil), int(d), int(chir), int(nout)
+        idx = _view(opidx, nout, np.int32)
+        nop = 1 + max(int(idx.max()), 0)
+        O = _view(ops, nop * d * d).reshape(nop, d, d)
+        X = _view(inp, chil * d * chir).reshape(chil, d, chir)
+        o = _view(out, (nout - 1) * int(out_stride) + chil * d * chir)
+        for k in range(nout):
+            op = np.eye(d) if idx[k] < 0 else O[idx[k]]
+            o[k * out_stride:k * out_stride + chil * d * chir] = np.einsum("xs,asb->axb", op, X).reshape(-1)
+        return OK
+
+    def tn_pair_contract(self, chil, d, chir, m, t, alpha, out, stream):
+        self._count("tn_pair_contract")
+        chil, d, chir = int(chil), int(d), int(chir)
+        Mv = _view(m, chil * d * chir).reshape(chil, d, chir)
+        Tv = _view(t, chil * d * chir).reshape(chil, d, chir)
+        o = _view(out, d * d)
+        o += alpha * np.einsum("xpz,xsz->ps", Mv, Tv).reshape(-1)
+        return OK
+
+    # -- matvec / Lanczos -------------------------------------------------------------
+    def _heff(self, ds):
+        cl, d, cr = int(ds.chil), int(ds.d), int(ds.chir)
+        wl = _view(ds.wl, (cl * d) ** 2).reshape(cl * d, cl * d) if ds.wl else None
+        wr = _view(ds.wr, (d * cr) ** 2).reshape(d * cr, d * cr) if ds.wr else None
+        ns = int(ds.nstr)
+        sl = _view(ds.sl, ns * cl * cl).reshape(ns, cl, cl) if ns else None
+        sr = _view(ds.sr, ns * cr * cr).reshape(ns, cr, cr) if ns else None
+
+        def mv(x):
+            x = np.asarray(x).reshape(cl, d, cr)
+            y = np.zeros_like(x)
+            if wl is not None:
+                y += (wl @ x.reshape(cl * d, cr)).reshape(cl, d, cr)
+            if wr is not None:
+                y += (x.reshape(cl, d * cr) @ wr.T).reshape(cl, d, cr)
+            for k in range(ns):
+                y += np.einsum("xa,asb,yb->xsy", sl[k], x, sr[k])
+            return y.reshape(-1)
+        return mv, cl * d * cr
+
+    def tn_matvec_workspace_bytes(self, desc, prec):
+        return 0
+
+    def tn_matvec(self, desc, psi, y, alpha, beta, prec, ws, wsb, stream):
+        self._count("tn_matvec")
+        mv, n = self._heff(_struct(desc))
+        x = _view(psi, n).copy()
+        _view(y, n)[:] = beta * x + alpha * mv(x)
+        return OK
+
+    def tn_lanczos_workspace_bytes(self, desc, opts):
+        return 0
+
+    def tn_lanczos(self, desc, psi, opts, ws, wsb, res, stream):
+        self._count("tn_lanczos")
+        ds, o, r = _struct(desc), _struct(opts), _struct(res)
+        mv, n = self._heff(ds)
+        x0 = _view(psi, n).copy()
+        calls = [0]
+
+        def f(v):
+            calls[0] += 1
+            return mv(v)
+        if n <= 2:
+            H = np.stack([mv(e) for e in np.eye(n)], axis=1)
+            w, v = np.linalg.eigh(H)
+            e, vec = w[0], v[:, 0]
+        else:
+            w, v = eigsh(LinearOperator((n, n), matvec=f, dtype=float), k=1, which="SA", v0=x0, tol=1e-13)
+            e, vec = w[0], v[:, 0]
+        _view(psi, n)[:] = vec / np.linalg.norm(vec)
+        r.energy = float(e)
+        r.energy_fp64 = float(e)
+        r.residual = float(np.linalg.norm(mv(vec) - e * vec))
+        r.matvecs = calls[0]
+        r.restarts = 0
+        r.converged = 1
+        return OK
+
+    # -- decompositions -------------------------------------------------------------------
+    def tn_qr_workspace_bytes(self, m, n):
+        return 0
+
+    def tn_qr(self, m, n, a, sAm, sAn, q, sQm, sQn, r, sRm, sRn, ws, wsb, stream):
+        self._count("tn_qr")
+        m, n = int(m), int(n)
+        k = min(m, n)
+        A = _strided(a, (m, n), (sAm, sAn)).copy()
+        Q, R = np.linalg.qr(A)
+        if _addr(q):
+            _strided(q, (m, k), (sQm, sQn))[...] = Q[:, :k]
+        if _addr(r):
+            _strided(r, (k, n), (sRm, sRn))[...] = R[:k]
+        return OK
+
+    def tn_singular_values_workspace_bytes(self, k, n):
+        return 0
+
+    def tn_singular_values(self, k, n, x, sr, sc, out, tol, sweeps, ws, wsb, stream):
+        self._count("tn_singular_values")
+        X = _strided(x, (int(k), int(n)), (sr, sc)).copy()
+        _view(out, int(k))[:] = np.linalg.svd(X, compute_uv=False)[: int(k)]
+        return OK
+
+
+def install():
+    """Route tnalg_gb300's C-ABI calls to a fresh FakeLib (host tensors accepted)."""
+    from tnalg_gb300 import _lib
+    fake = FakeLib()
+    _lib.install_test_backend(fake)
+    return fake
+
+
+def uninstall():
+    from tnalg_gb300 import _lib
+    _lib.install_test_backend(None)

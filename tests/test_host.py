@@ -1,0 +1,137 @@
+"""Host-side logic on CPU: the drop-in parameter API, the coupling-list compiler and the
+sweep orchestration (run through a numpy test double of the C ABI), and the built library's
+exported symbols."""
+import contextlib
+import ctypes
+import io
+import os
+import re
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+
+def _quiet(fn, *a, **k):
+    with contextlib.redirect_stdout(io.StringIO()):
+        return fn(*a, **k)
+
+
+# -- parameters -------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("name", ["chain_n12_chi16", "chain_n12_chi16_h", "longrange_n8_chi8", "jigsaw_s1_n9_chi12"])
+def test_parameters_reproduce_reference_tables(name):
+    from tnalg_gb300 import Parameters as pm
+    m, g = gc.meta()[name], gc.load(name)
+    lat = m["lattice"]
+    para = pm.generate_parameters_dmrg(lat)
+    para.update(l=m["l"], chi=m["chi"], hx=m["hx"], hz=m["hz"])
+    if lat == "chain":
+        para.update(jxy=1, jz=1)
+    if lat == "longRange":
+        para.update(jxy=1.0, jz=1.0)
+    para = pm.make_consistent_parameter_dmrg(para)
+    np.testing.assert_array_equal(np.asarray(para["index1"]), g["index1"])
+    np.testing.assert_array_equal(np.asarray(para["index2"]), g["index2"])
+    np.testing.assert_allclose(np.ravel(para["coeff1"]), g["coeff1"])
+    np.testing.assert_allclose(np.ravel(para["coeff2"]), g["coeff2"])
+    np.testing.assert_allclose(np.stack([np.real(o) for o in para["op"]]), g["op"])
+    assert para["d"] == m["d"] and para["l"] == m["l"]
+
+
+def test_parameters_accept_runtime_strings():
+    from tnalg_gb300 import Parameters as pm
+    lat = "".join(["ch", "ain"])  # not interned
+    para = pm.generate_parameters_dmrg(lat)
+    assert para["index2"].shape == (3 * (para["l"] - 1), 4)
+    with pytest.raises(ValueError):
+        pm.generate_parameters_dmrg("kagome")
+
+
+def test_square_and_husimi_generators():
+    from tnalg_gb300 import HamiltonianModule as hm, Parameters as pm
+    p = pm.generate_parameters_dmrg("square")
+    assert p["l"] == 16 and p["positions_h2"].shape == (24, 2)
+    h = pm.generate_parameters_dmrg("husimi")
+    pos = hm.positions_husimi(2)
+    assert h["l"] == int(pos.max()) + 1 and pos.shape[0] % 3 == 0
+    full = hm.positions_fully_connected(5)
+    assert full.shape == (10, 2)
+
+
+# -- coupling-list compiler ---------------------------------------------------------------
+
+
+def test_term_filter_and_orientation():
+    from tnalg_gb300 import engine as E
+    ops = [np.eye(2), np.zeros((2, 2)), np.zeros((2, 2)), np.diag([0.5, -0.5])]
+    one, two = E.canonical_terms([[0, 3], [1, 1], [2, 3]], [1.0, 1.0, 1e-13], [[3, 1, 3, 0], [0, 2, 3, 3]],
+                                 [0.5, 1e-20], ops, 1e-12)
+    assert one == [(0, 3, 1.0)]                 # zero operator and tiny coefficient dropped
+    assert two == [(1, 3, 0, 3, 0.5)]           # oriented i < j with operators swapped
+    with pytest.raises(ValueError):
+        E.canonical_terms([], [], [[1, 1, 3, 3]], [1.0], ops, 1e-12)
+
+
+def test_open_operator_sets_chain_and_long_range():
+    from tnalg_gb300 import engine as E
+    ops = [np.eye(2)] * 6
+    two = [(i, i + 1, a, b, 1.0) for i in range(4) for a, b in ((4, 5), (5, 4), (3, 3))]
+    m = E.Model(5, 2, ops, [], two, "cpu")
+    assert len(m.open_left[0]) == 0 and len(m.open_left[5]) == 0
+    assert all(len(m.open_left[b]) == 3 for b in range(1, 5))
+    assert m.straddle_groups(2) == ([], [], 0)
+    two = [(0, 4, 3, 3, 0.5), (0, 3, 3, 3, 0.25), (1, 3, 4, 5, 1.0)]
+    m = E.Model(5, 2, ops, [], two, "cpu")
+    sl, sr, ng = m.straddle_groups(2)
+    assert ng == 2  # two distinct left operators, three right ones -> grouped by the left side
+    assert sorted(c for _, _, c in sr) == [0.25, 0.5, 1.0]
+
+
+# -- orchestration through the test double ---------------------------------------------------
+
+
+@pytest.mark.parametrize("name", ["chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8"])
+def test_sweep_orchestration_matches_reference(name, fake_backend):
+    from tnalg_gb300 import DMRG_anyH
+    g, m = gc.load(name), gc.meta()[name]
+    np.random.seed(m["seed"])
+    ob, A, info, para = _quiet(DMRG_anyH.dmrg_finite_size, gc.para_of(name, device="cpu"))
+    assert abs(ob["e_per_site"] - float(g["e_per_site"])) <= 1e-10 * abs(float(g["e_per_site"]))
+    np.testing.assert_allclose(np.ravel(ob["eb_full"]), g["eb_full"], atol=1e-8)
+    np.testing.assert_allclose(np.ravel(ob["mz"]), g["mz"], atol=1e-8)
+    np.testing.assert_allclose(ob["corr_z"], g["corr_z_nocache"], atol=1e-8)
+    np.testing.assert_allclose(np.ravel(A.ent), g["ent"], atol=1e-8)
+    assert (A.virtual_dim == g["virtual_dim"]).all()
+    assert info["solves"] == 2 * (m["l"] - 1) * m["sweep_time"]
+
+
+def test_pickle_roundtrip(fake_backend):
+    import pickle
+    from tnalg_gb300.MPSClass import MpsOpenBoundaryClass
+    np.random.seed(3)
+    A = MpsOpenBoundaryClass(6, 2, 4, device="cpu")
+    A.correct_orthogonal_center(0)
+    B = pickle.loads(pickle.dumps(A))
+    assert B.center == 0 and (B.virtual_dim == A.virtual_dim).all()
+    for a, b in zip(A.mps, B.mps):
+        np.testing.assert_array_equal(a, b)
+
+
+# -- the built library -------------------------------------------------------------------------
+
+
+def test_library_exports_header_symbols():
+    from tnalg_gb300 import _lib, build
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    header = open(os.path.join(os.path.dirname(gc.GOLDEN), "..", "include", "tnalg_gb300.h")).read()
+    declared = set(re.findall(r"^\s*(?:const char\*|int|size_t)\s+(tn_\w+)\(", header, re.M))
+    assert declared, "no declarations parsed"
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    missing = [s for s in sorted(declared) if not hasattr(lib, s)]
+    assert not missing, missing
+    assert declared <= set(_lib.exported_symbols()) | {"tn_version"}
+    assert lib.tn_version() >= 100

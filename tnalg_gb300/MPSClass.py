@@ -1,0 +1,362 @@
+"""MpsOpenBoundaryClass on one GB300 (drop-in for T-Nalg's MPSClass.MpsOpenBoundaryClass).
+
+Constructor signature, attribute names and the methods used by the finite-size
+DMRG (MPSClass.py:53-1098) are kept; the tensors live on the GPU and every
+numeric step runs in libtnalg_gb300.so. ``mps`` returns host (numpy) copies in
+the reference layout, so user code and pickling see the same objects as with
+the reference.
+
+Differences a user can observe:
+  * ``is_parallel`` / ``is_env_parallel_lmr`` / ``par_pool`` / ``eig_way`` /
+    ``is_save_op`` are accepted and ignored: there is one device path, equivalent
+    to the reference's eig_way=1 matrix-free local solve with cached operators.
+  * Two-body rows with i > j are oriented to i < j (the reference applies the
+    wrong site operator for such rows in classify_and_update_env, MPSClass.py:717-728).
+  * observe_correlators_from_middle never reads stale cached operators (with
+    is_save_op=True the reference's corr_z after calculate_entanglement_spectrum
+    does; its is_save_op=False values are what this class returns).
+  * Operators must be real (spin 'sy' enters only through complex-free products
+    in the Heisenberg expansion).
+"""
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import engine as E
+from .HamiltonianModule import spin_operators
+
+
+def random_open_mps(l, d, chi):
+    """Global numpy RNG, draw order of TensorBasicModule.py:181-186 (site 0, site l-1, then 1..l-2)."""
+    mps = [None] * l
+    mps[0] = np.random.randn(1, d, chi)
+    mps[l - 1] = np.random.randn(chi, d, 1)
+    for n in range(1, l - 1):
+        mps[n] = np.random.randn(chi, d, chi)
+    return mps
+
+
+def ones_open_mps(l, d, chi):
+    """TensorBasicModule.py ones_open_mps: all-ones tensors."""
+    return [np.ones((1, d, chi))] + [np.ones((chi, d, chi)) for _ in range(l - 2)] + [np.ones((chi, d, 1))]
+
+
+def entanglement_entropy(lm, tol=1e-20):
+    """TensorBasicModule.py:786-801: -2 sum lm^2 ln lm over lm > tol."""
+    lm = np.sort(np.reshape(lm, -1))[::-1]
+    lm = lm[lm > tol]
+    return float(-2.0 * np.dot(lm ** 2, np.log(lm)))
+
+
+class MpsBasic:
+    def __init__(self):
+        self.version = "gb300-1"
+        self.operators = list()
+
+
+class MpsOpenBoundaryClass(MpsBasic):
+    """Open-boundary MPS (MPSClass.py:26-106) resident on a CUDA device."""
+
+    def __init__(self, length, d, chi, spin="half", way="qr", ini_way="r", operators=None, debug=False,
+                 is_parallel=False, is_save_op=False, eig_way=0, par_pool=None, is_env_parallel_lmr=True,
+                 device="cuda", precision="fp64", tensors=None):
+        MpsBasic.__init__(self)
+        self.spin = spin
+        self.phys_dim = d
+        self.decomp_way = way
+        self.length = length
+        self.lm = [np.zeros(0) for _ in range(length - 1)]
+        self.ent = np.zeros((length - 1, 1))
+        if tensors is None:
+            if ini_way == "r":
+                tensors = random_open_mps(length, d, chi)
+            elif ini_way == "1":
+                tensors = ones_open_mps(length, d, chi)
+            else:
+                raise ValueError("ini_way must be 'r' or '1'")
+        if operators is None:
+            op = spin_operators(spin)
+            operators = [op["id"], op["sx"], op["sy"], op["sz"], op["su"], op["sd"]]
+        self.operators = operators
+        self._is_save_op = is_save_op
+        self._is_parallel = is_parallel
+        self._is_env_parallel_lmr = is_env_parallel_lmr
+        self._debug = debug
+        self.eig_way = eig_way
+        self.pool = None
+        self.lanczos = {"max_krylov": 40, "max_restarts": 50, "check_every": 3, "tol_cap": 0.0,
+                        "mixed_floor": 2e-6, "refine": None}
+        self.last_solve = None
+        self._model_key = None
+        self._dev = E.DeviceMPS(tensors, d, device, precision=precision)
+        self.solve_energies = []
+
+    # -- reference attributes ---------------------------------------------------
+    @property
+    def mps(self):
+        return self._dev.numpy_tensors()
+
+    @property
+    def mps_device(self):
+        return self._dev.mps
+
+    @property
+    def virtual_dim(self):
+        return self._dev.virtual_dim
+
+    @property
+    def center(self):
+        return self._dev.center
+
+    @center.setter
+    def center(self, value):
+        self._dev.center = value
+
+    @property
+    def orthogonality(self):
+        return self._dev.orthogonality.reshape(-1, 1)
+
+    @property
+    def precision(self):
+        return {v: k for k, v in L.PRECISIONS.items() if k in ("fp64", "tf32x3")}[self._dev.precision]
+
+    def set_precision(self, precision):
+        self._dev.precision = L.PRECISIONS[precision]
+        self._dev.set_model(None)
+        self._model_key = None
+
+    @property
+    def stats(self):
+        return self._dev.stats
+
+    # -- gauge -------------------------------------------------------------------
+    def orthogonalize_mps(self, l0, l1):
+        """MPSClass.py:143-167 (QR moves; 'svd' moves also record the Schmidt values)."""
+        if self.decomp_way == "svd":
+            self._svd_moves(l0, l1)
+        else:
+            self._dev.orthogonalize_mps(l0, l1)
+
+    def central_orthogonalization(self, lc, l0=0, l1=-1):
+        """MPSClass.py:170-185."""
+        if l1 == -1:
+            l1 = self.length - 1
+        self.orthogonalize_mps(l0, lc)
+        self.orthogonalize_mps(l1, lc)
+        self._dev.center = lc
+
+    def correct_orthogonal_center(self, p=-1):
+        """MPSClass.py:188-198."""
+        if p < -0.5 and self.center < -0.5:
+            p = self.check_orthogonal_center(if_print=False)
+        elif p < -0.5:
+            p = self.center
+        if self.center < -0.5:
+            self.central_orthogonalization(p)
+        elif self.center != p:
+            self.orthogonalize_mps(self.center, p)
+        self._dev.center = p
+
+    def check_orthogonal_center(self, expected_center=-2, if_print=True):
+        """Centre implied by the orthogonality flags (MPSClass.py:989-1022, without prints)."""
+        if self.center > -0.5:
+            return self.center
+        o = self._dev.orthogonality
+        left = np.nonzero(o == -1)[0]
+        right = np.nonzero(o == 1)[0]
+        lpos = left[-1] if left.size else -1
+        if right.size and lpos + 2 == right[0]:
+            return lpos + 1
+        return lpos + 1
+
+    def _svd_moves(self, l0, l1):
+        """QR moves plus the singular values of each R factor (the reference's 'svd' decomposition
+        stores lm at MPSClass.py:154-155,163-164; the Schmidt values of a bond are the singular
+        values of R)."""
+        dev = self._dev
+        lib = L.load()
+        step = 1 if l0 < l1 else -1
+        for n in range(l0, l1, step):
+            if step > 0:
+                dev.qr_left(n)
+                R = dev._last_r
+                bond = n
+            else:
+                dev.qr_right(n)
+                R = dev._last_r
+                bond = n - 1
+            if self.center > -1:
+                k, nn = R.shape
+                sv = torch.empty(k, dtype=torch.float64, device=dev.device)
+                wp, wb = dev.ws2.args(lib.tn_singular_values_workspace_bytes(k, nn))
+                L.check(lib.tn_singular_values(k, nn, L.ptr(R), nn, 1, L.ptr(sv), 1e-15, 60, wp, wb,
+                                               L.stream_handle()), "singular values")
+                s = np.sort(sv.cpu().numpy())[::-1]
+                self.lm[bond] = s[: min(R.shape)]
+        if l0 < l1:
+            dev.orthogonality[l0:l1] = -1
+            dev.orthogonality[l1] = 0
+        elif l0 > l1:
+            dev.orthogonality[l1 + 1:l0 + 1] = 1
+            dev.orthogonality[l1] = 0
+
+    # -- local update ------------------------------------------------------------
+    def _model(self, index1, index2, coeff1, coeff2, tol):
+        key = (id(index1), id(index2), id(coeff1), id(coeff2), float(tol),
+               np.asarray(index2).tobytes(), np.asarray(coeff2, dtype=float).tobytes(),
+               np.asarray(index1).tobytes(), np.asarray(coeff1, dtype=float).tobytes())
+        if key != self._model_key:
+            one, two = E.canonical_terms(index1, coeff1, index2, coeff2, self.operators, tol)
+            used = {sn for _, sn, _ in one} | {a for *_, a, b, c in two} | {b for *_, b, c in two}
+            for k in used:
+                if np.any(np.abs(np.imag(np.asarray(self.operators[k], dtype=complex))) > 0):
+                    raise ValueError("operator %d is complex; the GPU path is real FP64" % k)
+            model = E.Model(self.length, self.phys_dim, self.operators, one, two, self._dev.device)
+            self._dev.set_model(model)
+            self._model_key = key
+        return self._dev.model
+
+    def update_tensor_eigs(self, p, index1, index2, coeff1, coeff2, tau, is_real, tol=1e-16):
+        """MPSClass.py:778-809: move the centre to p and replace site p by the lowest eigenvector
+        of its effective Hamiltonian. Returns the eigenvalue of H_eff."""
+        self._model(index1, index2, coeff1, coeff2, tol)
+        self.correct_orthogonal_center(p)
+        o = self.lanczos
+        res = self._dev.solve(p, tol, tau, tol_cap=o["tol_cap"], max_krylov=o["max_krylov"],
+                              max_restarts=o["max_restarts"], check_every=o["check_every"], refine=o["refine"],
+                              mixed_floor=o["mixed_floor"])
+        self.last_solve = res
+        e = res.energy_fp64 if res.energy_fp64 != 0.0 or res.energy == 0.0 else res.energy
+        self.solve_energies.append(e)
+        return e
+
+    def effective_hamiltonian_dmrg(self, p, index1, index2, coeff1, coeff2, tol=1e-12):
+        """Dense H_eff at the centre p (MPSClass.py:532-580), built column by column with
+        tn_matvec; only for small bond dimensions."""
+        self._model(index1, index2, coeff1, coeff2, tol)
+        self.correct_orthogonal_center(p)
+        s = [int(x) for x in self._dev.mps[p].shape]
+        n = int(np.prod(s))
+        eye = torch.eye(n, dtype=torch.float64, device=self._dev.device)
+        cols = [self._dev.apply_heff(p, eye[k].reshape(s), precision=L.PREC_FP64) for k in range(n)]
+        h = torch.stack([c.reshape(-1) for c in cols], dim=1)
+        return h.cpu().numpy(), s
+
+    # -- observables ---------------------------------------------------------------
+    def _ensure_obs_model(self):
+        if self._dev.model is None:
+            self._dev.set_model(E.Model(self.length, self.phys_dim, self.operators, [], [], self._dev.device))
+
+    def observe_magnetization(self, sn):
+        """MPSClass.py:911-921: <operators[sn]> on every site, shape (length, 1)."""
+        self._ensure_obs_model()
+        v1, _ = E.observe(self._dev, [(i, sn) for i in range(self.length)], [])
+        return v1.reshape(-1, 1)
+
+    def observe_bond_energy(self, index2, coeff2):
+        """MPSClass.py:923-934: coeff * <op_i op_j> for every row of index2, shape (nh, 1)."""
+        self._ensure_obs_model()
+        idx = np.asarray(index2).reshape(-1, 4)
+        c2 = np.ravel(np.asarray(coeff2, dtype=float))
+        _, v2 = E.observe(self._dev, [], [tuple(int(x) for x in r) for r in idx])
+        return (c2 * v2).reshape(-1, 1)
+
+    def observation_s1(self, inputs):
+        sn, position = inputs
+        self._ensure_obs_model()
+        return float(E.observe(self._dev, [(int(position), int(sn))], [])[0][0])
+
+    def observation_s1_s2(self, inputs):
+        ssn, positions = inputs
+        self._ensure_obs_model()
+        q = (int(positions[0]), int(positions[1]), int(ssn[0]), int(ssn[1]))
+        return float(E.observe(self._dev, [], [q])[1][0])
+
+    def observe_correlators_from_middle(self, op1, op2, ob_len=None):
+        """MPSClass.py:936-952 (Python round() of length/2 for the middle site)."""
+        self._ensure_obs_model()
+        if ob_len is None:
+            ob_len = self.length
+        pairs = []
+        pos1 = round(self.length / 2)
+        pos2 = pos1 + 1
+        n = 0
+        while pos1 > -0.1 and pos2 < self.length and ob_len > -0.1:
+            pairs.append((pos1, pos2, op1, op2))
+            if n % 2 == 0:
+                pos1 -= 1
+            else:
+                pos2 += 1
+            n += 1
+            ob_len -= 1
+        if not pairs:
+            return np.zeros(0)
+        return E.observe(self._dev, [], pairs)[1]
+
+    def calculate_entanglement_spectrum(self, if_fast=True):
+        """MPSClass.py:812-832: SVD-type moves to the ends and back fill lm."""
+        way, c0 = self.decomp_way, self.center
+        self.decomp_way = "svd"
+        if if_fast and c0 > -0.5:
+            p0, p1 = self.length - 1, 0
+            for n in range(self.length - 1):
+                if self.lm[n].size == 0:
+                    p0 = min(p0, n)
+                    p1 = max(p1, n)
+            self.correct_orthogonal_center(p0)
+            self.correct_orthogonal_center(p1 + 1)
+            self.correct_orthogonal_center(c0)
+        else:
+            self.correct_orthogonal_center(0)
+            self.correct_orthogonal_center(self.length - 1)
+            if c0 > 0:
+                self.correct_orthogonal_center(c0)
+        self.decomp_way = way
+
+    def calculate_entanglement_entropy(self):
+        """MPSClass.py:834-839."""
+        for i in range(self.length - 1):
+            self.ent[i] = -1 if self.lm[i].size == 0 else entanglement_entropy(self.lm[i])
+
+    def norm_mps(self):
+        """MPSClass.py:954-966 (norm of the centre tensor)."""
+        if self.center < -0.5:
+            raise RuntimeError("norm_mps needs a central-orthogonal MPS")
+        return float(torch.linalg.vector_norm(self._dev.mps[self.center]).item())
+
+    def report_yourself(self):
+        print("center: " + str(self.center))
+        print("orthogonality:" + str(self.orthogonality.T))
+        print("virtual bond dimensions: " + str(self.virtual_dim))
+
+    def clean_to_save(self):
+        """MPSClass.py:1090-1098: drop cached environments and the thread pool."""
+        self._dev.set_model(None)
+        self._model_key = None
+        self.pool = None
+
+    # -- pickling: host copies in the reference layout -----------------------------
+    def __getstate__(self):
+        st = {k: v for k, v in self.__dict__.items() if k != "_dev"}
+        st["_mps_host"] = self.mps
+        st["_virtual_dim"] = np.array(self.virtual_dim)
+        st["_center"] = self.center
+        st["_orthogonality"] = np.array(self._dev.orthogonality)
+        st["_precision"] = self.precision
+        st["_device"] = str(self._dev.device)
+        st["last_solve"] = None
+        st["_model_key"] = None
+        return st
+
+    def __setstate__(self, st):
+        tensors = st.pop("_mps_host")
+        vd = st.pop("_virtual_dim")
+        c = st.pop("_center")
+        orth = st.pop("_orthogonality")
+        prec = st.pop("_precision")
+        dev = st.pop("_device")
+        self.__dict__.update(st)
+        self._dev = E.DeviceMPS(tensors, self.phys_dim, dev, precision=prec)
+        self._dev.virtual_dim = vd
+        self._dev.center = c
+        self._dev.orthogonality = orth

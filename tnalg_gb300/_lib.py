@@ -1,0 +1,173 @@
+"""ctypes binding of libtnalg_gb300.so (the C ABI declared in include/tnalg_gb300.h).
+
+The product path has no CPU fallback: every call requires CUDA FP64 tensors and
+raises if the library is missing or a call fails.
+"""
+import ctypes
+import os
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libtnalg_gb300.so")
+
+TN_OK, TN_ERR_ARG, TN_ERR_CUDA, TN_ERR_WORKSPACE, TN_ERR_NOCONV, TN_ERR_NUMERIC, TN_ERR_TIMEOUT = range(7)
+PREC_FP64, PREC_TF32X3 = 0, 1
+PRECISIONS = {"fp64": PREC_FP64, "tf32x3": PREC_TF32X3, "3xtf32": PREC_TF32X3, "mixed": PREC_TF32X3}
+
+c_i64 = ctypes.c_int64
+c_dbl = ctypes.c_double
+c_vp = ctypes.c_void_p
+c_int = ctypes.c_int
+c_sz = ctypes.c_size_t
+
+
+class TnError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("tnalg_gb300 error %d: %s" % (status, msg))
+        self.status = status
+
+
+class BlockTerm(ctypes.Structure):
+    _fields_ = [("slot", ctypes.c_int32), ("op", ctypes.c_int32), ("coeff", ctypes.c_double)]
+
+
+class SiteDesc(ctypes.Structure):
+    _fields_ = [("chil", c_i64), ("d", c_i64), ("chir", c_i64), ("wl", c_vp), ("wr", c_vp),
+                ("nstr", c_i64), ("sl", c_vp), ("sr", c_vp)]
+
+
+class LanczosOpts(ctypes.Structure):
+    _fields_ = [("eigs_tol", c_dbl), ("tau", c_dbl), ("tol_cap", c_dbl), ("mixed_floor", c_dbl),
+                ("max_krylov", ctypes.c_int32), ("max_restarts", ctypes.c_int32), ("check_every", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("refine", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class LanczosResult(ctypes.Structure):
+    _fields_ = [("energy", c_dbl), ("residual", c_dbl), ("energy_fp64", c_dbl), ("matvecs", ctypes.c_int32),
+                ("restarts", ctypes.c_int32), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+_SIGS = {
+    "tn_last_error": (ctypes.c_char_p, []),
+    "tn_version": (c_int, []),
+    "tn_device_info": (c_int, [c_vp, c_vp, c_vp]),
+    "tn_gemm": (c_int, [c_int, c_i64, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64,
+                        c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_dbl, c_dbl, c_vp, c_sz, c_vp]),
+    "tn_gemm_workspace_bytes": (c_sz, [c_int, c_i64, c_i64, c_i64, c_i64]),
+    "tn_assemble_block": (c_int, [c_int, c_i64, c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp]),
+    "tn_combine_slots": (c_int, [c_i64, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp]),
+    "tn_apply_site_ops": (c_int, [c_i64, c_i64, c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp]),
+    "tn_pair_contract": (c_int, [c_i64, c_i64, c_i64, c_vp, c_vp, c_dbl, c_vp, c_vp]),
+    "tn_matvec": (c_int, [c_vp, c_vp, c_vp, c_dbl, c_dbl, c_int, c_vp, c_sz, c_vp]),
+    "tn_matvec_workspace_bytes": (c_sz, [c_vp, c_int]),
+    "tn_lanczos": (c_int, [c_vp, c_vp, c_vp, c_vp, c_sz, c_vp, c_vp]),
+    "tn_lanczos_workspace_bytes": (c_sz, [c_vp, c_vp]),
+    "tn_qr": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_sz, c_vp]),
+    "tn_qr_workspace_bytes": (c_sz, [c_i64, c_i64]),
+    "tn_singular_values": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
+    "tn_singular_values_workspace_bytes": (c_sz, [c_i64, c_i64]),
+    "tn_dot": (c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "tn_scale": (c_int, [c_i64, c_vp, c_dbl, c_vp, c_vp]),
+    "tn_set_identity": (c_int, [c_i64, c_vp, c_i64, c_vp]),
+}
+
+_lib = None
+_host_test = False
+
+
+def install_test_backend(fake):
+    """Tests only: route calls to `fake` (an object with the tn_* functions) and accept CPU
+    tensors. Never called by the library itself."""
+    global _lib, _host_test
+    _lib = fake
+    _host_test = fake is not None
+
+
+def load(path=None):
+    """Load the library (once). Raises if it is missing: there is no fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError("libtnalg_gb300.so not found at %s; run tnalg_gb300.build.build() first" % path)
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def check(status, what=""):
+    if status != TN_OK:
+        msg = load().tn_last_error().decode(errors="replace")
+        raise TnError(status, (what + ": " if what else "") + msg)
+
+
+def ptr(t):
+    if t is None:
+        return None
+    if not t.is_cuda and not _host_test:
+        raise TypeError("tnalg_gb300 requires CUDA tensors (got %s)" % t.device)
+    return c_vp(t.data_ptr())
+
+
+def stream_handle():
+    if _host_test:
+        return c_vp(0)
+    return c_vp(torch.cuda.current_stream().cuda_stream)
+
+
+class Workspace:
+    """Grow-only device scratch buffer owned by one MPS (or engine)."""
+
+    def __init__(self, device):
+        self.device = device
+        self.buf = None
+
+    def get(self, nbytes):
+        nbytes = int(max(nbytes, 256))
+        if self.buf is None or self.buf.numel() < nbytes:
+            self.buf = torch.empty(int(nbytes * 1.25) + 256, dtype=torch.uint8, device=self.device)
+        return self.buf
+
+    def args(self, nbytes):
+        b = self.get(nbytes)
+        return c_vp(b.data_ptr()), c_sz(b.numel())
+
+
+def gemm(A, B, C, M, N, K, sA, sB, sC, *, Cin=None, batch=1, bstrides=(0, 0, 0), nred=1, rstrides=(0, 0),
+         alpha=1.0, beta=0.0, precision=PREC_FP64, ws=None):
+    """C = alpha * sum_r A.B + beta * Cin over flat CUDA buffers with explicit element strides.
+
+    sA = (sAm, sAk), sB = (sBk, sBn), sC = (sCm, sCn); tensors may be views (their data_ptr is used).
+    """
+    lib = load()
+    if ws is not None:
+        need = lib.tn_gemm_workspace_bytes(precision, M, N, K, batch)
+        wp, wb = ws.args(need)
+    else:
+        wp, wb = None, 0
+    check(lib.tn_gemm(precision, M, N, K, ptr(A), sA[0], sA[1], ptr(B), sB[0], sB[1], ptr(C), sC[0], sC[1],
+                      ptr(Cin) if Cin is not None else None, batch, bstrides[0], bstrides[1], bstrides[2], nred,
+                      rstrides[0], rstrides[1], alpha, beta, wp, wb, stream_handle()), "gemm")
+
+
+def terms_tensor(terms, device):
+    """list of (slot, op, coeff) -> device buffer of tn_block_term structs (16 bytes each)."""
+    n = len(terms)
+    arr = (BlockTerm * max(n, 1))()
+    for i, (slot, op, c) in enumerate(terms):
+        arr[i].slot = int(slot)
+        arr[i].op = int(op)
+        arr[i].coeff = float(c)
+    raw = bytes(arr)[: 16 * max(n, 1)]
+    host = torch.frombuffer(bytearray(raw), dtype=torch.uint8)
+    return host.to(device), n

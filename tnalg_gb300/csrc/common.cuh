@@ -1,0 +1,54 @@
+// Shared helpers for the tnalg_gb300 CUDA kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "tnalg_gb300.h"
+
+#define TN_CHECK_LAUNCH()                                   \
+  do {                                                      \
+    cudaError_t e_ = cudaGetLastError();                    \
+    if (e_ != cudaSuccess) return tn_record_error(e_);      \
+  } while (0)
+
+#define TN_CUDA(call)                                       \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return tn_record_error(e_);      \
+  } while (0)
+
+// Records the CUDA error text for tn_last_error() and maps it to a status code.
+int tn_record_error(cudaError_t e);
+int tn_fail(int status, const char* msg);
+
+__host__ __device__ static inline int64_t tn_cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+__device__ __forceinline__ double tn_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ float tn_warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Internal launchers shared between translation units.
+struct TnGemmF64 {
+  int64_t M, N, K;
+  const double* A; int64_t sAm, sAk;
+  const double* B; int64_t sBk, sBn;
+  double* C; int64_t sCm, sCn;
+  const double* Cin;  // nullptr: beta scales C itself
+  int64_t batch; int64_t sAb, sBb, sCb;
+  int64_t nred; int64_t sAr, sBr;
+  double alpha, beta;
+};
+int tn_gemm_f64_launch(const TnGemmF64& g, cudaStream_t s);
+int tn_gemm_f64_ws(const TnGemmF64& g, void* ws, size_t ws_bytes, cudaStream_t s);
+size_t tn_gemm_f64_ws_bytes(int64_t M, int64_t N, int64_t batch);
+int tn_sm_count();

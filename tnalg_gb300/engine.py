@@ -1,0 +1,618 @@
+"""Device-resident one-site DMRG engine behind MpsOpenBoundaryClass.
+
+Host-side orchestration only: every contraction, decomposition and eigen-solve
+is a call into libtnalg_gb300.so (include/tnalg_gb300.h).
+
+Effective operators (the reference's effect_s / effect_ss caches and
+classify_and_update_env buckets, MPSClass.py:202-325,474-530,684-733) are kept
+per bond as one stacked device tensor:
+
+    EL[b] : (1 + |open_left(b)|, chi_b, chi_b)   slot 0 = sum of all terms inside sites < b,
+            slot 1+k = operator open_left(b)[k] = (site i, op a) of a two-body term i < b <= j
+    ER[b] : (1 + |open_right(b)|, chi_b, chi_b)  mirror for sites >= b
+
+and are updated incrementally when the centre moves (one block-operator GEMM
+pair per carried operator) instead of being rebuilt from the chain end as the
+reference does (MPSClass.py:491-502).
+"""
+from collections import OrderedDict
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+
+# ---------------------------------------------------------------------------
+# coupling-list compiler
+
+
+def canonical_terms(index1, coeff1, index2, coeff2, ops, tol):
+    """Filtered, oriented term lists (the filters of MPSClass.py:643-652).
+
+    One-body rows [site, op] with |coeff| > tol and ||op|| > tol; two-body rows
+    [i, j, a, b] with |coeff| > tol, oriented so that i < j (environment_s1_s2
+    sorts positions, MPSClass.py:345-347; the orientation also fixes the
+    operator used for the '1_sn_0' / '0_sn_1' buckets).
+    """
+    one, two = [], []
+    idx1 = np.asarray(index1).reshape(-1, 2) if np.size(index1) else np.zeros((0, 2), int)
+    idx2 = np.asarray(index2).reshape(-1, 4) if np.size(index2) else np.zeros((0, 4), int)
+    c1 = np.ravel(np.asarray(coeff1, dtype=float)) if np.size(coeff1) else np.zeros(0)
+    c2 = np.ravel(np.asarray(coeff2, dtype=float)) if np.size(coeff2) else np.zeros(0)
+    for n in range(idx1.shape[0]):
+        q, sn = int(idx1[n, 0]), int(idx1[n, 1])
+        if abs(c1[n]) > tol and np.linalg.norm(np.reshape(np.asarray(ops[sn]), -1)) > tol:
+            one.append((q, sn, float(c1[n])))
+    for n in range(idx2.shape[0]):
+        i, j, a, b = (int(x) for x in idx2[n])
+        if abs(c2[n]) > tol:
+            if i == j:
+                raise ValueError("two-body term with both operators on site %d" % i)
+            if i > j:
+                i, j, a, b = j, i, b, a
+            two.append((i, j, a, b, float(c2[n])))
+    return one, two
+
+
+class Model:
+    """Per-bond / per-site tables derived from the coupling lists (static for a run)."""
+
+    def __init__(self, length, d, ops, one, two, device):
+        self.length = length
+        self.d = d
+        self.device = device
+        ops_np = np.stack([np.real(np.asarray(o, dtype=complex)).astype(float) for o in ops])
+        if ops_np.shape[1:] != (d, d):
+            raise ValueError("operators must be %dx%d" % (d, d))
+        self.ops_np = ops_np
+        self.ops = torch.tensor(ops_np, dtype=torch.float64, device=device)
+        self.one = one
+        self.two = two
+        Ln = length
+        self.one_at = [[] for _ in range(Ln)]
+        for q, sn, c in one:
+            if not 0 <= q < Ln:
+                raise ValueError("one-body term on site %d outside 0..%d" % (q, Ln - 1))
+            self.one_at[q].append((sn, c))
+        for i, j, a, b, c in two:
+            if not (0 <= i < Ln and 0 <= j < Ln):
+                raise ValueError("two-body term (%d,%d) outside 0..%d" % (i, j, Ln - 1))
+        # open operators per bond b (0..L): term (i, j) is open at b iff i < b <= j
+        self.open_left = []
+        self.open_right = []
+        for b in range(Ln + 1):
+            lk = OrderedDict()
+            rk = OrderedDict()
+            for i, j, a, bo, c in two:
+                if i < b <= j:
+                    lk.setdefault((i, a), None)
+                    rk.setdefault((j, bo), None)
+            self.open_left.append({k: s + 1 for s, k in enumerate(lk)})
+            self.open_right.append({k: s + 1 for s, k in enumerate(rk)})
+        self._tables = {}
+
+    # -- block-operator term lists (slot, op, coeff) ----------------------------
+    def left_block_terms(self, p):
+        """W_L at site p: H_L(p) (x) 1 + 1 (x) O_site(p) + sum_{(i,p)} c C_L(i,a) (x) op_b."""
+        t = [(0, -1, 1.0)]
+        t += [(-1, sn, c) for sn, c in self.one_at[p]]
+        ol = self.open_left[p]
+        for i, j, a, b, c in self.two:
+            if j == p:
+                t.append((ol[(i, a)], b, c))
+        return t
+
+    def right_block_terms(self, p, with_site=True):
+        """W_R at site p: 1 (x) H_R(p+1) [+ O_site(p) (x) 1] + sum_{(p,j)} c op_a (x) C_R(j,b)."""
+        t = [(0, -1, 1.0)]
+        if with_site:
+            t += [(-1, sn, c) for sn, c in self.one_at[p]]
+        orr = self.open_right[p + 1]
+        for i, j, a, b, c in self.two:
+            if i == p:
+                t.append((orr[(j, b)], a, c))
+        return t
+
+    def left_carry_plan(self, b):
+        """How each slot of EL[b+1] is produced from EL[b] and site b: ('carry', old_slot) or ('fresh', op)."""
+        plan = []
+        for (i, a), slot in self.open_left[b + 1].items():
+            plan.append(("carry", self.open_left[b][(i, a)]) if i < b else ("fresh", a))
+        return plan
+
+    def right_carry_plan(self, b):
+        """Slots of ER[b] from ER[b+1] and site b."""
+        plan = []
+        for (j, bo), slot in self.open_right[b].items():
+            plan.append(("carry", self.open_right[b + 1][(j, bo)]) if j > b else ("fresh", bo))
+        return plan
+
+    def straddle_groups(self, p):
+        """Straddling terms i < p < j as sum_g SL_g (x) 1 (x) SR_g, grouped on the smaller side.
+
+        Returns (sl_terms, sr_terms, ngroups) for tn_combine_slots (op field = group id).
+        """
+        ol, orr = self.open_left[p], self.open_right[p + 1]
+        pairs = {}
+        for i, j, a, b, c in self.two:
+            if i < p < j:
+                key = (ol[(i, a)], orr[(j, b)])
+                pairs[key] = pairs.get(key, 0.0) + c
+        if not pairs:
+            return [], [], 0
+        us = sorted({u for u, _ in pairs})
+        vs = sorted({v for _, v in pairs})
+        sl, sr = [], []
+        if len(us) <= len(vs):
+            for g, u in enumerate(us):
+                sl.append((u, g, 1.0))
+                for (uu, v), c in pairs.items():
+                    if uu == u:
+                        sr.append((v, g, c))
+            return sl, sr, len(us)
+        for g, v in enumerate(vs):
+            sr.append((v, g, 1.0))
+            for (u, vv), c in pairs.items():
+                if vv == v:
+                    sl.append((u, g, c))
+        return sl, sr, len(vs)
+
+    def table(self, key, terms):
+        """Cached device copy of a term list."""
+        hit = self._tables.get(key)
+        if hit is None:
+            hit = L.terms_tensor(terms, self.device)
+            self._tables[key] = hit
+        return hit
+
+    def opidx(self, key, ops):
+        hit = self._tables.get(key)
+        if hit is None:
+            hit = torch.tensor(list(ops) if ops else [0], dtype=torch.int32, device=self.device)
+            self._tables[key] = hit
+        return hit
+
+
+# ---------------------------------------------------------------------------
+# device MPS
+
+
+class DeviceMPS:
+    """Open-boundary MPS on one GPU with incrementally updated environments."""
+
+    def __init__(self, tensors, d, device, precision="fp64"):
+        self.device = torch.device(device)
+        if self.device.type != "cuda" and not L._host_test:
+            raise RuntimeError("tnalg_gb300 runs on CUDA devices only")
+        L.load()
+        self.length = len(tensors)
+        self.d = d
+        self.mps = [torch.as_tensor(np.ascontiguousarray(t), dtype=torch.float64).to(self.device) for t in tensors]
+        self.virtual_dim = np.array([1] + [int(t.shape[2]) for t in tensors])
+        self.center = -1
+        self.orthogonality = np.zeros(self.length)
+        self.precision = L.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self.ws = L.Workspace(self.device)
+        self.ws2 = L.Workspace(self.device)
+        self.model = None
+        self.EL = [None] * (self.length + 1)
+        self.ER = [None] * (self.length + 1)
+        self.el_upto = -1      # EL[0..el_upto] valid
+        self.er_from = self.length + 1   # ER[er_from..L] valid
+        self.stats = {"matvecs": 0, "solves": 0, "restarts": 0, "unconverged": 0}
+
+    # -- model / environments ----------------------------------------------------
+    def set_model(self, model):
+        if self.model is not model:
+            self.model = model
+            self.EL = [None] * (self.length + 1)
+            self.ER = [None] * (self.length + 1)
+            self.el_upto = -1
+            self.er_from = self.length + 1
+
+    def _edge_envs(self):
+        m = self.model
+        if self.el_upto < 0:
+            self.EL[0] = torch.zeros((1 + len(m.open_left[0]), 1, 1), dtype=torch.float64, device=self.device)
+            self.el_upto = 0
+        if self.er_from > self.length:
+            self.ER[self.length] = torch.zeros((1 + len(m.open_right[self.length]), 1, 1), dtype=torch.float64,
+                                               device=self.device)
+            self.er_from = self.length
+
+    def tensor_changed(self, n):
+        """Environments that contracted site n become stale."""
+        self.el_upto = min(self.el_upto, n)
+        self.er_from = max(self.er_from, n + 1)
+
+    def ensure_envs(self, p):
+        self._edge_envs()
+        while self.el_upto < p:
+            self._left_update(self.el_upto)
+        while self.er_from > p + 1:
+            self._right_update(self.er_from - 1)
+
+    def _left_update(self, b):
+        """EL[b+1] from EL[b] and the left-canonical tensor at site b (transfer_left,
+        TensorBasicModule.py:530-573, for every carried operator at once)."""
+        m, A = self.model, self.mps[b]
+        cl, d, cr = A.shape
+        env = self.EL[b]
+        plan = m.left_carry_plan(b)
+        ns = 1 + len(plan)
+        lib, st = L.load(), L.stream_handle()
+        T = torch.empty((ns, cl * d * cr), dtype=torch.float64, device=self.device)
+        W = torch.empty((cl * d, cl * d), dtype=torch.float64, device=self.device)
+        terms, nt = m.table(("wl", b), m.left_block_terms(b))
+        L.check(lib.tn_assemble_block(0, cl, d, L.ptr(env), L.ptr(m.ops), L.ptr(terms), nt, L.ptr(W), st), "assemble")
+        L.gemm(W, A, T[0], cl * d, cr, cl * d, (cl * d, 1), (cr, 1), (cr, 1), precision=self.precision, ws=self.ws)
+        carry = [(k, s) for k, (kind, s) in enumerate(plan) if kind == "carry"]
+        fresh = [(k, a) for k, (kind, a) in enumerate(plan) if kind == "fresh"]
+        if carry:
+            # T[1+k] = EL[b][slot] . A(cl, d*cr); slots gathered into a contiguous stack first
+            g = torch.empty((len(carry), cl, cl), dtype=torch.float64, device=self.device)
+            gt, ng = m.table(("lg", b), [(s, q, 1.0) for q, (_, s) in enumerate(carry)])
+            L.check(lib.tn_combine_slots(cl, L.ptr(env), L.ptr(gt), ng, len(carry), L.ptr(g), st), "gather")
+            ks = [k for k, _ in carry]
+            if ks == list(range(ks[0], ks[0] + len(ks))):
+                L.gemm(g, A, T[1 + ks[0]], cl, d * cr, cl, (cl, 1), (d * cr, 1), (d * cr, 1), batch=len(carry),
+                       bstrides=(cl * cl, 0, cl * d * cr), precision=self.precision, ws=self.ws)
+            else:
+                for q, (k, _) in enumerate(carry):
+                    L.gemm(g[q], A, T[1 + k], cl, d * cr, cl, (cl, 1), (d * cr, 1), (d * cr, 1),
+                           precision=self.precision, ws=self.ws)
+        for k, a in fresh:
+            oi = m.opidx(("op", a), [a])
+            L.check(lib.tn_apply_site_ops(cl, d, cr, L.ptr(A), L.ptr(m.ops), L.ptr(oi), 1, L.ptr(T[1 + k]),
+                                          cl * d * cr, st), "site op")
+        out = torch.empty((ns, cr, cr), dtype=torch.float64, device=self.device)
+        L.gemm(A, T, out, cr, cr, cl * d, (1, cr), (cr, 1), (cr, 1), batch=ns, bstrides=(0, cl * d * cr, cr * cr),
+               precision=self.precision, ws=self.ws)
+        self.EL[b + 1] = out
+        self.el_upto = b + 1
+
+    def _right_update(self, b):
+        """ER[b] from ER[b+1] and the right-canonical tensor at site b (transfer_right,
+        TensorBasicModule.py:576-619)."""
+        m, B = self.model, self.mps[b]
+        cl, d, cr = B.shape
+        env = self.ER[b + 1]
+        plan = m.right_carry_plan(b)
+        ns = 1 + len(plan)
+        lib, st = L.load(), L.stream_handle()
+        T = torch.empty((ns, cl * d * cr), dtype=torch.float64, device=self.device)
+        W = torch.empty((d * cr, d * cr), dtype=torch.float64, device=self.device)
+        terms, nt = m.table(("wrf", b), m.right_block_terms(b, with_site=True))
+        L.check(lib.tn_assemble_block(1, cr, d, L.ptr(env), L.ptr(m.ops), L.ptr(terms), nt, L.ptr(W), st), "assemble")
+        # T0 = B(cl, d*cr) . W^T
+        L.gemm(B, W, T[0], cl, d * cr, d * cr, (d * cr, 1), (1, d * cr), (d * cr, 1), precision=self.precision,
+               ws=self.ws)
+        carry = [(k, s) for k, (kind, s) in enumerate(plan) if kind == "carry"]
+        fresh = [(k, a) for k, (kind, a) in enumerate(plan) if kind == "fresh"]
+        if carry:
+            g = torch.empty((len(carry), cr, cr), dtype=torch.float64, device=self.device)
+            gt, ng = m.table(("rg", b), [(s, q, 1.0) for q, (_, s) in enumerate(carry)])
+            L.check(lib.tn_combine_slots(cr, L.ptr(env), L.ptr(gt), ng, len(carry), L.ptr(g), st), "gather")
+            ks = [k for k, _ in carry]
+            if ks == list(range(ks[0], ks[0] + len(ks))):
+                L.gemm(B, g, T[1 + ks[0]], cl * d, cr, cr, (cr, 1), (1, cr), (cr, 1), batch=len(carry),
+                       bstrides=(0, cr * cr, cl * d * cr), precision=self.precision, ws=self.ws)
+            else:
+                for q, (k, _) in enumerate(carry):
+                    L.gemm(B, g[q], T[1 + k], cl * d, cr, cr, (cr, 1), (1, cr), (cr, 1), precision=self.precision,
+                           ws=self.ws)
+        for k, a in fresh:
+            oi = m.opidx(("op", a), [a])
+            L.check(lib.tn_apply_site_ops(cl, d, cr, L.ptr(B), L.ptr(m.ops), L.ptr(oi), 1, L.ptr(T[1 + k]),
+                                          cl * d * cr, st), "site op")
+        out = torch.empty((ns, cl, cl), dtype=torch.float64, device=self.device)
+        L.gemm(B, T, out, cl, cl, d * cr, (d * cr, 1), (1, d * cr), (cl, 1), batch=ns,
+               bstrides=(0, cl * d * cr, cl * cl), precision=self.precision, ws=self.ws)
+        self.ER[b] = out
+        self.er_from = b
+
+    # -- gauge -------------------------------------------------------------------
+    def qr_left(self, n):
+        """left2right_decompose_tensor + absorb_matrix2tensor(mps[n+1], R^T, 0)
+        (TensorBasicModule.py:314-348, 387-424; MPSClass.py:150-158)."""
+        A = self.mps[n]
+        cl, d, cr = A.shape
+        mm, nn = cl * d, cr
+        k = min(mm, nn)
+        lib, st = L.load(), L.stream_handle()
+        Q = torch.empty((cl, d, k), dtype=torch.float64, device=self.device)
+        R = torch.empty((k, nn), dtype=torch.float64, device=self.device)
+        wp, wb = self.ws2.args(lib.tn_qr_workspace_bytes(mm, nn))
+        L.check(lib.tn_qr(mm, nn, L.ptr(A), nn, 1, L.ptr(Q), k, 1, L.ptr(R), nn, 1, wp, wb, st), "qr")
+        nxt = self.mps[n + 1]
+        c2, d2, r2 = nxt.shape
+        new = torch.empty((k, d2, r2), dtype=torch.float64, device=self.device)
+        L.gemm(R, nxt, new, k, d2 * r2, nn, (nn, 1), (d2 * r2, 1), (d2 * r2, 1), ws=self.ws)
+        self.mps[n] = Q
+        self.mps[n + 1] = new
+        self._last_r = R
+        self.virtual_dim[n + 1] = k
+        self.tensor_changed(n)
+        self.tensor_changed(n + 1)
+
+    def qr_right(self, n):
+        """right2left_decompose_tensor + absorb_matrix2tensor(mps[n-1], R^T, 2)
+        (TensorBasicModule.py:351-384; MPSClass.py:159-167)."""
+        A = self.mps[n]
+        cl, d, cr = A.shape
+        mm, nn = d * cr, cl  # QR of A(cl, d*cr)^T
+        k = min(mm, nn)
+        lib, st = L.load(), L.stream_handle()
+        Bt = torch.empty((k, d, cr), dtype=torch.float64, device=self.device)
+        R = torch.empty((k, nn), dtype=torch.float64, device=self.device)
+        wp, wb = self.ws2.args(lib.tn_qr_workspace_bytes(mm, nn))
+        # a(i, j) = A[j, i]: sAm = 1, sAn = d*cr ; Q(i, j) -> Bt[j, i]: sQm = 1, sQn = d*cr
+        L.check(lib.tn_qr(mm, nn, L.ptr(A), 1, d * cr, L.ptr(Bt), 1, d * cr, L.ptr(R), nn, 1, wp, wb, st), "qr")
+        prv = self.mps[n - 1]
+        c0, d0, r0 = prv.shape
+        new = torch.empty((c0, d0, k), dtype=torch.float64, device=self.device)
+        # prv(c0*d0, cl) . R^T(cl, k)
+        L.gemm(prv, R, new, c0 * d0, k, nn, (nn, 1), (1, nn), (k, 1), ws=self.ws)
+        self.mps[n] = Bt
+        self.mps[n - 1] = new
+        self._last_r = R
+        self.virtual_dim[n] = k
+        self.tensor_changed(n)
+        self.tensor_changed(n - 1)
+
+    def orthogonalize_mps(self, l0, l1):
+        """MPSClass.py:143-167 with QR."""
+        if l0 < l1:
+            for n in range(l0, l1):
+                self.qr_left(n)
+            self.orthogonality[l0:l1] = -1
+            self.orthogonality[l1] = 0
+        elif l0 > l1:
+            for n in range(l0, l1, -1):
+                self.qr_right(n)
+            self.orthogonality[l1 + 1:l0 + 1] = 1
+            self.orthogonality[l1] = 0
+
+    def correct_orthogonal_center(self, p):
+        """MPSClass.py:188-198 for an explicit p."""
+        if self.center < 0:
+            self.orthogonalize_mps(0, p)
+            self.orthogonalize_mps(self.length - 1, p)
+        elif self.center != p:
+            self.orthogonalize_mps(self.center, p)
+        self.center = p
+
+    # -- local solve ---------------------------------------------------------------
+    def site_operator(self, p):
+        """Assemble the effective Hamiltonian of site p; returns (desc, keep-alive tensors)."""
+        m = self.model
+        self.ensure_envs(p)
+        cl, d, cr = self.mps[p].shape
+        lib, st = L.load(), L.stream_handle()
+        el, er = self.EL[p], self.ER[p + 1]
+        wl = torch.empty((cl * d, cl * d), dtype=torch.float64, device=self.device)
+        wr = torch.empty((d * cr, d * cr), dtype=torch.float64, device=self.device)
+        t, nt = m.table(("wl", p), m.left_block_terms(p))
+        L.check(lib.tn_assemble_block(0, cl, d, L.ptr(el), L.ptr(m.ops), L.ptr(t), nt, L.ptr(wl), st), "assemble")
+        t, nt = m.table(("wr", p), m.right_block_terms(p, with_site=False))
+        L.check(lib.tn_assemble_block(1, cr, d, L.ptr(er), L.ptr(m.ops), L.ptr(t), nt, L.ptr(wr), st), "assemble")
+        keep = [wl, wr]
+        slt, srt, ng = m.straddle_groups(p)
+        sl = sr = None
+        if ng:
+            sl = torch.empty((ng, cl, cl), dtype=torch.float64, device=self.device)
+            sr = torch.empty((ng, cr, cr), dtype=torch.float64, device=self.device)
+            a, na = m.table(("sl", p), slt)
+            b, nb = m.table(("sr", p), srt)
+            L.check(lib.tn_combine_slots(cl, L.ptr(el), L.ptr(a), na, ng, L.ptr(sl), st), "straddle")
+            L.check(lib.tn_combine_slots(cr, L.ptr(er), L.ptr(b), nb, ng, L.ptr(sr), st), "straddle")
+            keep += [sl, sr]
+        desc = L.SiteDesc(cl, d, cr, wl.data_ptr(), wr.data_ptr(), ng, sl.data_ptr() if ng else None,
+                          sr.data_ptr() if ng else None)
+        return desc, keep
+
+    def solve(self, p, eigs_tol, tau, *, tol_cap=0.0, max_krylov=40, max_restarts=50, check_every=3,
+              refine=None, mixed_floor=2e-6):
+        """Lowest eigenvector of H_eff at the centre p (MPSClass.py:778-809)."""
+        desc, keep = self.site_operator(p)
+        psi = self.mps[p].contiguous()
+        opts = L.LanczosOpts(float(eigs_tol), float(tau), float(tol_cap), float(mixed_floor), int(max_krylov),
+                             int(max_restarts), int(check_every), int(self.precision),
+                             int(self.precision != L.PREC_FP64 if refine is None else refine), 0)
+        lib = L.load()
+        need = lib.tn_lanczos_workspace_bytes(ctypes_ref(desc), ctypes_ref(opts))
+        wp, wb = self.ws.args(need)
+        res = L.LanczosResult()
+        status = lib.tn_lanczos(ctypes_ref(desc), L.ptr(psi), ctypes_ref(opts), wp, wb, ctypes_ref(res),
+                                L.stream_handle())
+        if status not in (L.TN_OK, L.TN_ERR_NOCONV):
+            L.check(status, "lanczos")
+        self.stats["solves"] += 1
+        self.stats["matvecs"] += res.matvecs
+        self.stats["restarts"] += res.restarts
+        if status == L.TN_ERR_NOCONV:
+            self.stats["unconverged"] += 1
+        self.mps[p] = psi
+        self.tensor_changed(p)
+        del keep
+        return res
+
+    def apply_heff(self, p, psi, alpha=1.0, beta=0.0, precision=None):
+        """y = beta*psi + alpha*H_eff psi at site p (tn_matvec)."""
+        desc, keep = self.site_operator(p)
+        y = torch.empty_like(psi)
+        prec = self.precision if precision is None else precision
+        lib = L.load()
+        wp, wb = self.ws.args(lib.tn_matvec_workspace_bytes(ctypes_ref(desc), prec))
+        L.check(lib.tn_matvec(ctypes_ref(desc), L.ptr(psi), L.ptr(y), float(alpha), float(beta), prec, wp, wb,
+                              L.stream_handle()), "matvec")
+        del keep
+        return y
+
+    def numpy_tensors(self):
+        return [t.detach().cpu().numpy() for t in self.mps]
+
+
+def ctypes_ref(obj):
+    import ctypes
+    return ctypes.byref(obj)
+
+
+# ---------------------------------------------------------------------------
+# observables (observation_s1 / observation_s1_s2, MPSClass.py:857-909)
+
+
+class _Observer:
+    """Expectation values of products of one-site operators on a canonical MPS.
+
+    For a centre c, sites < c are left-canonical and sites > c right-canonical, so a
+    product of operators on sites i <= j is contracted only over [min(i, c), max(j, c)]
+    with identity boundaries. Terms with j >= c are contracted left-to-right from an
+    identity (or the shared chain E_q for q > c); terms with j < c right-to-left.
+    Operator chains that share their first site and operator are contracted once.
+    """
+
+    def __init__(self, mps):
+        self.s = mps
+        self.dev = mps.device
+        self.c = mps.center
+        self.E = {}
+        self.F = {}
+        self.lib = L.load()
+        self.st = L.stream_handle()
+
+    # transfer helpers -------------------------------------------------------------
+    def _op_apply(self, X, shape, op):
+        cl, d, cr = shape
+        out = torch.empty_like(X)
+        oi = self.s.model.opidx(("op", op), [op])
+        L.check(self.lib.tn_apply_site_ops(cl, d, cr, L.ptr(X), L.ptr(self.s.model.ops), L.ptr(oi), 1, L.ptr(out),
+                                           cl * d * cr, self.st), "site op")
+        return out
+
+    def left_x(self, M, V):
+        """X = V . M(cl, d*cr) (V None = identity)."""
+        if V is None:
+            return M
+        cl, d, cr = M.shape
+        X = torch.empty_like(M)
+        L.gemm(V, M, X, cl, d * cr, cl, (cl, 1), (d * cr, 1), (d * cr, 1))
+        return X
+
+    def left_close(self, M, X):
+        """V' = M(cl*d, cr)^T . X(cl*d, cr)."""
+        cl, d, cr = M.shape
+        out = torch.empty((cr, cr), dtype=torch.float64, device=self.dev)
+        L.gemm(M, X, out, cr, cr, cl * d, (1, cr), (cr, 1), (cr, 1))
+        return out
+
+    def tl(self, M, V, op=None):
+        X = self.left_x(M, V)
+        if op is not None:
+            X = self._op_apply(X, M.shape, op)
+        return self.left_close(M, X)
+
+    def right_x(self, M, V):
+        """X = M(cl*d, cr) . V^T (V None = identity)."""
+        if V is None:
+            return M
+        cl, d, cr = M.shape
+        X = torch.empty_like(M)
+        L.gemm(M, V, X, cl * d, cr, cr, (cr, 1), (1, cr), (cr, 1))
+        return X
+
+    def right_close(self, M, X):
+        """V'[a', a] = sum M[a', (s b)] X[a, (s b)]."""
+        cl, d, cr = M.shape
+        out = torch.empty((cl, cl), dtype=torch.float64, device=self.dev)
+        L.gemm(M, X, out, cl, cl, d * cr, (d * cr, 1), (1, d * cr), (cl, 1))
+        return out
+
+    def tr(self, M, V, op=None):
+        X = self.right_x(M, V)
+        if op is not None:
+            X = self._op_apply(X, M.shape, op)
+        return self.right_close(M, X)
+
+    def E_at(self, q):
+        """Left environment (identity operators) at bond q; None means identity (q <= c)."""
+        if q <= self.c:
+            return None
+        if q not in self.E:
+            self.E[q] = self.tl(self.s.mps[q - 1], self.E_at(q - 1))
+        return self.E[q]
+
+    def F_at(self, q):
+        """Right environment at bond q; None means identity (q > c)."""
+        if q > self.c:
+            return None
+        if q not in self.F:
+            self.F[q] = self.tr(self.s.mps[q], self.F_at(q + 1))
+        return self.F[q]
+
+    def density(self, M, X, out):
+        cl, d, cr = M.shape
+        L.check(self.lib.tn_pair_contract(cl, d, cr, L.ptr(M), L.ptr(X), 1.0, L.ptr(out), self.st), "pair")
+
+    # queries ------------------------------------------------------------------------
+    def run(self, one, two):
+        """one: [(q, op)], two: [(i, j, a, b)] with i != j. Returns (vals_one, vals_two)."""
+        s = self.s
+        d = s.d
+        G1 = torch.zeros((max(len(one), 1), d, d), dtype=torch.float64, device=self.dev)
+        G2 = torch.zeros((max(len(two), 1), d, d), dtype=torch.float64, device=self.dev)
+        # one-body: local density at q
+        dens = {}
+        for k, (q, op) in enumerate(one):
+            if q not in dens:
+                M = s.mps[q]
+                X = self.left_x(M, self.E_at(q)) if q >= self.c else self.right_x(M, self.F_at(q + 1))
+                dens[q] = (M, X)
+            M, X = dens[q]
+            self.density(M, X, G1[k])
+        # two-body, grouped by the first operator of the contraction direction
+        fwd, bwd = {}, {}
+        closing = []
+        for k, (i, j, a, b) in enumerate(two):
+            if i > j:
+                i, j, a, b = j, i, b, a
+            if j >= self.c:
+                fwd.setdefault((i, a), []).append((j, b, k))
+                closing.append(b)
+            else:
+                bwd.setdefault((j, b), []).append((i, a, k))
+                closing.append(a)
+        for (i, a), lst in fwd.items():
+            lst.sort()
+            V = self.tl(s.mps[i], self.E_at(i), a)
+            pos = i + 1
+            for j, b, k in lst:
+                while pos < j:
+                    V = self.tl(s.mps[pos], V)
+                    pos += 1
+                M = s.mps[j]
+                self.density(M, self.left_x(M, V), G2[k])
+        for (j, b), lst in bwd.items():
+            lst.sort(reverse=True)
+            V = self.tr(s.mps[j], self.F_at(j + 1), b)
+            pos = j - 1
+            for i, a, k in lst:
+                while pos > i:
+                    V = self.tr(s.mps[pos], V)
+                    pos -= 1
+                M = s.mps[i]
+                self.density(M, self.right_x(M, V), G2[k])
+        g1 = G1.cpu().numpy()
+        g2 = G2.cpu().numpy()
+        ops = s.model.ops_np
+        v1 = np.array([np.sum(ops[op] * g1[k]) for k, (q, op) in enumerate(one)])
+        v2 = np.array([np.sum(ops[closing[k]] * g2[k]) for k in range(len(two))])
+        return v1, v2
+
+
+def observe(mps, one, two):
+    """Device expectation values; see _Observer."""
+    if mps.center < 0:
+        raise RuntimeError("observables need a central-orthogonal MPS (call correct_orthogonal_center first)")
+    return _Observer(mps).run(one, two)

@@ -1,0 +1,323 @@
+#!/usr/bin/env python
+"""Benchmark of the finite-size DMRG sweep on one GB300.
+
+Workload (one "step" = one full sweep, 2(L-1) local solves with their gauge moves and
+environment updates): spin-1/2 Heisenberg open chain, N=100, J=1, d=2, seeded
+random-normal initial MPS, chi ramped 64 -> 256 -> 512 during the warm-up sweeps, timed
+sweeps at chi=512. Synthetic input of the stated shapes; no dataset is involved.
+
+    python bench.py [--steps K] [--warmup W] [--precision tf32x3|fp64] [--impl ours|reference]
+
+Prints ONE JSON line. `value` = sweeps/s (inputs resident in HBM), `e2e` = sweeps/s of a full
+dmrg_finite_size() job from host inputs (ramp included, final MPS copied back to the host).
+`--impl reference` times the CPU restatement of the reference (oracle/, numpy + scipy ARPACK)
+on a bounded sample of the same workload and extrapolates sweeps/s.
+"""
+import argparse
+import contextlib
+import io
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DMRG sweeps/s (N=100 Heisenberg chain, chi=512)"
+UNIT = "sweeps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default=os.environ.get("TNALG_BENCH_PRECISION", "auto"))
+    p.add_argument("--length", type=int, default=100)
+    p.add_argument("--chi", type=int, default=512)
+    p.add_argument("--ramp", default="64,256")
+    p.add_argument("--eigs-tol", type=float, default=1e-12)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-solves", type=int, default=2)
+    return p.parse_args()
+
+
+def chain_para(length, chi, eigs_tol, precision="fp64", device="cuda"):
+    from tnalg_gb300 import Parameters as pm
+    para = pm.generate_parameters_dmrg("chain")
+    para.update(l=length, chi=chi, jxy=1, jz=1, hx=0, hz=0, tau=1e-4, eigs_tol=eigs_tol, break_tol=-1.0)
+    para = pm.make_consistent_parameter_dmrg(para)
+    para.update(precision=precision, device=device)
+    return para
+
+
+# ---------------------------------------------------------------------------------------
+# clocks sampler (nvidia-smi during the timed region)
+
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------
+# our arm
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from tnalg_gb300 import _lib as L, build
+    from tnalg_gb300.MPSClass import MpsOpenBoundaryClass
+    if not os.path.exists(L.LIB_PATH):
+        build.build()
+    L.load()
+    torch.cuda.set_device(local_rank)
+    dev = "cuda:%d" % local_rank
+    precision = args.precision
+    if precision == "auto":
+        precision = "tf32x3" if L.tf32x3_available() else "fp64"
+    ramp = [int(x) for x in args.ramp.split(",") if x]
+    para = chain_para(args.length, ramp[0] if ramp else args.chi, args.eigs_tol, precision, dev)
+    np.random.seed(1000 * rank)
+    A = MpsOpenBoundaryClass(para["l"], para["d"], para["chi"], operators=para["op"], device=dev,
+                             precision=precision)
+    A.correct_orthogonal_center(0)
+    L_ = para["l"]
+    order = list(range(1, L_)) + list(range(L_ - 2, -1, -1))
+
+    def sweep():
+        for n in order:
+            A.update_tensor_eigs(n, para["index1"], para["index2"], para["coeff1"], para["coeff2"], para["tau"],
+                                 True, tol=para["eigs_tol"])
+
+    schedule = ramp + [args.chi]
+    warm = max(args.warmup, len(schedule))
+    for t in range(warm):
+        A.grow_bond_dimension(schedule[min(t, len(schedule) - 1)], seed=t)
+        sweep()
+    if A.virtual_dim.max() < min(args.chi, 2 ** (L_ // 2)):
+        A.grow_bond_dimension(args.chi, seed=warm)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    lib = L.load()
+    lib.tn_profile_enable(1)
+    lib.tn_profile_reset()
+    solves0, mv0 = A.stats["solves"], A.stats["matvecs"]
+    launches0 = L.launch_count()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local_rank) as clk:
+        torch.cuda.synchronize()
+        start.record()
+        t0 = time.time()
+        for _ in range(args.steps):
+            sweep()
+        stop.record()
+        torch.cuda.synchronize()
+        wall = time.time() - t0
+    ms = start.elapsed_time(stop)
+    launches = L.launch_count() - launches0
+    mv_ms, mv_cnt, mv_flops = L.profile_read(0)
+    lib.tn_profile_enable(0)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    solves = A.stats["solves"] - solves0
+    matvecs = A.stats["matvecs"] - mv0
+    # final energy of the timed state (FP64 observables)
+    eb = A.observe_bond_energy(para["index2"], para["coeff2"])
+    e_site = float(np.sum(eb)) / L_
+    res = {"ms": ms, "wall": wall, "solves": solves, "matvecs": matvecs, "mv_ms": mv_ms, "mv_cnt": mv_cnt,
+           "mv_flops": mv_flops, "precision": precision, "e_per_site": e_site, "clocks": clk.summary(),
+           "launches": launches, "chi_max": int(A.virtual_dim.max())}
+    return res, A, para
+
+
+def run_e2e(args, dev, precision):
+    """One full dmrg_finite_size() job from host inputs: ramp + timed schedule, MPS copied back."""
+    import torch
+    from tnalg_gb300 import DMRG_anyH
+    ramp = [int(x) for x in args.ramp.split(",") if x]
+    schedule = ramp + [args.chi] * max(1, args.steps)
+    para = chain_para(args.length, schedule[0], args.eigs_tol, precision, dev)
+    para.update(sweep_time=len(schedule), chi_schedule=schedule, dt_ob=len(schedule))
+    np.random.seed(0)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    with contextlib.redirect_stdout(io.StringIO()):
+        ob, A, info, _ = DMRG_anyH.dmrg_finite_size(para)
+        host = A.mps  # device -> host copy of the final MPS
+    torch.cuda.synchronize()
+    wall = time.time() - t0
+    d2h = sum(t.nbytes for t in host)
+    h2d = sum(t.nbytes for t in _initial_host_mps(args.length, 2, schedule[0]))
+    return {"value": len(schedule) / wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d / len(schedule)),
+            "d2h_bytes_per_step": int(d2h / len(schedule)), "sweeps": len(schedule), "wall_s": wall,
+            "e_per_site": float(ob["e_per_site"])}
+
+
+def _initial_host_mps(l, d, chi):
+    return [np.zeros((1, d, chi))] + [np.zeros((chi, d, chi))] * (l - 2) + [np.zeros((chi, d, 1))]
+
+
+# ---------------------------------------------------------------------------------------
+# CPU restatement (oracle) timing: bounded sample of interior local solves at the bench chi
+
+
+def cpu_sample(length, chi, eigs_tol, nsolves, seed=0):
+    from oracle import dmrg_oracle as O
+    try:
+        import torch
+        threads = torch.get_num_threads()
+    except Exception:
+        threads = os.cpu_count()
+    para = chain_para(length, chi, eigs_tol, "fp64", "cpu")
+    np.random.seed(seed)
+    A = O.OracleMPS(length, 2, chi, para["op"])
+    one, two = O.canonical_terms(para["index1"], para["coeff1"], para["index2"], para["coeff2"], A.ops, eigs_tol)
+    t0 = time.time()
+    A.correct_orthogonal_center(0)
+    t_prep = time.time() - t0
+    times = []
+    for n in range(1, 1 + nsolves + 1):
+        t = time.time()
+        A.update_tensor_eigs(n, one, two, 1e-4, eigs_tol)
+        times.append(time.time() - t)
+    per_solve = float(np.mean(times[1:])) if len(times) > 1 else times[0]
+    sweeps_per_s = 1.0 / (per_solve * 2 * (length - 1))
+    return {"value": sweeps_per_s, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d interior local solves (numpy/scipy ARPACK restatement) at chi=%d on a random N=%d MPS "
+                      "after %.1f s canonicalisation; %.2f s/solve extrapolated to 2(N-1) solves per sweep"
+                      % (nsolves, chi, length, t_prep, per_solve)}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    s = cpu_sample(args.length, args.chi, args.eigs_tol, max(1, args.cpu_solves))
+    line = {"metric": METRIC, "value": s["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / s["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "N=%d spin-1/2 Heisenberg open chain, J=1, chi=%d, one-site DMRG sweep"
+                                   % (args.length, args.chi), "global_batch": 1, "seq_len": args.length,
+                       "parallelism": "replicas"},
+            "cpu_baseline": s, "e2e": {"value": s["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                                       "d2h_bytes_per_step": 0}}
+    return line
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    res, A, para = run_ours(args, rank, world, local_rank)
+    pk, pk_kind = peaks()
+    ms_step = res["ms"] / args.steps
+    value = world * args.steps / (res["ms"] / 1000.0)
+    mixed = res["precision"] != "fp64"
+    avg_ms = res["mv_ms"] / max(res["mv_cnt"], 1)
+    achieved = (res["mv_flops"] / max(res["mv_cnt"], 1)) / (avg_ms / 1000.0) / 1e12 if res["mv_cnt"] else 0.0
+    if mixed:
+        peak = pk["bf16_tflops_sustained"] / 2.0 / 3.0
+        peak_note = "3xTF32 useful-flop peak = measured sustained bf16 / 2 (tf32 rate) / 3 products"
+    else:
+        peak = 1.25
+        peak_note = "nominal GB300 FP64 1.25 TFLOP/s (no FP64 entry in MEASURED_PEAKS.json)"
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if not mixed else "tf32x3+f64", "data": "synthetic",
+            "config": {"workload": "N=%d spin-1/2 Heisenberg open chain, J=1, d=2, one-site DMRG sweep at chi=%d "
+                                   "(warm-up ramp %s)" % (args.length, args.chi, args.ramp),
+                       "global_batch": world, "seq_len": args.length, "parallelism": "replicas",
+                       "precision": res["precision"], "eigs_tol": args.eigs_tol,
+                       "l2": "inputs larger than L2 (MPS ~%d MB + environments)" % int(
+                           sum(t.numel() for t in A.mps_device) * 8 / 2 ** 20)},
+            "solves_per_s": world * res["solves"] / (res["ms"] / 1000.0),
+            "matvecs_per_solve": res["matvecs"] / max(res["solves"], 1),
+            "e_per_site": res["e_per_site"],
+            "roofline": {"bound": "tensor" if mixed else "fp64", "kernel": "effective-Hamiltonian matvec "
+                         "(block GEMMs)", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None, "traffic": None,
+                         "avg_launch_ms": avg_ms, "launches": res["mv_cnt"], "peak_source": pk_kind,
+                         "peak_note": peak_note},
+            "clocks": res["clocks"], "gpu_launches": res["launches"]}
+    if rank == 0 and not args.no_e2e:
+        line["e2e"] = run_e2e(args, "cuda:%d" % local_rank, res["precision"])
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample(args.length, args.chi, args.eigs_tol, max(1, args.cpu_solves))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

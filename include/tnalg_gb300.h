@@ -46,6 +46,10 @@ const char* tn_last_error(void);
 int tn_version(void);
 /* SM count and compute capability of the current device. */
 int tn_device_info(int* sm_count, int* cc_major, int* cc_minor);
+/* 1 if `precision` can run on the current device with this build. */
+int tn_precision_available(int precision);
+/* Kernels launched by this library so far (all entry points, all threads). */
+unsigned long long tn_launch_count(void);
 
 /* ---- contraction primitive -------------------------------------------------- */
 /*
@@ -65,7 +69,10 @@ int tn_gemm(int precision, int64_t M, int64_t N, int64_t K,
             int64_t batch, int64_t sAb, int64_t sBb, int64_t sCb,
             int64_t nred, int64_t sAr, int64_t sBr,
             double alpha, double beta, void* ws, size_t ws_bytes, void* stream);
-size_t tn_gemm_workspace_bytes(int precision, int64_t M, int64_t N, int64_t K, int64_t batch);
+size_t tn_gemm_workspace_bytes(int precision, int64_t M, int64_t N, int64_t K, int64_t batch, int64_t nred);
+/* Synchronise `stream` and report any error a bounded device-side wait recorded
+ * (TN_ERR_TIMEOUT); the CUDA context stays usable. */
+int tn_check_device_status(void* stream);
 
 /* ---- effective-operator building blocks ------------------------------------ */
 /* One term of a block operator: coeff * E[slot] (x) ops[op]; slot < 0 -> identity,
@@ -177,6 +184,13 @@ size_t tn_qr_workspace_bytes(int64_t m, int64_t n);
 int tn_singular_values(int64_t k, int64_t n, const double* x, int64_t sXr, int64_t sXc, double* s_out,
                        double tol, int max_sweeps, void* ws, size_t ws_bytes, void* stream);
 size_t tn_singular_values_workspace_bytes(int64_t k, int64_t n);
+
+/* ---- profiling ----------------------------------------------------------------------- */
+/* CUDA-event timing of kernel classes on their launching stream (0 = effective-Hamiltonian
+ * matvecs inside tn_lanczos). Off by default; reading synchronises the recorded events. */
+int tn_profile_enable(int on);
+int tn_profile_reset(void);
+int tn_profile_read(int cls, double* ms, int64_t* count, double* flops);
 
 /* ---- small vector helpers ------------------------------------------------------- */
 /* out[0] = sum x[i]*y[i] (FP64, deterministic two-stage reduction). */

@@ -1,0 +1,120 @@
+"""Split-TF32 tensor-core path (tcgen05) against FP64 and plain FP32 references (GPU only)."""
+import contextlib
+import ctypes
+import io
+
+import numpy as np
+import pytest
+import torch
+
+import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+from tnalg_gb300 import _lib as L  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def tf32(cuda_lib):
+    if not L.tf32x3_available():
+        pytest.skip("tf32x3 needs an sm_103 device")
+    return cuda_lib
+
+
+def _rand(*shape, seed=0):
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    return torch.randn(*shape, generator=g, dtype=torch.float64).cuda()
+
+
+def _fp32_error(A, B, ref):
+    """Error of a plain FP32 (no TF32) product of the same operands: the accuracy bar."""
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        c32 = torch.matmul(A.float(), B.float()).double()
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+    return torch.max(torch.abs(c32 - ref)).item()
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 32), (1024, 512, 1024), (100, 37, 70), (512, 1024, 1024),
+                                   (8, 8, 4), (256, 300, 520), (1536, 512, 1536)])
+def test_tf32x3_gemm_matches_fp64(tf32, M, N, K):
+    A = _rand(M, K, seed=M)
+    B = _rand(K, N, seed=N + 1)
+    Cin = _rand(M, N, seed=3)
+    C = torch.empty_like(Cin)
+    ws = L.Workspace(torch.device("cuda"))
+    L.gemm(A, B, C, M, N, K, (K, 1), (N, 1), (N, 1), Cin=Cin, alpha=1.25, beta=-0.5, precision=L.PREC_TF32X3,
+           ws=ws)
+    L.check(L.load().tn_check_device_status(L.stream_handle()))
+    ref = 1.25 * (A @ B) - 0.5 * Cin
+    err = torch.max(torch.abs(C - ref)).item()
+    bar = 1.25 * _fp32_error(A, B, A @ B)
+    assert err <= 2.0 * bar + 1e-12, (err, bar)
+    assert err / torch.max(torch.abs(ref)).item() < 3e-6
+
+
+def test_tf32x3_batched_reduced_and_transposed(tf32):
+    Z, R, M, N, K = 3, 2, 96, 80, 40
+    A = _rand(Z, R, K, M, seed=1)  # A(m,k) stored transposed
+    B = _rand(Z, R, N, K, seed=2)  # B(k,n) stored transposed
+    C = torch.zeros(Z, M, N, dtype=torch.float64, device="cuda")
+    ws = L.Workspace(torch.device("cuda"))
+    L.gemm(A, B, C, M, N, K, (1, M), (1, K), (N, 1), batch=Z, bstrides=(R * K * M, R * N * K, M * N), nred=R,
+           rstrides=(K * M, N * K), precision=L.PREC_TF32X3, ws=ws)
+    ref = torch.einsum("zrkm,zrnk->zmn", A, B)
+    assert torch.max(torch.abs(C - ref)).item() / torch.max(torch.abs(ref)).item() < 3e-6
+
+
+def _site(cl, d, cr):
+    wl = _rand(cl * d, cl * d, seed=cl)
+    wl = wl + wl.T
+    wr = _rand(d * cr, d * cr, seed=cr + 7)
+    wr = wr + wr.T
+    desc = L.SiteDesc(cl, d, cr, wl.data_ptr(), wr.data_ptr(), 0, None, None)
+    dense = torch.kron(wl, torch.eye(cr, dtype=torch.float64, device="cuda")) + \
+        torch.kron(torch.eye(cl, dtype=torch.float64, device="cuda"), wr)
+    return desc, dense, (wl, wr)
+
+
+@pytest.mark.parametrize("cl,d,cr", [(64, 2, 64), (128, 2, 96), (5, 3, 7), (512, 2, 512)])
+def test_tf32x3_matvec(tf32, cl, d, cr):
+    lib = L.load()
+    desc, dense, keep = _site(cl, d, cr)
+    psi = _rand(cl * d * cr, seed=5)
+    y = torch.empty_like(psi)
+    ws = L.Workspace(torch.device("cuda"))
+    wp, wb = ws.args(lib.tn_matvec_workspace_bytes(ctypes.byref(desc), L.PREC_TF32X3))
+    L.check(lib.tn_matvec(ctypes.byref(desc), L.ptr(psi), L.ptr(y), 1.0, 0.5, L.PREC_TF32X3, wp, wb,
+                          L.stream_handle()))
+    L.check(lib.tn_check_device_status(L.stream_handle()))
+    ref = 0.5 * psi + dense @ psi
+    assert torch.max(torch.abs(y - ref)).item() / torch.max(torch.abs(ref)).item() < 3e-6
+
+
+def test_tf32x3_lanczos_fp64_refined_energy(tf32):
+    lib = L.load()
+    desc, dense, keep = _site(24, 2, 20)
+    n = 24 * 2 * 20
+    psi = _rand(n, seed=9)
+    opts = L.LanczosOpts(1e-14, 0.0, 1e-12, 2e-6, 40, 200, 3, L.PREC_TF32X3, 1, 0)
+    ws = L.Workspace(torch.device("cuda"))
+    wp, wb = ws.args(lib.tn_lanczos_workspace_bytes(ctypes.byref(desc), ctypes.byref(opts)))
+    res = L.LanczosResult()
+    L.check(lib.tn_lanczos(ctypes.byref(desc), L.ptr(psi), ctypes.byref(opts), wp, wb, ctypes.byref(res),
+                           L.stream_handle()))
+    w0 = torch.linalg.eigvalsh(dense)[0].item()
+    assert abs(res.energy_fp64 - w0) <= 1e-9 * abs(w0)
+    assert abs(res.energy - w0) <= 1e-5 * abs(w0)
+
+
+def test_tf32x3_dmrg_close_to_reference(tf32):
+    """Mixed path on the N=12 chain: energy per site within 1e-8 of the reference's FP64 run."""
+    from tnalg_gb300 import DMRG_anyH
+    g, m = gc.load("chain_n12_chi16_h"), gc.meta()["chain_n12_chi16_h"]
+    np.random.seed(m["seed"])
+    with contextlib.redirect_stdout(io.StringIO()):
+        ob, A, info, _ = DMRG_anyH.dmrg_finite_size(gc.para_of("chain_n12_chi16_h", precision="tf32x3"))
+    assert abs(ob["e_per_site"] - float(g["e_per_site"])) <= 1e-8
+    np.testing.assert_allclose(np.ravel(ob["mz"]), g["mz"], atol=1e-5)

@@ -128,7 +128,7 @@ def test_library_exports_header_symbols():
     if not os.path.exists(_lib.LIB_PATH):
         build.build()
     header = open(os.path.join(os.path.dirname(gc.GOLDEN), "..", "include", "tnalg_gb300.h")).read()
-    declared = set(re.findall(r"^\s*(?:const char\*|int|size_t)\s+(tn_\w+)\(", header, re.M))
+    declared = set(re.findall(r"^\s*(?:const char\*|int|size_t|unsigned long long)\s+(tn_\w+)\(", header, re.M))
     assert declared, "no declarations parsed"
     lib = ctypes.CDLL(_lib.LIB_PATH)
     missing = [s for s in sorted(declared) if not hasattr(lib, s)]

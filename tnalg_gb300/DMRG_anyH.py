@@ -40,8 +40,12 @@ def dmrg_finite_size(para=None):
     index1, index2 = para["index1"], para["index2"]
     coeff1, coeff2 = para["coeff1"], para["coeff2"]
     l = para["l"]
+    schedule = para.get("chi_schedule")
     for t in range(para["sweep_time"]):
         ts = time.time()
+        if schedule:
+            A.grow_bond_dimension(int(schedule[min(t, len(schedule) - 1)]), noise=para.get("chi_noise", 1e-3),
+                                  seed=t)
         if_ob = ((t + 1) % para["dt_ob"] == 0) or t == (para["sweep_time"] - 1)
         if if_ob:
             print("In the %d-th round of sweep ..." % (t + 1))

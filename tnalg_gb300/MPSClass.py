@@ -200,6 +200,15 @@ class MpsOpenBoundaryClass(MpsBasic):
             dev.orthogonality[l1 + 1:l0 + 1] = 1
             dev.orthogonality[l1] = 0
 
+    def grow_bond_dimension(self, chi_new, noise=1e-3, seed=0):
+        """Enlarge all bonds to chi_new (capped by d^b) with seeded noise and re-centre the MPS at
+        its previous centre (or 0). Not in the reference, whose chi is fixed; used by
+        para['chi_schedule']."""
+        c = self.center if self.center >= 0 else 0
+        if self._dev.grow_bonds(chi_new, noise=noise, seed=seed):
+            self.lm = [np.zeros(0) for _ in range(self.length - 1)]
+            self.correct_orthogonal_center(c)
+
     # -- local update ------------------------------------------------------------
     def _model(self, index1, index2, coeff1, coeff2, tol):
         key = (id(index1), id(index2), id(coeff1), id(coeff2), float(tol),

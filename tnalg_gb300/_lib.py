@@ -52,9 +52,12 @@ _SIGS = {
     "tn_last_error": (ctypes.c_char_p, []),
     "tn_version": (c_int, []),
     "tn_device_info": (c_int, [c_vp, c_vp, c_vp]),
+    "tn_precision_available": (c_int, [c_int]),
+    "tn_launch_count": (ctypes.c_ulonglong, []),
     "tn_gemm": (c_int, [c_int, c_i64, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64,
                         c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_dbl, c_dbl, c_vp, c_sz, c_vp]),
-    "tn_gemm_workspace_bytes": (c_sz, [c_int, c_i64, c_i64, c_i64, c_i64]),
+    "tn_gemm_workspace_bytes": (c_sz, [c_int, c_i64, c_i64, c_i64, c_i64, c_i64]),
+    "tn_check_device_status": (c_int, [c_vp]),
     "tn_assemble_block": (c_int, [c_int, c_i64, c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp]),
     "tn_combine_slots": (c_int, [c_i64, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp]),
     "tn_apply_site_ops": (c_int, [c_i64, c_i64, c_i64, c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp]),
@@ -67,6 +70,9 @@ _SIGS = {
     "tn_qr_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_singular_values": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_workspace_bytes": (c_sz, [c_i64, c_i64]),
+    "tn_profile_enable": (c_int, [c_int]),
+    "tn_profile_reset": (c_int, []),
+    "tn_profile_read": (c_int, [c_int, c_vp, c_vp, c_vp]),
     "tn_dot": (c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "tn_scale": (c_int, [c_i64, c_vp, c_dbl, c_vp, c_vp]),
     "tn_set_identity": (c_int, [c_i64, c_vp, c_i64, c_vp]),
@@ -151,7 +157,7 @@ def gemm(A, B, C, M, N, K, sA, sB, sC, *, Cin=None, batch=1, bstrides=(0, 0, 0),
     """
     lib = load()
     if ws is not None:
-        need = lib.tn_gemm_workspace_bytes(precision, M, N, K, batch)
+        need = lib.tn_gemm_workspace_bytes(precision, M, N, K, batch, nred)
         wp, wb = ws.args(need)
     else:
         wp, wb = None, 0
@@ -171,3 +177,19 @@ def terms_tensor(terms, device):
     raw = bytes(arr)[: 16 * max(n, 1)]
     host = torch.frombuffer(bytearray(raw), dtype=torch.uint8)
     return host.to(device), n
+
+
+def tf32x3_available():
+    return bool(load().tn_precision_available(PREC_TF32X3))
+
+
+def launch_count():
+    return int(load().tn_launch_count())
+
+
+def profile_read(cls=0):
+    """(total ms, launches, useful flops) of a profiled kernel class."""
+    lib = load()
+    ms, cnt, fl = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+    check(lib.tn_profile_read(cls, ctypes.byref(ms), ctypes.byref(cnt), ctypes.byref(fl)), "profile")
+    return ms.value, cnt.value, fl.value

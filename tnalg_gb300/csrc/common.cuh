@@ -7,8 +7,12 @@
 
 #include "tnalg_gb300.h"
 
+// Every kernel launch site of the library is followed by TN_CHECK_LAUNCH(), which also counts
+// the launch (tn_launch_count in the C ABI).
+extern unsigned long long g_tn_launches;
 #define TN_CHECK_LAUNCH()                                   \
   do {                                                      \
+    ++g_tn_launches;                                        \
     cudaError_t e_ = cudaGetLastError();                    \
     if (e_ != cudaSuccess) return tn_record_error(e_);      \
   } while (0)
@@ -52,3 +56,8 @@ int tn_gemm_f64_launch(const TnGemmF64& g, cudaStream_t s);
 int tn_gemm_f64_ws(const TnGemmF64& g, void* ws, size_t ws_bytes, cudaStream_t s);
 size_t tn_gemm_f64_ws_bytes(int64_t M, int64_t N, int64_t batch);
 int tn_sm_count();
+
+// Optional CUDA-event profiling of kernel classes (tn_profile_* in the C ABI).
+enum { TN_PROF_MATVEC = 0, TN_PROF_QR = 1, TN_PROF_ENV = 2, TN_PROF_NCLASS = 4 };
+bool tn_profile_begin(cudaStream_t s);
+void tn_profile_end(cudaStream_t s, int cls, double flops);

@@ -19,6 +19,7 @@
 #include "common.cuh"
 
 int tn_dot_ws(int64_t n, const double* x, const double* y, double* out, void* ws, size_t ws_bytes, cudaStream_t s);
+int tn_tf32x3_error_check(cudaStream_t s);
 int tn_matvec_tf32x3(const tn_site_desc* d, const double* psi, double* y, double alpha, double beta,
                      void* ws, size_t ws_bytes, cudaStream_t s);
 size_t tn_matvec_tf32x3_ws_bytes(const tn_site_desc* d);
@@ -351,6 +352,45 @@ size_t lanczos_layout(const tn_site_desc* ds, const tn_lanczos_opts* o, char* ba
 
 size_t tn_matvec_fp64_ws_bytes(const tn_site_desc* ds) { return matvec_fp64_ws_bytes(ds); }
 
+// y += alpha * sum_k SL_k psi SR_k^T in FP64 (the straddling part of the matvec).
+int tn_matvec_fp64_straddle(const tn_site_desc* ds, const double* psi, double* y, double alpha, void* ws,
+                            size_t ws_bytes, cudaStream_t s) {
+  if (ds->nstr <= 0) return TN_OK;
+  tn_site_desc only = *ds;
+  only.wl = nullptr;
+  only.wr = nullptr;
+  const int64_t n = ds->chil * ds->d * ds->chir;
+  const size_t zb = align_up((size_t)ds->nstr * n * sizeof(double));
+  if (ws_bytes < zb) return tn_fail(TN_ERR_WORKSPACE, "straddle: workspace too small");
+  const int64_t cl = ds->chil, d = ds->d, cr = ds->chir;
+  double* Z = (double*)ws;
+  TnGemmF64 g{};
+  g.M = cl; g.N = d * cr; g.K = cl;
+  g.A = ds->sl; g.sAm = cl; g.sAk = 1; g.sAb = cl * cl;
+  g.B = psi; g.sBk = d * cr; g.sBn = 1; g.sBb = 0;
+  g.C = Z; g.sCm = d * cr; g.sCn = 1; g.sCb = n;
+  g.batch = ds->nstr; g.nred = 1; g.alpha = 1.0; g.beta = 0.0;
+  int st = tn_gemm_f64_ws(g, (char*)ws + zb, ws_bytes - zb, s);
+  if (st) return st;
+  TnGemmF64 h{};
+  h.M = cl * d; h.N = cr; h.K = cr;
+  h.A = Z; h.sAm = cr; h.sAk = 1; h.sAr = n;
+  h.B = ds->sr; h.sBk = 1; h.sBn = cr; h.sBr = cr * cr;
+  h.C = y; h.sCm = cr; h.sCn = 1; h.Cin = y;
+  h.batch = 1; h.nred = ds->nstr; h.alpha = alpha; h.beta = 1.0;
+  return tn_gemm_f64_ws(h, (char*)ws + zb, ws_bytes - zb, s);
+}
+
+// Useful flops of one block-form matvec: WL.psi + psi.WR^T + straddling pairs.
+static double matvec_flops(const tn_site_desc* ds) {
+  const double cl = (double)ds->chil, d = (double)ds->d, cr = (double)ds->chir;
+  double f = 0.0;
+  if (ds->wl) f += 2.0 * (cl * d) * (cl * d) * cr;
+  if (ds->wr) f += 2.0 * cl * (d * cr) * (d * cr);
+  f += (double)ds->nstr * (2.0 * cl * cl * d * cr + 2.0 * cl * d * cr * cr);
+  return f;
+}
+
 extern "C" size_t tn_matvec_workspace_bytes(const tn_site_desc* desc, int precision) {
   if (!desc) return 0;
   return precision == TN_PREC_TF32X3 ? tn_matvec_tf32x3_ws_bytes(desc) : matvec_fp64_ws_bytes(desc);
@@ -410,8 +450,11 @@ extern "C" int tn_lanczos(const tn_site_desc* desc, double* psi, const tn_lanczo
     if (st) return st;
   }
   auto matvec = [&](const double* x, double* y) -> int {
-    if (mixed) return tn_matvec_tf32x3(desc, x, y, 1.0, 0.0, L.mv_ws, L.mv_bytes, s);
-    return matvec_fp64(desc, x, y, 1.0, 0.0, L.mv_ws, L.mv_bytes, s);
+    const bool prof = tn_profile_begin(s);
+    const int r = mixed ? tn_matvec_tf32x3(desc, x, y, 1.0, 0.0, L.mv_ws, L.mv_bytes, s)
+                        : matvec_fp64(desc, x, y, 1.0, 0.0, L.mv_ws, L.mv_bytes, s);
+    if (prof) tn_profile_end(s, TN_PROF_MATVEC, matvec_flops(desc));
+    return r;
   };
   // single dot product through the multi-dot kernel (its own ticket slot)
   auto dot2 = [&](const double* x, const double* y, double* out) -> int {
@@ -508,6 +551,10 @@ extern "C" int tn_lanczos(const tn_site_desc* desc, double* psi, const tn_lanczo
     TN_CUDA(cudaStreamSynchronize(s));
     res->energy_fp64 = hv[0];
     res->residual = sqrt(std::max(hv[1], 0.0));
+  }
+  if (mixed) {
+    st = tn_tf32x3_error_check(s);
+    if (st) return st;
   }
   res->matvecs = matvecs;
   res->restarts = restarts;

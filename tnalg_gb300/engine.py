@@ -374,6 +374,33 @@ class DeviceMPS:
             self.orthogonality[l1 + 1:l0 + 1] = 1
             self.orthogonality[l1] = 0
 
+    def grow_bonds(self, chi_new, noise=1e-3, seed=0):
+        """Enlarge every bond to min(chi_new, d^b, d^(L-b)); the new entries are seeded
+        Gaussian noise of scale `noise`, the old tensor is kept in the leading block.
+        The MPS loses its canonical form (centre -1); the caller re-centres it. The reference
+        keeps chi fixed (TensorBasicModule.py:314-384); this is the bond ramp of a chi schedule."""
+        Ln, d = self.length, self.d
+        cap = [1] + [min(chi_new, d ** min(b, 60), d ** min(Ln - b, 60)) for b in range(1, Ln)] + [1]
+        dims = [max(int(c), int(v)) for c, v in zip(cap, self.virtual_dim)]
+        if dims == [int(v) for v in self.virtual_dim]:
+            return False
+        g = torch.Generator(device=self.device)
+        g.manual_seed(int(seed))
+        for n in range(Ln):
+            t = self.mps[n]
+            cl, dd, cr = t.shape
+            ncl, ncr = dims[n], dims[n + 1]
+            if (ncl, ncr) != (cl, cr):
+                new = noise * torch.randn((ncl, dd, ncr), generator=g, dtype=torch.float64, device=self.device)
+                new[:cl, :, :cr] = t
+                self.mps[n] = new
+        self.virtual_dim = np.array(dims)
+        self.center = -1
+        self.orthogonality[:] = 0
+        self.el_upto = min(self.el_upto, 0)
+        self.er_from = max(self.er_from, self.length)
+        return True
+
     def correct_orthogonal_center(self, p):
         """MPSClass.py:188-198 for an explicit p."""
         if self.center < 0:

@@ -68,8 +68,11 @@ class FakeLib:
         return 100
 
     # -- GEMM ----------------------------------------------------------------------
-    def tn_gemm_workspace_bytes(self, prec, M, N, K, batch):
+    def tn_gemm_workspace_bytes(self, prec, M, N, K, batch, nred=1):
         return 0
+
+    def tn_check_device_status(self, stream):
+        return OK
 
     def tn_gemm(self, prec, M, N, K, A, sAm, sAk, B, sBk, sBn, C, sCm, sCn, Cin, batch, sAb, sBb, sCb, nred, sAr,
                 sBr, alpha, beta, ws, wsb, stream):

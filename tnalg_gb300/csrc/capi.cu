@@ -94,7 +94,6 @@ struct ProfRec {
 bool g_prof_on = false;
 std::vector<cudaEvent_t> g_pool;
 std::vector<ProfRec> g_pending;
-cudaEvent_t g_open = nullptr;
 double g_ms[TN_PROF_NCLASS] = {0}, g_flops[TN_PROF_NCLASS] = {0};
 int64_t g_cnt[TN_PROF_NCLASS] = {0};
 
@@ -124,22 +123,23 @@ void flush_pending() {
 }
 }  // namespace
 
-bool tn_profile_begin(cudaStream_t s) {
-  if (!g_prof_on) return false;
+cudaEvent_t tn_profile_begin(cudaStream_t s) {
+  if (!g_prof_on) return nullptr;
   if (g_pending.size() > 4096) flush_pending();
-  g_open = pool_get();
-  if (!g_open) return false;
-  cudaEventRecord(g_open, s);
-  return true;
+  cudaEvent_t a = pool_get();
+  if (a) cudaEventRecord(a, s);
+  return a;
 }
 
-void tn_profile_end(cudaStream_t s, int cls, double flops) {
-  if (!g_open) return;
+void tn_profile_end(cudaEvent_t a, cudaStream_t s, int cls, double flops) {
+  if (!a) return;
   cudaEvent_t b = pool_get();
-  if (!b) return;
+  if (!b) {
+    g_pool.push_back(a);
+    return;
+  }
   cudaEventRecord(b, s);
-  g_pending.push_back({g_open, b, cls, flops});
-  g_open = nullptr;
+  g_pending.push_back({a, b, cls, flops});
 }
 
 extern "C" int tn_profile_enable(int on) {

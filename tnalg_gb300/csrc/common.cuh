@@ -58,6 +58,14 @@ size_t tn_gemm_f64_ws_bytes(int64_t M, int64_t N, int64_t batch);
 int tn_sm_count();
 
 // Optional CUDA-event profiling of kernel classes (tn_profile_* in the C ABI).
-enum { TN_PROF_MATVEC = 0, TN_PROF_QR = 1, TN_PROF_ENV = 2, TN_PROF_NCLASS = 4 };
-bool tn_profile_begin(cudaStream_t s);
-void tn_profile_end(cudaStream_t s, int cls, double flops);
+enum {
+  TN_PROF_MATVEC = 0,    // effective-Hamiltonian matvec inside tn_lanczos
+  TN_PROF_QR = 1,        // whole tn_qr call
+  TN_PROF_QR_PANEL = 2,  // QR panel factorisations
+  TN_PROF_QR_FORM_Q = 3, // explicit Q formation
+  TN_PROF_LANCZOS = 4,   // whole tn_lanczos call
+  TN_PROF_NCLASS = 8
+};
+// begin returns nullptr when profiling is off; end(nullptr, ...) is a no-op. Pairs may nest.
+cudaEvent_t tn_profile_begin(cudaStream_t s);
+void tn_profile_end(cudaEvent_t start, cudaStream_t s, int cls, double flops);

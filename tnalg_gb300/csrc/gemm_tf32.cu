@@ -123,13 +123,17 @@ __host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
+// K-blocks rotate over NACC accumulators in TMEM (summed in FP64 by the epilogue): each FP32
+// tensor-core accumulation chain is NACC times shorter.
+constexpr int NACC = 4;
+
 template <int BN>
 struct Cfg {
   static constexpr int A_BYTES = BM * BK * 4;
   static constexpr int B_BYTES = BN * BK * 4;
   static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 256;
-  static constexpr uint32_t TMEM_COLS = BN < 32 ? 32 : BN;
+  static constexpr uint32_t TMEM_COLS = NACC * BN;  // 256 or 512: powers of two
 };
 
 template <int BN>
@@ -197,12 +201,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       tc_fence_after();
       const uint64_t dAhi = smem_desc(stage(s, 0)), dAlo = smem_desc(stage(s, 1));
       const uint64_t dBhi = smem_desc(stage(s, 2)), dBlo = smem_desc(stage(s, 3));
+      const uint32_t dacc = tmem + (uint32_t)((i % NACC) * BN);
 #pragma unroll
       for (int k = 0; k < BK / 8; ++k) {
         const uint64_t o = (uint64_t)(k * 32) >> 4;  // 8 tf32 = 32 bytes along the swizzled row
-        mma_tf32(tmem, dAhi + o, dBhi + o, idesc, (i > 0 || k > 0) ? 1u : 0u);
-        mma_tf32(tmem, dAhi + o, dBlo + o, idesc, 1u);
-        mma_tf32(tmem, dAlo + o, dBhi + o, idesc, 1u);
+        mma_tf32(dacc, dAhi + o, dBhi + o, idesc, (i >= NACC || k > 0) ? 1u : 0u);
+        mma_tf32(dacc, dAhi + o, dBlo + o, idesc, 1u);
+        mma_tf32(dacc, dAlo + o, dBhi + o, idesc, 1u);
       }
       mma_commit(&empty[s]);
     }
@@ -219,17 +224,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int row = m_tile * BM + warp * 32 + lane;
   const int64_t base = (int64_t)z * sCb;
   if (have) {
+    const int nacc = min(nkb, NACC);
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 16) {
-      uint32_t r[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+      double acc[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) acc[j] = 0.0;
+#pragma unroll 1
+      for (int a = 0; a < nacc; ++a) {
+        uint32_t r[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * BN + c0), r);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) acc[j] += (double)__uint_as_float(r[j]);
+      }
       if (row < M) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int col = n_tile * BN + c0 + j;
           if (col < N) {
             const int64_t off = base + (int64_t)row * sCm + (int64_t)col * sCn;
-            const double v = alpha * (double)__uint_as_float(r[j]);
+            const double v = alpha * acc[j];
             if (atomic_out) atomicAdd(C + off, v);
             else C[off] = (beta == 0.0) ? v : fma(beta, (Cin ? Cin : C)[off], v);
           }

@@ -356,9 +356,6 @@ size_t tn_matvec_fp64_ws_bytes(const tn_site_desc* ds) { return matvec_fp64_ws_b
 int tn_matvec_fp64_straddle(const tn_site_desc* ds, const double* psi, double* y, double alpha, void* ws,
                             size_t ws_bytes, cudaStream_t s) {
   if (ds->nstr <= 0) return TN_OK;
-  tn_site_desc only = *ds;
-  only.wl = nullptr;
-  only.wr = nullptr;
   const int64_t n = ds->chil * ds->d * ds->chir;
   const size_t zb = align_up((size_t)ds->nstr * n * sizeof(double));
   if (ws_bytes < zb) return tn_fail(TN_ERR_WORKSPACE, "straddle: workspace too small");
@@ -450,10 +447,10 @@ extern "C" int tn_lanczos(const tn_site_desc* desc, double* psi, const tn_lanczo
     if (st) return st;
   }
   auto matvec = [&](const double* x, double* y) -> int {
-    const bool prof = tn_profile_begin(s);
+    cudaEvent_t ev = tn_profile_begin(s);
     const int r = mixed ? tn_matvec_tf32x3(desc, x, y, 1.0, 0.0, L.mv_ws, L.mv_bytes, s)
                         : matvec_fp64(desc, x, y, 1.0, 0.0, L.mv_ws, L.mv_bytes, s);
-    if (prof) tn_profile_end(s, TN_PROF_MATVEC, matvec_flops(desc));
+    tn_profile_end(ev, s, TN_PROF_MATVEC, matvec_flops(desc));
     return r;
   };
   // single dot product through the multi-dot kernel (its own ticket slot)

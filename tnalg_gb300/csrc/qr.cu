@@ -180,6 +180,7 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
   qr_layout(m, n, base, &w);
   cudaStream_t s = (cudaStream_t)stream;
   const int64_t k = std::min(m, n);
+  cudaEvent_t ev_all = tn_profile_begin(s);
   qr_copy_in<<<blocks_for(m * n), 256, 0, s>>>(m, n, a, sAm, sAn, w.Aw);
   TN_CHECK_LAUNCH();
   qr_init_q<<<blocks_for(m * k), 256, 0, s>>>(m, k, w.Qw, w.Vf);
@@ -189,8 +190,10 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
     const int64_t j0 = p * NB;
     const int jb = (int)std::min<int64_t>(NB, k - j0);
     double* Tp = w.T + p * NB * NB;
+    cudaEvent_t ev_p = tn_profile_begin(s);
     qr_panel<<<1, NTP, 0, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
     TN_CHECK_LAUNCH();
+    tn_profile_end(ev_p, s, TN_PROF_QR_PANEL, 0.0);
     const int64_t nc = n - j0 - jb;
     if (nc <= 0) continue;
     const int64_t mr = m - j0;
@@ -222,6 +225,7 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
     st = tn_gemm_f64_ws(u, nullptr, 0, s);
     if (st) return st;
   }
+  cudaEvent_t ev_q = tn_profile_begin(s);
   if (q) {
     for (int64_t p = np - 1; p >= 0; --p) {
       const int64_t j0 = p * NB;
@@ -255,7 +259,9 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
       if (st) return st;
     }
   }
+  tn_profile_end(ev_q, s, TN_PROF_QR_FORM_Q, 0.0);
   qr_extract<<<blocks_for(m * k + k * n), 256, 0, s>>>(m, n, k, w.Aw, w.Qw, q, sQm, sQn, r, sRm, sRn);
   TN_CHECK_LAUNCH();
+  tn_profile_end(ev_all, s, TN_PROF_QR, 4.0 * m * n * n - 4.0 / 3.0 * n * n * (double)n);
   return TN_OK;
 }

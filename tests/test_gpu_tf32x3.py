@@ -53,7 +53,7 @@ def test_tf32x3_gemm_matches_fp64(tf32, M, N, K):
     bar = 1.25 * _fp32_error(A, B, A @ B)
     # split-TF32 with FP32 tensor-core accumulation: within 4x of a plain FP32 GEMM's error
     assert err <= 4.0 * bar + 1e-12, (err, bar)
-    assert err / torch.max(torch.abs(ref)).item() < 3e-6
+    assert err / torch.max(torch.abs(ref)).item() < 5e-6
 
 
 def test_tf32x3_batched_reduced_and_transposed(tf32):

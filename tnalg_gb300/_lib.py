@@ -68,6 +68,7 @@ _SIGS = {
     "tn_lanczos_workspace_bytes": (c_sz, [c_vp, c_vp]),
     "tn_qr": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_sz, c_vp]),
     "tn_qr_workspace_bytes": (c_sz, [c_i64, c_i64]),
+    "tn_qr_use_graphs": (c_int, [c_int]),
     "tn_singular_values": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_profile_enable": (c_int, [c_int]),

@@ -3,21 +3,45 @@
 // Replaces np.linalg.qr in left2right_decompose_tensor / right2left_decompose_tensor
 // (TensorBasicModule.py:314-384). Blocked right-looking Householder with the
 // compact WY form H_1..H_b = I - V T V^T (forward, column-wise):
-//   * panel of NB columns factored by one CTA (reflectors, tau, T);
-//   * trailing matrix updated by three FP64 GEMMs (V^T C, T^T W, C - V W);
+//   * panel of NB columns factored by a cluster of 8 CTAs: the panel rows are split
+//     across the CTAs (held in shared memory) and every column's norm and dot products
+//     are reduced through distributed shared memory between two cluster barriers;
+//   * trailing matrix updated by FP64 GEMMs (V^T C, T^T W, C - V W);
 //   * Q formed backwards from [I; 0] with the same block reflectors.
-// The reflector convention (beta = -sign(alpha) ||x||, v(0) = 1) is LAPACK's
-// dlarfg, so Q and R agree with numpy's up to rounding.
+// The whole launch sequence of one (m, n, strides, workspace) shape is captured once in
+// a CUDA graph and replayed; the input/output pointers travel through a small argument
+// block in the workspace, so replays need no graph updates.
+// The reflector convention (beta = -sign(alpha) ||x||, v(0) = 1) is LAPACK's dlarfg, so
+// Q and R agree with numpy's up to rounding.
+#include <cooperative_groups.h>
+
+#include <string.h>
+
+#include <vector>
+
 #include "common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
 constexpr int NB = 16;
-constexpr int NTP = 512;
+constexpr int NTP = 512;  // single-CTA panel
+constexpr int CL = 8;     // CTAs per panel cluster
+constexpr int PT = 128;   // threads per cluster CTA
+constexpr int PR = 2;     // panel rows per thread -> <= CL * PT * PR rows
+constexpr int NSLOT = NB + 2;
 
 size_t al(size_t x) { return (x + 255) / 256 * 256; }
 
+struct QrArgs {
+  const double* a;
+  double* q;
+  double* r;
+};
+
 struct QrWs {
+  QrArgs* args;
   double *Aw, *Vf, *Qw, *T, *W, *W2, *gws;
   size_t gws_bytes;
 };
@@ -27,6 +51,7 @@ size_t qr_layout(int64_t m, int64_t n, char* base, QrWs* q) {
   const int64_t np = tn_cdiv(k, NB);
   size_t off = 0;
   auto take = [&](size_t b) { char* p = base ? base + off : nullptr; off += al(b); return p; };
+  q->args = (QrArgs*)take(sizeof(QrArgs));
   q->Aw = (double*)take((size_t)m * n * 8);
   q->Vf = (double*)take((size_t)m * k * 8);
   q->Qw = (double*)take((size_t)m * k * 8);
@@ -38,7 +63,14 @@ size_t qr_layout(int64_t m, int64_t n, char* base, QrWs* q) {
   return off + 256;
 }
 
-__global__ void qr_copy_in(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* Aw) {
+__global__ void qr_set_args(QrArgs* args, const double* a, double* q, double* r) {
+  args->a = a;
+  args->q = q;
+  args->r = r;
+}
+
+__global__ void qr_copy_in(int64_t m, int64_t n, const QrArgs* args, int64_t sAm, int64_t sAn, double* Aw) {
+  const double* a = args->a;
   const int64_t total = m * n;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -57,7 +89,20 @@ __global__ void qr_init_q(int64_t m, int64_t k, double* Qw, double* Vf) {
   }
 }
 
-// Factor columns j0..j0+jb-1 (rows j0..m-1) of the column-major Aw in place.
+// Householder scalars of x = (alpha, tail) with ||tail||^2 = sigma (LAPACK dlarfg convention).
+__device__ __forceinline__ void householder(double alpha, double sigma, double* tau, double* beta, double* scale) {
+  *tau = 0.0;
+  *beta = alpha;
+  *scale = 0.0;
+  if (sigma > 0.0) {
+    const double nrm = sqrt(alpha * alpha + sigma);
+    *beta = alpha >= 0.0 ? -nrm : nrm;
+    *tau = (*beta - alpha) / *beta;
+    *scale = 1.0 / (alpha - *beta);
+  }
+}
+
+// Factor columns j0..j0+jb-1 (rows j0..m-1) of the column-major Aw in place; one CTA.
 __global__ void __launch_bounds__(NTP) qr_panel(int64_t m, int64_t j0, int jb, double* Aw, double* Vf, double* T) {
   __shared__ double red[NTP / 32][NB];
   __shared__ double vals[NB];
@@ -69,7 +114,6 @@ __global__ void __launch_bounds__(NTP) qr_panel(int64_t m, int64_t j0, int jb, d
   for (int c = 0; c < jb; ++c) {
     const int64_t j = j0 + c;
     double* x = Aw + j * m;
-    // (1) sigma = ||x(j+1:m)||^2
     double p = 0.0;
     for (int64_t i = j + 1 + tid; i < m; i += NTP) p = fma(x[i], x[i], p);
     p = tn_warp_sum(p);
@@ -78,27 +122,17 @@ __global__ void __launch_bounds__(NTP) qr_panel(int64_t m, int64_t j0, int jb, d
     if (tid == 0) {
       double sigma = 0.0;
       for (int w = 0; w < NTP / 32; ++w) sigma += red[w][0];
-      const double alpha = x[j];
-      double tau = 0.0, beta = alpha, scale = 0.0;
-      if (sigma > 0.0) {
-        const double nrm = sqrt(alpha * alpha + sigma);
-        beta = alpha >= 0.0 ? -nrm : nrm;
-        tau = (beta - alpha) / beta;
-        scale = 1.0 / (alpha - beta);
-      }
-      sc[0] = tau; sc[1] = beta; sc[2] = scale;
+      householder(x[j], sigma, &sc[0], &sc[1], &sc[2]);
     }
     __syncthreads();
     const double tau = sc[0], scale = sc[2];
-    // (2) reflector v: v(j) = 1, v(i>j) = x(i)*scale; R(j,j) = beta
     double* v = Vf + j * m;
     for (int64_t i = j + tid; i < m; i += NTP) {
       if (i == j) { v[i] = 1.0; x[i] = sc[1]; }
       else { const double vi = x[i] * scale; v[i] = vi; x[i] = 0.0; }
     }
     __syncthreads();
-    // (3)+(4): dots of v with the remaining panel columns and with earlier reflectors
-    const int nr = jb - c - 1;  // remaining columns
+    const int nr = jb - c - 1;
     double acc[NB];
 #pragma unroll
     for (int q = 0; q < NB; ++q) acc[q] = 0.0;
@@ -127,7 +161,6 @@ __global__ void __launch_bounds__(NTP) qr_panel(int64_t m, int64_t j0, int jb, d
       for (int q = 0; q < nr; ++q) Aw[(j + 1 + q) * m + i] -= tau * vals[q] * vi;
     }
     if (tid == 0) {
-      // T(0:c, c) = -tau * T(0:c, 0:c) * (V(:,0:c)^T v);  T(c,c) = tau
       double z[NB];
       for (int q = 0; q < c; ++q) z[q] = -tau * vals[nr + q];
       for (int r = 0; r < c; ++r) {
@@ -142,8 +175,153 @@ __global__ void __launch_bounds__(NTP) qr_panel(int64_t m, int64_t j0, int jb, d
   for (int i = tid; i < NB * NB; i += NTP) T[i] = Ts[i / NB][i % NB];
 }
 
-__global__ void qr_extract(int64_t m, int64_t n, int64_t k, const double* Aw, const double* Qw, double* q,
-                           int64_t sQm, int64_t sQn, double* r, int64_t sRm, int64_t sRn) {
+// The same panel factorisation spread over a cluster of CL CTAs. CTA `rank` owns panel rows
+// [r0, r1) in shared memory; per column two cluster barriers separate (a) the partial
+// norm, (b) the partial dot products, each summed by every CTA from all ranks' slots.
+// Slots are double-buffered across columns. Dynamic shared memory: P and Vs,
+// (PT*PR) x (NB+1) doubles each.
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
+    qr_panel_cluster(int64_t m, int64_t j0, int jb, double* Aw, double* Vf, double* T) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  extern __shared__ double dyn[];
+  double(*P)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dyn);
+  double(*Vs)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dyn + PT * PR * (NB + 1));
+  __shared__ double slot[2][NSLOT];
+  __shared__ double red[PT / 32][NSLOT];
+  __shared__ double tot[NSLOT];
+  __shared__ double Ts[NB][NB];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int64_t chunk = tn_cdiv(m - j0, CL);
+  const int64_t r0 = j0 + rank * chunk;
+  const int64_t r1 = (m < r0 + chunk) ? m : r0 + chunk;
+  const int nr = r1 > r0 ? (int)(r1 - r0) : 0;
+  for (int e = tid; e < nr * jb; e += PT) {
+    const int rr = e % nr, c = e / nr;
+    P[rr][c] = Aw[(j0 + c) * m + r0 + rr];
+  }
+  for (int e = tid; e < NB * NB; e += PT) Ts[e / NB][e % NB] = 0.0;
+  __syncthreads();
+  int buf = 0;
+  for (int c = 0; c < jb; ++c) {
+    const int64_t j = j0 + c;
+    // (a) partial ||x(j+1:)||^2 and the diagonal entry alpha (owned by one rank)
+    double ps = 0.0, pa = 0.0;
+#pragma unroll
+    for (int q = 0; q < PR; ++q) {
+      const int rr = tid + q * PT;
+      if (rr < nr) {
+        const int64_t i = r0 + rr;
+        const double x = P[rr][c];
+        if (i > j) ps = fma(x, x, ps);
+        else if (i == j) pa = x;
+      }
+    }
+    ps = tn_warp_sum(ps);
+    pa = tn_warp_sum(pa);
+    if (lane == 0) { red[wid][0] = ps; red[wid][1] = pa; }
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0, a = 0.0;
+      for (int w = 0; w < PT / 32; ++w) { s += red[w][0]; a += red[w][1]; }
+      slot[buf][0] = s;
+      slot[buf][1] = a;
+    }
+    cluster.sync();
+    if (tid < 2) {
+      double t = 0.0;
+      for (int r = 0; r < CL; ++r) t += cluster.map_shared_rank(&slot[buf][0], r)[tid];
+      tot[tid] = t;
+    }
+    __syncthreads();
+    double tau, beta, scale;
+    householder(tot[1], tot[0], &tau, &beta, &scale);
+#pragma unroll
+    for (int q = 0; q < PR; ++q) {
+      const int rr = tid + q * PT;
+      if (rr < nr) {
+        const int64_t i = r0 + rr;
+        double v = 0.0;
+        if (i == j) { v = 1.0; P[rr][c] = beta; }
+        else if (i > j) { v = P[rr][c] * scale; P[rr][c] = 0.0; }
+        Vs[rr][c] = v;
+      }
+    }
+    __syncthreads();
+    // (b) partial dots with the remaining panel columns and with this panel's earlier reflectors
+    const int nrem = jb - c - 1;
+    const int nd = nrem + c;
+    double acc[NB];
+#pragma unroll
+    for (int t = 0; t < NB; ++t) acc[t] = 0.0;
+#pragma unroll
+    for (int q = 0; q < PR; ++q) {
+      const int rr = tid + q * PT;
+      if (rr < nr) {
+        const double v = Vs[rr][c];
+        if (v != 0.0) {
+#pragma unroll
+          for (int t = 0; t < NB; ++t) {
+            if (t < nrem) acc[t] = fma(v, P[rr][c + 1 + t], acc[t]);
+            else if (t < nd) acc[t] = fma(v, Vs[rr][t - nrem], acc[t]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < NB; ++t) {
+      const double s = tn_warp_sum(acc[t]);
+      if (lane == 0) red[wid][2 + t] = s;
+    }
+    __syncthreads();
+    if (tid < nd) {
+      double s = 0.0;
+      for (int w = 0; w < PT / 32; ++w) s += red[w][2 + tid];
+      slot[buf][2 + tid] = s;
+    }
+    cluster.sync();
+    if (tid < nd) {
+      double t = 0.0;
+      for (int r = 0; r < CL; ++r) t += cluster.map_shared_rank(&slot[buf][0], r)[2 + tid];
+      tot[2 + tid] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < PR; ++q) {
+      const int rr = tid + q * PT;
+      if (rr < nr) {
+        const double v = Vs[rr][c];
+        if (v != 0.0)
+          for (int t = 0; t < nrem; ++t) P[rr][c + 1 + t] -= tau * tot[2 + t] * v;
+      }
+    }
+    if (tid == 0) {
+      double z[NB];
+      for (int q = 0; q < c; ++q) z[q] = -tau * tot[2 + nrem + q];
+      for (int r = 0; r < c; ++r) {
+        double t = 0.0;
+        for (int q = r; q < c; ++q) t = fma(Ts[r][q], z[q], t);
+        Ts[r][c] = t;
+      }
+      Ts[c][c] = tau;
+    }
+    __syncthreads();
+    buf ^= 1;
+  }
+  for (int e = tid; e < nr * jb; e += PT) {
+    const int rr = e % nr, c = e / nr;
+    Aw[(j0 + c) * m + r0 + rr] = P[rr][c];
+    Vf[(j0 + c) * m + r0 + rr] = Vs[rr][c];
+  }
+  if (rank == 0)
+    for (int e = tid; e < NB * NB; e += PT) T[e] = Ts[e / NB][e % NB];
+  cluster.sync();  // no CTA leaves while another may still read its slots
+}
+
+__global__ void qr_extract(int64_t m, int64_t n, int64_t k, const double* Aw, const double* Qw, const QrArgs* args,
+                           int64_t sQm, int64_t sQn, int64_t sRm, int64_t sRn) {
+  double* q = args->q;
+  double* r = args->r;
   const int64_t tq = m * k, tr = k * n;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < tq + tr;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -162,71 +340,64 @@ int blocks_for(int64_t total) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(total, 256), 8LL * tn_sm_count()));
 }
 
-}  // namespace
+constexpr size_t kClusterSmem = (size_t)2 * PT * PR * (NB + 1) * sizeof(double);
 
-extern "C" size_t tn_qr_workspace_bytes(int64_t m, int64_t n) {
-  if (m <= 0 || n <= 0) return 0;
-  QrWs q;
-  return qr_layout(m, n, nullptr, &q);
+int launch_panel(int64_t m, int64_t j0, int jb, const QrWs& w, double* Tp, cudaStream_t s) {
+  if (m - j0 <= (int64_t)CL * PT * PR) {
+    static bool attr = false;
+    if (!attr) {
+      TN_CUDA(cudaFuncSetAttribute(qr_panel_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmem));
+      attr = true;
+    }
+    qr_panel_cluster<<<CL, PT, kClusterSmem, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
+  } else {
+    qr_panel<<<1, NTP, 0, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
+  }
+  TN_CHECK_LAUNCH();
+  return TN_OK;
 }
 
-extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* q, int64_t sQm,
-                     int64_t sQn, double* r, int64_t sRm, int64_t sRn, void* ws, size_t ws_bytes, void* stream) {
-  if (m <= 0 || n <= 0 || !a) return tn_fail(TN_ERR_ARG, "qr: bad shape");
-  QrWs w;
-  const size_t need = qr_layout(m, n, nullptr, &w);
-  if (!ws || ws_bytes < need) return tn_fail(TN_ERR_WORKSPACE, "qr: workspace too small");
-  char* base = (char*)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
-  qr_layout(m, n, base, &w);
-  cudaStream_t s = (cudaStream_t)stream;
+// Every launch of one QR except qr_set_args (pointer-free, graph-capturable).
+int qr_body(int64_t m, int64_t n, int64_t sAm, int64_t sAn, int64_t sQm, int64_t sQn, int64_t sRm, int64_t sRn,
+            bool want_q, const QrWs& w, cudaStream_t s) {
   const int64_t k = std::min(m, n);
-  cudaEvent_t ev_all = tn_profile_begin(s);
-  qr_copy_in<<<blocks_for(m * n), 256, 0, s>>>(m, n, a, sAm, sAn, w.Aw);
+  qr_copy_in<<<blocks_for(m * n), 256, 0, s>>>(m, n, w.args, sAm, sAn, w.Aw);
   TN_CHECK_LAUNCH();
   qr_init_q<<<blocks_for(m * k), 256, 0, s>>>(m, k, w.Qw, w.Vf);
   TN_CHECK_LAUNCH();
   const int64_t np = tn_cdiv(k, NB);
+  int st;
   for (int64_t p = 0; p < np; ++p) {
     const int64_t j0 = p * NB;
     const int jb = (int)std::min<int64_t>(NB, k - j0);
     double* Tp = w.T + p * NB * NB;
-    cudaEvent_t ev_p = tn_profile_begin(s);
-    qr_panel<<<1, NTP, 0, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
-    TN_CHECK_LAUNCH();
-    tn_profile_end(ev_p, s, TN_PROF_QR_PANEL, 0.0);
+    if ((st = launch_panel(m, j0, jb, w, Tp, s))) return st;
     const int64_t nc = n - j0 - jb;
     if (nc <= 0) continue;
     const int64_t mr = m - j0;
-    TnGemmF64 g{};
-    // W = V^T C
+    TnGemmF64 g{};  // W = V^T C
     g.M = jb; g.N = nc; g.K = mr;
     g.A = w.Vf + j0 + j0 * m; g.sAm = m; g.sAk = 1;
     g.B = w.Aw + j0 + (j0 + jb) * m; g.sBk = 1; g.sBn = m;
     g.C = w.W; g.sCm = nc; g.sCn = 1;
     g.batch = 1; g.nred = 1; g.alpha = 1.0; g.beta = 0.0;
-    int st = tn_gemm_f64_ws(g, w.gws, w.gws_bytes, s);
-    if (st) return st;
-    // W2 = T^T W
-    TnGemmF64 h{};
+    if ((st = tn_gemm_f64_ws(g, w.gws, w.gws_bytes, s))) return st;
+    TnGemmF64 h{};  // W2 = T^T W
     h.M = jb; h.N = nc; h.K = jb;
     h.A = Tp; h.sAm = 1; h.sAk = NB;
     h.B = w.W; h.sBk = nc; h.sBn = 1;
     h.C = w.W2; h.sCm = nc; h.sCn = 1;
     h.batch = 1; h.nred = 1; h.alpha = 1.0; h.beta = 0.0;
-    st = tn_gemm_f64_ws(h, nullptr, 0, s);
-    if (st) return st;
-    // C -= V W2
-    TnGemmF64 u{};
+    if ((st = tn_gemm_f64_ws(h, nullptr, 0, s))) return st;
+    TnGemmF64 u{};  // C -= V W2
     u.M = mr; u.N = nc; u.K = jb;
     u.A = w.Vf + j0 + j0 * m; u.sAm = 1; u.sAk = m;
     u.B = w.W2; u.sBk = nc; u.sBn = 1;
     u.C = w.Aw + j0 + (j0 + jb) * m; u.sCm = 1; u.sCn = m;
     u.batch = 1; u.nred = 1; u.alpha = -1.0; u.beta = 1.0;
-    st = tn_gemm_f64_ws(u, nullptr, 0, s);
-    if (st) return st;
+    if ((st = tn_gemm_f64_ws(u, nullptr, 0, s))) return st;
   }
-  cudaEvent_t ev_q = tn_profile_begin(s);
-  if (q) {
+  if (want_q) {
     for (int64_t p = np - 1; p >= 0; --p) {
       const int64_t j0 = p * NB;
       const int jb = (int)std::min<int64_t>(NB, k - j0);
@@ -239,29 +410,100 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
       g.B = w.Qw + j0 + j0 * m; g.sBk = 1; g.sBn = m;
       g.C = w.W; g.sCm = nc; g.sCn = 1;
       g.batch = 1; g.nred = 1; g.alpha = 1.0; g.beta = 0.0;
-      int st = tn_gemm_f64_ws(g, w.gws, w.gws_bytes, s);
-      if (st) return st;
+      if ((st = tn_gemm_f64_ws(g, w.gws, w.gws_bytes, s))) return st;
       TnGemmF64 h{};
       h.M = jb; h.N = nc; h.K = jb;
       h.A = Tp; h.sAm = NB; h.sAk = 1;
       h.B = w.W; h.sBk = nc; h.sBn = 1;
       h.C = w.W2; h.sCm = nc; h.sCn = 1;
       h.batch = 1; h.nred = 1; h.alpha = 1.0; h.beta = 0.0;
-      st = tn_gemm_f64_ws(h, nullptr, 0, s);
-      if (st) return st;
+      if ((st = tn_gemm_f64_ws(h, nullptr, 0, s))) return st;
       TnGemmF64 u{};
       u.M = mr; u.N = nc; u.K = jb;
       u.A = w.Vf + j0 + j0 * m; u.sAm = 1; u.sAk = m;
       u.B = w.W2; u.sBk = nc; u.sBn = 1;
       u.C = w.Qw + j0 + j0 * m; u.sCm = 1; u.sCn = m;
       u.batch = 1; u.nred = 1; u.alpha = -1.0; u.beta = 1.0;
-      st = tn_gemm_f64_ws(u, nullptr, 0, s);
-      if (st) return st;
+      if ((st = tn_gemm_f64_ws(u, nullptr, 0, s))) return st;
     }
   }
-  tn_profile_end(ev_q, s, TN_PROF_QR_FORM_Q, 0.0);
-  qr_extract<<<blocks_for(m * k + k * n), 256, 0, s>>>(m, n, k, w.Aw, w.Qw, q, sQm, sQn, r, sRm, sRn);
+  qr_extract<<<blocks_for(m * k + k * n), 256, 0, s>>>(m, n, k, w.Aw, w.Qw, w.args, sQm, sQn, sRm, sRn);
   TN_CHECK_LAUNCH();
-  tn_profile_end(ev_all, s, TN_PROF_QR, 4.0 * m * n * n - 4.0 / 3.0 * n * n * (double)n);
   return TN_OK;
+}
+
+// Graph cache: one executable graph per (shape, strides, workspace, outputs requested).
+struct QrGraph {
+  int64_t key[10];
+  cudaGraphExec_t exec;
+  unsigned long long kernels;  // kernel launches recorded into the graph
+};
+std::vector<QrGraph> g_graphs;
+bool g_use_graphs = true;
+
+}  // namespace
+
+extern "C" size_t tn_qr_workspace_bytes(int64_t m, int64_t n) {
+  if (m <= 0 || n <= 0) return 0;
+  QrWs q;
+  return qr_layout(m, n, nullptr, &q);
+}
+
+extern "C" int tn_qr_use_graphs(int on) {
+  g_use_graphs = on != 0;
+  return TN_OK;
+}
+
+extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* q, int64_t sQm,
+                     int64_t sQn, double* r, int64_t sRm, int64_t sRn, void* ws, size_t ws_bytes, void* stream) {
+  if (m <= 0 || n <= 0 || !a) return tn_fail(TN_ERR_ARG, "qr: bad shape");
+  QrWs w;
+  const size_t need = qr_layout(m, n, nullptr, &w);
+  if (!ws || ws_bytes < need) return tn_fail(TN_ERR_WORKSPACE, "qr: workspace too small");
+  char* base = (char*)(((uintptr_t)ws + 255) & ~(uintptr_t)255);
+  qr_layout(m, n, base, &w);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t ev_all = tn_profile_begin(s);
+  qr_set_args<<<1, 1, 0, s>>>(w.args, a, q, r);
+  TN_CHECK_LAUNCH();
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  TN_CUDA(cudaStreamIsCapturing(s, &cap));
+  int st;
+  if (!g_use_graphs || cap != cudaStreamCaptureStatusNone) {
+    st = qr_body(m, n, sAm, sAn, sQm, sQn, sRm, sRn, q != nullptr, w, s);
+  } else {
+    const int64_t key[10] = {m, n, sAm, sAn, sQm, sQn, sRm, sRn, (int64_t)(uintptr_t)base, q != nullptr};
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long kernels = 0;
+    for (auto& g : g_graphs)
+      if (memcmp(g.key, key, sizeof(key)) == 0) { exec = g.exec; kernels = g.kernels; break; }
+    if (!exec) {
+      cudaGraph_t graph;
+      TN_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      const unsigned long long launches0 = g_tn_launches;
+      st = qr_body(m, n, sAm, sAn, sQm, sQn, sRm, sRn, q != nullptr, w, s);
+      cudaError_t e = cudaStreamEndCapture(s, &graph);
+      kernels = g_tn_launches - launches0;
+      g_tn_launches = launches0;  // counted at every replay below
+      if (st) return st;
+      if (e != cudaSuccess) return tn_record_error(e);
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return tn_record_error(e);
+      if (g_graphs.size() >= 64) {
+        cudaGraphExecDestroy(g_graphs.front().exec);
+        g_graphs.erase(g_graphs.begin());
+      }
+      QrGraph gg;
+      memcpy(gg.key, key, sizeof(key));
+      gg.exec = exec;
+      gg.kernels = kernels;
+      g_graphs.push_back(gg);
+    }
+    TN_CUDA(cudaGraphLaunch(exec, s));
+    g_tn_launches += kernels;
+    st = TN_OK;
+  }
+  tn_profile_end(ev_all, s, TN_PROF_QR, 4.0 * m * n * n - 4.0 / 3.0 * n * n * (double)n);
+  return st;
 }

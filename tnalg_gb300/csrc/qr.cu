@@ -478,11 +478,15 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
     for (auto& g : g_graphs)
       if (memcmp(g.key, key, sizeof(key)) == 0) { exec = g.exec; kernels = g.kernels; break; }
     if (!exec) {
+      // capture on a private stream (the caller's may be the legacy default stream, which
+      // cannot capture); nothing runs during capture, the graph is launched on `s` below.
+      static cudaStream_t cs = nullptr;
+      if (!cs) TN_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       cudaGraph_t graph;
-      TN_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      TN_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
       const unsigned long long launches0 = g_tn_launches;
-      st = qr_body(m, n, sAm, sAn, sQm, sQn, sRm, sRn, q != nullptr, w, s);
-      cudaError_t e = cudaStreamEndCapture(s, &graph);
+      st = qr_body(m, n, sAm, sAn, sQm, sQn, sRm, sRn, q != nullptr, w, cs);
+      cudaError_t e = cudaStreamEndCapture(cs, &graph);
       kernels = g_tn_launches - launches0;
       g_tn_launches = launches0;  // counted at every replay below
       if (st) return st;

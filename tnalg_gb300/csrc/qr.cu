@@ -187,7 +187,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
   extern __shared__ double dyn[];
   double(*P)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dyn);
   double(*Vs)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dyn + PT * PR * (NB + 1));
-  __shared__ double slot[2][NSLOT];
+  __shared__ double gath[2][CL][NSLOT];  // partials pushed here by every rank (double-buffered)
+  __shared__ double mine[NSLOT];
   __shared__ double red[PT / 32][NSLOT];
   __shared__ double tot[NSLOT];
   __shared__ double Ts[NB][NB];
@@ -221,16 +222,20 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
     pa = tn_warp_sum(pa);
     if (lane == 0) { red[wid][0] = ps; red[wid][1] = pa; }
     __syncthreads();
-    if (tid == 0) {
-      double s = 0.0, a = 0.0;
-      for (int w = 0; w < PT / 32; ++w) { s += red[w][0]; a += red[w][1]; }
-      slot[buf][0] = s;
-      slot[buf][1] = a;
+    if (tid < 2) {
+      double s = 0.0;
+      for (int w = 0; w < PT / 32; ++w) s += red[w][tid];
+      mine[tid] = s;
+    }
+    __syncthreads();
+    if (tid < 2 * CL) {  // push (sigma, alpha) partials into every rank's gather slot
+      const int dst = tid >> 1, v = tid & 1;
+      cluster.map_shared_rank(&gath[buf][rank][0], dst)[v] = mine[v];
     }
     cluster.sync();
     if (tid < 2) {
       double t = 0.0;
-      for (int r = 0; r < CL; ++r) t += cluster.map_shared_rank(&slot[buf][0], r)[tid];
+      for (int r = 0; r < CL; ++r) t += gath[buf][r][tid];
       tot[tid] = t;
     }
     __syncthreads();
@@ -277,12 +282,17 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
     if (tid < nd) {
       double s = 0.0;
       for (int w = 0; w < PT / 32; ++w) s += red[w][2 + tid];
-      slot[buf][2 + tid] = s;
+      mine[2 + tid] = s;
+    }
+    __syncthreads();
+    for (int t = tid; t < nd * CL; t += PT) {  // push the dot partials to every rank
+      const int dst = t / nd, v = t % nd;
+      cluster.map_shared_rank(&gath[buf][rank][0], dst)[2 + v] = mine[2 + v];
     }
     cluster.sync();
     if (tid < nd) {
       double t = 0.0;
-      for (int r = 0; r < CL; ++r) t += cluster.map_shared_rank(&slot[buf][0], r)[2 + tid];
+      for (int r = 0; r < CL; ++r) t += gath[buf][r][2 + tid];
       tot[2 + tid] = t;
     }
     __syncthreads();

@@ -143,7 +143,9 @@ def run_ours(args, rank, world, local_rank):
     order = list(range(1, L_)) + list(range(L_ - 2, -1, -1))
 
     def sweep():
-        for n in order:
+        for k, n in enumerate(order):
+            if k == len(order) - 1:
+                A.refine_next_solve()
             A.update_tensor_eigs(n, para["index1"], para["index2"], para["coeff1"], para["coeff2"], para["tau"],
                                  True, tol=para["eigs_tol"])
 

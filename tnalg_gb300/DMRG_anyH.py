@@ -51,9 +51,11 @@ def dmrg_finite_size(para=None):
             print("In the %d-th round of sweep ..." % (t + 1))
         order = list(range(para["ob_position"] + 1, l)) + list(range(l - 2, -1, -1)) + \
             list(range(1, para["ob_position"]))
-        for n in order:
+        for k, n in enumerate(order):
             if para["if_print_detail"]:
                 print("update the %d-th tensor ..." % n)
+            if k == len(order) - 1:
+                A.refine_next_solve()
             A.update_tensor_eigs(n, index1, index2, coeff1, coeff2, para["tau"], para["is_real"],
                                  tol=para["eigs_tol"])
         info["sweeps"] = t + 1

@@ -84,8 +84,12 @@ class MpsOpenBoundaryClass(MpsBasic):
         self._debug = debug
         self.eig_way = eig_way
         self.pool = None
+        # refine: None = FP64 Rayleigh quotient after every mixed-precision solve, 0/1 = never/always,
+        # "last" = only for solves flagged with refine_next_solve() (dmrg_finite_size flags the last
+        # solve of every sweep)
         self.lanczos = {"max_krylov": 40, "max_restarts": 50, "check_every": 3, "tol_cap": 0.0,
-                        "mixed_floor": 2e-6, "refine": None}
+                        "mixed_floor": 2e-6, "refine": "last"}
+        self._refine_next = False
         self.last_solve = None
         self._model_key = None
         self._dev = E.DeviceMPS(tensors, d, device, precision=precision)
@@ -229,15 +233,26 @@ class MpsOpenBoundaryClass(MpsBasic):
         """MPSClass.py:778-809: move the centre to p and replace site p by the lowest eigenvector
         of its effective Hamiltonian. Returns the eigenvalue of H_eff."""
         self._model(index1, index2, coeff1, coeff2, tol)
-        self.correct_orthogonal_center(p)
+        if self.decomp_way == "svd":
+            self.correct_orthogonal_center(p)
+        else:
+            self._dev.move_center_for_solve(p)
         o = self.lanczos
+        refine = o["refine"]
+        if refine == "last":  # FP64 Rayleigh quotient only when the caller marks the solve
+            refine = 1 if self._refine_next else 0
+        self._refine_next = False
         res = self._dev.solve(p, tol, tau, tol_cap=o["tol_cap"], max_krylov=o["max_krylov"],
-                              max_restarts=o["max_restarts"], check_every=o["check_every"], refine=o["refine"],
+                              max_restarts=o["max_restarts"], check_every=o["check_every"], refine=refine,
                               mixed_floor=o["mixed_floor"])
         self.last_solve = res
         e = res.energy_fp64 if res.energy_fp64 != 0.0 or res.energy == 0.0 else res.energy
         self.solve_energies.append(e)
         return e
+
+    def refine_next_solve(self):
+        """Have the next update_tensor_eigs end with an FP64 residual and Rayleigh quotient."""
+        self._refine_next = True
 
     def effective_hamiltonian_dmrg(self, p, index1, index2, coeff1, coeff2, tol=1e-12):
         """Dense H_eff at the centre p (MPSClass.py:532-580), built column by column with
@@ -354,6 +369,7 @@ class MpsOpenBoundaryClass(MpsBasic):
         st["_precision"] = self.precision
         st["_device"] = str(self._dev.device)
         st["last_solve"] = None
+        st["_refine_next"] = False
         st["_model_key"] = None
         return st
 

@@ -28,8 +28,8 @@ namespace {
 constexpr int NB = 16;
 constexpr int NTP = 512;  // single-CTA panel
 constexpr int CL = 8;     // CTAs per panel cluster
-constexpr int PT = 128;   // threads per cluster CTA
-constexpr int PR = 2;     // panel rows per thread -> <= CL * PT * PR rows
+constexpr int PW = 32;    // one warp per cluster CTA
+constexpr int PRW = 8;    // panel rows per lane -> <= CL * PW * PRW rows
 constexpr int NSLOT = NB + 2;
 
 size_t al(size_t x) { return (x + 255) / 256 * 256; }
@@ -175,42 +175,70 @@ __global__ void __launch_bounds__(NTP) qr_panel(int64_t m, int64_t j0, int jb, d
   for (int i = tid; i < NB * NB; i += NTP) T[i] = Ts[i / NB][i % NB];
 }
 
-// The same panel factorisation spread over a cluster of CL CTAs. CTA `rank` owns panel rows
-// [r0, r1) in shared memory; per column two cluster barriers separate (a) the partial
-// norm, (b) the partial dot products, each summed by every CTA from all ranks' slots.
-// Slots are double-buffered across columns. Dynamic shared memory: P and Vs,
-// (PT*PR) x (NB+1) doubles each.
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
+// The same panel factorisation spread over a cluster of CL CTAs of ONE warp each. CTA `rank`
+// owns panel rows [r0, r0 + nr) in shared memory (PRW rows per lane). GB300 issues FP64 at ~2
+// lanes/clock/SM, so every FP64 warp instruction costs ~16 cycles whatever it computes: the
+// kernel keeps the FP64 instruction count per column low (one warp, a transposing 16-value warp
+// reduction, unpredicated dot slots, a lane-parallel T column). Per column, each CTA pushes its
+// partial sums into every rank's `gath` slot (remote shared-memory stores) and a cluster barrier
+// publishes them; slots are double-buffered across columns.
+__device__ __forceinline__ void warp_reduce16(double (&a)[16], int lane) {
+  // afterwards lanes 2i and 2i+1 hold the warp-wide sum of slot i
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const bool up = lane & 16;
+    const double send = up ? a[i] : a[i + 8], keep = up ? a[i + 8] : a[i];
+    a[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const bool up = lane & 8;
+    const double send = up ? a[i] : a[i + 4], keep = up ? a[i + 4] : a[i];
+    a[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const bool up = lane & 4;
+    const double send = up ? a[i] : a[i + 2], keep = up ? a[i + 2] : a[i];
+    a[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  {
+    const bool up = lane & 2;
+    const double send = up ? a[0] : a[1], keep = up ? a[1] : a[0];
+    a[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  a[0] += __shfl_xor_sync(0xffffffffu, a[0], 1);
+}
+
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PW)
     qr_panel_cluster(int64_t m, int64_t j0, int jb, double* Aw, double* Vf, double* T) {
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   extern __shared__ double dyn[];
   double(*P)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dyn);
-  double(*Vs)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dyn + PT * PR * (NB + 1));
-  __shared__ double gath[2][CL][NSLOT];  // partials pushed here by every rank (double-buffered)
-  __shared__ double mine[NSLOT];
-  __shared__ double red[PT / 32][NSLOT];
-  __shared__ double tot[NSLOT];
+  double(*Vs)[NB + 1] = reinterpret_cast<double(*)[NB + 1]>(dyn + PW * PRW * (NB + 1));
+  __shared__ double gath[2][CL][NSLOT];
   __shared__ double Ts[NB][NB];
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int lane = threadIdx.x;
   const int64_t chunk = tn_cdiv(m - j0, CL);
   const int64_t r0 = j0 + rank * chunk;
   const int64_t r1 = (m < r0 + chunk) ? m : r0 + chunk;
   const int nr = r1 > r0 ? (int)(r1 - r0) : 0;
-  for (int e = tid; e < nr * jb; e += PT) {
+  for (int e = lane; e < PW * PRW * (NB + 1); e += PW) (&Vs[0][0])[e] = 0.0;
+  for (int e = lane; e < nr * jb; e += PW) {
     const int rr = e % nr, c = e / nr;
     P[rr][c] = Aw[(j0 + c) * m + r0 + rr];
   }
-  for (int e = tid; e < NB * NB; e += PT) Ts[e / NB][e % NB] = 0.0;
-  __syncthreads();
+  for (int e = lane; e < NB * NB; e += PW) Ts[e / NB][e % NB] = 0.0;
+  __syncwarp();
   int buf = 0;
   for (int c = 0; c < jb; ++c) {
     const int64_t j = j0 + c;
-    // (a) partial ||x(j+1:)||^2 and the diagonal entry alpha (owned by one rank)
+    // (a) partial ||x(j+1:)||^2 and the diagonal entry alpha
     double ps = 0.0, pa = 0.0;
 #pragma unroll
-    for (int q = 0; q < PR; ++q) {
-      const int rr = tid + q * PT;
+    for (int q = 0; q < PRW; ++q) {
+      const int rr = lane + q * PW;
       if (rr < nr) {
         const int64_t i = r0 + rr;
         const double x = P[rr][c];
@@ -220,112 +248,85 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
     }
     ps = tn_warp_sum(ps);
     pa = tn_warp_sum(pa);
-    if (lane == 0) { red[wid][0] = ps; red[wid][1] = pa; }
-    __syncthreads();
-    if (tid < 2) {
-      double s = 0.0;
-      for (int w = 0; w < PT / 32; ++w) s += red[w][tid];
-      mine[tid] = s;
-    }
-    __syncthreads();
-    if (tid < 2 * CL) {  // push (sigma, alpha) partials into every rank's gather slot
-      const int dst = tid >> 1, v = tid & 1;
-      cluster.map_shared_rank(&gath[buf][rank][0], dst)[v] = mine[v];
-    }
+    if (lane < 2 * CL) cluster.map_shared_rank(&gath[buf][rank][0], lane >> 1)[lane & 1] = (lane & 1) ? pa : ps;
     cluster.sync();
-    if (tid < 2) {
-      double t = 0.0;
-      for (int r = 0; r < CL; ++r) t += gath[buf][r][tid];
-      tot[tid] = t;
-    }
-    __syncthreads();
-    double tau, beta, scale;
-    householder(tot[1], tot[0], &tau, &beta, &scale);
+    double sigma = 0.0, alpha = 0.0;
 #pragma unroll
-    for (int q = 0; q < PR; ++q) {
-      const int rr = tid + q * PT;
+    for (int r = 0; r < CL; ++r) { sigma += gath[buf][r][0]; alpha += gath[buf][r][1]; }
+    double tau, beta, scale;
+    householder(alpha, sigma, &tau, &beta, &scale);
+    double vq[PRW];
+#pragma unroll
+    for (int q = 0; q < PRW; ++q) {
+      const int rr = lane + q * PW;
+      vq[q] = 0.0;
       if (rr < nr) {
         const int64_t i = r0 + rr;
-        double v = 0.0;
-        if (i == j) { v = 1.0; P[rr][c] = beta; }
-        else if (i > j) { v = P[rr][c] * scale; P[rr][c] = 0.0; }
-        Vs[rr][c] = v;
+        if (i == j) { vq[q] = 1.0; P[rr][c] = beta; }
+        else if (i > j) { vq[q] = P[rr][c] * scale; P[rr][c] = 0.0; }
+        Vs[rr][c] = vq[q];
       }
     }
-    __syncthreads();
-    // (b) partial dots with the remaining panel columns and with this panel's earlier reflectors
+    __syncwarp();
+    // (b) dot products: slot t < nrem with panel column c+1+t, slot t >= nrem with reflector t-nrem
     const int nrem = jb - c - 1;
     const int nd = nrem + c;
-    double acc[NB];
+    double acc[16];
 #pragma unroll
-    for (int t = 0; t < NB; ++t) acc[t] = 0.0;
+    for (int t = 0; t < 16; ++t) acc[t] = 0.0;
 #pragma unroll
-    for (int q = 0; q < PR; ++q) {
-      const int rr = tid + q * PT;
-      if (rr < nr) {
-        const double v = Vs[rr][c];
-        if (v != 0.0) {
+    for (int q = 0; q < PRW; ++q) {
+      const int rr = lane + q * PW;
+      if (rr < nr && vq[q] != 0.0) {
 #pragma unroll
-          for (int t = 0; t < NB; ++t) {
-            if (t < nrem) acc[t] = fma(v, P[rr][c + 1 + t], acc[t]);
-            else if (t < nd) acc[t] = fma(v, Vs[rr][t - nrem], acc[t]);
-          }
+        for (int t = 0; t < 16; ++t) {
+          const double* src = (t < nrem) ? &P[rr][c + 1 + t] : &Vs[rr][t - nrem];
+          acc[t] = fma(vq[q], *src, acc[t]);
         }
       }
     }
+    warp_reduce16(acc, lane);
+    const int slot_i = (lane >> 1) & 15;
+    if (slot_i < nd) {
+      const int half = lane & 1;
 #pragma unroll
-    for (int t = 0; t < NB; ++t) {
-      const double s = tn_warp_sum(acc[t]);
-      if (lane == 0) red[wid][2 + t] = s;
-    }
-    __syncthreads();
-    if (tid < nd) {
-      double s = 0.0;
-      for (int w = 0; w < PT / 32; ++w) s += red[w][2 + tid];
-      mine[2 + tid] = s;
-    }
-    __syncthreads();
-    for (int t = tid; t < nd * CL; t += PT) {  // push the dot partials to every rank
-      const int dst = t / nd, v = t % nd;
-      cluster.map_shared_rank(&gath[buf][rank][0], dst)[2 + v] = mine[2 + v];
+      for (int dd = 0; dd < CL / 2; ++dd)
+        cluster.map_shared_rank(&gath[buf][rank][0], half * (CL / 2) + dd)[2 + slot_i] = acc[0];
     }
     cluster.sync();
-    if (tid < nd) {
-      double t = 0.0;
-      for (int r = 0; r < CL; ++r) t += gath[buf][r][2 + tid];
-      tot[2 + tid] = t;
-    }
-    __syncthreads();
+    double wt = 0.0;
+    if (slot_i < nd) {
 #pragma unroll
-    for (int q = 0; q < PR; ++q) {
-      const int rr = tid + q * PT;
-      if (rr < nr) {
-        const double v = Vs[rr][c];
-        if (v != 0.0)
-          for (int t = 0; t < nrem; ++t) P[rr][c + 1 + t] -= tau * tot[2 + t] * v;
+      for (int r = 0; r < CL; ++r) wt += gath[buf][r][2 + slot_i];
+    }
+    // rank-1 update of the remaining panel columns: P(:, c+1+t) -= tau * w_t * v
+    for (int t = 0; t < nrem; ++t) {
+      const double coef = tau * __shfl_sync(0xffffffffu, wt, 2 * t);
+#pragma unroll
+      for (int q = 0; q < PRW; ++q) {
+        const int rr = lane + q * PW;
+        if (rr < nr && vq[q] != 0.0) P[rr][c + 1 + t] = fma(-coef, vq[q], P[rr][c + 1 + t]);
       }
     }
-    if (tid == 0) {
-      double z[NB];
-      for (int q = 0; q < c; ++q) z[q] = -tau * tot[2 + nrem + q];
-      for (int r = 0; r < c; ++r) {
-        double t = 0.0;
-        for (int q = r; q < c; ++q) t = fma(Ts[r][q], z[q], t);
-        Ts[r][c] = t;
-      }
-      Ts[c][c] = tau;
+    // T(0:c, c) = -tau * T(0:c, 0:c) * (V(:, 0:c)^T v); lane r owns row r
+    double tr = 0.0;
+    for (int qq = 0; qq < c; ++qq) {
+      const double z = -tau * __shfl_sync(0xffffffffu, wt, 2 * (nrem + qq));
+      if (lane < c && qq >= lane) tr = fma(Ts[lane][qq], z, tr);
     }
-    __syncthreads();
+    if (lane < c) Ts[lane][c] = tr;
+    if (lane == 0) Ts[c][c] = tau;
+    __syncwarp();
     buf ^= 1;
   }
-  for (int e = tid; e < nr * jb; e += PT) {
+  for (int e = lane; e < nr * jb; e += PW) {
     const int rr = e % nr, c = e / nr;
     Aw[(j0 + c) * m + r0 + rr] = P[rr][c];
     Vf[(j0 + c) * m + r0 + rr] = Vs[rr][c];
   }
   if (rank == 0)
-    for (int e = tid; e < NB * NB; e += PT) T[e] = Ts[e / NB][e % NB];
-  cluster.sync();  // no CTA leaves while another may still read its slots
+    for (int e = lane; e < NB * NB; e += PW) T[e] = Ts[e / NB][e % NB];
+  cluster.sync();  // no CTA leaves while another may still write into its slots
 }
 
 __global__ void qr_extract(int64_t m, int64_t n, int64_t k, const double* Aw, const double* Qw, const QrArgs* args,
@@ -350,16 +351,16 @@ int blocks_for(int64_t total) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(total, 256), 8LL * tn_sm_count()));
 }
 
-constexpr size_t kClusterSmem = (size_t)2 * PT * PR * (NB + 1) * sizeof(double);
+constexpr size_t kClusterSmem = (size_t)2 * PW * PRW * (NB + 1) * sizeof(double);
 
 int launch_panel(int64_t m, int64_t j0, int jb, const QrWs& w, double* Tp, cudaStream_t s) {
-  if (m - j0 <= (int64_t)CL * PT * PR) {
+  if (m - j0 <= (int64_t)CL * PW * PRW) {
     static bool attr = false;
     if (!attr) {
       TN_CUDA(cudaFuncSetAttribute(qr_panel_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmem));
       attr = true;
     }
-    qr_panel_cluster<<<CL, PT, kClusterSmem, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
+    qr_panel_cluster<<<CL, PW, kClusterSmem, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
   } else {
     qr_panel<<<1, NTP, 0, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
   }

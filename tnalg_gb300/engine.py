@@ -313,7 +313,7 @@ class DeviceMPS:
         self.er_from = b
 
     # -- gauge -------------------------------------------------------------------
-    def qr_left(self, n):
+    def qr_left(self, n, seed_only=False):
         """left2right_decompose_tensor + absorb_matrix2tensor(mps[n+1], R^T, 0)
         (TensorBasicModule.py:314-348, 387-424; MPSClass.py:150-158)."""
         A = self.mps[n]
@@ -328,7 +328,10 @@ class DeviceMPS:
         nxt = self.mps[n + 1]
         c2, d2, r2 = nxt.shape
         new = torch.empty((k, d2, r2), dtype=torch.float64, device=self.device)
-        L.gemm(R, nxt, new, k, d2 * r2, nn, (nn, 1), (d2 * r2, 1), (d2 * r2, 1), ws=self.ws)
+        # seed_only: site n+1 is re-solved next, so R.mps[n+1] is only the Lanczos start vector
+        # and may use the working precision; otherwise it carries the state and stays FP64.
+        L.gemm(R, nxt, new, k, d2 * r2, nn, (nn, 1), (d2 * r2, 1), (d2 * r2, 1), ws=self.ws,
+               precision=self.precision if seed_only else L.PREC_FP64)
         self.mps[n] = Q
         self.mps[n + 1] = new
         self._last_r = R
@@ -336,7 +339,7 @@ class DeviceMPS:
         self.tensor_changed(n)
         self.tensor_changed(n + 1)
 
-    def qr_right(self, n):
+    def qr_right(self, n, seed_only=False):
         """right2left_decompose_tensor + absorb_matrix2tensor(mps[n-1], R^T, 2)
         (TensorBasicModule.py:351-384; MPSClass.py:159-167)."""
         A = self.mps[n]
@@ -353,7 +356,8 @@ class DeviceMPS:
         c0, d0, r0 = prv.shape
         new = torch.empty((c0, d0, k), dtype=torch.float64, device=self.device)
         # prv(c0*d0, cl) . R^T(cl, k)
-        L.gemm(prv, R, new, c0 * d0, k, nn, (nn, 1), (1, nn), (k, 1), ws=self.ws)
+        L.gemm(prv, R, new, c0 * d0, k, nn, (nn, 1), (1, nn), (k, 1), ws=self.ws,
+               precision=self.precision if seed_only else L.PREC_FP64)
         self.mps[n] = Bt
         self.mps[n - 1] = new
         self._last_r = R
@@ -400,6 +404,22 @@ class DeviceMPS:
         self.el_upto = min(self.el_upto, 0)
         self.er_from = max(self.er_from, self.length)
         return True
+
+    def move_center_for_solve(self, p):
+        """Centre to p ahead of a local solve at p: a one-site move seeds site p in the working
+        precision (the solve replaces it); longer moves go through correct_orthogonal_center."""
+        if self.center == p - 1 and p >= 1:
+            self.qr_left(p - 1, seed_only=True)
+            self.orthogonality[p - 1] = -1
+            self.orthogonality[p] = 0
+            self.center = p
+        elif self.center == p + 1:
+            self.qr_right(p + 1, seed_only=True)
+            self.orthogonality[p + 1] = 1
+            self.orthogonality[p] = 0
+            self.center = p
+        else:
+            self.correct_orthogonal_center(p)
 
     def correct_orthogonal_center(self, p):
         """MPSClass.py:188-198 for an explicit p."""

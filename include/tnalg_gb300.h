@@ -173,6 +173,16 @@ int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn,
           double* q, int64_t sQm, int64_t sQn, double* r, int64_t sRm, int64_t sRn,
           void* ws, size_t ws_bytes, void* stream);
 size_t tn_qr_workspace_bytes(int64_t m, int64_t n);
+/*
+ * Gauge move of the mixed-precision sweep: same outputs as tn_qr, but Q comes from an FP32
+ * Householder QR re-orthogonalised in FP64 (||Q^T Q - I|| ~ 1e-12, col(Q) = col(A) to FP32
+ * accuracy) and R is accurate to FP32 only. Meant for moves whose R is absorbed into a site
+ * that is re-optimised next (the seed of the next local solve). q is required.
+ */
+int tn_qr_mixed(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn,
+                double* q, int64_t sQm, int64_t sQn, double* r, int64_t sRm, int64_t sRn,
+                void* ws, size_t ws_bytes, void* stream);
+size_t tn_qr_mixed_workspace_bytes(int64_t m, int64_t n);
 /* tn_qr replays one captured CUDA graph per (shape, strides, workspace) (default on); 0 turns
  * replay off (plain launches). A stream that is already capturing always gets plain launches. */
 int tn_qr_use_graphs(int on);

@@ -114,6 +114,30 @@ def test_tf32x3_lanczos_fp64_refined_energy(tf32):
     assert abs(res.energy - w0) <= 1e-5 * abs(w0)
 
 
+@pytest.mark.parametrize("m,n,cond", [(1024, 512, 1.0), (1024, 512, 1e10), (256, 128, 1e6), (96, 200, 1e3)])
+def test_qr_mixed_orthonormal_and_spanning(tf32, m, n, cond):
+    """FP32 Householder + FP64 re-orthogonalisation: Q orthonormal to ~1e-12 at any conditioning,
+    col(Q) = col(A) to FP32 accuracy, R accurate to FP32."""
+    lib = L.load()
+    k = min(m, n)
+    g = torch.Generator(device="cpu").manual_seed(m + n)
+    U, _ = torch.linalg.qr(torch.randn(m, k, generator=g, dtype=torch.float64))
+    V, _ = torch.linalg.qr(torch.randn(n, k, generator=g, dtype=torch.float64))
+    s = torch.logspace(0, -np.log10(cond), k, dtype=torch.float64)
+    A = ((U * s) @ V.T).cuda()
+    Q = torch.empty((m, k), dtype=torch.float64, device="cuda")
+    R = torch.empty((k, n), dtype=torch.float64, device="cuda")
+    ws = L.Workspace(torch.device("cuda"))
+    wp, wb = ws.args(lib.tn_qr_mixed_workspace_bytes(m, n))
+    L.check(lib.tn_qr_mixed(m, n, L.ptr(A), n, 1, L.ptr(Q), k, 1, L.ptr(R), n, 1, wp, wb, L.stream_handle()))
+    L.check(lib.tn_check_device_status(L.stream_handle()))
+    eye = torch.eye(k, dtype=torch.float64, device="cuda")
+    assert torch.max(torch.abs(Q.T @ Q - eye)).item() < 1e-11
+    resid = A - Q @ (Q.T @ A)
+    assert torch.linalg.matrix_norm(resid).item() / torch.linalg.matrix_norm(A).item() < 1e-5
+    assert torch.linalg.matrix_norm(Q @ R - A).item() / torch.linalg.matrix_norm(A).item() < 1e-5
+
+
 def test_tf32x3_dmrg_close_to_reference(tf32):
     """Mixed path on the N=12 chain: energy per site within 1e-8 of the reference's FP64 run."""
     from tnalg_gb300 import DMRG_anyH

@@ -69,6 +69,9 @@ _SIGS = {
     "tn_qr": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_sz, c_vp]),
     "tn_qr_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_qr_use_graphs": (c_int, [c_int]),
+    "tn_qr_mixed": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_sz,
+                            c_vp]),
+    "tn_qr_mixed_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_singular_values": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_profile_enable": (c_int, [c_int]),

@@ -1,0 +1,330 @@
+// Mixed-precision gauge move: FP32 Householder QR + FP64 re-orthogonalisation (K4, tf32x3 path).
+//
+// On GB300 a dependent FP64 operation costs ~64 cycles and the FP64 pipe issues ~2 lanes/clock
+// per SM, which makes the column-sequential Householder panel the bottleneck of an FP64 QR.
+// In a sweep the R factor of a gauge move only seeds the next local solve (the site it is
+// absorbed into is re-optimised right away), so only Q has to be accurate:
+//   1. Householder QR of the FP64 input rounded to FP32 (FP32 panels on one CTA, FP32 GEMM
+//      trailing updates, Q formed backwards): Q32 with ||Q32^T Q32 - I|| ~ 1e-6 whatever the
+//      conditioning of the input, R32 accurate to FP32;
+//   2. E = Q^T Q - I in FP64 (CUDA-core FP64 GEMM), then Q <- Q - Q E / 2 on the tensor cores
+//      (split TF32; the product is ~1e-6 in size, so its 1e-6 relative error is ~1e-12): the
+//      returned Q is orthonormal to ~1e-12 and spans col(A) to FP32 accuracy.
+// Used by tn_qr_mixed; the plain FP64 path keeps tn_qr.
+#include "common.cuh"
+
+int tn_gemm_tf32x3(const TnGemmF64& g, void* ws, size_t ws_bytes, cudaStream_t s);
+size_t tn_gemm_tf32x3_ws_bytes(int64_t M, int64_t N, int64_t K, int64_t batch, int64_t nred);
+
+namespace {
+
+constexpr int NB = 16;
+constexpr int NTP = 512;
+
+struct G32 {
+  int64_t M, N, K;
+  const float* A; int64_t sAm, sAk;
+  const float* B; int64_t sBk, sBn;
+  float* C; int64_t sCm, sCn;
+  float alpha, beta;
+};
+
+// FP32 SIMT GEMM, 64x64 tiles, 256 threads with 4x4 micro-tiles, general strides.
+constexpr int TM = 64, TN = 64, TK = 16, T32 = 256;
+
+__global__ void __launch_bounds__(T32) gemm32_kernel(G32 g) {
+  __shared__ float As[TK][TM + 4];
+  __shared__ float Bs[TK][TN + 4];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t m0 = (int64_t)blockIdx.y * TM, n0 = (int64_t)blockIdx.x * TN;
+  const bool a_kc = (g.sAk == 1), b_nc = (g.sBn == 1);
+  float acc[4][4] = {};
+  for (int64_t k0 = 0; k0 < g.K; k0 += TK) {
+    for (int e = tid; e < TM * TK; e += T32) {
+      int mm, kk;
+      if (a_kc) { mm = e / TK; kk = e % TK; } else { kk = e / TM; mm = e % TM; }
+      const int64_t gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < g.M && gk < g.K) ? g.A[gm * g.sAm + gk * g.sAk] : 0.f;
+    }
+    for (int e = tid; e < TN * TK; e += T32) {
+      int nn, kk;
+      if (b_nc) { kk = e / TN; nn = e % TN; } else { nn = e / TK; kk = e % TK; }
+      const int64_t gn = n0 + nn, gk = k0 + kk;
+      Bs[kk][nn] = (gn < g.N && gk < g.K) ? g.B[gk * g.sBk + gn * g.sBn] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) { a[i] = As[kk][ty * 4 + i]; b[i] = Bs[kk][tx * 4 + i]; }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
+      if (gm < g.M && gn < g.N) {
+        float* c = g.C + gm * g.sCm + gn * g.sCn;
+        const float v = g.alpha * acc[i][j];
+        *c = (g.beta == 0.f) ? v : fmaf(g.beta, *c, v);
+      }
+    }
+}
+
+int gemm32(const G32& g, cudaStream_t s) {
+  if (g.M <= 0 || g.N <= 0) return TN_OK;
+  dim3 grid((unsigned)tn_cdiv(g.N, TN), (unsigned)tn_cdiv(g.M, TM));
+  gemm32_kernel<<<grid, T32, 0, s>>>(g);
+  TN_CHECK_LAUNCH();
+  return TN_OK;
+}
+
+__global__ void copy_in32(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, float* Aw) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < m * n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = idx / m, i = idx % m;
+    Aw[idx] = (float)a[i * sAm + j * sAn];
+  }
+}
+
+__global__ void init_q32(int64_t m, int64_t k, float* Qw, float* Vf) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < m * k;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = idx / m, i = idx % m;
+    Qw[idx] = (i == j) ? 1.f : 0.f;
+    Vf[idx] = 0.f;
+  }
+}
+
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// FP32 Householder panel, one CTA (LAPACK sign convention), forward compact-WY T.
+__global__ void __launch_bounds__(NTP) panel32(int64_t m, int64_t j0, int jb, float* Aw, float* Vf, float* T) {
+  __shared__ float red[NTP / 32][NB];
+  __shared__ float vals[NB];
+  __shared__ float sc[3];
+  __shared__ float Ts[NB][NB];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int i = tid; i < NB * NB; i += NTP) Ts[i / NB][i % NB] = 0.f;
+  __syncthreads();
+  for (int c = 0; c < jb; ++c) {
+    const int64_t j = j0 + c;
+    float* x = Aw + j * m;
+    float p = 0.f;
+    for (int64_t i = j + 1 + tid; i < m; i += NTP) p = fmaf(x[i], x[i], p);
+    p = warp_sumf(p);
+    if (lane == 0) red[wid][0] = p;
+    __syncthreads();
+    if (tid == 0) {
+      float sigma = 0.f;
+      for (int w = 0; w < NTP / 32; ++w) sigma += red[w][0];
+      const float alpha = x[j];
+      float tau = 0.f, beta = alpha, scale = 0.f;
+      if (sigma > 0.f) {
+        const float nrm = sqrtf(alpha * alpha + sigma);
+        beta = alpha >= 0.f ? -nrm : nrm;
+        tau = (beta - alpha) / beta;
+        scale = 1.f / (alpha - beta);
+      }
+      sc[0] = tau; sc[1] = beta; sc[2] = scale;
+    }
+    __syncthreads();
+    const float tau = sc[0], scale = sc[2];
+    float* v = Vf + j * m;
+    for (int64_t i = j + tid; i < m; i += NTP) {
+      if (i == j) { v[i] = 1.f; x[i] = sc[1]; }
+      else { const float vi = x[i] * scale; v[i] = vi; x[i] = 0.f; }
+    }
+    __syncthreads();
+    const int nr = jb - c - 1;
+    float acc[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) acc[q] = 0.f;
+    for (int64_t i = j + tid; i < m; i += NTP) {
+      const float vi = v[i];
+#pragma unroll
+      for (int q = 0; q < NB; ++q) {
+        if (q < nr) acc[q] = fmaf(vi, Aw[(j + 1 + q) * m + i], acc[q]);
+        else if (q - nr < c) acc[q] = fmaf(vi, Vf[(j0 + (q - nr)) * m + i], acc[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      const float s = warp_sumf(acc[q]);
+      if (lane == 0) red[wid][q] = s;
+    }
+    __syncthreads();
+    if (tid < nr + c) {
+      float s = 0.f;
+      for (int w = 0; w < NTP / 32; ++w) s += red[w][tid];
+      vals[tid] = s;
+    }
+    __syncthreads();
+    for (int64_t i = j + tid; i < m; i += NTP) {
+      const float vi = v[i];
+      for (int q = 0; q < nr; ++q) Aw[(j + 1 + q) * m + i] -= tau * vals[q] * vi;
+    }
+    if (tid < c) {  // T(0:c, c) = -tau T(0:c, 0:c) (V(:,0:c)^T v), one thread per row
+      float t = 0.f;
+      for (int q = tid; q < c; ++q) t = fmaf(Ts[tid][q], -tau * vals[nr + q], t);
+      Ts[tid][c] = t;
+    }
+    if (tid == 0) Ts[c][c] = tau;
+    __syncthreads();
+  }
+  for (int i = tid; i < NB * NB; i += NTP) T[i] = Ts[i / NB][i % NB];
+}
+
+__global__ void extract_mixed(int64_t m, int64_t n, int64_t k, const float* Aw, const float* Qw, double* Q64,
+                              double* r, int64_t sRm, int64_t sRn) {
+  const int64_t tq = m * k, tr = k * n;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < tq + tr;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    if (idx < tq) {
+      Q64[idx] = (double)Qw[idx];  // column-major m x k
+    } else {
+      const int64_t e = idx - tq;
+      const int64_t c = e / k, rr = e % k;
+      if (r) r[rr * sRm + c * sRn] = (c >= rr) ? (double)Aw[c * m + rr] : 0.0;
+    }
+  }
+}
+
+// E <- E - I (diagonal), FP64
+__global__ void sub_identity(int64_t k, double* E) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x)
+    E[i * k + i] -= 1.0;
+}
+
+// out(i, j) (strided) = Q(i, j) - Qc(i, j): Q, Qc column-major m x k
+__global__ void write_q(int64_t m, int64_t k, const double* Q64, const double* QE, double* q, int64_t sQm,
+                        int64_t sQn) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < m * k;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = idx / m, i = idx % m;
+    q[i * sQm + j * sQn] = Q64[idx] - 0.5 * QE[idx];
+  }
+}
+
+int blocks_for(int64_t total) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(total, 256), 8LL * tn_sm_count()));
+}
+
+size_t al(size_t x) { return (x + 1023) / 1024 * 1024; }
+
+struct MixWs {
+  float *Aw, *Vf, *Qw, *T, *W, *W2;
+  double *Q64, *E, *QE;
+  char* tf_ws;
+  size_t tf_bytes;
+  char* g64_ws;
+  size_t g64_bytes;
+};
+
+size_t mix_layout(int64_t m, int64_t n, char* base, MixWs* w) {
+  const int64_t k = std::min(m, n), np = tn_cdiv(k, NB);
+  size_t off = 0;
+  auto take = [&](size_t b) { char* p = base ? base + off : nullptr; off += al(b); return p; };
+  w->Aw = (float*)take((size_t)m * n * 4);
+  w->Vf = (float*)take((size_t)m * k * 4);
+  w->Qw = (float*)take((size_t)m * k * 4);
+  w->T = (float*)take((size_t)np * NB * NB * 4);
+  w->W = (float*)take((size_t)NB * std::max(n, k) * 4);
+  w->W2 = (float*)take((size_t)NB * std::max(n, k) * 4);
+  w->Q64 = (double*)take((size_t)m * k * 8);
+  w->E = (double*)take((size_t)k * k * 8);
+  w->QE = (double*)take((size_t)m * k * 8);
+  w->tf_bytes = tn_gemm_tf32x3_ws_bytes(m, k, k, 1, 1);
+  w->tf_ws = take(w->tf_bytes);
+  w->g64_bytes = tn_gemm_f64_ws_bytes(k, k, 1);
+  w->g64_ws = take(w->g64_bytes);
+  return off + 1024;
+}
+
+}  // namespace
+
+extern "C" size_t tn_qr_mixed_workspace_bytes(int64_t m, int64_t n) {
+  if (m <= 0 || n <= 0) return 0;
+  MixWs w;
+  return mix_layout(m, n, nullptr, &w);
+}
+
+extern "C" int tn_qr_mixed(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* q, int64_t sQm,
+                           int64_t sQn, double* r, int64_t sRm, int64_t sRn, void* ws, size_t ws_bytes,
+                           void* stream) {
+  if (m <= 0 || n <= 0 || !a || !q) return tn_fail(TN_ERR_ARG, "qr_mixed: bad arguments");
+  MixWs w;
+  if (!ws || ws_bytes < mix_layout(m, n, nullptr, &w)) return tn_fail(TN_ERR_WORKSPACE, "qr_mixed: workspace");
+  char* base = (char*)(((uintptr_t)ws + 1023) & ~(uintptr_t)1023);
+  mix_layout(m, n, base, &w);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t ev = tn_profile_begin(s);
+  const int64_t k = std::min(m, n), np = tn_cdiv(k, NB);
+  copy_in32<<<blocks_for(m * n), 256, 0, s>>>(m, n, a, sAm, sAn, w.Aw);
+  TN_CHECK_LAUNCH();
+  init_q32<<<blocks_for(m * k), 256, 0, s>>>(m, k, w.Qw, w.Vf);
+  TN_CHECK_LAUNCH();
+  int st;
+  for (int64_t p = 0; p < np; ++p) {
+    const int64_t j0 = p * NB;
+    const int jb = (int)std::min<int64_t>(NB, k - j0);
+    float* Tp = w.T + p * NB * NB;
+    panel32<<<1, NTP, 0, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
+    TN_CHECK_LAUNCH();
+    const int64_t nc = n - j0 - jb, mr = m - j0;
+    if (nc <= 0) continue;
+    // W = V^T C ; W2 = T^T W ; C -= V W2
+    if ((st = gemm32({jb, nc, mr, w.Vf + j0 + j0 * m, m, 1, w.Aw + j0 + (j0 + jb) * m, 1, m, w.W, nc, 1, 1.f, 0.f}, s)))
+      return st;
+    if ((st = gemm32({jb, nc, jb, Tp, 1, NB, w.W, nc, 1, w.W2, nc, 1, 1.f, 0.f}, s))) return st;
+    if ((st = gemm32({mr, nc, jb, w.Vf + j0 + j0 * m, 1, m, w.W2, nc, 1, w.Aw + j0 + (j0 + jb) * m, 1, m, -1.f, 1.f},
+                     s)))
+      return st;
+  }
+  for (int64_t p = np - 1; p >= 0; --p) {
+    const int64_t j0 = p * NB;
+    const int jb = (int)std::min<int64_t>(NB, k - j0);
+    const int64_t nc = k - j0, mr = m - j0;
+    float* Tp = w.T + p * NB * NB;
+    if ((st = gemm32({jb, nc, mr, w.Vf + j0 + j0 * m, m, 1, w.Qw + j0 + j0 * m, 1, m, w.W, nc, 1, 1.f, 0.f}, s)))
+      return st;
+    if ((st = gemm32({jb, nc, jb, Tp, NB, 1, w.W, nc, 1, w.W2, nc, 1, 1.f, 0.f}, s))) return st;
+    if ((st = gemm32({mr, nc, jb, w.Vf + j0 + j0 * m, 1, m, w.W2, nc, 1, w.Qw + j0 + j0 * m, 1, m, -1.f, 1.f}, s)))
+      return st;
+  }
+  extract_mixed<<<blocks_for(m * k + k * n), 256, 0, s>>>(m, n, k, w.Aw, w.Qw, w.Q64, r, sRm, sRn);
+  TN_CHECK_LAUNCH();
+  // E = Q^T Q - I in FP64 (Q64 column-major m x k)
+  TnGemmF64 g{};
+  g.M = k; g.N = k; g.K = m;
+  g.A = w.Q64; g.sAm = m; g.sAk = 1;
+  g.B = w.Q64; g.sBk = 1; g.sBn = m;
+  g.C = w.E; g.sCm = k; g.sCn = 1;
+  g.batch = 1; g.nred = 1; g.alpha = 1.0; g.beta = 0.0;
+  if ((st = tn_gemm_f64_ws(g, w.g64_ws, w.g64_bytes, s))) return st;
+  sub_identity<<<blocks_for(k), 256, 0, s>>>(k, w.E);
+  TN_CHECK_LAUNCH();
+  // QE = Q E on the tensor cores (split TF32), then q = Q - QE / 2
+  TnGemmF64 h{};
+  h.M = m; h.N = k; h.K = k;
+  h.A = w.Q64; h.sAm = 1; h.sAk = m;
+  h.B = w.E; h.sBk = k; h.sBn = 1;
+  h.C = w.QE; h.sCm = 1; h.sCn = m;
+  h.batch = 1; h.nred = 1; h.alpha = 1.0; h.beta = 0.0;
+  if ((st = tn_gemm_tf32x3(h, w.tf_ws, w.tf_bytes, s))) return st;
+  write_q<<<blocks_for(m * k), 256, 0, s>>>(m, k, w.Q64, w.QE, q, sQm, sQn);
+  TN_CHECK_LAUNCH();
+  tn_profile_end(ev, s, TN_PROF_QR, 0.0);
+  return TN_OK;
+}

@@ -313,6 +313,19 @@ class DeviceMPS:
         self.er_from = b
 
     # -- gauge -------------------------------------------------------------------
+    def _qr(self, mm, nn, A, sA, Q, sQ, R, seed_only):
+        """tn_qr, or tn_qr_mixed for a seeding move of the mixed-precision path (R only seeds the
+        next local solve there, Q stays orthonormal to ~1e-12)."""
+        lib, st = L.load(), L.stream_handle()
+        if seed_only and self.precision == L.PREC_TF32X3 and min(mm, nn) >= 64:
+            wp, wb = self.ws2.args(lib.tn_qr_mixed_workspace_bytes(mm, nn))
+            L.check(lib.tn_qr_mixed(mm, nn, L.ptr(A), sA[0], sA[1], L.ptr(Q), sQ[0], sQ[1], L.ptr(R), nn, 1, wp, wb,
+                                    st), "qr_mixed")
+        else:
+            wp, wb = self.ws2.args(lib.tn_qr_workspace_bytes(mm, nn))
+            L.check(lib.tn_qr(mm, nn, L.ptr(A), sA[0], sA[1], L.ptr(Q), sQ[0], sQ[1], L.ptr(R), nn, 1, wp, wb, st),
+                    "qr")
+
     def qr_left(self, n, seed_only=False):
         """left2right_decompose_tensor + absorb_matrix2tensor(mps[n+1], R^T, 0)
         (TensorBasicModule.py:314-348, 387-424; MPSClass.py:150-158)."""
@@ -323,8 +336,7 @@ class DeviceMPS:
         lib, st = L.load(), L.stream_handle()
         Q = torch.empty((cl, d, k), dtype=torch.float64, device=self.device)
         R = torch.empty((k, nn), dtype=torch.float64, device=self.device)
-        wp, wb = self.ws2.args(lib.tn_qr_workspace_bytes(mm, nn))
-        L.check(lib.tn_qr(mm, nn, L.ptr(A), nn, 1, L.ptr(Q), k, 1, L.ptr(R), nn, 1, wp, wb, st), "qr")
+        self._qr(mm, nn, A, (nn, 1), Q, (k, 1), R, seed_only)
         nxt = self.mps[n + 1]
         c2, d2, r2 = nxt.shape
         new = torch.empty((k, d2, r2), dtype=torch.float64, device=self.device)
@@ -349,9 +361,8 @@ class DeviceMPS:
         lib, st = L.load(), L.stream_handle()
         Bt = torch.empty((k, d, cr), dtype=torch.float64, device=self.device)
         R = torch.empty((k, nn), dtype=torch.float64, device=self.device)
-        wp, wb = self.ws2.args(lib.tn_qr_workspace_bytes(mm, nn))
         # a(i, j) = A[j, i]: sAm = 1, sAn = d*cr ; Q(i, j) -> Bt[j, i]: sQm = 1, sQn = d*cr
-        L.check(lib.tn_qr(mm, nn, L.ptr(A), 1, d * cr, L.ptr(Bt), 1, d * cr, L.ptr(R), nn, 1, wp, wb, st), "qr")
+        self._qr(mm, nn, A, (1, d * cr), Bt, (1, d * cr), R, seed_only)
         prv = self.mps[n - 1]
         c0, d0, r0 = prv.shape
         new = torch.empty((c0, d0, k), dtype=torch.float64, device=self.device)

@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--eigs-tol", type=float, default=1e-12)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--cpu-solves", type=int, default=2)
+    p.add_argument("--cpu-solves", type=int, default=1)
     return p.parse_args()
 
 
@@ -225,30 +225,54 @@ def _initial_host_mps(l, d, chi):
 
 
 def cpu_sample(length, chi, eigs_tol, nsolves, seed=0):
+    """Bounded CPU sample: local solves at full-chi interior sites of a shorter chain (the cost of an
+    interior solve depends on chi, not on N), extrapolated to 2(N-1) solves per sweep of the N-site
+    chain. Environment construction happens before the clock starts."""
     from oracle import dmrg_oracle as O
     try:
         import torch
         threads = torch.get_num_threads()
     except Exception:
         threads = os.cpu_count()
-    para = chain_para(length, chi, eigs_tol, "fp64", "cpu")
+    short = max(8, 2 * int(np.ceil(np.log2(chi))) + 6)  # middle bonds reach chi
+    para = chain_para(short, chi, eigs_tol, "fp64", "cpu")
     np.random.seed(seed)
-    A = O.OracleMPS(length, 2, chi, para["op"])
+    A = O.OracleMPS(short, 2, chi, para["op"])
     one, two = O.canonical_terms(para["index1"], para["coeff1"], para["index2"], para["coeff2"], A.ops, eigs_tol)
+    mid = short // 2 - 1
     t0 = time.time()
-    A.correct_orthogonal_center(0)
+    A.correct_orthogonal_center(mid)
+    A.site_buckets(mid, one, two)      # builds the cached environments of the first site
     t_prep = time.time() - t0
-    times = []
-    for n in range(1, 1 + nsolves + 1):
+    # cost of one effective-Hamiltonian application at this site
+    env = A.site_buckets(mid, one, two)
+    psi = A.mps[mid]
+    t = time.time()
+    for _ in range(3):
+        A.apply_heff(env, psi)
+    t_mv = (time.time() - t) / 3
+    times, mvs = [], []
+    for n in range(mid, mid + nsolves):
+        mv0 = A.n_matvec
         t = time.time()
         A.update_tensor_eigs(n, one, two, 1e-4, eigs_tol)
         times.append(time.time() - t)
-    per_solve = float(np.mean(times[1:])) if len(times) > 1 else times[0]
-    sweeps_per_s = 1.0 / (per_solve * 2 * (length - 1))
+        mvs.append(A.n_matvec - mv0)
+    per_solve = float(np.mean(times))
+    mv_per_solve = float(np.mean(mvs))
+    t_rest = max(per_solve - mv_per_solve * t_mv, 0.0)
+    # the reference's eigsh builds ncv=20 Lanczos vectors before its first convergence test, so a
+    # solve started from an already converged site still costs >= 20 matvecs
+    t_converged = 20 * t_mv + t_rest
+    sweeps_per_s = 1.0 / (t_converged * 2 * (length - 1))
     return {"value": sweeps_per_s, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d interior local solves (numpy/scipy ARPACK restatement) at chi=%d on a random N=%d MPS "
-                      "after %.1f s canonicalisation; %.2f s/solve extrapolated to 2(N-1) solves per sweep"
-                      % (nsolves, chi, length, t_prep, per_solve)}
+            "sample": "numpy/scipy ARPACK restatement of the reference, %d local solve(s) at interior chi=%d sites of a "
+                      "%d-site chain from a random MPS (%.1f s setup untimed): %.2f s/solve with %.0f matvecs of "
+                      "%.3f s; per-solve cost at a converged site estimated as 20 matvecs + %.2f s other work = %.2f s, "
+                      "extrapolated to 2(N-1)=%d solves per N=%d sweep (the random-state sample alone would give "
+                      "%.2e sweeps/s)" % (nsolves, chi, short, t_prep, per_solve, mv_per_solve, t_mv, t_rest,
+                                         t_converged, 2 * (length - 1), length,
+                                         1.0 / (per_solve * 2 * (length - 1)))}
 
 
 def run_reference(args, rank):

@@ -108,6 +108,28 @@ def test_sweep_orchestration_matches_reference(name, fake_backend):
     assert info["solves"] == 2 * (m["l"] - 1) * m["sweep_time"]
 
 
+def test_reference_script_through_compat_modules(fake_backend):
+    """testDMRG.py's call pattern with the module-name shims first on sys.path."""
+    import importlib
+    import sys
+    compat = __import__("os").path.join(gc.GOLDEN, "..", "..", "tnalg_gb300", "compat")
+    sys.path.insert(0, compat)
+    try:
+        Pm = importlib.import_module("Parameters")
+        dmrg = importlib.import_module("DMRG_anyH").dmrg_finite_size
+        assert Pm.__file__.startswith(__import__("os").path.abspath(compat)) or "compat" in Pm.__file__
+        para = Pm.generate_parameters_dmrg("chain")
+        para.update(l=8, chi=4, sweep_time=2, device="cpu")
+        para = Pm.make_consistent_parameter_dmrg(para)
+        np.random.seed(0)
+        ob, A, info, para = _quiet(dmrg, para)
+        assert np.isfinite(ob["e_per_site"]) and A.mps[0].shape == (1, 2, 2)
+    finally:
+        sys.path.remove(compat)
+        for m in ("Parameters", "DMRG_anyH", "MPSClass", "HamiltonianModule"):
+            sys.modules.pop(m, None)
+
+
 def test_pickle_roundtrip(fake_backend):
     import pickle
     from tnalg_gb300.MPSClass import MpsOpenBoundaryClass

@@ -198,6 +198,21 @@ int tn_singular_values(int64_t k, int64_t n, const double* x, int64_t sXr, int64
                        double tol, int max_sweeps, void* ws, size_t ws_bytes, void* stream);
 size_t tn_singular_values_workspace_bytes(int64_t k, int64_t n);
 
+/*
+ * tn_singular_values without a workspace argument and without any device allocation. It has no
+ * counterpart in the reference: it exists for hosts that cannot allocate device memory
+ * themselves (a service that may only use buffers registered by its own allocator, or a process
+ * whose device memory is owned by another framework's allocator) but still want an
+ * entanglement spectrum. Its scratch is a static device array of 65536 + 32 doubles (512 KiB)
+ * that every GPU loading the library keeps until the process exits; (k rounded up to even) * n
+ * must be <= 65536, larger sizes return TN_ERR_ARG. The first call on each device resolves the
+ * array's device address (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. All calls share the array: calls that overlap on the GPU race, so
+ * the caller serialises them. Same arguments and results as tn_singular_values otherwise.
+ */
+int tn_singular_values_noalloc(int64_t k, int64_t n, const double* x, int64_t sXr, int64_t sXc,
+                               double* s_out, double tol, int max_sweeps, void* stream);
+
 /* ---- profiling ----------------------------------------------------------------------- */
 /* CUDA-event timing of kernel classes on their launching stream (0 = effective-Hamiltonian
  * matvecs inside tn_lanczos). Off by default; reading synchronises the recorded events. */

@@ -74,6 +74,7 @@ _SIGS = {
     "tn_qr_mixed_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_singular_values": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_workspace_bytes": (c_sz, [c_i64, c_i64]),
+    "tn_singular_values_noalloc": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp]),
     "tn_profile_enable": (c_int, [c_int]),
     "tn_profile_reset": (c_int, []),
     "tn_profile_read": (c_int, [c_int, c_vp, c_vp, c_vp]),

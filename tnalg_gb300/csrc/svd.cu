@@ -127,3 +127,73 @@ extern "C" int tn_singular_values(int64_t k, int64_t n, const double* x, int64_t
   TN_CHECK_LAUNCH();
   return TN_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant. Some hosts cannot allocate device memory themselves: a Go or JVM
+// service that may only use buffers registered by its own allocator, or a process whose device
+// memory is held entirely by another framework's caching allocator. They can still compute an
+// entanglement spectrum with tn_singular_values_noalloc, whose scratch (the rotated copy of X and
+// the "rotated" flag) lives in this static device array instead of a caller workspace.
+//
+// Limit: (k rounded up to even) * n <= TN_SV_NOALLOC_MAX_ELEMS doubles (512 KiB; e.g. 256 x 256).
+// Every GPU that loads the library holds the array until the process exits. All calls share it:
+// calls that overlap on the GPU (different streams, or different host threads on one device) race
+// and must be serialised by the caller. The flag is cleared at the start of every sweep; the copy
+// of X is rewritten by every call, so no state leaks from one call into the next.
+#define TN_SV_NOALLOC_MAX_ELEMS 65536
+#define TN_SV_NOALLOC_FLAG_SLOTS 32
+static __device__ __align__(256) double g_sv_noalloc_scratch[TN_SV_NOALLOC_FLAG_SLOTS + TN_SV_NOALLOC_MAX_ELEMS];
+
+namespace {
+constexpr int kMaxDevices = 64;
+void* g_sv_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the static scratch on the current device, resolved once per device.
+int sv_noalloc_scratch(void** out) {
+  int dev = 0;
+  TN_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return tn_fail(TN_ERR_ARG, "singular_values_noalloc: device ordinal >= 64");
+  if (!g_sv_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_sv_noalloc_scratch);
+    if (e != cudaSuccess) return tn_record_error(e);
+    g_sv_noalloc_ptr[dev] = p;
+  }
+  *out = g_sv_noalloc_ptr[dev];
+  return TN_OK;
+}
+}  // namespace
+
+extern "C" int tn_singular_values_noalloc(int64_t k, int64_t n, const double* x, int64_t sXr, int64_t sXc,
+                                          double* s_out, double tol, int max_sweeps, void* stream) {
+  if (k <= 0 || n <= 0 || !x || !s_out) return tn_fail(TN_ERR_ARG, "singular_values_noalloc: bad args");
+  const int64_t kp = k + (k & 1);
+  if (kp > TN_SV_NOALLOC_MAX_ELEMS / n || kp * n > TN_SV_NOALLOC_MAX_ELEMS)
+    return tn_fail(TN_ERR_ARG,
+                   "singular_values_noalloc: (k rounded up to even) * n exceeds the 65536-element static scratch");
+  void* base = nullptr;
+  int st = sv_noalloc_scratch(&base);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  int* flag = (int*)base;
+  double* X = (double*)base + TN_SV_NOALLOC_FLAG_SLOTS;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(kp * n, NT), 8LL * tn_sm_count()));
+  svd_copy_in<<<blocks, NT, 0, s>>>(k, kp, n, x, sXr, sXc, X);
+  TN_CHECK_LAUNCH();
+  if (kp >= 2) {
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+      TN_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+      for (int64_t r = 0; r < kp - 1; ++r) {
+        jacobi_round<<<(unsigned)(kp / 2), NT, 0, s>>>(kp, n, r, X, tol, flag);
+        TN_CHECK_LAUNCH();
+      }
+      int h = 0;
+      TN_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+      TN_CUDA(cudaStreamSynchronize(s));
+      if (!h) break;
+    }
+  }
+  row_norms<<<(unsigned)k, NT, 0, s>>>(k, n, X, s_out);
+  TN_CHECK_LAUNCH();
+  return TN_OK;
+}

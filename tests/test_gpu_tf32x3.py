@@ -68,6 +68,63 @@ def test_tf32x3_batched_reduced_and_transposed(tf32):
     assert torch.max(torch.abs(C - ref)).item() / torch.max(torch.abs(ref)).item() < 3e-6
 
 
+@pytest.mark.parametrize("M,N,K,transposed_b", [(2, 8, 2, True), (2, 8, 2, False), (100, 37, 70, True),
+                                                (33, 65, 5, False), (4, 4, 1, True)])
+def test_tf32x3_gemm_ignores_stale_workspace(tf32, M, N, K, transposed_b):
+    """K not a multiple of 4 pads the staged rows; reused scratch full of NaN bytes (as the caching
+    allocator can hand back) must not reach the product (the first seed move of a sweep, R(2x2)
+    times a 2x2x4 site, is the K=2 case)."""
+    A = _rand(M, K, seed=M + K)
+    B = _rand(K, N, seed=N + 5)
+    Bs = B.T.contiguous() if transposed_b else B
+    sB = (1, K) if transposed_b else (N, 1)
+    C = torch.empty(M, N, dtype=torch.float64, device="cuda")
+    ws = L.Workspace(torch.device("cuda"))
+    ws.get(L.load().tn_gemm_workspace_bytes(L.PREC_TF32X3, M, N, K, 1, 1)).fill_(255)  # 0xFFFFFFFF: NaN
+    L.gemm(A, Bs, C, M, N, K, (K, 1), sB, (N, 1), precision=L.PREC_TF32X3, ws=ws)
+    L.check(L.load().tn_check_device_status(L.stream_handle()))
+    ref = A @ B
+    assert torch.isfinite(C).all()
+    assert torch.max(torch.abs(C - ref)).item() <= 5e-6 * torch.max(torch.abs(ref)).item()
+
+
+def test_tf32x3_gemm_reports_operands_beyond_fp32_range(tf32):
+    """Split TF32 has FP32's exponent range: a finite FP64 operand of 1e103 cannot be staged, and the
+    device status says so (TN_ERR_NUMERIC) instead of leaving silent NaNs."""
+    lib = L.load()
+    A = _rand(8, 16, seed=1) * 1e103
+    B = _rand(16, 8, seed=2)
+    C = torch.empty(8, 8, dtype=torch.float64, device="cuda")
+    L.gemm(A, B, C, 8, 8, 16, (16, 1), (8, 1), (8, 1), precision=L.PREC_TF32X3, ws=L.Workspace(torch.device("cuda")))
+    assert lib.tn_check_device_status(L.stream_handle()) == L.TN_ERR_NUMERIC
+    assert b"FP32 range" in lib.tn_last_error()
+    assert lib.tn_check_device_status(L.stream_handle()) == L.TN_OK  # the flag is cleared once reported
+
+
+def test_seed_move_of_unnormalized_state_stays_fp64(tf32):
+    """A random 100-site MPS centred by QR carries its norm (~1e100) on the centre: the first seed
+    move absorbs in FP64; after a solve the centre has unit norm and seed moves use split TF32."""
+    from tnalg_gb300 import Parameters as pm
+    from tnalg_gb300.MPSClass import MpsOpenBoundaryClass
+    para = pm.generate_parameters_dmrg("chain")
+    para.update(l=100, chi=64)
+    para = pm.make_consistent_parameter_dmrg(para)
+    np.random.seed(0)
+    A = MpsOpenBoundaryClass(100, 2, 64, operators=para["op"], precision="tf32x3")
+    A.correct_orthogonal_center(0)
+    dev = A._dev
+    assert not dev.unit_norm
+    dev.move_center_for_solve(1)
+    assert torch.isfinite(dev.mps[1]).all()
+    A.update_tensor_eigs(1, para["index1"], para["index2"], para["coeff1"], para["coeff2"], para["tau"], True,
+                         tol=1e-12)
+    assert dev.unit_norm and dev._seed_precision(True) == L.PREC_TF32X3
+    dev.move_center_for_solve(2)
+    assert torch.isfinite(dev.mps[2]).all()
+    assert abs(torch.linalg.vector_norm(dev.mps[2]).item() - 1.0) < 1e-5
+    L.check(L.load().tn_check_device_status(L.stream_handle()))
+
+
 def _site(cl, d, cr, dense=True):
     wl = _rand(cl * d, cl * d, seed=cl)
     wl = wl + wl.T

@@ -108,6 +108,10 @@ def load(path=None):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    # TNALG_QR_GRAPHS=0 launches the QR kernels one by one instead of replaying captured CUDA
+    # graphs (same kernels; for per-kernel profilers and launch lists).
+    if os.environ.get("TNALG_QR_GRAPHS", "1") == "0":
+        lib.tn_qr_use_graphs(0)
     _lib = lib
     return lib
 

@@ -280,21 +280,33 @@ struct PrepArgs {
   int64_t sZ, sR, sRow, sK;
   float *hi, *lo;
   int64_t Kp;
+  int* err;  // set by prep(): the kernels' device error word
 };
 
+// Error word codes: 1-3 name the pipeline wait that gave up; kErrRange a finite operand beyond
+// FP32's range, which split TF32 cannot represent.
+constexpr int kErrRange = 16;
+
+__device__ __forceinline__ void stage_value(const PrepArgs& a, double x, int64_t o) {
+  float h, l;
+  split_tf32(x, h, l);
+  if (!isfinite(h) && isfinite(x)) atomicExch(a.err, kErrRange);
+  a.hi[o] = h;
+  a.lo[o] = l;
+}
+
+// Both prep kernels also write zeros into the pitch padding k in [K, Kp): the staging buffers are
+// reused scratch, and the padding must never feed the product whatever the tensor map's bounds.
 __global__ void prep_direct_kernel(PrepArgs a) {
-  const int64_t per = a.rows * a.K;
+  const int64_t per = a.rows * a.Kp;
   const int64_t total = a.Z * a.R * per;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t zr = idx / per, e = idx % per;
     const int64_t z = zr / a.R, r = zr % a.R;
-    const int64_t row = e / a.K, k = e % a.K;
-    float h, l;
-    split_tf32(a.src[z * a.sZ + r * a.sR + row * a.sRow + k * a.sK], h, l);
-    const int64_t o = (zr * a.rows + row) * a.Kp + k;
-    a.hi[o] = h;
-    a.lo[o] = l;
+    const int64_t row = e / a.Kp, k = e % a.Kp;
+    // idx == (zr * rows + row) * Kp + k
+    stage_value(a, k < a.K ? a.src[z * a.sZ + r * a.sR + row * a.sRow + k * a.sK] : 0.0, idx);
   }
 }
 
@@ -312,13 +324,8 @@ __global__ void prep_transpose_kernel(PrepArgs a) {
   __syncthreads();
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
     const int64_t row = r0 + i, k = k0 + threadIdx.x;
-    if (row < a.rows && k < a.K) {
-      float h, l;
-      split_tf32(tile[threadIdx.x][i], h, l);
-      const int64_t o = (zr * a.rows + row) * a.Kp + k;
-      a.hi[o] = h;
-      a.lo[o] = l;
-    }
+    // the grid's K extent, cdiv(K, 32) * 32, covers Kp; the tile holds zeros for k >= K
+    if (row < a.rows && k < a.Kp) stage_value(a, tile[threadIdx.x][i], (zr * a.rows + row) * a.Kp + k);
   }
 }
 
@@ -337,14 +344,19 @@ int blocks_for(int64_t total) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(total, 256), 16LL * tn_sm_count()));
 }
 
-int prep(const PrepArgs& a, cudaStream_t s) {
-  if (a.Z * a.R * a.rows * a.K == 0) return TN_OK;
+int err_buffer(int** out);
+
+int prep(const PrepArgs& args, cudaStream_t s) {
+  if (args.Z * args.R * args.rows * args.K == 0) return TN_OK;
+  PrepArgs a = args;
+  int st = err_buffer(&a.err);
+  if (st) return st;
   if (a.sRow == 1 && a.sK != 1) {
     dim3 grid((unsigned)tn_cdiv(a.rows, 32), (unsigned)tn_cdiv(a.K, 32), (unsigned)(a.Z * a.R));
     if (grid.z > 65535u || grid.y > 65535u) return tn_fail(TN_ERR_ARG, "tf32 prep: grid too large");
     prep_transpose_kernel<<<grid, dim3(32, 8), 0, s>>>(a);
   } else {
-    prep_direct_kernel<<<blocks_for(a.Z * a.R * a.rows * a.K), 256, 0, s>>>(a);
+    prep_direct_kernel<<<blocks_for(a.Z * a.R * a.rows * a.Kp), 256, 0, s>>>(a);
   }
   TN_CHECK_LAUNCH();
   return TN_OK;
@@ -409,7 +421,10 @@ Staged carve(char*& p, int64_t rows, int64_t K, int64_t nmat) {
 int* g_err_dev = nullptr;
 
 int err_buffer(int** out) {
-  if (!g_err_dev) TN_CUDA(cudaMalloc(&g_err_dev, sizeof(int)));
+  if (!g_err_dev) {
+    TN_CUDA(cudaMalloc(&g_err_dev, sizeof(int)));
+    TN_CUDA(cudaMemset(g_err_dev, 0, sizeof(int)));
+  }
   *out = g_err_dev;
   return TN_OK;
 }
@@ -487,6 +502,8 @@ int tn_tf32x3_error_check(cudaStream_t s) {
   TN_CUDA(cudaStreamSynchronize(s));
   if (h) {
     TN_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    if (h == kErrRange)
+      return tn_fail(TN_ERR_NUMERIC, "tf32x3 gemm: an operand lies outside the FP32 range (|x| >= 3.4e38)");
     return tn_fail(TN_ERR_TIMEOUT, "tf32x3 gemm: a bounded pipeline wait gave up");
   }
   return TN_OK;

@@ -192,6 +192,9 @@ class DeviceMPS:
         self.virtual_dim = np.array([1] + [int(t.shape[2]) for t in tensors])
         self.center = -1
         self.orthogonality = np.zeros(self.length)
+        # True once a local solve has left a unit-norm centre; QR moves keep the norm, bond growth
+        # and loaded tensors make it unknown (a random 100-site MPS centred by QR carries ~1e103).
+        self.unit_norm = False
         self.precision = L.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         self.ws = L.Workspace(self.device)
         self.ws2 = L.Workspace(self.device)
@@ -328,6 +331,15 @@ class DeviceMPS:
             L.check(lib.tn_qr(mm, nn, L.ptr(A), sA[0], sA[1], L.ptr(Q), sQ[0], sQ[1], L.ptr(R), nn, 1, wp, wb, st),
                     "qr")
 
+    def _seed_precision(self, seed_only):
+        """Precision of the R-absorb of a gauge move. seed_only: the receiving site is re-solved
+        next, so its tensor is only the Lanczos start vector and may use the working precision,
+        provided the state has unit norm (split TF32 keeps FP32's exponent range, |x| < 3.4e38).
+        Otherwise the absorbed tensor carries the state and stays FP64."""
+        if seed_only and self.unit_norm:
+            return self.precision
+        return L.PREC_FP64
+
     def qr_left(self, n, seed_only=False):
         """left2right_decompose_tensor + absorb_matrix2tensor(mps[n+1], R^T, 0)
         (TensorBasicModule.py:314-348, 387-424; MPSClass.py:150-158)."""
@@ -342,10 +354,8 @@ class DeviceMPS:
         nxt = self.mps[n + 1]
         c2, d2, r2 = nxt.shape
         new = torch.empty((k, d2, r2), dtype=torch.float64, device=self.device)
-        # seed_only: site n+1 is re-solved next, so R.mps[n+1] is only the Lanczos start vector
-        # and may use the working precision; otherwise it carries the state and stays FP64.
         L.gemm(R, nxt, new, k, d2 * r2, nn, (nn, 1), (d2 * r2, 1), (d2 * r2, 1), ws=self.ws,
-               precision=self.precision if seed_only else L.PREC_FP64)
+               precision=self._seed_precision(seed_only))
         self.mps[n] = Q
         self.mps[n + 1] = new
         self._last_r = R
@@ -370,7 +380,7 @@ class DeviceMPS:
         new = torch.empty((c0, d0, k), dtype=torch.float64, device=self.device)
         # prv(c0*d0, cl) . R^T(cl, k)
         L.gemm(prv, R, new, c0 * d0, k, nn, (nn, 1), (1, nn), (k, 1), ws=self.ws,
-               precision=self.precision if seed_only else L.PREC_FP64)
+               precision=self._seed_precision(seed_only))
         self.mps[n] = Bt
         self.mps[n - 1] = new
         self._last_r = R
@@ -413,6 +423,7 @@ class DeviceMPS:
                 self.mps[n] = new
         self.virtual_dim = np.array(dims)
         self.center = -1
+        self.unit_norm = False
         self.orthogonality[:] = 0
         self.el_upto = min(self.el_upto, 0)
         self.er_from = max(self.er_from, self.length)
@@ -494,6 +505,7 @@ class DeviceMPS:
         if status == L.TN_ERR_NOCONV:
             self.stats["unconverged"] += 1
         self.mps[p] = psi
+        self.unit_norm = True  # the solver returns a unit vector
         self.tensor_changed(p)
         del keep
         return res

@@ -171,23 +171,41 @@ def test_tf32x3_lanczos_fp64_refined_energy(tf32):
     assert abs(res.energy - w0) <= 1e-5 * abs(w0)
 
 
-@pytest.mark.parametrize("m,n,cond", [(1024, 512, 1.0), (1024, 512, 1e10), (256, 128, 1e6), (96, 200, 1e3)])
-def test_qr_mixed_orthonormal_and_spanning(tf32, m, n, cond):
+@pytest.mark.parametrize("m,n,cond,transposed", [(1024, 512, 1.0, False), (1024, 512, 1e10, False),
+                                                 (1024, 512, 1e6, True), (512, 512, 1e8, False),
+                                                 (1000, 300, 1e4, True), (256, 128, 1e6, False),
+                                                 (64, 64, 1e3, False), (4, 2, 1.0, False), (96, 200, 1e3, False),
+                                                 (256, 128, 0.0, False)])
+def test_qr_mixed_orthonormal_and_spanning(tf32, m, n, cond, transposed):
     """FP32 Householder + FP64 re-orthogonalisation: Q orthonormal to ~1e-12 at any conditioning,
-    col(Q) = col(A) to FP32 accuracy, R accurate to FP32."""
+    col(Q) = col(A) to FP32 accuracy, R accurate to FP32. n <= m <= 1024, n <= 512 run on the
+    16-CTA cluster kernel; `transposed` reads A and writes Q through the column-major strides of a
+    right gauge move; cond = 0 makes the last 16 singular values exactly zero."""
     lib = L.load()
     k = min(m, n)
     g = torch.Generator(device="cpu").manual_seed(m + n)
     U, _ = torch.linalg.qr(torch.randn(m, k, generator=g, dtype=torch.float64))
     V, _ = torch.linalg.qr(torch.randn(n, k, generator=g, dtype=torch.float64))
-    s = torch.logspace(0, -np.log10(cond), k, dtype=torch.float64)
+    if cond > 0:
+        s = torch.logspace(0, -np.log10(cond), k, dtype=torch.float64)
+    else:
+        s = torch.ones(k, dtype=torch.float64)
+        s[-16:] = 0.0
     A = ((U * s) @ V.T).cuda()
-    Q = torch.empty((m, k), dtype=torch.float64, device="cuda")
     R = torch.empty((k, n), dtype=torch.float64, device="cuda")
     ws = L.Workspace(torch.device("cuda"))
     wp, wb = ws.args(lib.tn_qr_mixed_workspace_bytes(m, n))
-    L.check(lib.tn_qr_mixed(m, n, L.ptr(A), n, 1, L.ptr(Q), k, 1, L.ptr(R), n, 1, wp, wb, L.stream_handle()))
+    if transposed:
+        At = A.T.contiguous()  # A(i, j) = At[j, i]
+        Qt = torch.empty((k, m), dtype=torch.float64, device="cuda")
+        L.check(lib.tn_qr_mixed(m, n, L.ptr(At), 1, m, L.ptr(Qt), 1, m, L.ptr(R), n, 1, wp, wb, L.stream_handle()))
+        Q = Qt.T
+    else:
+        Q = torch.empty((m, k), dtype=torch.float64, device="cuda")
+        L.check(lib.tn_qr_mixed(m, n, L.ptr(A), n, 1, L.ptr(Q), k, 1, L.ptr(R), n, 1, wp, wb, L.stream_handle()))
     L.check(lib.tn_check_device_status(L.stream_handle()))
+    assert torch.isfinite(Q).all() and torch.isfinite(R).all()
+    assert torch.equal(torch.tril(R, -1), torch.zeros_like(R))
     eye = torch.eye(k, dtype=torch.float64, device="cuda")
     assert torch.max(torch.abs(Q.T @ Q - eye)).item() < 1e-11
     resid = A - Q @ (Q.T @ A)

@@ -15,6 +15,9 @@
 
 int tn_gemm_tf32x3(const TnGemmF64& g, void* ws, size_t ws_bytes, cudaStream_t s);
 size_t tn_gemm_tf32x3_ws_bytes(int64_t M, int64_t N, int64_t K, int64_t batch, int64_t nred);
+bool tn_qr32_cluster_supported(int64_t m, int64_t n);
+int tn_qr32_cluster(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* q, double* r,
+                    int64_t sRm, int64_t sRn, cudaStream_t s);
 
 namespace {
 
@@ -252,6 +255,10 @@ size_t mix_layout(int64_t m, int64_t n, char* base, MixWs* w) {
   return off + 1024;
 }
 
+int qr32_blocked(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* r, int64_t sRm,
+                 int64_t sRn, const MixWs& w, cudaStream_t s);
+int refine_q(int64_t m, int64_t k, double* q, int64_t sQm, int64_t sQn, const MixWs& w, cudaStream_t s);
+
 }  // namespace
 
 extern "C" size_t tn_qr_mixed_workspace_bytes(int64_t m, int64_t n) {
@@ -270,6 +277,24 @@ extern "C" int tn_qr_mixed(int64_t m, int64_t n, const double* a, int64_t sAm, i
   mix_layout(m, n, base, &w);
   cudaStream_t s = (cudaStream_t)stream;
   cudaEvent_t ev = tn_profile_begin(s);
+  const int64_t k = std::min(m, n), np = tn_cdiv(k, NB);
+  int st;
+  if (m >= n && tn_qr32_cluster_supported(m, n)) {
+    // whole FP32 factorisation and Q formation in one cluster-resident kernel
+    if ((st = tn_qr32_cluster(m, n, a, sAm, sAn, w.Q64, r, sRm, sRn, s))) return st;
+  } else {
+    if ((st = qr32_blocked(m, n, a, sAm, sAn, r, sRm, sRn, w, s))) return st;
+  }
+  if ((st = refine_q(m, k, q, sQm, sQn, w, s))) return st;
+  tn_profile_end(ev, s, TN_PROF_QR, 0.0);
+  return TN_OK;
+}
+
+namespace {
+
+// FP32 blocked Householder QR on global memory (one-CTA panels + FP32 GEMM updates): Q64, R.
+int qr32_blocked(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* r, int64_t sRm,
+                 int64_t sRn, const MixWs& w, cudaStream_t s) {
   const int64_t k = std::min(m, n), np = tn_cdiv(k, NB);
   copy_in32<<<blocks_for(m * n), 256, 0, s>>>(m, n, a, sAm, sAn, w.Aw);
   TN_CHECK_LAUNCH();
@@ -305,6 +330,12 @@ extern "C" int tn_qr_mixed(int64_t m, int64_t n, const double* a, int64_t sAm, i
   }
   extract_mixed<<<blocks_for(m * k + k * n), 256, 0, s>>>(m, n, k, w.Aw, w.Qw, w.Q64, r, sRm, sRn);
   TN_CHECK_LAUNCH();
+  return TN_OK;
+}
+
+// FP64 re-orthogonalisation of Q64 (column-major m x k, FP32-accurate) into q (strided).
+int refine_q(int64_t m, int64_t k, double* q, int64_t sQm, int64_t sQn, const MixWs& w, cudaStream_t s) {
+  int st;
   // E = Q^T Q - I in FP64 (Q64 column-major m x k)
   TnGemmF64 g{};
   g.M = k; g.N = k; g.K = m;
@@ -325,6 +356,7 @@ extern "C" int tn_qr_mixed(int64_t m, int64_t n, const double* a, int64_t sAm, i
   if ((st = tn_gemm_tf32x3(h, w.tf_ws, w.tf_bytes, s))) return st;
   write_q<<<blocks_for(m * k), 256, 0, s>>>(m, k, w.Q64, w.QE, q, sQm, sQn);
   TN_CHECK_LAUNCH();
-  tn_profile_end(ev, s, TN_PROF_QR, 0.0);
   return TN_OK;
 }
+
+}  // namespace

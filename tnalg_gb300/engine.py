@@ -15,6 +15,7 @@ and are updated incrementally when the centre moves (one block-operator GEMM
 pair per carried operator) instead of being rebuilt from the chain end as the
 reference does (MPSClass.py:491-502).
 """
+import os
 from collections import OrderedDict
 
 import numpy as np
@@ -204,8 +205,9 @@ class DeviceMPS:
         self.el_upto = -1      # EL[0..el_upto] valid
         self.er_from = self.length + 1   # ER[er_from..L] valid
         self.stats = {"matvecs": 0, "solves": 0, "restarts": 0, "unconverged": 0}
-        # tn_qr_mixed for seeding moves of the tf32x3 path; off until it beats tn_qr at chi >= 256
-        self.mixed_qr = False
+        # tn_qr_mixed (FP32 cluster QR + FP64 re-orthogonalisation) for the seeding moves of the
+        # tf32x3 path; TNALG_MIXED_QR=0 keeps every move on the FP64 Householder QR
+        self.mixed_qr = os.environ.get("TNALG_MIXED_QR", "1") != "0"
 
     # -- model / environments ----------------------------------------------------
     def set_model(self, model):
@@ -322,7 +324,8 @@ class DeviceMPS:
         """tn_qr, or tn_qr_mixed for a seeding move of the mixed-precision path (R only seeds the
         next local solve there, Q stays orthonormal to ~1e-12)."""
         lib, st = L.load(), L.stream_handle()
-        if self.mixed_qr and seed_only and self.precision == L.PREC_TF32X3 and min(mm, nn) >= 64:
+        if (self.mixed_qr and seed_only and self.unit_norm and self.precision == L.PREC_TF32X3
+                and min(mm, nn) >= 64):
             wp, wb = self.ws2.args(lib.tn_qr_mixed_workspace_bytes(mm, nn))
             L.check(lib.tn_qr_mixed(mm, nn, L.ptr(A), sA[0], sA[1], L.ptr(Q), sQ[0], sQ[1], L.ptr(R), nn, 1, wp, wb,
                                     st), "qr_mixed")

@@ -10,6 +10,9 @@
 // Every kernel launch site of the library is followed by TN_CHECK_LAUNCH(), which also counts
 // the launch (tn_launch_count in the C ABI).
 extern unsigned long long g_tn_launches;
+
+// Code written into the device error word by the cluster QR when a panel wait times out.
+constexpr int TN_DEVERR_QR_WAIT = 32;
 #define TN_CHECK_LAUNCH()                                   \
   do {                                                      \
     ++g_tn_launches;                                        \

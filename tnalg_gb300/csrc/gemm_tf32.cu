@@ -504,10 +504,15 @@ int tn_tf32x3_error_check(cudaStream_t s) {
     TN_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     if (h == kErrRange)
       return tn_fail(TN_ERR_NUMERIC, "tf32x3 gemm: an operand lies outside the FP32 range (|x| >= 3.4e38)");
+    if (h == TN_DEVERR_QR_WAIT) return tn_fail(TN_ERR_TIMEOUT, "qr32 cluster: a bounded panel wait gave up");
     return tn_fail(TN_ERR_TIMEOUT, "tf32x3 gemm: a bounded pipeline wait gave up");
   }
   return TN_OK;
 }
+
+// The device error word shared by the library's kernels (bounded waits, range checks); read and
+// cleared by tn_check_device_status.
+int tn_device_error_word(int** out) { return err_buffer(out); }
 
 size_t tn_gemm_tf32x3_ws_bytes(int64_t M, int64_t N, int64_t K, int64_t batch, int64_t nred) {
   const int64_t zr = batch * std::max<int64_t>(nred, 1);

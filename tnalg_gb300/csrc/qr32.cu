@@ -1,12 +1,13 @@
-// Mixed-precision gauge move: FP32 Householder QR + FP64 re-orthogonalisation (K4, tf32x3 path).
+// Mixed-precision gauge move: FP32 Householder QR + FP64 re-orthogonalisation (split-TF32 path).
 //
 // On GB300 a dependent FP64 operation costs ~64 cycles and the FP64 pipe issues ~2 lanes/clock
 // per SM, which makes the column-sequential Householder panel the bottleneck of an FP64 QR.
 // In a sweep the R factor of a gauge move only seeds the next local solve (the site it is
 // absorbed into is re-optimised right away), so only Q has to be accurate:
-//   1. Householder QR of the FP64 input rounded to FP32 (FP32 panels on one CTA, FP32 GEMM
-//      trailing updates, Q formed backwards): Q32 with ||Q32^T Q32 - I|| ~ 1e-6 whatever the
-//      conditioning of the input, R32 accurate to FP32;
+//   1. Householder QR of the FP64 input rounded to FP32: Q32 with ||Q32^T Q32 - I|| ~ 1e-6
+//      whatever the conditioning of the input, R32 accurate to FP32. For n <= m <= 1024,
+//      n <= 512 the whole factorisation runs in one 16-CTA cluster kernel (qr_cluster.cu);
+//      otherwise one-CTA FP32 panels with FP32 GEMM trailing updates, Q formed backwards;
 //   2. E = Q^T Q - I in FP64 (CUDA-core FP64 GEMM), then Q <- Q - Q E / 2 on the tensor cores
 //      (split TF32; the product is ~1e-6 in size, so its 1e-6 relative error is ~1e-12): the
 //      returned Q is orthonormal to ~1e-12 and spans col(A) to FP32 accuracy.
@@ -16,8 +17,9 @@
 int tn_gemm_tf32x3(const TnGemmF64& g, void* ws, size_t ws_bytes, cudaStream_t s);
 size_t tn_gemm_tf32x3_ws_bytes(int64_t M, int64_t N, int64_t K, int64_t batch, int64_t nred);
 bool tn_qr32_cluster_supported(int64_t m, int64_t n);
+size_t tn_qr32_cluster_scratch_floats(int64_t m, int64_t n);
 int tn_qr32_cluster(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* q, double* r,
-                    int64_t sRm, int64_t sRn, cudaStream_t s);
+                    int64_t sRm, int64_t sRn, float* scratch, cudaStream_t s);
 
 namespace {
 
@@ -227,7 +229,7 @@ int blocks_for(int64_t total) {
 size_t al(size_t x) { return (x + 1023) / 1024 * 1024; }
 
 struct MixWs {
-  float *Aw, *Vf, *Qw, *T, *W, *W2;
+  float *Aw, *Vf, *Qw, *T, *W, *W2, *Vc;
   double *Q64, *E, *QE;
   char* tf_ws;
   size_t tf_bytes;
@@ -245,6 +247,7 @@ size_t mix_layout(int64_t m, int64_t n, char* base, MixWs* w) {
   w->T = (float*)take((size_t)np * NB * NB * 4);
   w->W = (float*)take((size_t)NB * std::max(n, k) * 4);
   w->W2 = (float*)take((size_t)NB * std::max(n, k) * 4);
+  w->Vc = (float*)take(tn_qr32_cluster_scratch_floats(m, k) * 4);
   w->Q64 = (double*)take((size_t)m * k * 8);
   w->E = (double*)take((size_t)k * k * 8);
   w->QE = (double*)take((size_t)m * k * 8);
@@ -281,7 +284,7 @@ extern "C" int tn_qr_mixed(int64_t m, int64_t n, const double* a, int64_t sAm, i
   int st;
   if (m >= n && tn_qr32_cluster_supported(m, n)) {
     // whole FP32 factorisation and Q formation in one cluster-resident kernel
-    if ((st = tn_qr32_cluster(m, n, a, sAm, sAn, w.Q64, r, sRm, sRn, s))) return st;
+    if ((st = tn_qr32_cluster(m, n, a, sAm, sAn, w.Q64, r, sRm, sRn, w.Vc, s))) return st;
   } else {
     if ((st = qr32_blocked(m, n, a, sAm, sAn, r, sRm, sRn, w, s))) return st;
   }

@@ -1,61 +1,60 @@
 // FP32 Householder QR of one m x n matrix (n <= m <= 1024, n <= 512) by ONE 16-CTA thread-block
-// cluster, the matrix resident in registers for the whole factorisation and Q formation.
+// cluster (blocked, column-distributed), with Q formed in the same kernel.
 //
 // Role: step 1 of the mixed-precision gauge move (tn_qr_mixed): the FP32 factors it returns are
 // re-orthogonalised in FP64 afterwards, so only backward stability in FP32 is needed here.
 //
-// Why a cluster: a Householder QR is a chain of n dependent column steps. On GB300 FP64 runs at
-// ~2 lanes/clock/SM with a 64-cycle dependent latency, so the steps are done in FP32, and every
-// step is one reduction over all rows: with the rows spread over 16 SMs the per-step cost is a
-// distributed-shared-memory reduction (two cluster barriers) instead of a kernel launch and a
-// round trip through global memory.
-//
-// Layout: CTA `rank` of the cluster owns rows [64 rank, 64 rank + 64); thread c of every CTA
-// owns column c, so a thread keeps its column's 64 local rows in registers (a[64]). Column c's
-// reductions are owned by CTA (c % 16), slot c / 16.
-//
-// Column step j of the factorisation (LAPACK dgeqr2/dlarfg conventions, beta = -sign(x1)||x||,
-// v(j) = 1, tau = (beta - x1) / beta, v(g > j) = x(g) / (x1 - beta)):
-//   1. thread c >= j: s_c = sum over local rows g >= j of x(g) a(g, c) (x = column j); thread j
-//      instead forms the local sum of squares strictly below the pivot; the CTA holding row j
-//      also publishes the pivot row a(j, c). Partials are pushed into the owner CTA's slots.
-//   2. barrier; each owner forms w_c = v^T a_c = a(j,c) + (s_c - x1 a(j,c)) / (x1 - beta),
-//      f_c = tau w_c, writes R(j, c) = a(j, c) - f_c and pushes f_c to every CTA.
-//   3. barrier; every thread c > j updates a(g, c) -= v(g) f_c for its rows; thread j stores v.
-// Q is then formed in place backwards (LAPACK dorg2r): step j applies H_j to columns c > j
-// (one reduction of v^T q_c per column, same pattern) and sets column j to H_j e_j.
+// Why this shape: a Householder QR is a chain of n dependent column steps, each a reduction over
+// the rows. On GB300 FP64 issues ~2 lanes/clock/SM with a 64-cycle dependent latency, so the
+// steps run in FP32; and a reduction across SMs (cluster barrier + distributed shared memory,
+// ~1 us) per column would dominate, so every column step stays inside one CTA:
+//   * CTA q owns the column block [32q, 32q + 32) for ALL rows, in shared memory (column-major,
+//     odd leading dimension 1025, so row-parallel and column-parallel accesses are both free of
+//     bank conflicts). Panel q is factorised by CTA q alone (LAPACK dgeqr2 conventions per column,
+//     then the compact-WY factor T of dlarft, forward/columnwise), using __syncthreads only.
+//   * CTA q publishes V_q (row-major m x 32 in global memory, unit diagonal, zeros above) and T_q,
+//     then arrives on mbarrier ready[q] of every CTA of the cluster (release at cluster scope).
+//   * CTA q' > q waits on its own ready[q] (bounded) and applies H_q^T = I - V_q T_q^T V_q^T to
+//     its block (two 32-wide block products over the rows, FP32 FMA, one lane per column).
+//   * Q = H_0 H_1 ... E is formed blockwise too: once its panel is done, CTA q sets its block to
+//     the identity columns and applies H_q, ..., H_0 (only those reach rows >= 32p of column
+//     block q), independently of the other CTAs, overlapping their remaining factorisation.
+// Every wait is bounded by a clock budget; on timeout the CTA records an error code, skips its
+// remaining work and still joins the final cluster barrier.
 #include "common.cuh"
+
+int tn_device_error_word(int** out);
 
 namespace {
 
-constexpr int CL = 16;          // CTAs per cluster (non-portable size)
-constexpr int RPC = 64;         // rows per CTA
-constexpr int NT = 512;         // threads per CTA = maximum number of columns
-constexpr int SLOTS = NT / CL;  // reduction slots owned per CTA
+constexpr int CL = 16;           // CTAs per cluster (non-portable size)
+constexpr int BW = 32;           // columns per CTA = panel width
+constexpr int NT = 512;          // threads per CTA
+constexpr int NW = NT / 32;      // warps per CTA
+constexpr int MMAX = 1024;       // maximum rows
+constexpr int LDC = MMAX + 1;    // leading dimension of the shared column block
+constexpr int LDW = BW + 1;
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
-struct __align__(16) QcShared {
-  float xb[2][RPC];      // pivot column of the current / next step (local rows, zero above)
-  float vs[2][RPC];      // Householder vector, local rows (v(j) = 1, zero above j)
-  float red[CL][SLOTS];  // partial dots pushed by every CTA for the columns this CTA owns
-  float piv[SLOTS];      // pivot-row entries a(j, c) of the owned columns
-  float sj[CL];          // partial sums of squares below the pivot, one per CTA
-  float x1;              // the pivot a(j, j)
-  float fb[NT];          // update coefficients f_c of every column (all-gathered)
-  float tau[NT];         // tau_j of every reflector
+constexpr int LDW2 = BW + 4;     // W2 row pitch (16-byte aligned rows)
+
+struct Smem {
+  float C[BW * LDC];          // own column block, column-major
+  float Wred[NW * BW * LDW];  // per-warp partial products
+  float W2[BW * LDW2];        // W2 = op(T) W, 16-byte aligned rows
+  float T[BW * LDW];          // T of this CTA's panel
+  float G[BW * LDW];          // G(l, i) = v_l^T v_i of the panel, l < i
+  float red[NW * LDW];        // per-warp partials of the panel reductions
+  float f[BW];                // update coefficients of the current panel column
+  float tau[BW];              // tau of every reflector of the panel
+  float piv;                  // the current pivot a(j, j)
+  unsigned long long ready[CL];  // mbarrier per panel
+  int failed;
 };
 
-// Store v into the copy of `local` (this CTA's shared variable) held by cluster CTA `rank`.
-__device__ __forceinline__ void st_remote(const float* local, int rank, float v) {
-  uint32_t ra;
-  const uint32_t la = (uint32_t)__cvta_generic_to_shared(local);
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(la), "r"(rank));
-  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v) : "memory");
-}
+constexpr size_t kSmemBytes = sizeof(Smem) + 16;
 
-// Cluster-wide barrier; release/acquire order the remote stores issued before it.
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ int cluster_rank() {
   uint32_t r;
@@ -63,211 +62,434 @@ __device__ __forceinline__ int cluster_rank() {
   return (int)r;
 }
 
-// Rows in chunks of 16 with a compiler fence between chunks: at most 16 broadcast values from
-// shared memory are live next to the 64-register column (no spills at 128 registers/thread).
-constexpr int CH = 16;
-
-// sum_i a[i] * x[i] over the 64 local rows, x in shared memory (16-byte aligned)
-__device__ __forceinline__ float dot_rows(const float (&a)[RPC], const float* x) {
-  float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
-#pragma unroll
-  for (int ch = 0; ch < RPC; ch += CH) {
-#pragma unroll
-    for (int i = ch; i < ch + CH; i += 4) {
-      const float4 v = *reinterpret_cast<const float4*>(x + i);
-      p0 = fmaf(a[i], v.x, p0);
-      p1 = fmaf(a[i + 1], v.y, p1);
-      p2 = fmaf(a[i + 2], v.z, p2);
-      p3 = fmaf(a[i + 3], v.w, p3);
-    }
-    asm volatile("" ::: "memory");
-  }
-  return (p0 + p1) + (p2 + p3);
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-// a[i] -= v[i] * f over the 64 local rows, v in shared memory
-__device__ __forceinline__ void axpy_rows(float (&a)[RPC], const float* v, float f) {
-#pragma unroll
-  for (int ch = 0; ch < RPC; ch += CH) {
-#pragma unroll
-    for (int i = ch; i < ch + CH; i += 4) {
-      const float4 w = *reinterpret_cast<const float4*>(v + i);
-      a[i] = fmaf(-w.x, f, a[i]);
-      a[i + 1] = fmaf(-w.y, f, a[i + 1]);
-      a[i + 2] = fmaf(-w.z, f, a[i + 2]);
-      a[i + 3] = fmaf(-w.w, f, a[i + 3]);
-    }
-    asm volatile("" ::: "memory");
+// Arrive (release, cluster scope) on the copy of mbarrier `bar` held by cluster CTA `rank`.
+__device__ __forceinline__ void remote_arrive(unsigned long long* bar, int rank) {
+  uint32_t ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_u32(bar)), "r"(rank));
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(ra) : "memory");
+}
+
+// Bounded wait for phase 0 of a local mbarrier (acquire, cluster scope).
+__device__ __forceinline__ bool wait_ready(unsigned long long* bar) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], 0;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar))
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
   }
+}
+
+// Sum over the 32 lanes of 32 values at once: on return lane L holds sum over lanes of v[L].
+__device__ __forceinline__ float warp_transpose_sum(float (&v)[BW], int lane) {
+#pragma unroll
+  for (int half = 16; half >= 1; half >>= 1) {
+    const bool upper = (lane & half) != 0;
+#pragma unroll
+    for (int i = 0; i < half; ++i) {
+      // keep the half of the vector this lane is responsible for, send the other half
+      const float send = upper ? v[i] : v[i + half];
+      const float keep = upper ? v[i + half] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, half);
+    }
+  }
+  return v[0];
+}
+
+// C(rows >= r0) <- (I - V op(T) V^T) C over the 32 columns of this CTA's block, with V the
+// published row-major m x 32 panel (global memory, read through L1) and op(T) = T^T when trans_t.
+// Both products are register-blocked 8 x 8 per thread, so every value loaded feeds 8 FMAs (a lane
+// that receives a whole 32-wide row per row of work is bound by the load/store unit's 128 B/clock
+// register fill, four times below the FMA rate):
+//   W = V^T C  (32 x 32): thread = (8 reflectors kb, 8 columns cb) x row group g (32 groups);
+//   C -= V W2  (rows x 32): thread = 8 rows x 8 columns cb.
+__device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ Vp, const float* __restrict__ Tp,
+                            bool trans_t) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  // T staged in sh.G (free outside the panel factorisation)
+  for (int o = t; o < BW * BW; o += NT) sh.G[(o / BW) * LDW + o % BW] = Tp[o];
+  {
+    const int tile = t & 15, kb = tile >> 2, cb = tile & 3, g = t >> 4;
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+    for (int r = r0 + g; r < m; r += 32) {
+      const float4* vr = reinterpret_cast<const float4*>(Vp + (size_t)r * BW + 8 * kb);
+      const float4 v0 = vr[0], v1 = vr[1];
+      const float v[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+      float cv[8];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) cv[b] = sh.C[(8 * cb + b) * LDC + r];
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(v[a], cv[b], acc[a][b]);
+    }
+    // lanes l and l ^ 16 hold the same tile for neighbouring row groups
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) acc[a][b] += __shfl_xor_sync(0xffffffffu, acc[a][b], 16);
+    if (lane < 16) {
+      float* Wp = sh.Wred + warp * BW * LDW;
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) Wp[(8 * kb + a) * LDW + 8 * cb + b] = acc[a][b];
+    }
+  }
+  __syncthreads();
+  // reduce the warps' partials into Wred[0]
+  for (int o = t; o < BW * BW; o += NT) {
+    const int k = o / BW, c = o % BW;
+    float s = 0.f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) s += sh.Wred[w * BW * LDW + k * LDW + c];
+    sh.Wred[k * LDW + c] = s;
+  }
+  __syncthreads();
+  // W2 = op(T) W (T upper triangular), stored with a 16-byte aligned row pitch
+  for (int o = t; o < BW * BW; o += NT) {
+    const int k = o / BW, c = o % BW;
+    float s = 0.f;
+    if (trans_t) {
+      for (int l = 0; l <= k; ++l) s = fmaf(sh.G[l * LDW + k], sh.Wred[l * LDW + c], s);
+    } else {
+      for (int l = k; l < BW; ++l) s = fmaf(sh.G[k * LDW + l], sh.Wred[l * LDW + c], s);
+    }
+    sh.W2[k * LDW2 + c] = s;
+  }
+  __syncthreads();
+  // C -= V W2: 8 rows x 8 columns per thread
+  {
+    const int cb = t & 3, g = t >> 2;
+    for (int rb = r0 + 8 * g; rb < m; rb += 8 * (NT / 4)) {
+      float out[8][8];
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) out[a][b] = 0.f;
+#pragma unroll
+      for (int k4 = 0; k4 < BW / 4; ++k4) {
+        float v[8][4];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          const int r = rb + a;
+          const float4 x = (r < m) ? reinterpret_cast<const float4*>(Vp + (size_t)r * BW)[k4]
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+          v[a][0] = x.x;
+          v[a][1] = x.y;
+          v[a][2] = x.z;
+          v[a][3] = x.w;
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const float4* wr = reinterpret_cast<const float4*>(sh.W2 + (4 * k4 + kk) * LDW2 + 8 * cb);
+          const float4 w0 = wr[0], w1 = wr[1];
+          const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+          for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) out[a][b] = fmaf(v[a][kk], w[b], out[a][b]);
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        const int r = rb + a;
+        if (r < m) {
+#pragma unroll
+          for (int b = 0; b < 8; ++b) sh.C[(8 * cb + b) * LDC + r] -= out[a][b];
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Householder QR of this CTA's panel (columns 0..jb-1 of the block, rows >= j0 = 32 q), then its
+// compact-WY factor T (dlarft, forward, columnwise) in sh.T. The panel is held in registers while
+// it is factorised: thread t owns rows t and t + NT of the 32 columns (a[2][32]), and the column
+// loop is unrolled at compile time (PanelStep<I>) so every column index is static.
+struct PanelCtx {
+  float a[2][BW];
+  float s;  // this thread's part of the sum of squares below the current pivot
+  int m, j0, jb, t, lane, warp;
+};
+
+template <int I>
+__device__ __forceinline__ void panel_step(Smem& sh, PanelCtx& P) {
+  if (I >= P.jb) return;
+  const int j = P.j0 + I;
+  float s = P.s;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (P.lane == 0) sh.red[P.warp * LDW + BW] = s;
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr)
+    if (P.t + rr * NT == j) sh.piv = P.a[rr][I];
+  __syncthreads();
+  // reflector, computed redundantly by every thread
+  float sig = 0.f;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) sig += sh.red[w * LDW + BW];
+  const float x1 = sh.piv;
+  float beta = x1, tau = 0.f, scale = 0.f;
+  if (sig > 0.f) {
+    const float nrm = sqrtf(fmaf(x1, x1, sig));
+    beta = (x1 >= 0.f) ? -nrm : nrm;
+    tau = (beta - x1) / beta;
+    scale = 1.f / (x1 - beta);
+  }
+  // v (v(j) = 1) kept below the pivot; products of v with every other panel column: c > I gives
+  // the column update, c < I the Gram entries v_c^T v_I of T
+  float v[2];
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr) {
+    const int r = P.t + rr * NT;
+    v[rr] = 0.f;
+    if (r < P.m) {
+      if (r > j) {
+        P.a[rr][I] *= scale;
+        v[rr] = P.a[rr][I];
+      } else if (r == j) {
+        v[rr] = 1.f;
+      }
+    }
+  }
+  float p[BW];
+#pragma unroll
+  for (int c = 0; c < BW; ++c) p[c] = (c == I) ? 0.f : fmaf(v[0], P.a[0][c], v[1] * P.a[1][c]);
+  const float ws = warp_transpose_sum(p, P.lane);
+  sh.red[P.warp * LDW + P.lane] = ws;
+  __syncthreads();
+  if (P.warp == 0) {
+    float tot = 0.f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) tot += sh.red[w * LDW + P.lane];
+    sh.f[P.lane] = (P.lane > I && P.lane < P.jb) ? tau * tot : 0.f;
+    if (P.lane < I) sh.G[P.lane * LDW + I] = tot;
+    if (P.lane == 0) sh.tau[I] = tau;
+  }
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr)
+    if (P.t + rr * NT == j) P.a[rr][I] = beta;  // R(j, j)
+  __syncthreads();
+  // column update, and the next column's sum of squares below its pivot
+  float fc[BW];
+#pragma unroll
+  for (int c4 = 0; c4 < BW / 4; ++c4) {
+    const float4 f4 = reinterpret_cast<const float4*>(sh.f)[c4];
+    fc[4 * c4] = f4.x;
+    fc[4 * c4 + 1] = f4.y;
+    fc[4 * c4 + 2] = f4.z;
+    fc[4 * c4 + 3] = f4.w;
+  }
+  float s2 = 0.f;
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr) {
+#pragma unroll
+    for (int c = I + 1; c < BW; ++c) P.a[rr][c] = fmaf(-v[rr], fc[c], P.a[rr][c]);
+    if (I + 1 < BW) {
+      const int r = P.t + rr * NT;
+      const float y = (r > j + 1) ? P.a[rr][(I + 1) % BW] : 0.f;
+      s2 = fmaf(y, y, s2);
+    }
+  }
+  P.s = s2;
+  // no barrier here: the next step rewrites red/piv before its first barrier and f after its
+  // second, and every reader of this step's values has passed this step's later barriers
+}
+
+template <int I>
+struct PanelLoop {
+  static __device__ __forceinline__ void run(Smem& sh, PanelCtx& P) {
+    panel_step<I>(sh, P);
+    PanelLoop<I + 1>::run(sh, P);
+  }
+};
+template <>
+struct PanelLoop<BW> {
+  static __device__ __forceinline__ void run(Smem&, PanelCtx&) {}
+};
+
+__device__ void factor_panel(Smem& sh, int m, int j0, int jb) {
+  PanelCtx P;
+  P.m = m;
+  P.j0 = j0;
+  P.jb = jb;
+  P.t = threadIdx.x;
+  P.lane = P.t & 31;
+  P.warp = P.t >> 5;
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr) {
+    const int r = P.t + rr * NT;
+#pragma unroll
+    for (int c = 0; c < BW; ++c) P.a[rr][c] = (r < m) ? sh.C[c * LDC + r] : 0.f;
+  }
+  P.s = 0.f;
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr) {
+    const int r = P.t + rr * NT;
+    if (r > j0 && r < m) P.s = fmaf(P.a[rr][0], P.a[rr][0], P.s);
+  }
+  PanelLoop<0>::run(sh, P);
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr) {
+    const int r = P.t + rr * NT;
+    if (r < m) {
+#pragma unroll
+      for (int c = 0; c < BW; ++c) sh.C[c * LDC + r] = P.a[rr][c];
+    }
+  }
+  // T(k, i) = -tau_i sum_{l=k}^{i-1} T(k, l) G(l, i), T(i, i) = tau_i: lane k of warp 0 runs row k
+  // with the row in registers
+  if (P.warp == 0) {
+    const int k = P.lane;
+    float tr[BW];
+#pragma unroll
+    for (int i = 0; i < BW; ++i) {
+      float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+      for (int l = 0; l < i; ++l) {
+        const float g = sh.G[l * LDW + i];
+        if (l & 1) a1 = fmaf((l >= k) ? tr[l] : 0.f, g, a1);
+        else a0 = fmaf((l >= k) ? tr[l] : 0.f, g, a0);
+      }
+      const float ti = sh.tau[i];
+      tr[i] = (i >= jb || k >= jb || k > i) ? 0.f : ((k == i) ? ti : -ti * (a0 + a1));
+    }
+#pragma unroll
+    for (int i = 0; i < BW; ++i) sh.T[k * LDW + i] = tr[i];
+  }
+  __syncthreads();
 }
 
 __global__ void __launch_bounds__(NT, 1)
     qr32_cluster_kernel(int m, int n, const double* __restrict__ A, int64_t sAm, int64_t sAn, double* __restrict__ Q,
-                        double* __restrict__ R, int64_t sRm, int64_t sRn) {
-  __shared__ QcShared sh;
-  const int rank = cluster_rank();
-  const int c = threadIdx.x;
-  const int row0 = rank * RPC;
-
-  float a[RPC];
-#pragma unroll
-  for (int ch = 0; ch < RPC; ch += CH) {
-#pragma unroll
-    for (int i = ch; i < ch + CH; ++i) {
-      const int g = row0 + i;
-      a[i] = (c < n && g < m) ? (float)A[(int64_t)g * sAm + (int64_t)c * sAn] : 0.f;
+                        double* __restrict__ R, int64_t sRm, int64_t sRn, float* __restrict__ Vg,
+                        float* __restrict__ Tg, int* err) {
+  extern __shared__ unsigned char smem_raw[];
+  Smem& sh = *reinterpret_cast<Smem*>(((uintptr_t)smem_raw + 15) & ~(uintptr_t)15);
+  const int q = cluster_rank();
+  const int t = threadIdx.x;
+  const int col0 = q * BW;
+  const int jb = max(0, min(BW, n - col0));
+  if (t == 0) {
+    for (int p = 0; p < CL; ++p)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sh.ready[p])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    sh.failed = 0;
+  }
+  // own column block, FP64 -> FP32 (columns beyond n are zero)
+  if (sAn == 1) {
+    for (int e = t; e < m * BW; e += NT) {
+      const int r = e / BW, c = e % BW;
+      sh.C[c * LDC + r] = (c < jb) ? (float)A[(int64_t)r * sAm + col0 + c] : 0.f;
     }
-    asm volatile("" ::: "memory");
+  } else {
+    for (int e = t; e < m * BW; e += NT) {
+      const int c = e / m, r = e % m;
+      sh.C[c * LDC + r] = (c < jb) ? (float)A[(int64_t)r * sAm + (int64_t)(col0 + c) * sAn] : 0.f;
+    }
   }
-  if (R && c < n) {  // strictly lower part of R (n x n): zeros, rows spread over the cluster
-    int i0 = c + 1;
-    i0 += ((rank - i0) % CL + CL) % CL;
-    for (int i = i0; i < n; i += CL) R[(int64_t)i * sRm + (int64_t)c * sRn] = 0.0;
-  }
-  if (c == 0) {
-#pragma unroll
-    for (int i = 0; i < RPC; ++i) sh.xb[0][i] = a[i];
-  }
-  cluster_sync();  // every CTA is running (its shared memory exists) before the first remote store
+  cluster_sync();  // mbarriers of every CTA initialised before any remote arrive
 
-  // ---- factorisation ----
-  for (int j = 0; j < n; ++j) {
-    const float* X = sh.xb[j & 1];
-    const int lj = j - row0;  // local index of row j (outside [0, RPC) if another CTA holds it)
-    const bool own_pivot = lj >= 0 && lj < RPC;
-    if (c >= j && c < n) {
-      float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
-      if (c == j) {
-#pragma unroll
-        for (int i = 0; i < RPC; i += 4) {
-          p0 = fmaf(a[i], (i > lj) ? a[i] : 0.f, p0);
-          p1 = fmaf(a[i + 1], (i + 1 > lj) ? a[i + 1] : 0.f, p1);
-          p2 = fmaf(a[i + 2], (i + 2 > lj) ? a[i + 2] : 0.f, p2);
-          p3 = fmaf(a[i + 3], (i + 3 > lj) ? a[i + 3] : 0.f, p3);
+  if (jb > 0) {
+    // updates by the panels to the left, in order
+    for (int p = 0; p < q; ++p) {
+      if (!wait_ready(&sh.ready[p])) {
+        if (t == 0) atomicExch(err, TN_DEVERR_QR_WAIT);
+        sh.failed = 1;
+      }
+      __syncthreads();
+      if (sh.failed) break;
+      apply_block(sh, m, p * BW, Vg + (size_t)p * m * BW, Tg + p * BW * BW, true);
+    }
+    if (!sh.failed) {
+      factor_panel(sh, m, col0, jb);
+      // publish V_q (unit diagonal, zeros above) and T_q
+      float* Vq = Vg + (size_t)q * m * BW;
+      for (int e = t; e < m * BW; e += NT) {
+        const int r = e / BW, c = e % BW;
+        const int d = col0 + c;
+        Vq[e] = (c < jb && r >= d) ? ((r == d) ? 1.f : sh.C[c * LDC + r]) : 0.f;
+      }
+      for (int e = t; e < BW * BW; e += NT) {
+        const int k = e / BW, l = e % BW;
+        Tg[q * BW * BW + e] = (k < jb && l < jb) ? sh.T[k * LDW + l] : 0.f;
+      }
+      __threadfence();
+      __syncthreads();
+      if (t < CL) remote_arrive(&sh.ready[q], t);
+      // R block (not needed by the other CTAs): rows <= diagonal from the block, zeros below
+      if (R) {
+        for (int e = t; e < n * BW; e += NT) {
+          const int r = e / BW, c = e % BW;
+          if (c < jb) {
+            const int d = col0 + c;
+            R[(int64_t)r * sRm + (int64_t)d * sRn] = (r <= d) ? (double)sh.C[c * LDC + r] : 0.0;
+          }
         }
       }
-      const float p = (c == j) ? (p0 + p1) + (p2 + p3) : dot_rows(a, X);
-      float pv = 0.f;
-      if (own_pivot) {
-#pragma unroll
-        for (int i = 0; i < RPC; ++i) pv = (i == lj) ? a[i] : pv;
+      __syncthreads();  // the block is read above before it is overwritten below
+      // Q block: identity columns, then H_q, ..., H_0
+      for (int e = t; e < m * BW; e += NT) {
+        const int c = e / m, r = e % m;
+        sh.C[c * LDC + r] = (c < jb && r == col0 + c) ? 1.f : 0.f;
       }
-      if (c == j) {
-        for (int q = 0; q < CL; ++q) {
-          st_remote(&sh.sj[rank], q, p);
-          if (own_pivot) st_remote(&sh.x1, q, pv);
-        }
-      } else {
-        const int q = c % CL, t = c / CL;
-        st_remote(&sh.red[rank][t], q, p);
-        if (own_pivot) st_remote(&sh.piv[t], q, pv);
+      __syncthreads();
+      for (int p = q; p >= 0; --p) apply_block(sh, m, p * BW, Vg + (size_t)p * m * BW, Tg + p * BW * BW, false);
+      for (int e = t; e < m * jb; e += NT) {
+        const int c = e / m, r = e % m;
+        Q[(int64_t)r + (int64_t)(col0 + c) * m] = (double)sh.C[c * LDC + r];
       }
-    }
-    cluster_sync();
-
-    float sig = 0.f;
-#pragma unroll
-    for (int q = 0; q < CL; ++q) sig += sh.sj[q];
-    const float x1 = sh.x1;
-    float beta = x1, tau = 0.f, scale = 0.f;
-    if (sig > 0.f) {
-      const float nrm = sqrtf(fmaf(x1, x1, sig));
-      beta = (x1 >= 0.f) ? -nrm : nrm;
-      tau = (beta - x1) / beta;
-      scale = 1.f / (x1 - beta);
-    }
-    if (c < SLOTS) {
-      const int col = c * CL + rank;
-      if (col > j && col < n) {
-        float s = 0.f;
-#pragma unroll
-        for (int q = 0; q < CL; ++q) s += sh.red[q][c];
-        const float a1 = sh.piv[c];
-        const float f = tau * fmaf(s - x1 * a1, scale, a1);
-        if (R) R[(int64_t)j * sRm + (int64_t)col * sRn] = (double)(a1 - f);
-        for (int q = 0; q < CL; ++q) st_remote(&sh.fb[col], q, f);
-      }
-    }
-    if (R && c == j && own_pivot) R[(int64_t)j * sRm + (int64_t)j * sRn] = (double)beta;
-    if (c == 0) sh.tau[j] = tau;
-    if (c < RPC) sh.vs[0][c] = (c > lj) ? X[c] * scale : (c == lj ? 1.f : 0.f);
-    cluster_sync();
-
-    if (c > j && c < n) {
-      axpy_rows(a, sh.vs[0], sh.fb[c]);
-      if (c == j + 1) {
-        float* Xn = sh.xb[(j + 1) & 1];
-#pragma unroll
-        for (int i = 0; i < RPC; ++i) Xn[i] = (i > lj) ? a[i] : 0.f;
-      }
-    } else if (c == j) {
-#pragma unroll
-      for (int i = 0; i < RPC; ++i) a[i] = (i > lj) ? a[i] * scale : a[i];
-    }
-    __syncthreads();  // the next pivot column is in shared memory
-  }
-
-  // ---- Q formation, backwards, in place ----
-  for (int j = n - 1; j >= 0; --j) {
-    const int lj = j - row0;
-    const float tj = sh.tau[j];
-    float* V = sh.vs[j & 1];
-    if (c == j) {
-#pragma unroll
-      for (int i = 0; i < RPC; ++i) V[i] = (i > lj) ? a[i] : (i == lj ? 1.f : 0.f);
-    }
-    __syncthreads();
-    if (c > j && c < n) st_remote(&sh.red[rank][c / CL], c % CL, dot_rows(a, V));
-    cluster_sync();
-    if (c < SLOTS) {
-      const int col = c * CL + rank;
-      if (col > j && col < n) {
-        float s = 0.f;
-#pragma unroll
-        for (int q = 0; q < CL; ++q) s += sh.red[q][c];
-        const float f = tj * s;
-        for (int q = 0; q < CL; ++q) st_remote(&sh.fb[col], q, f);
-      }
-    }
-    cluster_sync();
-    if (c > j && c < n) {
-      axpy_rows(a, V, sh.fb[c]);
-    } else if (c == j) {
-#pragma unroll
-      for (int i = 0; i < RPC; ++i) a[i] = (i > lj) ? -tj * a[i] : (i == lj ? 1.f - tj : 0.f);
     }
   }
-
-  if (c < n) {
-#pragma unroll
-    for (int i = 0; i < RPC; ++i) {
-      const int g = row0 + i;
-      if (g < m) Q[g + (int64_t)c * m] = (double)a[i];
-    }
-  }
+  cluster_sync();  // no CTA exits while another may still arrive on its barriers
 }
 
 int g_cluster_state = -1;  // -1 unknown, 0 unavailable, 1 available
+
+cudaLaunchConfig_t launch_config(cudaLaunchAttribute* at, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CL);
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = kSmemBytes;
+  cfg.stream = s;
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cfg;
+}
 
 }  // namespace
 
 // True when the 16-CTA cluster kernel can run this shape on the current device.
 bool tn_qr32_cluster_supported(int64_t m, int64_t n) {
-  if (n < 1 || n > NT || m < n || m > (int64_t)CL * RPC) return false;
+  if (n < 1 || n > (int64_t)CL * BW || m < n || m > MMAX) return false;
   if (g_cluster_state < 0) {
     g_cluster_state = 0;
     if (cudaFuncSetAttribute(qr32_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
-        cudaSuccess) {
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(CL);
-      cfg.blockDim = dim3(NT);
+            cudaSuccess &&
+        cudaFuncSetAttribute(qr32_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) ==
+            cudaSuccess) {
       cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = CL;
-      at[0].val.clusterDim.y = 1;
-      at[0].val.clusterDim.z = 1;
-      cfg.attrs = at;
-      cfg.numAttrs = 1;
+      cudaLaunchConfig_t cfg = launch_config(at, 0);
       int clusters = 0;
       if (cudaOccupancyMaxActiveClusters(&clusters, qr32_cluster_kernel, &cfg) == cudaSuccess && clusters > 0)
         g_cluster_state = 1;
@@ -277,22 +499,27 @@ bool tn_qr32_cluster_supported(int64_t m, int64_t n) {
   return g_cluster_state == 1;
 }
 
-// Q (column-major m x n, FP64 values of the FP32 factor) and, if R is given, R (n x n, strided).
+// Scratch floats for V and T of all panels of an m x n factorisation.
+size_t tn_qr32_cluster_scratch_floats(int64_t m, int64_t n) {
+  const int64_t np = tn_cdiv(n, BW);
+  return (size_t)np * (m * BW + BW * BW);
+}
+
+// Q (column-major m x n, FP64 values of the FP32 factor) and, if r is given, R (n x n, strided).
+// scratch: tn_qr32_cluster_scratch_floats(m, n) floats, 16-byte aligned.
 int tn_qr32_cluster(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* q, double* r,
-                    int64_t sRm, int64_t sRn, cudaStream_t s) {
+                    int64_t sRm, int64_t sRn, float* scratch, cudaStream_t s) {
   if (!tn_qr32_cluster_supported(m, n)) return tn_fail(TN_ERR_ARG, "qr32 cluster: unsupported shape or device");
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(CL);
-  cfg.blockDim = dim3(NT);
-  cfg.stream = s;
+  if (((uintptr_t)scratch & 15) != 0) return tn_fail(TN_ERR_ARG, "qr32 cluster: scratch misaligned");
+  int* err;
+  int st = tn_device_error_word(&err);
+  if (st) return st;
+  const int64_t np = tn_cdiv(n, BW);
+  float* Vg = scratch;
+  float* Tg = scratch + (size_t)np * m * BW;
   cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = CL;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  TN_CUDA(cudaLaunchKernelEx(&cfg, qr32_cluster_kernel, (int)m, (int)n, a, sAm, sAn, q, r, sRm, sRn));
+  cudaLaunchConfig_t cfg = launch_config(at, s);
+  TN_CUDA(cudaLaunchKernelEx(&cfg, qr32_cluster_kernel, (int)m, (int)n, a, sAm, sAn, q, r, sRm, sRn, Vg, Tg, err));
   TN_CHECK_LAUNCH();
   return TN_OK;
 }

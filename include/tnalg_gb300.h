@@ -108,7 +108,7 @@ int tn_apply_site_ops(int64_t chil, int64_t d, int64_t chir, const double* in, c
 int tn_pair_contract(int64_t chil, int64_t d, int64_t chir, const double* m, const double* t,
                      double alpha, double* out, void* stream);
 
-/* ---- effective Hamiltonian matvec (K1) ------------------------------------------ */
+/* ---- effective Hamiltonian matvec ----------------------------------------------- */
 typedef struct {
   int64_t chil, d, chir;
   const double* wl;   /* (chil*d)^2 left block incl. on-site terms, or NULL */
@@ -127,7 +127,7 @@ int tn_matvec(const tn_site_desc* desc, const double* psi, double* y, double alp
               int precision, void* ws, size_t ws_bytes, void* stream);
 size_t tn_matvec_workspace_bytes(const tn_site_desc* desc, int precision);
 
-/* ---- local eigensolver (K2) ----------------------------------------------------- */
+/* ---- local eigensolver ---------------------------------------------------------- */
 typedef struct {
   double eigs_tol;      /* tolerance as passed to the reference's eigsh */
   double tau;           /* the reference's shift; tol on ||Hx - t x|| = eigs_tol/tau*|1-tau*t| */
@@ -162,7 +162,7 @@ int tn_lanczos(const tn_site_desc* desc, double* psi_inout, const tn_lanczos_opt
                void* ws, size_t ws_bytes, tn_lanczos_result* result, void* stream);
 size_t tn_lanczos_workspace_bytes(const tn_site_desc* desc, const tn_lanczos_opts* opts);
 
-/* ---- gauge move (K4) ------------------------------------------------------------- */
+/* ---- gauge move ------------------------------------------------------------------ */
 /*
  * Thin Householder QR in FP64 of the m x n matrix A (general strides):
  * A = Q R, Q: m x k with orthonormal columns, R: k x n upper trapezoidal, k = min(m, n).
@@ -187,7 +187,7 @@ size_t tn_qr_mixed_workspace_bytes(int64_t m, int64_t n);
  * replay off (plain launches). A stream that is already capturing always gets plain launches. */
 int tn_qr_use_graphs(int on);
 
-/* ---- entanglement spectrum (K5) ----------------------------------------------------- */
+/* ---- entanglement spectrum ---------------------------------------------------------- */
 /*
  * Singular values of the k x n matrix X (general strides) by parallel one-sided
  * Jacobi in FP64; s_out (DEVICE, k values, unsorted). Replaces np.linalg.svd in the
@@ -212,6 +212,24 @@ size_t tn_singular_values_workspace_bytes(int64_t k, int64_t n);
  */
 int tn_singular_values_noalloc(int64_t k, int64_t n, const double* x, int64_t sXr, int64_t sXc,
                                double* s_out, double tol, int max_sweeps, void* stream);
+
+/*
+ * Singular values of `count` independent matrices at once (the same FP64 Jacobi algorithm, one
+ * launch per round for the whole batch): the R factors of every bond collected by one sweep of
+ * gauge moves, which is how calculate_entanglement_spectrum (MPSClass.py:812-832) fills lm for
+ * all bonds. items is a HOST array; x and s_out in every item are DEVICE pointers. ws: 256-byte
+ * aligned DEVICE scratch of tn_singular_values_batched_workspace_bytes(count, items) bytes.
+ * Synchronises stream. No counterpart in the reference (which takes one SVD per move).
+ */
+typedef struct tn_sv_item {
+  int64_t k, n;        /* rows, columns */
+  const double* x;     /* DEVICE, element (r, c) at x[r * sXr + c * sXc] */
+  int64_t sXr, sXc;
+  double* s_out;       /* DEVICE, k singular values (unsorted) */
+} tn_sv_item;
+int tn_singular_values_batched(int count, const tn_sv_item* items, double tol, int max_sweeps, void* ws,
+                               size_t ws_bytes, void* stream);
+size_t tn_singular_values_batched_workspace_bytes(int count, const tn_sv_item* items);
 
 /* ---- profiling ----------------------------------------------------------------------- */
 /* CUDA-event timing of kernel classes on their launching stream (0 = effective-Hamiltonian

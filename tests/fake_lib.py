@@ -227,6 +227,23 @@ class FakeLib:
         _view(out, int(k))[:] = np.linalg.svd(X, compute_uv=False)[: int(k)]
         return OK
 
+    def tn_singular_values_batched_workspace_bytes(self, count, items):
+        return 0
+
+    def tn_singular_values_batched(self, count, items, tol, sweeps, ws, wsb, stream):
+        self._count("tn_singular_values_batched")
+        arr = ctypes.cast(items, ctypes.POINTER(ItemStruct()))
+        for b in range(int(count)):
+            it = arr[b]
+            X = _strided(it.x, (int(it.k), int(it.n)), (it.sXr, it.sXc)).copy()
+            _view(it.s_out, int(it.k))[:] = np.linalg.svd(X, compute_uv=False)[: int(it.k)]
+        return OK
+
+
+def ItemStruct():
+    from tnalg_gb300 import _lib
+    return _lib.SvItem
+
 
 def install():
     """Route tnalg_gb300's C-ABI calls to a fresh FakeLib (host tensors accepted)."""

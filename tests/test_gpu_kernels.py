@@ -138,6 +138,23 @@ def test_singular_values_match_numpy(cuda_lib):
         np.testing.assert_allclose(s, ref, atol=1e-13 * ref[0], rtol=1e-11)
 
 
+def test_singular_values_batched_match_numpy(cuda_lib):
+    """One batched call over matrices of different shapes (an odd row count, a transposed view,
+    a 512 x 512 bond matrix), to 1e-13 of each matrix's largest value."""
+    mats = []
+    for k, n, seed in ((12, 12, 1), (33, 40, 2), (5, 9, 3), (512, 512, 4), (64, 64, 5)):
+        X = _rand(k, n, seed=seed)
+        X[:, : k // 3] *= 1e-4  # spread the spectrum
+        mats.append(X)
+    mats.append(_rand(40, 30, seed=6).T)  # 30 x 40 read through strides (1, 30)
+    spectra = L.singular_values_batched(mats)
+    L.check(L.load().tn_check_device_status(L.stream_handle()))
+    tol = 1e-13
+    for X, s in zip(mats, spectra):
+        ref = np.linalg.svd(X.cpu().numpy(), compute_uv=False)
+        np.testing.assert_allclose(s[: len(ref)], ref, atol=tol * ref[0], rtol=0)
+
+
 def test_block_assembly_and_site_ops(cuda_lib):
     lib = L.load()
     chi, d = 6, 2

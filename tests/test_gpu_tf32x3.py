@@ -88,6 +88,30 @@ def test_tf32x3_gemm_ignores_stale_workspace(tf32, M, N, K, transposed_b):
     assert torch.max(torch.abs(C - ref)).item() <= 5e-6 * torch.max(torch.abs(ref)).item()
 
 
+@pytest.mark.parametrize("m,n", [(1024, 512), (300, 200), (96, 200)])
+def test_qr_mixed_any_fp64_magnitude(tf32, m, n):
+    """tn_qr_mixed scales its input by an exact power of two before the FP32 factorisation (the
+    cluster kernel for n <= m <= 1024, n <= 512, the blocked path otherwise): inputs scaled by
+    2^500 and 2^-500 give bit-for-bit the same FP32 problem, hence the same Q and an exactly
+    scaled R."""
+    lib = L.load()
+    k = min(m, n)
+    A = _rand(m, n, seed=m * n)
+    outs = []
+    for f in (1.0, 2.0 ** 500, 2.0 ** -500):
+        Q = torch.empty((m, k), dtype=torch.float64, device="cuda")
+        R = torch.empty((k, n), dtype=torch.float64, device="cuda")
+        ws = L.Workspace(torch.device("cuda"))
+        wp, wb = ws.args(lib.tn_qr_mixed_workspace_bytes(m, n))
+        L.check(lib.tn_qr_mixed(m, n, L.ptr(A * f), n, 1, L.ptr(Q), k, 1, L.ptr(R), n, 1, wp, wb, L.stream_handle()))
+        L.check(lib.tn_check_device_status(L.stream_handle()))
+        assert torch.isfinite(Q).all() and torch.isfinite(R).all()
+        outs.append((Q, R / f))
+    for Q, R in outs[1:]:
+        torch.testing.assert_close(Q, outs[0][0], rtol=0, atol=1e-12)
+        torch.testing.assert_close(R, outs[0][1], rtol=1e-12, atol=1e-12 * torch.max(torch.abs(outs[0][1])).item())
+
+
 def test_tf32x3_gemm_reports_operands_beyond_fp32_range(tf32):
     """Split TF32 has FP32's exponent range: a finite FP64 operand of 1e103 cannot be staged, and the
     device status says so (TN_ERR_NUMERIC) instead of leaving silent NaNs."""

@@ -176,26 +176,24 @@ class MpsOpenBoundaryClass(MpsBasic):
     def _svd_moves(self, l0, l1):
         """QR moves plus the singular values of each R factor (the reference's 'svd' decomposition
         stores lm at MPSClass.py:154-155,163-164; the Schmidt values of a bond are the singular
-        values of R)."""
+        values of R). Each R is kept and all of them go through one batched Jacobi call at the
+        end: along a sweep of moves the left sites of a bond are left-canonical and the right sites
+        right-canonical when its R is formed, so the bonds' spectra are independent."""
         dev = self._dev
-        lib = L.load()
         step = 1 if l0 < l1 else -1
+        collected = []
         for n in range(l0, l1, step):
             if step > 0:
                 dev.qr_left(n)
-                R = dev._last_r
                 bond = n
             else:
                 dev.qr_right(n)
-                R = dev._last_r
                 bond = n - 1
             if self.center > -1:
-                k, nn = R.shape
-                sv = torch.empty(k, dtype=torch.float64, device=dev.device)
-                wp, wb = dev.ws2.args(lib.tn_singular_values_workspace_bytes(k, nn))
-                L.check(lib.tn_singular_values(k, nn, L.ptr(R), nn, 1, L.ptr(sv), 1e-15, 60, wp, wb,
-                                               L.stream_handle()), "singular values")
-                s = np.sort(sv.cpu().numpy())[::-1]
+                collected.append((bond, dev._last_r))
+        if collected:
+            spectra = L.singular_values_batched([R for _, R in collected], ws=dev.ws2)
+            for (bond, R), s in zip(collected, spectra):
                 self.lm[bond] = s[: min(R.shape)]
         if l0 < l1:
             dev.orthogonality[l0:l1] = -1
@@ -211,7 +209,13 @@ class MpsOpenBoundaryClass(MpsBasic):
         c = self.center if self.center >= 0 else 0
         if self._dev.grow_bonds(chi_new, noise=noise, seed=seed):
             self.lm = [np.zeros(0) for _ in range(self.length - 1)]
-            self.correct_orthogonal_center(c)
+            # the grown state is re-optimised by the next sweep: its gauge moves may use the
+            # mixed-precision QR
+            self._dev.fast_gauge = True
+            try:
+                self.correct_orthogonal_center(c)
+            finally:
+                self._dev.fast_gauge = False
 
     # -- local update ------------------------------------------------------------
     def _model(self, index1, index2, coeff1, coeff2, tol):
@@ -315,27 +319,40 @@ class MpsOpenBoundaryClass(MpsBasic):
             ob_len -= 1
         if not pairs:
             return np.zeros(0)
-        return E.observe(self._dev, [], pairs)[1]
+        # O(N^2) transfer steps: the mixed-precision path runs them in split TF32 (~1e-7 of the
+        # correlations); energies and one-site observables stay FP64
+        return E.observe(self._dev, [], pairs, precision=self._dev.precision)[1]
 
     def calculate_entanglement_spectrum(self, if_fast=True):
-        """MPSClass.py:812-832: SVD-type moves to the ends and back fill lm."""
+        """MPSClass.py:812-832: moves to the ends and back fill lm. The reference takes an SVD at
+        every move of the three passes; the spectra do not depend on the pass, and the middle
+        pass crosses every bond that is filled, so only its moves record singular values (one
+        batched call). On the mixed-precision path the moves use the mixed-precision QR (the
+        state is then kept to ~1e-7)."""
         way, c0 = self.decomp_way, self.center
-        self.decomp_way = "svd"
-        if if_fast and c0 > -0.5:
-            p0, p1 = self.length - 1, 0
-            for n in range(self.length - 1):
-                if self.lm[n].size == 0:
-                    p0 = min(p0, n)
-                    p1 = max(p1, n)
-            self.correct_orthogonal_center(p0)
-            self.correct_orthogonal_center(p1 + 1)
-            self.correct_orthogonal_center(c0)
-        else:
-            self.correct_orthogonal_center(0)
-            self.correct_orthogonal_center(self.length - 1)
-            if c0 > 0:
+        self._dev.fast_gauge = True
+        try:
+            if if_fast and c0 > -0.5:
+                p0, p1 = self.length - 1, 0
+                for n in range(self.length - 1):
+                    if self.lm[n].size == 0:
+                        p0 = min(p0, n)
+                        p1 = max(p1, n)
+                self.correct_orthogonal_center(p0)
+                self.decomp_way = "svd"
+                self.correct_orthogonal_center(p1 + 1)
+                self.decomp_way = way
                 self.correct_orthogonal_center(c0)
-        self.decomp_way = way
+            else:
+                self.correct_orthogonal_center(0)
+                self.decomp_way = "svd"
+                self.correct_orthogonal_center(self.length - 1)
+                self.decomp_way = way
+                if c0 > 0:
+                    self.correct_orthogonal_center(c0)
+        finally:
+            self.decomp_way = way
+            self._dev.fast_gauge = False
 
     def calculate_entanglement_entropy(self):
         """MPSClass.py:834-839."""

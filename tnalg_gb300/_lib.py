@@ -6,6 +6,7 @@ raises if the library is missing or a call fails.
 import ctypes
 import os
 
+import numpy as np
 import torch
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -43,6 +44,10 @@ class LanczosOpts(ctypes.Structure):
                 ("precision", ctypes.c_int32), ("refine", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class SvItem(ctypes.Structure):
+    _fields_ = [("k", c_i64), ("n", c_i64), ("x", c_vp), ("sXr", c_i64), ("sXc", c_i64), ("s_out", c_vp)]
+
+
 class LanczosResult(ctypes.Structure):
     _fields_ = [("energy", c_dbl), ("residual", c_dbl), ("energy_fp64", c_dbl), ("matvecs", ctypes.c_int32),
                 ("restarts", ctypes.c_int32), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32)]
@@ -75,6 +80,8 @@ _SIGS = {
     "tn_singular_values": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_singular_values_noalloc": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp]),
+    "tn_singular_values_batched": (c_int, [c_int, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
+    "tn_singular_values_batched_workspace_bytes": (c_sz, [c_int, c_vp]),
     "tn_profile_enable": (c_int, [c_int]),
     "tn_profile_reset": (c_int, []),
     "tn_profile_read": (c_int, [c_int, c_vp, c_vp, c_vp]),
@@ -186,6 +193,29 @@ def terms_tensor(terms, device):
     raw = bytes(arr)[: 16 * max(n, 1)]
     host = torch.frombuffer(bytearray(raw), dtype=torch.uint8)
     return host.to(device), n
+
+
+def singular_values_batched(mats, ws=None, tol=1e-15, max_sweeps=60):
+    """Singular values (descending, numpy) of a list of 2-D CUDA tensors in one batched FP64 call."""
+    if not mats:
+        return []
+    lib = load()
+    outs = [torch.empty(int(M.shape[0]), dtype=torch.float64, device=M.device) for M in mats]
+    items = (SvItem * len(mats))()
+    for b, (M, o) in enumerate(zip(mats, outs)):
+        items[b].k, items[b].n = int(M.shape[0]), int(M.shape[1])
+        items[b].x = ptr(M).value
+        items[b].sXr, items[b].sXc = int(M.stride(0)), int(M.stride(1))
+        items[b].s_out = ptr(o).value
+    table = ctypes.cast(items, c_vp)
+    need = lib.tn_singular_values_batched_workspace_bytes(len(mats), table)
+    ws = ws or Workspace(mats[0].device)
+    buf = ws.get(need + 256)
+    base = (buf.data_ptr() + 255) // 256 * 256
+    check(lib.tn_singular_values_batched(len(mats), table, tol, max_sweeps, c_vp(base),
+                                         c_sz(buf.numel() - (base - buf.data_ptr())), stream_handle()),
+          "singular values")
+    return [np.sort(o.cpu().numpy())[::-1] for o in outs]
 
 
 def tf32x3_available():

@@ -1,4 +1,4 @@
-// Effective-Hamiltonian matvec (K1) and the device-resident Lanczos eigensolver (K2).
+// Effective-Hamiltonian matvec and the device-resident Lanczos eigensolver.
 //
 // The matvec replaces update_tensor_eigs_f_handle_optimized (MPSClass.py:755-776):
 //   H_eff psi = WL.psi(chi_l d, chi_r) + psi(chi_l, d chi_r).WR^T + sum_k SL_k psi SR_k^T

@@ -1,4 +1,4 @@
-// FP64 Householder QR for the DMRG gauge move (K4).
+// FP64 Householder QR for the DMRG gauge move.
 //
 // Replaces np.linalg.qr in left2right_decompose_tensor / right2left_decompose_tensor
 // (TensorBasicModule.py:314-384). Blocked right-looking Householder with the

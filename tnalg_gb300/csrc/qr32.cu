@@ -4,8 +4,9 @@
 // per SM, which makes the column-sequential Householder panel the bottleneck of an FP64 QR.
 // In a sweep the R factor of a gauge move only seeds the next local solve (the site it is
 // absorbed into is re-optimised right away), so only Q has to be accurate:
-//   1. Householder QR of the FP64 input rounded to FP32: Q32 with ||Q32^T Q32 - I|| ~ 1e-6
-//      whatever the conditioning of the input, R32 accurate to FP32. For n <= m <= 1024,
+//   1. Householder QR of the FP64 input scaled by a power of two (exact; any finite FP64 input fits
+//      FP32) and rounded to FP32: Q32 with ||Q32^T Q32 - I|| ~ 1e-6 whatever the conditioning of
+//      the input, R32 accurate to FP32 and scaled back. For n <= m <= 1024,
 //      n <= 512 the whole factorisation runs in one 16-CTA cluster kernel (qr_cluster.cu);
 //      otherwise one-CTA FP32 panels with FP32 GEMM trailing updates, Q formed backwards;
 //   2. E = Q^T Q - I in FP64 (CUDA-core FP64 GEMM), then Q <- Q - Q E / 2 on the tensor cores
@@ -91,11 +92,34 @@ int gemm32(const G32& g, cudaStream_t s) {
   return TN_OK;
 }
 
-__global__ void copy_in32(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, float* Aw) {
+// max |a| as the bits of a non-negative double (ordered like the values), into *amax (zeroed)
+__global__ void amax_kernel(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn,
+                            unsigned long long* amax) {
+  double mx = 0.0;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < m * n;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = idx / m, i = idx % m;
-    Aw[idx] = (float)a[i * sAm + j * sAn];
+    mx = fmax(mx, fabs(a[i * sAm + j * sAn]));
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(amax, (unsigned long long)__double_as_longlong(mx));
+}
+
+// exponent of the power of two that brings max |a| to [1, 2) (0 for a zero or non-finite max)
+__device__ __forceinline__ int scale_exponent(const unsigned long long* amax) {
+  const double mx = __longlong_as_double((long long)*amax);
+  return (mx > 0.0 && isfinite(mx)) ? ilogb(mx) : 0;
+}
+
+// FP64 -> FP32 copy scaled by an exact power of two, so any finite FP64 input fits FP32
+__global__ void copy_in32(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, float* Aw,
+                          const unsigned long long* amax) {
+  const double down = ldexp(1.0, -scale_exponent(amax));
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < m * n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = idx / m, i = idx % m;
+    Aw[idx] = (float)(a[i * sAm + j * sAn] * down);
   }
 }
 
@@ -192,7 +216,8 @@ __global__ void __launch_bounds__(NTP) panel32(int64_t m, int64_t j0, int jb, fl
 }
 
 __global__ void extract_mixed(int64_t m, int64_t n, int64_t k, const float* Aw, const float* Qw, double* Q64,
-                              double* r, int64_t sRm, int64_t sRn) {
+                              double* r, int64_t sRm, int64_t sRn, const unsigned long long* amax) {
+  const double up = ldexp(1.0, scale_exponent(amax));
   const int64_t tq = m * k, tr = k * n;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < tq + tr;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -201,7 +226,7 @@ __global__ void extract_mixed(int64_t m, int64_t n, int64_t k, const float* Aw, 
     } else {
       const int64_t e = idx - tq;
       const int64_t c = e / k, rr = e % k;
-      if (r) r[rr * sRm + c * sRn] = (c >= rr) ? (double)Aw[c * m + rr] : 0.0;
+      if (r) r[rr * sRm + c * sRn] = (c >= rr) ? (double)Aw[c * m + rr] * up : 0.0;
     }
   }
 }
@@ -231,6 +256,7 @@ size_t al(size_t x) { return (x + 1023) / 1024 * 1024; }
 struct MixWs {
   float *Aw, *Vf, *Qw, *T, *W, *W2, *Vc;
   double *Q64, *E, *QE;
+  unsigned long long* amax;
   char* tf_ws;
   size_t tf_bytes;
   char* g64_ws;
@@ -249,6 +275,7 @@ size_t mix_layout(int64_t m, int64_t n, char* base, MixWs* w) {
   w->W2 = (float*)take((size_t)NB * std::max(n, k) * 4);
   w->Vc = (float*)take(tn_qr32_cluster_scratch_floats(m, k) * 4);
   w->Q64 = (double*)take((size_t)m * k * 8);
+  w->amax = (unsigned long long*)take(sizeof(unsigned long long));
   w->E = (double*)take((size_t)k * k * 8);
   w->QE = (double*)take((size_t)m * k * 8);
   w->tf_bytes = tn_gemm_tf32x3_ws_bytes(m, k, k, 1, 1);
@@ -299,7 +326,10 @@ namespace {
 int qr32_blocked(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn, double* r, int64_t sRm,
                  int64_t sRn, const MixWs& w, cudaStream_t s) {
   const int64_t k = std::min(m, n), np = tn_cdiv(k, NB);
-  copy_in32<<<blocks_for(m * n), 256, 0, s>>>(m, n, a, sAm, sAn, w.Aw);
+  TN_CUDA(cudaMemsetAsync(w.amax, 0, sizeof(unsigned long long), s));
+  amax_kernel<<<blocks_for(m * n), 256, 0, s>>>(m, n, a, sAm, sAn, w.amax);
+  TN_CHECK_LAUNCH();
+  copy_in32<<<blocks_for(m * n), 256, 0, s>>>(m, n, a, sAm, sAn, w.Aw, w.amax);
   TN_CHECK_LAUNCH();
   init_q32<<<blocks_for(m * k), 256, 0, s>>>(m, k, w.Qw, w.Vf);
   TN_CHECK_LAUNCH();
@@ -331,7 +361,7 @@ int qr32_blocked(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn
     if ((st = gemm32({mr, nc, jb, w.Vf + j0 + j0 * m, 1, m, w.W2, nc, 1, w.Qw + j0 + j0 * m, 1, m, -1.f, 1.f}, s)))
       return st;
   }
-  extract_mixed<<<blocks_for(m * k + k * n), 256, 0, s>>>(m, n, k, w.Aw, w.Qw, w.Q64, r, sRm, sRn);
+  extract_mixed<<<blocks_for(m * k + k * n), 256, 0, s>>>(m, n, k, w.Aw, w.Qw, w.Q64, r, sRm, sRn, w.amax);
   TN_CHECK_LAUNCH();
   return TN_OK;
 }

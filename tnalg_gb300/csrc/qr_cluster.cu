@@ -49,6 +49,8 @@ struct Smem {
   float tau[BW];              // tau of every reflector of the panel
   float piv;                  // the current pivot a(j, j)
   unsigned long long ready[CL];  // mbarrier per panel
+  double amax[CL];            // largest |a| of every CTA's block
+  double wmax[NW];            // per-warp maxima of this CTA's block
   int failed;
 };
 
@@ -181,7 +183,7 @@ __device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ V
       for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int b = 0; b < 8; ++b) out[a][b] = 0.f;
-#pragma unroll
+#pragma unroll 1
       for (int k4 = 0; k4 < BW / 4; ++k4) {
         float v[8][4];
 #pragma unroll
@@ -219,144 +221,124 @@ __device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ V
 }
 
 // Householder QR of this CTA's panel (columns 0..jb-1 of the block, rows >= j0 = 32 q), then its
-// compact-WY factor T (dlarft, forward, columnwise) in sh.T. The panel is held in registers while
-// it is factorised: thread t owns rows t and t + NT of the 32 columns (a[2][32]), and the column
-// loop is unrolled at compile time (PanelStep<I>) so every column index is static.
-struct PanelCtx {
+// compact-WY factor T (dlarft, forward, columnwise) in sh.T.
+// The panel is held in registers: thread t owns rows t and t + NT of the 32 columns, a[2][32], used
+// as a ring. At step i the slots 0..31-i hold the unfinished columns i..31 (slot 0 = the pivot
+// column) and the slots 32-i..31 hold the finished reflectors v_0..v_{i-1} (masked: 0 above the
+// diagonal, 1 on it). Every step works on slot 0 and then rotates the ring by one, so all steps run
+// the same code with static register indices (a fully unrolled column loop does not fit the
+// instruction cache), and one transposed reduction per step yields both the column-update
+// coefficients (unfinished slots) and the Gram entries v_l^T v_i of T (finished slots).
+__device__ void factor_panel(Smem& sh, int m, int j0, int jb) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   float a[2][BW];
-  float s;  // this thread's part of the sum of squares below the current pivot
-  int m, j0, jb, t, lane, warp;
-};
-
-template <int I>
-__device__ __forceinline__ void panel_step(Smem& sh, PanelCtx& P) {
-  if (I >= P.jb) return;
-  const int j = P.j0 + I;
-  float s = P.s;
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (P.lane == 0) sh.red[P.warp * LDW + BW] = s;
-#pragma unroll
-  for (int rr = 0; rr < 2; ++rr)
-    if (P.t + rr * NT == j) sh.piv = P.a[rr][I];
-  __syncthreads();
-  // reflector, computed redundantly by every thread
-  float sig = 0.f;
-#pragma unroll
-  for (int w = 0; w < NW; ++w) sig += sh.red[w * LDW + BW];
-  const float x1 = sh.piv;
-  float beta = x1, tau = 0.f, scale = 0.f;
-  if (sig > 0.f) {
-    const float nrm = sqrtf(fmaf(x1, x1, sig));
-    beta = (x1 >= 0.f) ? -nrm : nrm;
-    tau = (beta - x1) / beta;
-    scale = 1.f / (x1 - beta);
-  }
-  // v (v(j) = 1) kept below the pivot; products of v with every other panel column: c > I gives
-  // the column update, c < I the Gram entries v_c^T v_I of T
-  float v[2];
 #pragma unroll
   for (int rr = 0; rr < 2; ++rr) {
-    const int r = P.t + rr * NT;
-    v[rr] = 0.f;
-    if (r < P.m) {
-      if (r > j) {
-        P.a[rr][I] *= scale;
-        v[rr] = P.a[rr][I];
-      } else if (r == j) {
-        v[rr] = 1.f;
+    const int r = t + rr * NT;
+#pragma unroll
+    for (int c = 0; c < BW; ++c) a[rr][c] = (r < m) ? sh.C[c * LDC + r] : 0.f;
+  }
+  float s = 0.f;  // this thread's part of the sum of squares below the current pivot
+#pragma unroll
+  for (int rr = 0; rr < 2; ++rr) {
+    const int r = t + rr * NT;
+    if (r > j0 && r < m) s = fmaf(a[rr][0], a[rr][0], s);
+  }
+#pragma unroll 1
+  for (int i = 0; i < jb; ++i) {
+    const int j = j0 + i;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sh.red[warp * LDW + BW] = s;
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr)
+      if (t + rr * NT == j) sh.piv = a[rr][0];
+    __syncthreads();
+    // reflector, computed redundantly by every thread
+    float sig = 0.f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) sig += sh.red[w * LDW + BW];
+    const float x1 = sh.piv;
+    float beta = x1, tau = 0.f, scale = 0.f;
+    if (sig > 0.f) {
+      const float nrm = sqrtf(fmaf(x1, x1, sig));
+      beta = (x1 >= 0.f) ? -nrm : nrm;
+      tau = (beta - x1) / beta;
+      scale = 1.f / (x1 - beta);
+    }
+    // v_i (masked) of this thread's rows; the pivot slot keeps v below the diagonal
+    float v[2];
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+      const int r = t + rr * NT;
+      v[rr] = 0.f;
+      if (r < m) {
+        if (r > j) {
+          a[rr][0] *= scale;
+          v[rr] = a[rr][0];
+        } else if (r == j) {
+          v[rr] = 1.f;
+        }
       }
     }
-  }
-  float p[BW];
+    float p[BW];
+    p[0] = 0.f;
 #pragma unroll
-  for (int c = 0; c < BW; ++c) p[c] = (c == I) ? 0.f : fmaf(v[0], P.a[0][c], v[1] * P.a[1][c]);
-  const float ws = warp_transpose_sum(p, P.lane);
-  sh.red[P.warp * LDW + P.lane] = ws;
-  __syncthreads();
-  if (P.warp == 0) {
-    float tot = 0.f;
+    for (int c = 1; c < BW; ++c) p[c] = fmaf(v[0], a[0][c], v[1] * a[1][c]);
+    const float ws = warp_transpose_sum(p, lane);
+    sh.red[warp * LDW + lane] = ws;
+    __syncthreads();
+    if (warp == 0) {
+      float tot = 0.f;
 #pragma unroll
-    for (int w = 0; w < NW; ++w) tot += sh.red[w * LDW + P.lane];
-    sh.f[P.lane] = (P.lane > I && P.lane < P.jb) ? tau * tot : 0.f;
-    if (P.lane < I) sh.G[P.lane * LDW + I] = tot;
-    if (P.lane == 0) sh.tau[I] = tau;
-  }
-#pragma unroll
-  for (int rr = 0; rr < 2; ++rr)
-    if (P.t + rr * NT == j) P.a[rr][I] = beta;  // R(j, j)
-  __syncthreads();
-  // column update, and the next column's sum of squares below its pivot
-  float fc[BW];
-#pragma unroll
-  for (int c4 = 0; c4 < BW / 4; ++c4) {
-    const float4 f4 = reinterpret_cast<const float4*>(sh.f)[c4];
-    fc[4 * c4] = f4.x;
-    fc[4 * c4 + 1] = f4.y;
-    fc[4 * c4 + 2] = f4.z;
-    fc[4 * c4 + 3] = f4.w;
-  }
-  float s2 = 0.f;
-#pragma unroll
-  for (int rr = 0; rr < 2; ++rr) {
-#pragma unroll
-    for (int c = I + 1; c < BW; ++c) P.a[rr][c] = fmaf(-v[rr], fc[c], P.a[rr][c]);
-    if (I + 1 < BW) {
-      const int r = P.t + rr * NT;
-      const float y = (r > j + 1) ? P.a[rr][(I + 1) % BW] : 0.f;
-      s2 = fmaf(y, y, s2);
+      for (int w = 0; w < NW; ++w) tot += sh.red[w * LDW + lane];
+      const bool unfinished = lane >= 1 && lane <= BW - 1 - i && i + lane < jb;
+      sh.f[lane] = unfinished ? tau * tot : 0.f;
+      if (lane >= BW - i) sh.G[(lane - BW + i) * LDW + i] = tot;  // slot 32 - i + l holds v_l
+      if (lane == 0) sh.tau[i] = tau;
     }
-  }
-  P.s = s2;
-  // no barrier here: the next step rewrites red/piv before its first barrier and f after its
-  // second, and every reader of this step's values has passed this step's later barriers
-}
-
-template <int I>
-struct PanelLoop {
-  static __device__ __forceinline__ void run(Smem& sh, PanelCtx& P) {
-    panel_step<I>(sh, P);
-    PanelLoop<I + 1>::run(sh, P);
-  }
-};
-template <>
-struct PanelLoop<BW> {
-  static __device__ __forceinline__ void run(Smem&, PanelCtx&) {}
-};
-
-__device__ void factor_panel(Smem& sh, int m, int j0, int jb) {
-  PanelCtx P;
-  P.m = m;
-  P.j0 = j0;
-  P.jb = jb;
-  P.t = threadIdx.x;
-  P.lane = P.t & 31;
-  P.warp = P.t >> 5;
 #pragma unroll
-  for (int rr = 0; rr < 2; ++rr) {
-    const int r = P.t + rr * NT;
+    for (int rr = 0; rr < 2; ++rr)
+      if (t + rr * NT == j) a[rr][0] = beta;  // R(j, j)
+    __syncthreads();
+    // column update of the unfinished slots (f is zero on the finished ones), and the next
+    // column's sum of squares below its pivot
+    float fc[BW];
 #pragma unroll
-    for (int c = 0; c < BW; ++c) P.a[rr][c] = (r < m) ? sh.C[c * LDC + r] : 0.f;
-  }
-  P.s = 0.f;
-#pragma unroll
-  for (int rr = 0; rr < 2; ++rr) {
-    const int r = P.t + rr * NT;
-    if (r > j0 && r < m) P.s = fmaf(P.a[rr][0], P.a[rr][0], P.s);
-  }
-  PanelLoop<0>::run(sh, P);
-#pragma unroll
-  for (int rr = 0; rr < 2; ++rr) {
-    const int r = P.t + rr * NT;
-    if (r < m) {
-#pragma unroll
-      for (int c = 0; c < BW; ++c) sh.C[c * LDC + r] = P.a[rr][c];
+    for (int c4 = 0; c4 < BW / 4; ++c4) {
+      const float4 f4 = reinterpret_cast<const float4*>(sh.f)[c4];
+      fc[4 * c4] = f4.x;
+      fc[4 * c4 + 1] = f4.y;
+      fc[4 * c4 + 2] = f4.z;
+      fc[4 * c4 + 3] = f4.w;
     }
+    s = 0.f;
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+#pragma unroll
+      for (int c = 1; c < BW; ++c) a[rr][c] = fmaf(-v[rr], fc[c], a[rr][c]);
+      const int r = t + rr * NT;
+      const float y = (r > j + 1) ? a[rr][1] : 0.f;
+      s = fmaf(y, y, s);
+    }
+    // retire the pivot column: R part and v to shared memory, masked v into the ring
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+      const int r = t + rr * NT;
+      if (r < m) sh.C[i * LDC + r] = a[rr][0];
+      const float done = v[rr];
+#pragma unroll
+      for (int c = 0; c < BW - 1; ++c) a[rr][c] = a[rr][c + 1];
+      a[rr][BW - 1] = done;
+    }
+    // no barrier here: the next step rewrites red/piv before its first barrier and f after its
+    // second, and every reader of this step's values has passed this step's later barriers
   }
+  __syncthreads();
   // T(k, i) = -tau_i sum_{l=k}^{i-1} T(k, l) G(l, i), T(i, i) = tau_i: lane k of warp 0 runs row k
   // with the row in registers
-  if (P.warp == 0) {
-    const int k = P.lane;
+  if (warp == 0) {
+    const int k = lane;
     float tr[BW];
 #pragma unroll
     for (int i = 0; i < BW; ++i) {
@@ -392,19 +374,49 @@ __global__ void __launch_bounds__(NT, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sh.failed = 0;
   }
-  // own column block, FP64 -> FP32 (columns beyond n are zero)
-  if (sAn == 1) {
-    for (int e = t; e < m * BW; e += NT) {
-      const int r = e / BW, c = e % BW;
-      sh.C[c * LDC + r] = (c < jb) ? (float)A[(int64_t)r * sAm + col0 + c] : 0.f;
+  // element e of this CTA's block (columns beyond n are zero), coalesced along the unit stride
+  auto elem = [&](int e, int& r, int& c) -> double {
+    if (sAn == 1) {
+      r = e / BW;
+      c = e % BW;
+    } else {
+      c = e / m;
+      r = e % m;
     }
-  } else {
+    return (c < jb) ? A[(int64_t)r * sAm + (int64_t)(col0 + c) * sAn] : 0.0;
+  };
+  cluster_sync();  // every CTA of the cluster is running before any remote store into it
+  // largest |a| of the block, published to every CTA: the whole matrix is scaled by one power of
+  // two (exact) so that any finite FP64 input fits FP32; R is scaled back on output
+  {
+    double mx = 0.0;
     for (int e = t; e < m * BW; e += NT) {
-      const int c = e / m, r = e % m;
-      sh.C[c * LDC + r] = (c < jb) ? (float)A[(int64_t)r * sAm + (int64_t)(col0 + c) * sAn] : 0.f;
+      int r, c;
+      mx = fmax(mx, fabs(elem(e, r, c)));
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((t & 31) == 0) sh.wmax[t >> 5] = mx;
+    __syncthreads();
+    if (t < CL) {
+      double cm = 0.0;
+      for (int w = 0; w < NW; ++w) cm = fmax(cm, sh.wmax[w]);
+      uint32_t ra;
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_u32(&sh.amax[q])), "r"(t));
+      asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(ra), "d"(cm) : "memory");
     }
   }
-  cluster_sync();  // mbarriers of every CTA initialised before any remote arrive
+  cluster_sync();  // maxima published; mbarriers of every CTA initialised before any remote arrive
+  double gmax = 0.0;
+  for (int p = 0; p < CL; ++p) gmax = fmax(gmax, sh.amax[p]);
+  const int ex = (gmax > 0.0 && isfinite(gmax)) ? ilogb(gmax) : 0;
+  const double down = ldexp(1.0, -ex), up = ldexp(1.0, ex);
+  for (int e = t; e < m * BW; e += NT) {
+    int r, c;
+    const double v = elem(e, r, c);
+    sh.C[c * LDC + r] = (float)(v * down);
+  }
+  __syncthreads();
 
   if (jb > 0) {
     // updates by the panels to the left, in order
@@ -439,7 +451,7 @@ __global__ void __launch_bounds__(NT, 1)
           const int r = e / BW, c = e % BW;
           if (c < jb) {
             const int d = col0 + c;
-            R[(int64_t)r * sRm + (int64_t)d * sRn] = (r <= d) ? (double)sh.C[c * LDC + r] : 0.0;
+            R[(int64_t)r * sRm + (int64_t)d * sRn] = (r <= d) ? (double)sh.C[c * LDC + r] * up : 0.0;
           }
         }
       }

@@ -1,4 +1,4 @@
-// One-sided (Hestenes) Jacobi singular values in FP64 (K5).
+// One-sided (Hestenes) Jacobi singular values in FP64 (entanglement spectrum).
 //
 // Replaces the np.linalg.svd of decompose(..., way='svd') used by
 // calculate_entanglement_spectrum (MPSClass.py:812-832,
@@ -10,6 +10,8 @@
 // k/2 independent pairs (one CTA each); a sweep is k-1 rounds. The host reads a
 // single "rotated" flag per sweep and stops when a sweep rotates nothing.
 #include <math.h>
+
+#include <vector>
 
 #include "common.cuh"
 
@@ -126,6 +128,201 @@ extern "C" int tn_singular_values(int64_t k, int64_t n, const double* x, int64_t
   row_norms<<<(unsigned)k, NT, 0, s>>>(k, n, X, s_out);
   TN_CHECK_LAUNCH();
   return TN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched variant: the singular values of many independent matrices (e.g. the R factors of every
+// bond of a chain) with one launch per Jacobi round for the whole batch, so the ~k launches per
+// sweep are paid once instead of once per matrix. Each matrix runs its own round-robin schedule
+// (round r uses r mod (kp - 1)); a matrix with fewer rows simply repeats rounds, which only
+// rotates pairs that are still non-orthogonal. FP64 throughout: with FP32 rows the rounded
+// rotations drift the row norms by ~1e-4 over the thousands of rotations a 512-row matrix takes.
+
+namespace {
+
+template <typename T>
+struct SvItem {
+  int64_t k, kp, n;
+  const double* x;
+  int64_t sXr, sXc;
+  double* s_out;
+  T* X;
+};
+
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__global__ void svb_copy_in(const SvItem<T>* items) {
+  const SvItem<T> it = items[blockIdx.y];
+  const int64_t total = it.kp * it.n;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = idx / it.n, c = idx % it.n;
+    it.X[idx] = r < it.k ? (T)it.x[r * it.sXr + c * it.sXc] : (T)0;
+  }
+}
+
+template <typename T>
+__global__ void svb_round(const SvItem<T>* items, int64_t r, T tol, int* rotated) {
+  const SvItem<T> it = items[blockIdx.y];
+  const int64_t i = blockIdx.x;
+  if (it.kp < 2 || i >= it.kp / 2) return;
+  const int64_t rr = r % (it.kp - 1);
+  const int64_t p = rr_player(i, rr, it.kp), q = rr_player(it.kp - 1 - i, rr, it.kp);
+  T* xp = it.X + p * it.n;
+  T* xq = it.X + q * it.n;
+  T a = 0, b = 0, g = 0;
+  for (int64_t t = threadIdx.x; t < it.n; t += blockDim.x) {
+    const T u = xp[t], v = xq[t];
+    a += u * u;
+    b += v * v;
+    g += u * v;
+  }
+  __shared__ T red[3][NT / 32];
+  __shared__ T cs[2];
+  a = warp_sum_t(a);
+  b = warp_sum_t(b);
+  g = warp_sum_t(g);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][wid] = a;
+    red[1][wid] = b;
+    red[2][wid] = g;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T A = 0, B = 0, G = 0;
+    for (int w = 0; w < NT / 32; ++w) {
+      A += red[0][w];
+      B += red[1][w];
+      G += red[2][w];
+    }
+    T c = 1, sn = 0;
+    if (G != (T)0 && fabs(G) > tol * sqrt(A * B)) {
+      const T zeta = (B - A) / (2 * G);
+      const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+      c = (T)1 / sqrt((T)1 + tt * tt);
+      sn = c * tt;
+      *rotated = 1;
+    }
+    cs[0] = c;
+    cs[1] = sn;
+  }
+  __syncthreads();
+  const T c = cs[0], sn = cs[1];
+  if (sn == (T)0) return;
+  for (int64_t t = threadIdx.x; t < it.n; t += blockDim.x) {
+    const T u = xp[t], v = xq[t];
+    xp[t] = c * u - sn * v;
+    xq[t] = sn * u + c * v;
+  }
+}
+
+template <typename T>
+__global__ void svb_row_norms(const SvItem<T>* items) {
+  const SvItem<T> it = items[blockIdx.y];
+  const int64_t r = blockIdx.x;
+  if (r >= it.k) return;
+  double a = 0.0;
+  for (int64_t t = threadIdx.x; t < it.n; t += blockDim.x) {
+    const double v = (double)it.X[r * it.n + t];
+    a = fma(v, v, a);
+  }
+  __shared__ double red[NT / 32];
+  a = tn_warp_sum(a);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double A = 0;
+    for (int w = 0; w < NT / 32; ++w) A += red[w];
+    it.s_out[r] = sqrt(A);
+  }
+}
+
+size_t svb_align(size_t x) { return (x + 255) / 256 * 256; }
+
+template <typename T>
+size_t svb_layout(int count, const tn_sv_item* items, char* base, std::vector<SvItem<T>>* out) {
+  size_t off = 256 + svb_align(sizeof(SvItem<T>) * (size_t)count);
+  for (int b = 0; b < count; ++b) {
+    const int64_t k = items[b].k, n = items[b].n, kp = k + (k & 1);
+    if (out) {
+      SvItem<T> it;
+      it.k = k;
+      it.kp = kp;
+      it.n = n;
+      it.x = items[b].x;
+      it.sXr = items[b].sXr;
+      it.sXc = items[b].sXc;
+      it.s_out = items[b].s_out;
+      it.X = (T*)(base + off);
+      out->push_back(it);
+    }
+    off += svb_align(sizeof(T) * (size_t)kp * n);
+  }
+  return off;
+}
+
+template <typename T>
+int svb_run(int count, const tn_sv_item* items, T tol, int max_sweeps, void* ws, cudaStream_t s) {
+  char* base = (char*)ws;
+  std::vector<SvItem<T>> host;
+  svb_layout<T>(count, items, base, &host);
+  int* flag = (int*)base;
+  SvItem<T>* dev_items = (SvItem<T>*)(base + 256);
+  TN_CUDA(cudaMemcpyAsync(dev_items, host.data(), sizeof(SvItem<T>) * host.size(), cudaMemcpyHostToDevice, s));
+  int64_t kpmax = 0, kmax = 0, nmax = 0;
+  for (const auto& it : host) {
+    kpmax = std::max(kpmax, it.kp);
+    kmax = std::max(kmax, it.k);
+    nmax = std::max(nmax, it.n);
+  }
+  const dim3 cgrid((unsigned)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(kpmax * nmax, NT), 64)), (unsigned)count);
+  svb_copy_in<T><<<cgrid, NT, 0, s>>>(dev_items);
+  TN_CHECK_LAUNCH();
+  if (kpmax >= 2) {
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+      TN_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+      for (int64_t r = 0; r < kpmax - 1; ++r) {
+        svb_round<T><<<dim3((unsigned)(kpmax / 2), (unsigned)count), NT, 0, s>>>(dev_items, r, tol, flag);
+        TN_CHECK_LAUNCH();
+      }
+      int h = 0;
+      TN_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+      TN_CUDA(cudaStreamSynchronize(s));
+      if (!h) break;
+    }
+  }
+  svb_row_norms<T><<<dim3((unsigned)std::max<int64_t>(kmax, 1), (unsigned)count), NT, 0, s>>>(dev_items);
+  TN_CHECK_LAUNCH();
+  // the item table is read by the launches above: keep the host copy alive until they ran
+  TN_CUDA(cudaStreamSynchronize(s));
+  return TN_OK;
+}
+
+}  // namespace
+
+extern "C" size_t tn_singular_values_batched_workspace_bytes(int count, const tn_sv_item* items) {
+  if (count <= 0 || !items) return 256;
+  return svb_layout<double>(count, items, nullptr, nullptr);
+}
+
+extern "C" int tn_singular_values_batched(int count, const tn_sv_item* items, double tol, int max_sweeps, void* ws,
+                                          size_t ws_bytes, void* stream) {
+  if (count <= 0) return TN_OK;
+  if (!items || count > 65535) return tn_fail(TN_ERR_ARG, "singular_values_batched: bad item table");
+  for (int b = 0; b < count; ++b)
+    if (items[b].k <= 0 || items[b].n <= 0 || !items[b].x || !items[b].s_out)
+      return tn_fail(TN_ERR_ARG, "singular_values_batched: bad item");
+  if (!ws || ws_bytes < tn_singular_values_batched_workspace_bytes(count, items) ||
+      ((uintptr_t)ws & 255) != 0)
+    return tn_fail(TN_ERR_WORKSPACE, "singular_values_batched: workspace too small or not 256-byte aligned");
+  return svb_run<double>(count, items, tol, max_sweeps, ws, (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------------------

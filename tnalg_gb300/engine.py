@@ -206,8 +206,11 @@ class DeviceMPS:
         self.er_from = self.length + 1   # ER[er_from..L] valid
         self.stats = {"matvecs": 0, "solves": 0, "restarts": 0, "unconverged": 0}
         # tn_qr_mixed (FP32 cluster QR + FP64 re-orthogonalisation) for the seeding moves of the
-        # tf32x3 path; TNALG_MIXED_QR=0 keeps every move on the FP64 Householder QR
+        # tf32x3 path, and for every move while fast_gauge is set (bond growth, entanglement
+        # spectrum: the state is then kept to ~1e-7); TNALG_MIXED_QR=0 keeps every move on the
+        # FP64 Householder QR
         self.mixed_qr = os.environ.get("TNALG_MIXED_QR", "1") != "0"
+        self.fast_gauge = False
 
     # -- model / environments ----------------------------------------------------
     def set_model(self, model):
@@ -321,10 +324,10 @@ class DeviceMPS:
 
     # -- gauge -------------------------------------------------------------------
     def _qr(self, mm, nn, A, sA, Q, sQ, R, seed_only):
-        """tn_qr, or tn_qr_mixed for a seeding move of the mixed-precision path (R only seeds the
-        next local solve there, Q stays orthonormal to ~1e-12)."""
+        """tn_qr, or tn_qr_mixed on the mixed-precision path for a seeding move (R only seeds the
+        next local solve) or while fast_gauge is set; Q stays orthonormal to ~1e-12 either way."""
         lib, st = L.load(), L.stream_handle()
-        if (self.mixed_qr and seed_only and self.unit_norm and self.precision == L.PREC_TF32X3
+        if (self.mixed_qr and (seed_only or self.fast_gauge) and self.precision == L.PREC_TF32X3
                 and min(mm, nn) >= 64):
             wp, wb = self.ws2.args(lib.tn_qr_mixed_workspace_bytes(mm, nn))
             L.check(lib.tn_qr_mixed(mm, nn, L.ptr(A), sA[0], sA[1], L.ptr(Q), sQ[0], sQ[1], L.ptr(R), nn, 1, wp, wb,
@@ -548,7 +551,7 @@ class _Observer:
     Operator chains that share their first site and operator are contracted once.
     """
 
-    def __init__(self, mps):
+    def __init__(self, mps, precision=L.PREC_FP64):
         self.s = mps
         self.dev = mps.device
         self.c = mps.center
@@ -556,6 +559,9 @@ class _Observer:
         self.F = {}
         self.lib = L.load()
         self.st = L.stream_handle()
+        # transfer products in FP64, or split TF32 for long operator strings of the mixed path
+        self.prec = int(precision)
+        self.ws = mps.ws if self.prec != L.PREC_FP64 else None
 
     # transfer helpers -------------------------------------------------------------
     def _op_apply(self, X, shape, op):
@@ -572,14 +578,14 @@ class _Observer:
             return M
         cl, d, cr = M.shape
         X = torch.empty_like(M)
-        L.gemm(V, M, X, cl, d * cr, cl, (cl, 1), (d * cr, 1), (d * cr, 1))
+        L.gemm(V, M, X, cl, d * cr, cl, (cl, 1), (d * cr, 1), (d * cr, 1), precision=self.prec, ws=self.ws)
         return X
 
     def left_close(self, M, X):
         """V' = M(cl*d, cr)^T . X(cl*d, cr)."""
         cl, d, cr = M.shape
         out = torch.empty((cr, cr), dtype=torch.float64, device=self.dev)
-        L.gemm(M, X, out, cr, cr, cl * d, (1, cr), (cr, 1), (cr, 1))
+        L.gemm(M, X, out, cr, cr, cl * d, (1, cr), (cr, 1), (cr, 1), precision=self.prec, ws=self.ws)
         return out
 
     def tl(self, M, V, op=None):
@@ -594,14 +600,14 @@ class _Observer:
             return M
         cl, d, cr = M.shape
         X = torch.empty_like(M)
-        L.gemm(M, V, X, cl * d, cr, cr, (cr, 1), (1, cr), (cr, 1))
+        L.gemm(M, V, X, cl * d, cr, cr, (cr, 1), (1, cr), (cr, 1), precision=self.prec, ws=self.ws)
         return X
 
     def right_close(self, M, X):
         """V'[a', a] = sum M[a', (s b)] X[a, (s b)]."""
         cl, d, cr = M.shape
         out = torch.empty((cl, cl), dtype=torch.float64, device=self.dev)
-        L.gemm(M, X, out, cl, cl, d * cr, (d * cr, 1), (1, d * cr), (cl, 1))
+        L.gemm(M, X, out, cl, cl, d * cr, (d * cr, 1), (1, d * cr), (cl, 1), precision=self.prec, ws=self.ws)
         return out
 
     def tr(self, M, V, op=None):
@@ -686,8 +692,8 @@ class _Observer:
         return v1, v2
 
 
-def observe(mps, one, two):
-    """Device expectation values; see _Observer."""
+def observe(mps, one, two, precision=L.PREC_FP64):
+    """Device expectation values; see _Observer. precision applies to the transfer products."""
     if mps.center < 0:
         raise RuntimeError("observables need a central-orthogonal MPS (call correct_orthogonal_center first)")
-    return _Observer(mps).run(one, two)
+    return _Observer(mps, precision).run(one, two)

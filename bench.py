@@ -181,6 +181,8 @@ def run_ours(args, rank, world, local_rank):
     ms = start.elapsed_time(stop)
     launches = L.launch_count() - launches0
     mv_ms, mv_cnt, mv_flops = L.profile_read(0)
+    qr_ms, qr_cnt, qr_flops = L.profile_read(1)
+    lz_ms, lz_cnt, _ = L.profile_read(4)
     lib.tn_profile_enable(0)
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -192,7 +194,8 @@ def run_ours(args, rank, world, local_rank):
     eb = A.observe_bond_energy(para["index2"], para["coeff2"])
     e_site = float(np.sum(eb)) / L_
     res = {"ms": ms, "wall": wall, "solves": solves, "matvecs": matvecs, "mv_ms": mv_ms, "mv_cnt": mv_cnt,
-           "mv_flops": mv_flops, "precision": precision, "e_per_site": e_site, "clocks": clk.summary(),
+           "mv_flops": mv_flops, "qr_ms": qr_ms, "qr_cnt": qr_cnt, "qr_flops": qr_flops, "lz_ms": lz_ms,
+           "lz_cnt": lz_cnt, "precision": precision, "e_per_site": e_site, "clocks": clk.summary(),
            "launches": launches, "chi_max": int(A.virtual_dim.max())}
     return res, A, para
 
@@ -313,14 +316,29 @@ def main():
     ms_step = res["ms"] / args.steps
     value = world * args.steps / (res["ms"] / 1000.0)
     mixed = res["precision"] != "fp64"
-    avg_ms = res["mv_ms"] / max(res["mv_cnt"], 1)
-    achieved = (res["mv_flops"] / max(res["mv_cnt"], 1)) / (avg_ms / 1000.0) / 1e12 if res["mv_cnt"] else 0.0
     if mixed:
         peak = pk["bf16_tflops_sustained"] / 2.0 / 3.0
         peak_note = "3xTF32 useful-flop peak = measured sustained bf16 / 2 (tf32 rate) / 3 products"
     else:
         peak = 1.25
         peak_note = "nominal GB300 FP64 1.25 TFLOP/s (no FP64 entry in MEASURED_PEAKS.json)"
+
+    def kernel_roofline(name, t_ms, cnt, flops, figure):
+        avg = t_ms / max(cnt, 1)
+        ach = (flops / max(cnt, 1)) / (avg / 1000.0) / 1e12 if cnt and avg > 0 else 0.0
+        return {"bound": "tensor" if mixed else "fp64", "kernel": name, "achieved": ach, "peak": peak,
+                "unit": "TFLOP/s", "frac": ach / peak if peak else None, "traffic": None, "avg_launch_ms": avg,
+                "launches": cnt, "flops_per_launch": flops / max(cnt, 1), "work_figure": figure,
+                "device_ms_per_sweep": t_ms / args.steps, "peak_source": pk_kind, "peak_note": peak_note}
+
+    mv_line = kernel_roofline("effective-Hamiltonian matvec (tcgen05 split-TF32 block GEMMs)" if mixed else
+                              "effective-Hamiltonian matvec (FP64 block GEMMs)", res["mv_ms"], res["mv_cnt"],
+                              res["mv_flops"], "F_mv = 2 d chil chir (chil (n_L + n_S) + chir (n_R + n_S))")
+    qr_line = kernel_roofline("gauge-move QR (tn_qr_mixed: FP32 cluster QR + FP64 re-orthogonalisation)" if mixed
+                              else "gauge-move QR (tn_qr: FP64 Householder)", res["qr_ms"], res["qr_cnt"],
+                              res["qr_flops"], "F_qr = 2 m n^2 - 2 n^3 / 3, m = d chi, n = chi")
+    # the roofline object describes the kernel class with the most device time in the timed sweeps
+    dominant, other = (qr_line, mv_line) if res["qr_ms"] > res["mv_ms"] else (mv_line, qr_line)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if not mixed else "tf32x3+f64", "data": "synthetic",
@@ -333,11 +351,11 @@ def main():
             "solves_per_s": world * res["solves"] / (res["ms"] / 1000.0),
             "matvecs_per_solve": res["matvecs"] / max(res["solves"], 1),
             "e_per_site": res["e_per_site"],
-            "roofline": {"bound": "tensor" if mixed else "fp64", "kernel": "effective-Hamiltonian matvec "
-                         "(block GEMMs)", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak if peak else None, "traffic": None,
-                         "avg_launch_ms": avg_ms, "launches": res["mv_cnt"], "peak_source": pk_kind,
-                         "peak_note": peak_note},
+            "roofline": dominant,
+            "roofline_other": other,
+            "device_ms_per_sweep": {"qr": res["qr_ms"] / args.steps, "lanczos_incl_matvec": res["lz_ms"] / args.steps,
+                                    "matvec": res["mv_ms"] / args.steps,
+                                    "rest": ms_step - (res["qr_ms"] + res["lz_ms"]) / args.steps},
             "clocks": res["clocks"], "gpu_launches": res["launches"]}
     if rank == 0 and not args.no_e2e:
         line["e2e"] = run_e2e(args, "cuda:%d" % local_rank, res["precision"])

@@ -423,8 +423,8 @@ extern "C" size_t tn_lanczos_workspace_bytes(const tn_site_desc* desc, const tn_
   return lanczos_layout(desc, opts, nullptr, &L);
 }
 
-extern "C" int tn_lanczos(const tn_site_desc* desc, double* psi, const tn_lanczos_opts* o, void* ws,
-                          size_t ws_bytes, tn_lanczos_result* res, void* stream) {
+static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_opts* o, void* ws,
+                        size_t ws_bytes, tn_lanczos_result* res, void* stream) {
   int st = check_desc(desc);
   if (st) return st;
   if (!psi || !o || !res) return tn_fail(TN_ERR_ARG, "lanczos: null argument");
@@ -557,4 +557,12 @@ extern "C" int tn_lanczos(const tn_site_desc* desc, double* psi, const tn_lanczo
   res->restarts = restarts;
   res->converged = converged ? 1 : 0;
   return converged ? TN_OK : TN_ERR_NOCONV;
+}
+
+extern "C" int tn_lanczos(const tn_site_desc* desc, double* psi, const tn_lanczos_opts* o, void* ws,
+                          size_t ws_bytes, tn_lanczos_result* res, void* stream) {
+  cudaEvent_t ev = tn_profile_begin((cudaStream_t)stream);
+  const int st = lanczos_impl(desc, psi, o, ws, ws_bytes, res, stream);
+  tn_profile_end(ev, (cudaStream_t)stream, TN_PROF_LANCZOS, 0.0);
+  return st;
 }

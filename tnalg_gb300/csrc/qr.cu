@@ -519,6 +519,7 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
     g_tn_launches += kernels;
     st = TN_OK;
   }
-  tn_profile_end(ev_all, s, TN_PROF_QR, 4.0 * m * n * n - 4.0 / 3.0 * n * n * (double)n);
+  // algorithmic work of the factorisation, 2mn^2 - 2n^3/3 (forming Q is not counted)
+  tn_profile_end(ev_all, s, TN_PROF_QR, 2.0 * m * n * (double)n - 2.0 / 3.0 * n * n * (double)n);
   return st;
 }

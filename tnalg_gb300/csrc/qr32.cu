@@ -316,7 +316,8 @@ extern "C" int tn_qr_mixed(int64_t m, int64_t n, const double* a, int64_t sAm, i
     if ((st = qr32_blocked(m, n, a, sAm, sAn, r, sRm, sRn, w, s))) return st;
   }
   if ((st = refine_q(m, k, q, sQm, sQn, w, s))) return st;
-  tn_profile_end(ev, s, TN_PROF_QR, 0.0);
+  // algorithmic work of the factorisation, 2mn^2 - 2n^3/3 (for m >= n; forming Q is not counted)
+  tn_profile_end(ev, s, TN_PROF_QR, 2.0 * m * k * (double)k - 2.0 / 3.0 * k * k * (double)k);
   return TN_OK;
 }
 

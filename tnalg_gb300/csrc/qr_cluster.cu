@@ -174,10 +174,13 @@ __device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ V
     sh.W2[k * LDW2 + c] = s;
   }
   __syncthreads();
-  // C -= V W2: 8 rows x 8 columns per thread
+  // C -= V W2: 8 rows x 8 columns per thread. The rows of a thread are 128 apart and a warp's 8
+  // row groups are consecutive, so with the odd pitch LDC the 32 lanes hit 32 distinct banks of C
+  // while the 4 lanes of a row group still share each V load (m - r0 <= 1024 = 8 * 128 rows).
   {
-    const int cb = t & 3, g = t >> 2;
-    for (int rb = r0 + 8 * g; rb < m; rb += 8 * (NT / 4)) {
+    const int cb = t & 3, base = ((t & 31) >> 2) + 8 * (t >> 5);
+    {
+      const int rb = r0 + base;
       float out[8][8];
 #pragma unroll
       for (int a = 0; a < 8; ++a)
@@ -188,7 +191,7 @@ __device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ V
         float v[8][4];
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
-          const int r = rb + a;
+          const int r = rb + 128 * a;
           const float4 x = (r < m) ? reinterpret_cast<const float4*>(Vp + (size_t)r * BW)[k4]
                                    : make_float4(0.f, 0.f, 0.f, 0.f);
           v[a][0] = x.x;
@@ -209,7 +212,7 @@ __device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ V
       }
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
-        const int r = rb + a;
+        const int r = rb + 128 * a;
         if (r < m) {
 #pragma unroll
           for (int b = 0; b < 8; ++b) sh.C[(8 * cb + b) * LDC + r] -= out[a][b];

@@ -38,6 +38,24 @@ __device__ __forceinline__ double tn_warp_sum(double v) {
   return v;
 }
 
+// Sum of part[0..count) by the whole block (every thread calls it; the result is returned in
+// thread 0). Deterministic for a given block size; the partials are read after a fence, for the
+// "last block of a grid reduces everyone's partials" pattern. Replaces a one-thread loop, whose
+// dependent FP64 adds (64-cycle latency on GB300) took ~10 us for a few hundred partials.
+__device__ __forceinline__ double tn_block_sum_partials(const double* part, unsigned count) {
+  __shared__ double tn_red_partials[32];
+  __threadfence();
+  double t = 0.0;
+  for (unsigned b = threadIdx.x; b < count; b += blockDim.x) t += ((const volatile double*)part)[b];
+  t = tn_warp_sum(t);
+  if ((threadIdx.x & 31) == 0) tn_red_partials[threadIdx.x >> 5] = t;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (unsigned w = 0; w < (blockDim.x + 31) / 32; ++w) s += tn_red_partials[w];
+  return s;
+}
+
 __device__ __forceinline__ float tn_warp_sumf(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -139,13 +139,12 @@ __global__ void multidot_kernel(int64_t n, int ncols, const double* __restrict__
     last = (atomicAdd(tickets + i, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double t = 0.0;
-    const volatile double* pp = part + (int64_t)i * gridDim.x;
-    for (unsigned b = 0; b < gridDim.x; ++b) t += pp[b];
-    out[i] = t;
-    tickets[i] = 0u;
+  if (last) {  // uniform over the block
+    const double t = tn_block_sum_partials(part + (int64_t)i * gridDim.x, gridDim.x);
+    if (threadIdx.x == 0) {
+      out[i] = t;
+      tickets[i] = 0u;
+    }
   }
 }
 
@@ -176,13 +175,12 @@ __global__ void multiaxpy_kernel(int64_t n, int ncols, const double* __restrict_
     last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double t = 0.0;
-    const volatile double* pp = part;
-    for (unsigned b = 0; b < gridDim.x; ++b) t += pp[b];
-    *nrm2 = t;
-    *ticket = 0u;
+  if (last) {  // uniform over the block
+    const double t = tn_block_sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      *nrm2 = t;
+      *ticket = 0u;
+    }
   }
 }
 

@@ -232,9 +232,15 @@ __global__ void extract_mixed(int64_t m, int64_t n, int64_t k, const float* Aw, 
 }
 
 // E <- E - I (diagonal), FP64
-__global__ void sub_identity(int64_t k, double* E) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x)
-    E[i * k + i] -= 1.0;
+// E (k x k, symmetric, computed on and above the diagonal blocks of size b): mirror the blocks
+// below the diagonal and subtract the identity
+__global__ void sym_sub_identity(int64_t k, int64_t b, double* E) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < k * k;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = idx / k, c = idx % k;
+    if (r == c) E[idx] -= 1.0;
+    else if (r / b > c / b) E[idx] = E[c * k + r];
+  }
 }
 
 // out(i, j) (strided) = Q(i, j) - Qc(i, j): Q, Qc column-major m x k
@@ -370,15 +376,21 @@ int qr32_blocked(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn
 // FP64 re-orthogonalisation of Q64 (column-major m x k, FP32-accurate) into q (strided).
 int refine_q(int64_t m, int64_t k, double* q, int64_t sQm, int64_t sQn, const MixWs& w, cudaStream_t s) {
   int st;
-  // E = Q^T Q - I in FP64 (Q64 column-major m x k)
-  TnGemmF64 g{};
-  g.M = k; g.N = k; g.K = m;
-  g.A = w.Q64; g.sAm = m; g.sAk = 1;
-  g.B = w.Q64; g.sBk = 1; g.sBn = m;
-  g.C = w.E; g.sCm = k; g.sCn = 1;
-  g.batch = 1; g.nred = 1; g.alpha = 1.0; g.beta = 0.0;
-  if ((st = tn_gemm_f64_ws(g, w.g64_ws, w.g64_bytes, s))) return st;
-  sub_identity<<<blocks_for(k), 256, 0, s>>>(k, w.E);
+  // E = Q^T Q - I in FP64 (Q64 column-major m x k). E is symmetric: only the blocks on and above
+  // the diagonal of an nb x nb block grid are computed, one batched GEMM per block diagonal d (the
+  // blocks (i, i + d) have uniform strides), and the blocks below are mirrored.
+  const int nb = (k >= 256 && k % 4 == 0) ? 4 : ((k >= 128 && k % 2 == 0) ? 2 : 1);
+  const int64_t b = k / nb;
+  for (int d = 0; d < nb; ++d) {
+    TnGemmF64 g{};
+    g.M = b; g.N = b; g.K = m;
+    g.A = w.Q64; g.sAm = m; g.sAk = 1; g.sAb = b * m;
+    g.B = w.Q64 + d * b * m; g.sBk = 1; g.sBn = m; g.sBb = b * m;
+    g.C = w.E + d * b; g.sCm = k; g.sCn = 1; g.sCb = b * k + b;
+    g.batch = nb - d; g.nred = 1; g.alpha = 1.0; g.beta = 0.0;
+    if ((st = tn_gemm_f64_ws(g, w.g64_ws, w.g64_bytes, s))) return st;
+  }
+  sym_sub_identity<<<blocks_for(k * k), 256, 0, s>>>(k, b, w.E);
   TN_CHECK_LAUNCH();
   // QE = Q E on the tensor cores (split TF32), then q = Q - QE / 2
   TnGemmF64 h{};

@@ -138,12 +138,12 @@ __global__ void dot_kernel(int64_t n, const double* __restrict__ x, const double
     last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double v = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) v += ((volatile double*)part)[b];
-    *out = v;
-    *ticket = 0u;
+  if (last) {  // uniform over the block
+    const double v = tn_block_sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      *out = v;
+      *ticket = 0u;
+    }
   }
 }
 

@@ -121,6 +121,22 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+def max_over_ranks(ms, world, device):
+    """Slowest rank's timed-region duration (replicas: every rank runs its own job)."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, steps, max_ms):
+    """Whole-job sweeps/s of `world` independent replicas that each ran `steps` sweeps, timed by the
+    slowest one."""
+    return world * steps / (max_ms / 1000.0)
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from tnalg_gb300 import _lib as L, build
@@ -184,10 +200,7 @@ def run_ours(args, rank, world, local_rank):
     qr_ms, qr_cnt, qr_flops = L.profile_read(1)
     lz_ms, lz_cnt, _ = L.profile_read(4)
     lib.tn_profile_enable(0)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     solves = A.stats["solves"] - solves0
     matvecs = A.stats["matvecs"] - mv0
     # final energy of the timed state (FP64 observables)
@@ -314,7 +327,7 @@ def main():
     res, A, para = run_ours(args, rank, world, local_rank)
     pk, pk_kind = peaks()
     ms_step = res["ms"] / args.steps
-    value = world * args.steps / (res["ms"] / 1000.0)
+    value = replica_throughput(world, args.steps, res["ms"])
     mixed = res["precision"] != "fp64"
     if mixed:
         peak = pk["bf16_tflops_sustained"] / 2.0 / 3.0

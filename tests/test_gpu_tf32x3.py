@@ -246,3 +246,32 @@ def test_tf32x3_dmrg_close_to_reference(tf32):
         ob, A, info, _ = DMRG_anyH.dmrg_finite_size(gc.para_of("chain_n12_chi16_h", precision="tf32x3"))
     assert abs(ob["e_per_site"] - float(g["e_per_site"])) <= 1e-8
     np.testing.assert_allclose(np.ravel(ob["mz"]), g["mz"], atol=1e-5)
+
+
+def test_tf32x3_chi128_sweeps_match_fp64(tf32):
+    """An N=24 XXZ chain in a transverse field, chi ramped to 128: the split-TF32 path (cluster QR for the
+    seeding moves, bond growth and spectrum pass; split-TF32 matvec, environments and correlator
+    strings) against the FP64 path on the same seed: energy per site to 1e-8; one-site and
+    two-site observables and entanglement entropies to 1e-5, the mixed path's bar on the N=12
+    golden case (the two runs take different Lanczos trajectories, and a state converged to
+    ~1e-9 in energy differs at ~1e-6 in its observables)."""
+    from tnalg_gb300 import DMRG_anyH, Parameters as pm
+    runs = {}
+    for prec in ("fp64", "tf32x3"):
+        para = pm.generate_parameters_dmrg("chain")
+        para.update(l=24, chi=32, jz=0.8, hx=0.1, sweep_time=4, chi_schedule=[32, 128, 128, 128], dt_ob=4,
+                    break_tol=-1.0, eigs_tol=1e-12, precision=prec)
+        para = pm.make_consistent_parameter_dmrg(para)
+        np.random.seed(7)
+        with contextlib.redirect_stdout(io.StringIO()):
+            ob, A, info, _ = DMRG_anyH.dmrg_finite_size(para)
+        runs[prec] = (ob, A)
+    (o64, A64), (o32, A32) = runs["fp64"], runs["tf32x3"]
+    assert A32.stats["qr_mixed"] > 0 and A64.stats["qr_mixed"] == 0
+    assert int(A32.virtual_dim.max()) == 128
+    assert abs(o32["e_per_site"] - o64["e_per_site"]) <= 1e-8
+    np.testing.assert_allclose(np.ravel(o32["mx"]), np.ravel(o64["mx"]), atol=1e-5)
+    np.testing.assert_allclose(np.ravel(o32["mz"]), np.ravel(o64["mz"]), atol=1e-5)
+    np.testing.assert_allclose(np.ravel(o32["corr_x"]), np.ravel(o64["corr_x"]), atol=1e-5)
+    np.testing.assert_allclose(np.ravel(o32["corr_z"]), np.ravel(o64["corr_z"]), atol=1e-5)
+    np.testing.assert_allclose(np.ravel(A32.ent), np.ravel(A64.ent), atol=1e-5)

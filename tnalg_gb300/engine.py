@@ -204,7 +204,7 @@ class DeviceMPS:
         self.ER = [None] * (self.length + 1)
         self.el_upto = -1      # EL[0..el_upto] valid
         self.er_from = self.length + 1   # ER[er_from..L] valid
-        self.stats = {"matvecs": 0, "solves": 0, "restarts": 0, "unconverged": 0}
+        self.stats = {"matvecs": 0, "solves": 0, "restarts": 0, "unconverged": 0, "qr_mixed": 0}
         # tn_qr_mixed (FP32 cluster QR + FP64 re-orthogonalisation) for the seeding moves of the
         # tf32x3 path, and for every move while fast_gauge is set (bond growth, entanglement
         # spectrum: the state is then kept to ~1e-7); TNALG_MIXED_QR=0 keeps every move on the
@@ -329,6 +329,7 @@ class DeviceMPS:
         lib, st = L.load(), L.stream_handle()
         if (self.mixed_qr and (seed_only or self.fast_gauge) and self.precision == L.PREC_TF32X3
                 and min(mm, nn) >= 64):
+            self.stats["qr_mixed"] += 1
             wp, wb = self.ws2.args(lib.tn_qr_mixed_workspace_bytes(mm, nn))
             L.check(lib.tn_qr_mixed(mm, nn, L.ptr(A), sA[0], sA[1], L.ptr(Q), sQ[0], sQ[1], L.ptr(R), nn, 1, wp, wb,
                                     st), "qr_mixed")

@@ -9,7 +9,8 @@
 //      the input, R32 accurate to FP32 and scaled back. For n <= m <= 1024,
 //      n <= 512 the whole factorisation runs in one 16-CTA cluster kernel (qr_cluster.cu);
 //      otherwise one-CTA FP32 panels with FP32 GEMM trailing updates, Q formed backwards;
-//   2. E = Q^T Q - I in FP64 (CUDA-core FP64 GEMM), then Q <- Q - Q E / 2 on the tensor cores
+//   2. E = Q^T Q - I to double-float accuracy on the FP32 pipe (Q32's entries are FP32 values, so
+//      every product is exact as a pair of floats), then Q <- Q - Q E / 2 on the tensor cores
 //      (split TF32; the product is ~1e-6 in size, so its 1e-6 relative error is ~1e-12): the
 //      returned Q is orthonormal to ~1e-12 and spans col(A) to FP32 accuracy.
 // Used by tn_qr_mixed; the plain FP64 path keeps tn_qr.
@@ -231,15 +232,98 @@ __global__ void extract_mixed(int64_t m, int64_t n, int64_t k, const float* Aw, 
   }
 }
 
-// E <- E - I (diagonal), FP64
-// E (k x k, symmetric, computed on and above the diagonal blocks of size b): mirror the blocks
-// below the diagonal and subtract the identity
-__global__ void sym_sub_identity(int64_t k, int64_t b, double* E) {
+// E = Q^T Q - I for a Q whose entries are FP32 values (column-major m x k, held in FP64), exact
+// to double-float accuracy on the FP32 pipe: each product a*b is split error-free into
+// h + fma(a, b, -h) (TwoProduct), the h are summed error-free (Knuth's TwoSum) into a running
+// FP32 head and all low-order parts into an FP32 tail (the compensated dot product "Dot2" of
+// Ogita, Rump and Oishi, SIAM J. Sci. Comput. 26 (2005)); every CTA sums at most GRAM_ROWS rows
+// of one 64 x 64 tile on or above the diagonal, so the tail's own rounding stays ~1e-16 for
+// columns of unit norm. Ten FP32 operations per product against one FP64 FMA: the FP64 pipe
+// issues 64 times fewer lanes per clock on this part.
+constexpr int GT = 64;          // output tile edge
+constexpr int GK = 32;          // rows per shared-memory stage
+constexpr int GRAM_ROWS = 128;  // rows summed per CTA (the split of the row range)
+constexpr int GNT = 256;
+
+// (the _rn intrinsics are never contracted into FMAs, which would break both transformations)
+__device__ __forceinline__ void dot2_step(float a, float b, float& hi, float& lo) {
+  const float h = __fmul_rn(a, b);
+  const float r = fmaf(a, b, -h);
+  const float t = __fadd_rn(hi, h);
+  const float z = __fsub_rn(t, hi);
+  const float q = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(h, z));
+  hi = t;
+  lo = __fadd_rn(lo, __fadd_rn(q, r));
+}
+
+__device__ __forceinline__ int gram_tile_id(int ib, int jb, int nt) { return ib * nt - ib * (ib - 1) / 2 + (jb - ib); }
+
+// part[(tile * nsplit + split) * GT * GT + li * GT + lj] = sum over the split's rows of
+// Q(r, 64 ib + li) Q(r, 64 jb + lj) for every tile jb >= ib (grid: tiles x splits). Thread (ti, tj)
+// owns rows ti + 16 a and columns tj + 16 b of the tile (a, b < 4), so both shared-memory reads of a
+// stage step are conflict-free.
+__global__ void __launch_bounds__(GNT) gram_dot2_kernel(int64_t m, int64_t k, const double* __restrict__ Q,
+                                                        int nsplit, double* __restrict__ part) {
+  __shared__ float As[GK][GT + 1], Bs[GK][GT + 1];
+  const int nt = (int)tn_cdiv(k, GT);
+  int tile = blockIdx.x, ib = 0;
+  while (tile >= nt - ib) {
+    tile -= nt - ib;
+    ++ib;
+  }
+  const int jb = ib + tile;
+  const int64_t r_begin = (int64_t)blockIdx.y * GRAM_ROWS, r_end = min(m, r_begin + GRAM_ROWS);
+  const int t = threadIdx.x, ti = t >> 4, tj = t & 15;
+  float hi[4][4], lo[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) hi[a][b] = lo[a][b] = 0.f;
+  for (int64_t r0 = r_begin; r0 < r_end; r0 += GK) {
+    for (int e = t; e < GK * GT; e += GNT) {
+      const int c = e / GK, rr = e % GK;  // a warp reads 32 consecutive rows of one column
+      const int64_t r = r0 + rr, ca = (int64_t)ib * GT + c, cb = (int64_t)jb * GT + c;
+      As[rr][c] = (r < r_end && ca < k) ? (float)Q[r + ca * m] : 0.f;
+      Bs[rr][c] = (r < r_end && cb < k) ? (float)Q[r + cb * m] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < GK; ++kk) {
+      float av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = As[kk][ti + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][tj + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) dot2_step(av[a], bv[b], hi[a][b], lo[a][b]);
+    }
+    __syncthreads();
+  }
+  double* out = part + ((size_t)gram_tile_id(ib, jb, nt) * nsplit + blockIdx.y) * GT * GT;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) out[(ti + 16 * a) * GT + tj + 16 * b] = (double)hi[a][b] + (double)lo[a][b];
+}
+
+// E (k x k, row-major) = sum of the splits' partial Gram tiles (mirrored below the diagonal) - I
+__global__ void gram_finish_kernel(int64_t k, int nsplit, const double* __restrict__ part, double* __restrict__ E) {
+  const int nt = (int)tn_cdiv(k, GT);
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < k * k;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = idx / k, c = idx % k;
-    if (r == c) E[idx] -= 1.0;
-    else if (r / b > c / b) E[idx] = E[c * k + r];
+    int64_t i = idx / k, j = idx % k;
+    if (i / GT > j / GT) {
+      const int64_t x = i;
+      i = j;
+      j = x;
+    }
+    const int ib = (int)(i / GT), jb = (int)(j / GT);
+    const double* p = part + (size_t)gram_tile_id(ib, jb, nt) * nsplit * GT * GT + (i % GT) * GT + (j % GT);
+    double s = 0.0;
+    for (int sp = 0; sp < nsplit; ++sp) s += p[(size_t)sp * GT * GT];
+    E[idx] = s - ((idx / k == idx % k) ? 1.0 : 0.0);
   }
 }
 
@@ -265,8 +349,7 @@ struct MixWs {
   unsigned long long* amax;
   char* tf_ws;
   size_t tf_bytes;
-  char* g64_ws;
-  size_t g64_bytes;
+  double* gram;  // partial Gram tiles of the re-orthogonalisation
 };
 
 size_t mix_layout(int64_t m, int64_t n, char* base, MixWs* w) {
@@ -286,8 +369,10 @@ size_t mix_layout(int64_t m, int64_t n, char* base, MixWs* w) {
   w->QE = (double*)take((size_t)m * k * 8);
   w->tf_bytes = tn_gemm_tf32x3_ws_bytes(m, k, k, 1, 1);
   w->tf_ws = take(w->tf_bytes);
-  w->g64_bytes = tn_gemm_f64_ws_bytes(k, k, 1);
-  w->g64_ws = take(w->g64_bytes);
+  {
+    const int64_t nt = tn_cdiv(k, GT), nsplit = tn_cdiv(m, GRAM_ROWS);
+    w->gram = (double*)take((size_t)(nt * (nt + 1) / 2) * nsplit * GT * GT * 8);
+  }
   return off + 1024;
 }
 
@@ -376,22 +461,15 @@ int qr32_blocked(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t sAn
 // FP64 re-orthogonalisation of Q64 (column-major m x k, FP32-accurate) into q (strided).
 int refine_q(int64_t m, int64_t k, double* q, int64_t sQm, int64_t sQn, const MixWs& w, cudaStream_t s) {
   int st;
-  // E = Q^T Q - I in FP64 (Q64 column-major m x k). E is symmetric: only the blocks on and above
-  // the diagonal of an nb x nb block grid are computed, one batched GEMM per block diagonal d (the
-  // blocks (i, i + d) have uniform strides), and the blocks below are mirrored.
-  const int nb = (k >= 256 && k % 4 == 0) ? 4 : ((k >= 128 && k % 2 == 0) ? 2 : 1);
-  const int64_t b = k / nb;
-  for (int d = 0; d < nb; ++d) {
-    TnGemmF64 g{};
-    g.M = b; g.N = b; g.K = m;
-    g.A = w.Q64; g.sAm = m; g.sAk = 1; g.sAb = b * m;
-    g.B = w.Q64 + d * b * m; g.sBk = 1; g.sBn = m; g.sBb = b * m;
-    g.C = w.E + d * b; g.sCm = k; g.sCn = 1; g.sCb = b * k + b;
-    g.batch = nb - d; g.nred = 1; g.alpha = 1.0; g.beta = 0.0;
-    if ((st = tn_gemm_f64_ws(g, w.g64_ws, w.g64_bytes, s))) return st;
+  // E = Q^T Q - I, double-float exact on the FP32 pipe (Q64 holds FP32 values)
+  {
+    const int nt = (int)tn_cdiv(k, GT), nsplit = (int)tn_cdiv(m, GRAM_ROWS);
+    gram_dot2_kernel<<<dim3((unsigned)(nt * (nt + 1) / 2), (unsigned)nsplit), GNT, 0, s>>>(m, k, w.Q64, nsplit,
+                                                                                          w.gram);
+    TN_CHECK_LAUNCH();
+    gram_finish_kernel<<<blocks_for(k * k), 256, 0, s>>>(k, nsplit, w.gram, w.E);
+    TN_CHECK_LAUNCH();
   }
-  sym_sub_identity<<<blocks_for(k * k), 256, 0, s>>>(k, b, w.E);
-  TN_CHECK_LAUNCH();
   // QE = Q E on the tensor cores (split TF32), then q = Q - QE / 2
   TnGemmF64 h{};
   h.M = m; h.N = k; h.K = k;

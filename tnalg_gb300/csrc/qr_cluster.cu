@@ -1,5 +1,5 @@
 // FP32 Householder QR of one m x n matrix (n <= m <= 1024, n <= 512) by ONE 16-CTA thread-block
-// cluster (blocked, column-distributed), with Q formed in the same kernel.
+// cluster (blocked, column-distributed), then Q formed by a wide grid.
 //
 // Role: step 1 of the mixed-precision gauge move (tn_qr_mixed): the FP32 factors it returns are
 // re-orthogonalised in FP64 afterwards, so only backward stability in FP32 is needed here.
@@ -16,9 +16,9 @@
 //     then arrives on mbarrier ready[q] of every CTA of the cluster (release at cluster scope).
 //   * CTA q' > q waits on its own ready[q] (bounded) and applies H_q^T = I - V_q T_q^T V_q^T to
 //     its block (two 32-wide block products over the rows, FP32 FMA, one lane per column).
-//   * Q = H_0 H_1 ... E is formed blockwise too: once its panel is done, CTA q sets its block to
-//     the identity columns and applies H_q, ..., H_0 (only those reach rows >= 32p of column
-//     block q), independently of the other CTAs, overlapping their remaining factorisation.
+//   * Q = H_0 H_1 ... E is formed by a second kernel over 64 CTAs (8 columns each) from the
+//     published V_p, T_p: the chain H_q, ..., H_0 of the last column block would otherwise run on
+//     one SM after the last panel while the rest of the cluster sits idle.
 // Every wait is bounded by a clock budget; on timeout the CTA records an error code, skips its
 // remaining work and still joins the final cluster barrier.
 #include "common.cuh"
@@ -108,15 +108,14 @@ __device__ __forceinline__ float warp_transpose_sum(float (&v)[BW], int lane) {
   return v[0];
 }
 
-// C(rows >= r0) <- (I - V op(T) V^T) C over the 32 columns of this CTA's block, with V the
-// published row-major m x 32 panel (global memory, read through L1) and op(T) = T^T when trans_t.
+// C(rows >= r0) <- H_p^T C = (I - V T^T V^T) C over the 32 columns of this CTA's block, with V the
+// published row-major m x 32 panel (global memory, read through L1).
 // Both products are register-blocked 8 x 8 per thread, so every value loaded feeds 8 FMAs (a lane
 // that receives a whole 32-wide row per row of work is bound by the load/store unit's 128 B/clock
 // register fill, four times below the FMA rate):
 //   W = V^T C  (32 x 32): thread = (8 reflectors kb, 8 columns cb) x row group g (32 groups);
 //   C -= V W2  (rows x 32): thread = 8 rows x 8 columns cb.
-__device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ Vp, const float* __restrict__ Tp,
-                            bool trans_t) {
+__device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ Vp, const float* __restrict__ Tp) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   // T staged in sh.G (free outside the panel factorisation)
   for (int o = t; o < BW * BW; o += NT) sh.G[(o / BW) * LDW + o % BW] = Tp[o];
@@ -162,15 +161,11 @@ __device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ V
     sh.Wred[k * LDW + c] = s;
   }
   __syncthreads();
-  // W2 = op(T) W (T upper triangular), stored with a 16-byte aligned row pitch
+  // W2 = T^T W (T upper triangular), stored with a 16-byte aligned row pitch
   for (int o = t; o < BW * BW; o += NT) {
     const int k = o / BW, c = o % BW;
     float s = 0.f;
-    if (trans_t) {
-      for (int l = 0; l <= k; ++l) s = fmaf(sh.G[l * LDW + k], sh.Wred[l * LDW + c], s);
-    } else {
-      for (int l = k; l < BW; ++l) s = fmaf(sh.G[k * LDW + l], sh.Wred[l * LDW + c], s);
-    }
+    for (int l = 0; l <= k; ++l) s = fmaf(sh.G[l * LDW + k], sh.Wred[l * LDW + c], s);
     sh.W2[k * LDW2 + c] = s;
   }
   __syncthreads();
@@ -362,8 +357,7 @@ __device__ void factor_panel(Smem& sh, int m, int j0, int jb) {
 }
 
 __global__ void __launch_bounds__(NT, 1)
-    qr32_cluster_kernel(int m, int n, const double* __restrict__ A, int64_t sAm, int64_t sAn, double* __restrict__ Q,
-                        double* __restrict__ R, int64_t sRm, int64_t sRn, float* __restrict__ Vg,
+    qr32_cluster_kernel(int m, int n, const double* __restrict__ A, int64_t sAm, int64_t sAn, double* __restrict__ R, int64_t sRm, int64_t sRn, float* __restrict__ Vg,
                         float* __restrict__ Tg, int* err) {
   extern __shared__ unsigned char smem_raw[];
   Smem& sh = *reinterpret_cast<Smem*>(((uintptr_t)smem_raw + 15) & ~(uintptr_t)15);
@@ -430,7 +424,7 @@ __global__ void __launch_bounds__(NT, 1)
       }
       __syncthreads();
       if (sh.failed) break;
-      apply_block(sh, m, p * BW, Vg + (size_t)p * m * BW, Tg + p * BW * BW, true);
+      apply_block(sh, m, p * BW, Vg + (size_t)p * m * BW, Tg + p * BW * BW);
     }
     if (!sh.failed) {
       factor_panel(sh, m, col0, jb);
@@ -458,21 +452,140 @@ __global__ void __launch_bounds__(NT, 1)
           }
         }
       }
-      __syncthreads();  // the block is read above before it is overwritten below
-      // Q block: identity columns, then H_q, ..., H_0
-      for (int e = t; e < m * BW; e += NT) {
-        const int c = e / m, r = e % m;
-        sh.C[c * LDC + r] = (c < jb && r == col0 + c) ? 1.f : 0.f;
-      }
-      __syncthreads();
-      for (int p = q; p >= 0; --p) apply_block(sh, m, p * BW, Vg + (size_t)p * m * BW, Tg + p * BW * BW, false);
-      for (int e = t; e < m * jb; e += NT) {
-        const int c = e / m, r = e % m;
-        Q[(int64_t)r + (int64_t)(col0 + c) * m] = (double)sh.C[c * LDC + r];
-      }
     }
   }
   cluster_sync();  // no CTA exits while another may still arrive on its barriers
+}
+
+// Q = H_0 H_1 ... H_{np-1} [I_n; 0] from the published V_p, T_p, formed by a wide grid after the
+// factorisation: one CTA per (column block q, chunk s of QF_CW columns). H_p with p > q leaves the
+// identity columns of block q unchanged (they are zero on rows >= 32p), so the CTA applies
+// H_q, ..., H_0 to its columns, each on rows >= 32p only. The chain of the last block (np applies)
+// bounds the kernel; inside the cluster the same chain ran on one SM after the last panel.
+constexpr int QF_CW = 8;    // columns of Q per CTA
+constexpr int QF_NT = 256;  // threads per CTA
+constexpr int QF_NW = QF_NT / 32;
+static_assert(BW * QF_CW == QF_NT && 4 * QF_NT >= MMAX, "one W element per thread, 4 rows per thread");
+
+__global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const float* __restrict__ Vg,
+                                                            const float* __restrict__ Tg, double* __restrict__ Q) {
+  __shared__ __align__(16) float X[MMAX * QF_CW];  // the CTA's Q columns, row-major m x 8
+  __shared__ __align__(16) float Wp[QF_NW][BW * QF_CW];
+  __shared__ __align__(16) float W[BW * QF_CW];
+  __shared__ __align__(16) float W2[BW * QF_CW];
+  __shared__ float T[BW * LDW];
+  constexpr int chunks = BW / QF_CW;
+  const int q = blockIdx.x / chunks, c0 = q * BW + (blockIdx.x % chunks) * QF_CW;
+  if (c0 >= n) return;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (int e = t; e < m * QF_CW; e += QF_NT) {
+    const int r = e / QF_CW, c = e % QF_CW;
+    X[e] = (r == c0 + c && c0 + c < n) ? 1.f : 0.f;
+  }
+  for (int p = q; p >= 0; --p) {
+    const float* __restrict__ Vp = Vg + (size_t)p * m * BW;
+    const float* __restrict__ Tp = Tg + p * BW * BW;
+    const int r0 = p * BW;
+    for (int o = t; o < BW * BW; o += QF_NT) T[(o / BW) * LDW + o % BW] = Tp[o];
+    __syncthreads();  // X (initial values or the previous update) and T are in place
+    // W = V_p^T X over rows >= r0: thread = (4 reflectors kq, row group g of 32), 4 x 8 partials
+    {
+      const int kq = lane & 7, g = warp * 4 + (lane >> 3);
+      float acc[4][QF_CW];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < QF_CW; ++b) acc[a][b] = 0.f;
+      for (int r = r0 + g; r < m; r += 32) {
+        const float4 v4 = reinterpret_cast<const float4*>(Vp + (size_t)r * BW)[kq];
+        const float4* xr = reinterpret_cast<const float4*>(X + r * QF_CW);
+        const float4 x0 = xr[0], x1 = xr[1];
+        const float v[4] = {v4.x, v4.y, v4.z, v4.w};
+        const float x[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < QF_CW; ++b) acc[a][b] = fmaf(v[a], x[b], acc[a][b]);
+      }
+      // the warp's 4 row groups differ in lane bits 3 and 4
+#pragma unroll
+      for (int o = 8; o <= 16; o <<= 1)
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < QF_CW; ++b) acc[a][b] += __shfl_xor_sync(0xffffffffu, acc[a][b], o);
+      if (lane < 8) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < QF_CW; ++b) Wp[warp][(4 * kq + a) * QF_CW + b] = acc[a][b];
+      }
+    }
+    __syncthreads();
+    {
+      float s = 0.f;
+#pragma unroll
+      for (int w = 0; w < QF_NW; ++w) s += Wp[w][t];
+      W[t] = s;
+    }
+    __syncthreads();
+    // W2 = T_p W (T upper triangular)
+    {
+      const int k = t / QF_CW, c = t % QF_CW;
+      float s = 0.f;
+      for (int l = k; l < BW; ++l) s = fmaf(T[k * LDW + l], W[l * QF_CW + c], s);
+      W2[t] = s;
+    }
+    __syncthreads();
+    // X -= V_p W2 over rows >= r0: thread t owns rows r0 + t + 256 i (i < 4) of the 8 columns, so
+    // every W2 value read from shared memory feeds 4 rows
+    {
+      float out[4][QF_CW];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int b = 0; b < QF_CW; ++b) out[i][b] = 0.f;
+#pragma unroll 1
+      for (int k4 = 0; k4 < BW / 4; ++k4) {
+        float v[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int r = r0 + t + QF_NT * i;
+          const float4 x = (r < m) ? reinterpret_cast<const float4*>(Vp + (size_t)r * BW)[k4]
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+          v[i][0] = x.x;
+          v[i][1] = x.y;
+          v[i][2] = x.z;
+          v[i][3] = x.w;
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const float4* wr = reinterpret_cast<const float4*>(W2 + (4 * k4 + kk) * QF_CW);
+          const float4 w0 = wr[0], w1 = wr[1];
+          const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int b = 0; b < QF_CW; ++b) out[i][b] = fmaf(v[i][kk], w[b], out[i][b]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int r = r0 + t + QF_NT * i;
+        if (r < m) {
+          float4* xr = reinterpret_cast<float4*>(X + r * QF_CW);
+          const float4 x0 = xr[0], x1 = xr[1];
+          xr[0] = make_float4(x0.x - out[i][0], x0.y - out[i][1], x0.z - out[i][2], x0.w - out[i][3]);
+          xr[1] = make_float4(x1.x - out[i][4], x1.y - out[i][5], x1.z - out[i][6], x1.w - out[i][7]);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = t; e < m * QF_CW; e += QF_NT) {
+    const int c = e / m, r = e % m;
+    if (c0 + c < n) Q[(int64_t)r + (int64_t)(c0 + c) * m] = (double)X[r * QF_CW + c];
+  }
 }
 
 int g_cluster_state = -1;  // -1 unknown, 0 unavailable, 1 available
@@ -534,7 +647,9 @@ int tn_qr32_cluster(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t 
   float* Tg = scratch + (size_t)np * m * BW;
   cudaLaunchAttribute at[1];
   cudaLaunchConfig_t cfg = launch_config(at, s);
-  TN_CUDA(cudaLaunchKernelEx(&cfg, qr32_cluster_kernel, (int)m, (int)n, a, sAm, sAn, q, r, sRm, sRn, Vg, Tg, err));
+  TN_CUDA(cudaLaunchKernelEx(&cfg, qr32_cluster_kernel, (int)m, (int)n, a, sAm, sAn, r, sRm, sRn, Vg, Tg, err));
+  TN_CHECK_LAUNCH();
+  qr32_form_q_kernel<<<(unsigned)(np * (BW / QF_CW)), QF_NT, 0, s>>>((int)m, (int)n, Vg, Tg, q);
   TN_CHECK_LAUNCH();
   return TN_OK;
 }

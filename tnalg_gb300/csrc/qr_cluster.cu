@@ -8,16 +8,21 @@
 // the rows. On GB300 FP64 issues ~2 lanes/clock/SM with a 64-cycle dependent latency, so the
 // steps run in FP32; and a reduction across SMs (cluster barrier + distributed shared memory,
 // ~1 us) per column would dominate, so every column step stays inside one CTA:
-//   * CTA q owns the column block [32q, 32q + 32) for ALL rows, in shared memory (column-major,
-//     odd leading dimension 1025, so row-parallel and column-parallel accesses are both free of
-//     bank conflicts). Panel q is factorised by CTA q alone (LAPACK dgeqr2 conventions per column,
-//     then the compact-WY factor T of dlarft, forward/columnwise), using __syncthreads only.
-//   * CTA q publishes V_q (row-major m x 32 in global memory, unit diagonal, zeros above) and T_q,
-//     then arrives on mbarrier ready[q] of every CTA of the cluster (release at cluster scope).
-//   * CTA q' > q waits on its own ready[q] (bounded) and applies H_q^T = I - V_q T_q^T V_q^T to
-//     its block (two 32-wide block products over the rows, FP32 FMA, one lane per column).
+//   * The columns form panels of 16 (block b = columns [16b, 16b + 16)); CTA q owns blocks q and
+//     q + 16 for ALL rows, in shared memory (column-major, odd leading dimension 1025, so
+//     row-parallel and column-parallel accesses are both free of bank conflicts). Panel b is
+//     factorised by its owner alone (LAPACK dgeqr2 conventions per column, then the compact-WY
+//     factor T of dlarft, forward/columnwise), using __syncthreads only.
+//   * The owner publishes V_b (row-major m x 16 in global memory, unit diagonal, zeros above) and
+//     T_b, then arrives on mbarrier ready[b] of every CTA of the cluster (release at cluster
+//     scope).
+//   * A CTA with blocks to the right of b waits on its own ready[b] (bounded), stages V_b in its
+//     shared memory once and applies H_b^T = I - V_b T_b^T V_b^T to those blocks. The chain of the
+//     factorisation is, per panel: stage V_b, apply it to block b + 1, factorise block b + 1,
+//     publish; every other update runs beside it. The block two panels ahead is updated after
+//     the factorisation, so it never delays the chain.
 //   * Q = H_0 H_1 ... E is formed by a second kernel over 64 CTAs (8 columns each) from the
-//     published V_p, T_p: the chain H_q, ..., H_0 of the last column block would otherwise run on
+//     published V_b, T_b: the chain H_q, ..., H_0 of the last column block would otherwise run on
 //     one SM after the last panel while the rest of the cluster sits idle.
 // Every wait is bounded by a clock budget; on timeout the CTA records an error code, skips its
 // remaining work and still joins the final cluster barrier.
@@ -28,33 +33,35 @@ int tn_device_error_word(int** out);
 namespace {
 
 constexpr int CL = 16;           // CTAs per cluster (non-portable size)
-constexpr int BW = 32;           // columns per CTA = panel width
+constexpr int BW = 16;           // columns per panel
+constexpr int NBMAX = 2 * CL;    // panels (two per CTA)
 constexpr int NT = 512;          // threads per CTA
 constexpr int NW = NT / 32;      // warps per CTA
 constexpr int MMAX = 1024;       // maximum rows
-constexpr int LDC = MMAX + 1;    // leading dimension of the shared column block
+constexpr int LDC = MMAX + 1;    // leading dimension of a shared column block
 constexpr int LDW = BW + 1;
+constexpr int LDW2 = BW + 4;     // W2 row pitch (16-byte aligned rows)
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
-constexpr int LDW2 = BW + 4;     // W2 row pitch (16-byte aligned rows)
-
 struct Smem {
-  float C[BW * LDC];          // own column block, column-major
+  float C[2][BW * LDC];       // own column blocks q and q + 16, column-major
+  float Vs[MMAX * BW];        // V of the panel being applied, row-major, 16-byte chunks swizzled
   float Wred[NW * BW * LDW];  // per-warp partial products
-  float W2[BW * LDW2];        // W2 = op(T) W, 16-byte aligned rows
-  float T[BW * LDW];          // T of this CTA's panel
-  float G[BW * LDW];          // G(l, i) = v_l^T v_i of the panel, l < i
+  float W2[BW * LDW2];        // W2 = T^T W, 16-byte aligned rows
+  float T[BW * LDW];          // T of the panel being factorised
+  float G[BW * LDW];          // G(l, i) = v_l^T v_i of the panel (l < i); T of the applied panel
   float red[NW * LDW];        // per-warp partials of the panel reductions
   float f[BW];                // update coefficients of the current panel column
   float tau[BW];              // tau of every reflector of the panel
   float piv;                  // the current pivot a(j, j)
-  unsigned long long ready[CL];  // mbarrier per panel
-  double amax[CL];            // largest |a| of every CTA's block
-  double wmax[NW];            // per-warp maxima of this CTA's block
+  unsigned long long ready[NBMAX];  // mbarrier per panel
+  double amax[CL];            // largest |a| of every CTA's blocks
+  double wmax[NW];            // per-warp maxima of this CTA's blocks
   int failed;
 };
 
 constexpr size_t kSmemBytes = sizeof(Smem) + 16;
+static_assert(kSmemBytes <= 227 * 1024, "shared memory budget of one CTA");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -92,10 +99,15 @@ __device__ __forceinline__ bool wait_ready(unsigned long long* bar) {
   }
 }
 
-// Sum over the 32 lanes of 32 values at once: on return lane L holds sum over lanes of v[L].
+// Float index of 16-byte chunk ch (0..3) of row r in Vs: the chunk index is XOR-ed with bits 1-2
+// of the row, so 8 consecutive rows at one chunk, and 4 consecutive rows at two chunks, fall on
+// distinct banks.
+__device__ __forceinline__ int vs_idx(int r, int ch) { return r * BW + ((ch ^ ((r >> 1) & 3)) << 2); }
+
+// Sum over the 32 lanes of 16 values at once: on return lane L holds sum over lanes of v[L & 15].
 __device__ __forceinline__ float warp_transpose_sum(float (&v)[BW], int lane) {
 #pragma unroll
-  for (int half = 16; half >= 1; half >>= 1) {
+  for (int half = BW / 2; half >= 1; half >>= 1) {
     const bool upper = (lane & half) != 0;
 #pragma unroll
     for (int i = 0; i < half; ++i) {
@@ -105,54 +117,73 @@ __device__ __forceinline__ float warp_transpose_sum(float (&v)[BW], int lane) {
       v[i] = keep + __shfl_xor_sync(0xffffffffu, send, half);
     }
   }
-  return v[0];
+  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 16);
 }
 
-// C(rows >= r0) <- H_p^T C = (I - V T^T V^T) C over the 32 columns of this CTA's block, with V the
-// published row-major m x 32 panel (global memory, read through L1).
-// Both products are register-blocked 8 x 8 per thread, so every value loaded feeds 8 FMAs (a lane
-// that receives a whole 32-wide row per row of work is bound by the load/store unit's 128 B/clock
-// register fill, four times below the FMA rate):
-//   W = V^T C  (32 x 32): thread = (8 reflectors kb, 8 columns cb) x row group g (32 groups);
-//   C -= V W2  (rows x 32): thread = 8 rows x 8 columns cb.
-__device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ Vp, const float* __restrict__ Tp) {
+// Vs(rows >= r0) <- V_p (published, row-major m x 16). Every thread issues all its loads before
+// its first store.
+__device__ void stage_v(Smem& sh, int m, int r0, const float* __restrict__ Vp) {
+  const int t = threadIdx.x;
+  const int total = (m - r0) * 4;  // 16-byte chunks
+  const float4* src = reinterpret_cast<const float4*>(Vp + (size_t)r0 * BW);
+  float4* dst = reinterpret_cast<float4*>(sh.Vs);
+  constexpr int PER = MMAX * 4 / NT;  // 8 chunks per thread at most
+  float4 x[PER];
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = t + NT * i;
+    x[i] = (e < total) ? src[e] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = t + NT * i;
+    if (e < total) dst[vs_idx(r0 + (e >> 2), e & 3) >> 2] = x[i];
+  }
+}
+
+// Block `slot` (rows >= r0) <- H_p^T C = (I - V T^T V^T) C with V = V_p staged in Vs and T = T_p.
+//   W = V^T C  (16 x 16): thread = (8 reflectors kb, 4 columns cb) x row group g (64 groups);
+//   C -= V W2  (rows x 16): thread = 8 rows (128 apart) x 4 columns cb.
+__device__ void apply_block(Smem& sh, int slot, int m, int r0, const float* __restrict__ Tp) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  // T staged in sh.G (free outside the panel factorisation)
+  float* Cs = sh.C[slot];
   for (int o = t; o < BW * BW; o += NT) sh.G[(o / BW) * LDW + o % BW] = Tp[o];
   {
-    const int tile = t & 15, kb = tile >> 2, cb = tile & 3, g = t >> 4;
-    float acc[8][8];
+    const int tile = t & 7, kb = tile >> 2, cb = tile & 3, g = t >> 3;
+    float acc[8][4];
 #pragma unroll
     for (int a = 0; a < 8; ++a)
 #pragma unroll
-      for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
-    for (int r = r0 + g; r < m; r += 32) {
-      const float4* vr = reinterpret_cast<const float4*>(Vp + (size_t)r * BW + 8 * kb);
-      const float4 v0 = vr[0], v1 = vr[1];
+      for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
+    for (int r = r0 + g; r < m; r += NT / 8) {
+      const float4 v0 = *reinterpret_cast<const float4*>(sh.Vs + vs_idx(r, 2 * kb));
+      const float4 v1 = *reinterpret_cast<const float4*>(sh.Vs + vs_idx(r, 2 * kb + 1));
       const float v[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
-      float cv[8];
+      float cv[4];
 #pragma unroll
-      for (int b = 0; b < 8; ++b) cv[b] = sh.C[(8 * cb + b) * LDC + r];
+      for (int b = 0; b < 4; ++b) cv[b] = Cs[(4 * cb + b) * LDC + r];
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(v[a], cv[b], acc[a][b]);
+        for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(v[a], cv[b], acc[a][b]);
     }
-    // lanes l and l ^ 16 hold the same tile for neighbouring row groups
+    // the warp's 4 row groups differ in lane bits 3 and 4
 #pragma unroll
-    for (int a = 0; a < 8; ++a)
+    for (int o = 8; o <= 16; o <<= 1)
 #pragma unroll
-      for (int b = 0; b < 8; ++b) acc[a][b] += __shfl_xor_sync(0xffffffffu, acc[a][b], 16);
-    if (lane < 16) {
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] += __shfl_xor_sync(0xffffffffu, acc[a][b], o);
+    if (lane < 8) {
       float* Wp = sh.Wred + warp * BW * LDW;
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) Wp[(8 * kb + a) * LDW + 8 * cb + b] = acc[a][b];
+        for (int b = 0; b < 4; ++b) Wp[(8 * kb + a) * LDW + 4 * cb + b] = acc[a][b];
     }
   }
   __syncthreads();
-  // reduce the warps' partials into Wred[0]
+  // reduce the warps' partials into Wred[0] (each thread reads and writes only its own element)
   for (int o = t; o < BW * BW; o += NT) {
     const int k = o / BW, c = o % BW;
     float s = 0.f;
@@ -161,7 +192,7 @@ __device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ V
     sh.Wred[k * LDW + c] = s;
   }
   __syncthreads();
-  // W2 = T^T W (T upper triangular), stored with a 16-byte aligned row pitch
+  // W2 = T^T W (T upper triangular)
   for (int o = t; o < BW * BW; o += NT) {
     const int k = o / BW, c = o % BW;
     float s = 0.f;
@@ -169,72 +200,68 @@ __device__ void apply_block(Smem& sh, int m, int r0, const float* __restrict__ V
     sh.W2[k * LDW2 + c] = s;
   }
   __syncthreads();
-  // C -= V W2: 8 rows x 8 columns per thread. The rows of a thread are 128 apart and a warp's 8
-  // row groups are consecutive, so with the odd pitch LDC the 32 lanes hit 32 distinct banks of C
-  // while the 4 lanes of a row group still share each V load (m - r0 <= 1024 = 8 * 128 rows).
+  // C -= V W2: a warp covers 32 consecutive rows of one column group (Vs reads conflict-free by the
+  // swizzle, W2 reads broadcast, C accesses on 32 distinct banks by the odd pitch)
   {
-    const int cb = t & 3, base = ((t & 31) >> 2) + 8 * (t >> 5);
-    {
-      const int rb = r0 + base;
-      float out[8][8];
+    const int rs = t & 127, cb = t >> 7;
+    float out[8][4];
 #pragma unroll
-      for (int a = 0; a < 8; ++a)
+    for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) out[a][b] = 0.f;
-#pragma unroll 1
-      for (int k4 = 0; k4 < BW / 4; ++k4) {
-        float v[8][4];
+      for (int b = 0; b < 4; ++b) out[a][b] = 0.f;
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          const int r = rb + 128 * a;
-          const float4 x = (r < m) ? reinterpret_cast<const float4*>(Vp + (size_t)r * BW)[k4]
-                                   : make_float4(0.f, 0.f, 0.f, 0.f);
-          v[a][0] = x.x;
-          v[a][1] = x.y;
-          v[a][2] = x.z;
-          v[a][3] = x.w;
-        }
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const float4* wr = reinterpret_cast<const float4*>(sh.W2 + (4 * k4 + kk) * LDW2 + 8 * cb);
-          const float4 w0 = wr[0], w1 = wr[1];
-          const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
-#pragma unroll
-          for (int a = 0; a < 8; ++a)
-#pragma unroll
-            for (int b = 0; b < 8; ++b) out[a][b] = fmaf(v[a][kk], w[b], out[a][b]);
-        }
-      }
+    for (int k4 = 0; k4 < BW / 4; ++k4) {
+      float v[8][4];
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
-        const int r = rb + 128 * a;
-        if (r < m) {
+        const int r = r0 + rs + 128 * a;
+        const float4 x = (r < m) ? *reinterpret_cast<const float4*>(sh.Vs + vs_idx(r, k4))
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+        v[a][0] = x.x;
+        v[a][1] = x.y;
+        v[a][2] = x.z;
+        v[a][3] = x.w;
+      }
 #pragma unroll
-          for (int b = 0; b < 8; ++b) sh.C[(8 * cb + b) * LDC + r] -= out[a][b];
-        }
+      for (int kk = 0; kk < 4; ++kk) {
+        const float4 w4 = *reinterpret_cast<const float4*>(sh.W2 + (4 * k4 + kk) * LDW2 + 4 * cb);
+        const float w[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) out[a][b] = fmaf(v[a][kk], w[b], out[a][b]);
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const int r = r0 + rs + 128 * a;
+      if (r < m) {
+#pragma unroll
+        for (int b = 0; b < 4; ++b) Cs[(4 * cb + b) * LDC + r] -= out[a][b];
       }
     }
   }
   __syncthreads();
 }
 
-// Householder QR of this CTA's panel (columns 0..jb-1 of the block, rows >= j0 = 32 q), then its
+// Householder QR of panel `slot` (columns 0..jb-1 of the block, rows >= j0 = 16 b), then its
 // compact-WY factor T (dlarft, forward, columnwise) in sh.T.
-// The panel is held in registers: thread t owns rows t and t + NT of the 32 columns, a[2][32], used
-// as a ring. At step i the slots 0..31-i hold the unfinished columns i..31 (slot 0 = the pivot
-// column) and the slots 32-i..31 hold the finished reflectors v_0..v_{i-1} (masked: 0 above the
+// The panel is held in registers: thread t owns rows t and t + NT of the 16 columns, a[2][16], used
+// as a ring. At step i the slots 0..15-i hold the unfinished columns i..15 (slot 0 = the pivot
+// column) and the slots 16-i..15 hold the finished reflectors v_0..v_{i-1} (masked: 0 above the
 // diagonal, 1 on it). Every step works on slot 0 and then rotates the ring by one, so all steps run
-// the same code with static register indices (a fully unrolled column loop does not fit the
-// instruction cache), and one transposed reduction per step yields both the column-update
-// coefficients (unfinished slots) and the Gram entries v_l^T v_i of T (finished slots).
-__device__ void factor_panel(Smem& sh, int m, int j0, int jb) {
+// the same code with static register indices, and one transposed reduction per step yields both
+// the column-update coefficients (unfinished slots) and the Gram entries v_l^T v_i of T (finished
+// slots).
+__device__ void factor_panel(Smem& sh, int slot, int m, int j0, int jb) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  float* Cs = sh.C[slot];
   float a[2][BW];
 #pragma unroll
   for (int rr = 0; rr < 2; ++rr) {
     const int r = t + rr * NT;
 #pragma unroll
-    for (int c = 0; c < BW; ++c) a[rr][c] = (r < m) ? sh.C[c * LDC + r] : 0.f;
+    for (int c = 0; c < BW; ++c) a[rr][c] = (r < m) ? Cs[c * LDC + r] : 0.f;
   }
   float s = 0.f;  // this thread's part of the sum of squares below the current pivot
 #pragma unroll
@@ -284,15 +311,15 @@ __device__ void factor_panel(Smem& sh, int m, int j0, int jb) {
 #pragma unroll
     for (int c = 1; c < BW; ++c) p[c] = fmaf(v[0], a[0][c], v[1] * a[1][c]);
     const float ws = warp_transpose_sum(p, lane);
-    sh.red[warp * LDW + lane] = ws;
+    if (lane < BW) sh.red[warp * LDW + lane] = ws;
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 0 && lane < BW) {
       float tot = 0.f;
 #pragma unroll
       for (int w = 0; w < NW; ++w) tot += sh.red[w * LDW + lane];
       const bool unfinished = lane >= 1 && lane <= BW - 1 - i && i + lane < jb;
       sh.f[lane] = unfinished ? tau * tot : 0.f;
-      if (lane >= BW - i) sh.G[(lane - BW + i) * LDW + i] = tot;  // slot 32 - i + l holds v_l
+      if (lane >= BW - i) sh.G[(lane - BW + i) * LDW + i] = tot;  // slot 16 - i + l holds v_l
       if (lane == 0) sh.tau[i] = tau;
     }
 #pragma unroll
@@ -323,7 +350,7 @@ __device__ void factor_panel(Smem& sh, int m, int j0, int jb) {
 #pragma unroll
     for (int rr = 0; rr < 2; ++rr) {
       const int r = t + rr * NT;
-      if (r < m) sh.C[i * LDC + r] = a[rr][0];
+      if (r < m) Cs[i * LDC + r] = a[rr][0];
       const float done = v[rr];
 #pragma unroll
       for (int c = 0; c < BW - 1; ++c) a[rr][c] = a[rr][c + 1];
@@ -335,7 +362,7 @@ __device__ void factor_panel(Smem& sh, int m, int j0, int jb) {
   __syncthreads();
   // T(k, i) = -tau_i sum_{l=k}^{i-1} T(k, l) G(l, i), T(i, i) = tau_i: lane k of warp 0 runs row k
   // with the row in registers
-  if (warp == 0) {
+  if (warp == 0 && lane < BW) {
     const int k = lane;
     float tr[BW];
 #pragma unroll
@@ -357,22 +384,25 @@ __device__ void factor_panel(Smem& sh, int m, int j0, int jb) {
 }
 
 __global__ void __launch_bounds__(NT, 1)
-    qr32_cluster_kernel(int m, int n, const double* __restrict__ A, int64_t sAm, int64_t sAn, double* __restrict__ R, int64_t sRm, int64_t sRn, float* __restrict__ Vg,
-                        float* __restrict__ Tg, int* err) {
+    qr32_cluster_kernel(int m, int n, const double* __restrict__ A, int64_t sAm, int64_t sAn, double* __restrict__ R,
+                        int64_t sRm, int64_t sRn, float* __restrict__ Vg, float* __restrict__ Tg, int* err) {
   extern __shared__ unsigned char smem_raw[];
   Smem& sh = *reinterpret_cast<Smem*>(((uintptr_t)smem_raw + 15) & ~(uintptr_t)15);
   const int q = cluster_rank();
   const int t = threadIdx.x;
-  const int col0 = q * BW;
-  const int jb = max(0, min(BW, n - col0));
+  const int nblk = (n + BW - 1) / BW;
+  const int blk[2] = {q, q + CL};  // own blocks, slot 0 and slot 1
+  int jbs[2];
+#pragma unroll
+  for (int sl = 0; sl < 2; ++sl) jbs[sl] = max(0, min(BW, n - blk[sl] * BW));
   if (t == 0) {
-    for (int p = 0; p < CL; ++p)
+    for (int p = 0; p < NBMAX; ++p)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sh.ready[p])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sh.failed = 0;
   }
-  // element e of this CTA's block (columns beyond n are zero), coalesced along the unit stride
-  auto elem = [&](int e, int& r, int& c) -> double {
+  // element e of block slot sl (columns beyond n are zero), coalesced along the unit stride
+  auto elem = [&](int sl, int e, int& r, int& c) -> double {
     if (sAn == 1) {
       r = e / BW;
       c = e % BW;
@@ -380,17 +410,18 @@ __global__ void __launch_bounds__(NT, 1)
       c = e / m;
       r = e % m;
     }
-    return (c < jb) ? A[(int64_t)r * sAm + (int64_t)(col0 + c) * sAn] : 0.0;
+    return (c < jbs[sl]) ? A[(int64_t)r * sAm + (int64_t)(blk[sl] * BW + c) * sAn] : 0.0;
   };
   cluster_sync();  // every CTA of the cluster is running before any remote store into it
-  // largest |a| of the block, published to every CTA: the whole matrix is scaled by one power of
+  // largest |a| of the blocks, published to every CTA: the whole matrix is scaled by one power of
   // two (exact) so that any finite FP64 input fits FP32; R is scaled back on output
   {
     double mx = 0.0;
-    for (int e = t; e < m * BW; e += NT) {
-      int r, c;
-      mx = fmax(mx, fabs(elem(e, r, c)));
-    }
+    for (int sl = 0; sl < 2; ++sl)
+      for (int e = t; e < m * BW; e += NT) {
+        int r, c;
+        mx = fmax(mx, fabs(elem(sl, e, r, c)));
+      }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((t & 31) == 0) sh.wmax[t >> 5] = mx;
@@ -408,64 +439,90 @@ __global__ void __launch_bounds__(NT, 1)
   for (int p = 0; p < CL; ++p) gmax = fmax(gmax, sh.amax[p]);
   const int ex = (gmax > 0.0 && isfinite(gmax)) ? ilogb(gmax) : 0;
   const double down = ldexp(1.0, -ex), up = ldexp(1.0, ex);
-  for (int e = t; e < m * BW; e += NT) {
-    int r, c;
-    const double v = elem(e, r, c);
-    sh.C[c * LDC + r] = (float)(v * down);
-  }
+  for (int sl = 0; sl < 2; ++sl)
+    for (int e = t; e < m * BW; e += NT) {
+      int r, c;
+      const double v = elem(sl, e, r, c);
+      sh.C[sl][c * LDC + r] = (float)(v * down);
+    }
   __syncthreads();
 
-  if (jb > 0) {
-    // updates by the panels to the left, in order
-    for (int p = 0; p < q; ++p) {
-      if (!wait_ready(&sh.ready[p])) {
-        if (t == 0) atomicExch(err, TN_DEVERR_QR_WAIT);
-        sh.failed = 1;
-      }
-      __syncthreads();
-      if (sh.failed) break;
-      apply_block(sh, m, p * BW, Vg + (size_t)p * m * BW, Tg + p * BW * BW);
+  // V_p into Vs (waiting for panel p first unless this CTA owns it); false after a failed wait
+  auto acquire = [&](int p) -> bool {
+    if (p % CL != q && !wait_ready(&sh.ready[p])) {
+      if (t == 0) atomicExch(err, TN_DEVERR_QR_WAIT);
+      sh.failed = 1;
     }
-    if (!sh.failed) {
-      factor_panel(sh, m, col0, jb);
-      // publish V_q (unit diagonal, zeros above) and T_q
-      float* Vq = Vg + (size_t)q * m * BW;
-      for (int e = t; e < m * BW; e += NT) {
+    __syncthreads();
+    if (sh.failed) return false;
+    stage_v(sh, m, p * BW, Vg + (size_t)p * m * BW);
+    __syncthreads();
+    return true;
+  };
+  auto apply = [&](int sl, int p) { apply_block(sh, sl, m, p * BW, Tg + p * BW * BW); };
+  // factorise block slot sl, publish V and T, release the waiters, write the R block
+  auto factor_publish = [&](int sl) {
+    const int b = blk[sl], jb = jbs[sl], col0 = b * BW;
+    factor_panel(sh, sl, m, col0, jb);
+    float* Vb = Vg + (size_t)b * m * BW;
+    for (int e = t; e < m * BW; e += NT) {
+      const int r = e / BW, c = e % BW;
+      const int d = col0 + c;
+      Vb[e] = (c < jb && r >= d) ? ((r == d) ? 1.f : sh.C[sl][c * LDC + r]) : 0.f;
+    }
+    for (int e = t; e < BW * BW; e += NT) {
+      const int k = e / BW, l = e % BW;
+      Tg[b * BW * BW + e] = (k < jb && l < jb) ? sh.T[k * LDW + l] : 0.f;
+    }
+    __threadfence();
+    __syncthreads();
+    if (t < CL) remote_arrive(&sh.ready[b], t);
+    // R block (not needed by the other CTAs): rows <= diagonal from the block, zeros below
+    if (R) {
+      for (int e = t; e < n * BW; e += NT) {
         const int r = e / BW, c = e % BW;
-        const int d = col0 + c;
-        Vq[e] = (c < jb && r >= d) ? ((r == d) ? 1.f : sh.C[c * LDC + r]) : 0.f;
-      }
-      for (int e = t; e < BW * BW; e += NT) {
-        const int k = e / BW, l = e % BW;
-        Tg[q * BW * BW + e] = (k < jb && l < jb) ? sh.T[k * LDW + l] : 0.f;
-      }
-      __threadfence();
-      __syncthreads();
-      if (t < CL) remote_arrive(&sh.ready[q], t);
-      // R block (not needed by the other CTAs): rows <= diagonal from the block, zeros below
-      if (R) {
-        for (int e = t; e < n * BW; e += NT) {
-          const int r = e / BW, c = e % BW;
-          if (c < jb) {
-            const int d = col0 + c;
-            R[(int64_t)r * sRm + (int64_t)d * sRn] = (r <= d) ? (double)sh.C[c * LDC + r] * up : 0.0;
-          }
+        if (c < jb) {
+          const int d = col0 + c;
+          R[(int64_t)r * sRm + (int64_t)d * sRn] = (r <= d) ? (double)sh.C[sl][c * LDC + r] * up : 0.0;
         }
       }
     }
+  };
+
+  if (jbs[0] > 0) {
+    const bool two = jbs[1] > 0;
+    // panels left of block q, in order; the last one reaches block q + 16 only after block q is
+    // factorised (it stays in Vs meanwhile)
+    for (int p = 0; p < blk[0]; ++p) {
+      if (!acquire(p)) break;
+      apply(0, p);
+      if (two && p < blk[0] - 1) apply(1, p);
+    }
+    if (!sh.failed) {
+      factor_publish(0);
+      if (two) {
+        if (blk[0] > 0) apply(1, blk[0] - 1);
+        for (int p = blk[0]; p < blk[1]; ++p) {
+          if (!acquire(p)) break;
+          apply(1, p);
+        }
+        if (!sh.failed) factor_publish(1);
+      }
+    }
   }
+  (void)nblk;
   cluster_sync();  // no CTA exits while another may still arrive on its barriers
 }
 
 // Q = H_0 H_1 ... H_{np-1} [I_n; 0] from the published V_p, T_p, formed by a wide grid after the
-// factorisation: one CTA per (column block q, chunk s of QF_CW columns). H_p with p > q leaves the
-// identity columns of block q unchanged (they are zero on rows >= 32p), so the CTA applies
-// H_q, ..., H_0 to its columns, each on rows >= 32p only. The chain of the last block (np applies)
-// bounds the kernel; inside the cluster the same chain ran on one SM after the last panel.
+// factorisation: one CTA per (column block q, chunk of QF_CW columns). H_p with p > q leaves the
+// identity columns of block q unchanged (they are zero on rows >= 16p), so the CTA applies
+// H_q, ..., H_0 to its columns, each on rows >= 16p only.
 constexpr int QF_CW = 8;    // columns of Q per CTA
-constexpr int QF_NT = 256;  // threads per CTA
+constexpr int QF_NT = 128;  // threads per CTA
 constexpr int QF_NW = QF_NT / 32;
-static_assert(BW * QF_CW == QF_NT && 4 * QF_NT >= MMAX, "one W element per thread, 4 rows per thread");
+constexpr int QF_ROWS = MMAX / QF_NT;  // rows per thread in the update
+static_assert(BW * QF_CW == QF_NT, "one W element per thread");
 
 __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const float* __restrict__ Vg,
                                                             const float* __restrict__ Tg, double* __restrict__ Q) {
@@ -490,7 +547,7 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
     __syncthreads();  // X (initial values or the previous update) and T are in place
     // W = V_p^T X over rows >= r0: thread = (4 reflectors kq, row group g of 32), 4 x 8 partials
     {
-      const int kq = lane & 7, g = warp * 4 + (lane >> 3);
+      const int kq = lane & 3, g = warp * 8 + (lane >> 2);
       float acc[4][QF_CW];
 #pragma unroll
       for (int a = 0; a < 4; ++a)
@@ -507,14 +564,14 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
 #pragma unroll
           for (int b = 0; b < QF_CW; ++b) acc[a][b] = fmaf(v[a], x[b], acc[a][b]);
       }
-      // the warp's 4 row groups differ in lane bits 3 and 4
+      // the warp's 8 row groups differ in lane bits 2..4
 #pragma unroll
-      for (int o = 8; o <= 16; o <<= 1)
+      for (int o = 4; o <= 16; o <<= 1)
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
           for (int b = 0; b < QF_CW; ++b) acc[a][b] += __shfl_xor_sync(0xffffffffu, acc[a][b], o);
-      if (lane < 8) {
+      if (lane < 4) {
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -537,19 +594,19 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
       W2[t] = s;
     }
     __syncthreads();
-    // X -= V_p W2 over rows >= r0: thread t owns rows r0 + t + 256 i (i < 4) of the 8 columns, so
-    // every W2 value read from shared memory feeds 4 rows
+    // X -= V_p W2 over rows >= r0: thread t owns rows r0 + t + 128 i of the 8 columns, so every W2
+    // value read from shared memory feeds QF_ROWS rows
     {
-      float out[4][QF_CW];
+      float out[QF_ROWS][QF_CW];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < QF_ROWS; ++i)
 #pragma unroll
         for (int b = 0; b < QF_CW; ++b) out[i][b] = 0.f;
 #pragma unroll 1
       for (int k4 = 0; k4 < BW / 4; ++k4) {
-        float v[4][4];
+        float v[QF_ROWS][4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < QF_ROWS; ++i) {
           const int r = r0 + t + QF_NT * i;
           const float4 x = (r < m) ? reinterpret_cast<const float4*>(Vp + (size_t)r * BW)[k4]
                                    : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -564,13 +621,13 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
           const float4 w0 = wr[0], w1 = wr[1];
           const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
+          for (int i = 0; i < QF_ROWS; ++i)
 #pragma unroll
             for (int b = 0; b < QF_CW; ++b) out[i][b] = fmaf(v[i][kk], w[b], out[i][b]);
         }
       }
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
+      for (int i = 0; i < QF_ROWS; ++i) {
         const int r = r0 + t + QF_NT * i;
         if (r < m) {
           float4* xr = reinterpret_cast<float4*>(X + r * QF_CW);
@@ -609,7 +666,7 @@ cudaLaunchConfig_t launch_config(cudaLaunchAttribute* at, cudaStream_t s) {
 
 // True when the 16-CTA cluster kernel can run this shape on the current device.
 bool tn_qr32_cluster_supported(int64_t m, int64_t n) {
-  if (n < 1 || n > (int64_t)CL * BW || m < n || m > MMAX) return false;
+  if (n < 1 || n > (int64_t)NBMAX * BW || m < n || m > MMAX) return false;
   if (g_cluster_state < 0) {
     g_cluster_state = 0;
     if (cudaFuncSetAttribute(qr32_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==

@@ -49,7 +49,8 @@ struct Smem {
   float Wred[NW * BW * LDW];  // per-warp partial products
   float W2[BW * LDW2];        // W2 = T^T W, 16-byte aligned rows
   float T[BW * LDW];          // T of the panel being factorised
-  float G[BW * LDW];          // G(l, i) = v_l^T v_i of the panel (l < i); T of the applied panel
+  float G[BW * LDW];          // G(l, i) = v_l^T v_i of the panel being factorised (l < i)
+  float Tapp[BW * LDW];       // T of the panel being applied
   float red[NW * LDW];        // per-warp partials of the panel reductions
   float f[BW];                // update coefficients of the current panel column
   float tau[BW];              // tau of every reflector of the panel
@@ -120,10 +121,11 @@ __device__ __forceinline__ float warp_transpose_sum(float (&v)[BW], int lane) {
   return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 16);
 }
 
-// Vs(rows >= r0) <- V_p (published, row-major m x 16). Every thread issues all its loads before
-// its first store.
-__device__ void stage_v(Smem& sh, int m, int r0, const float* __restrict__ Vp) {
+// Vs(rows >= r0) <- V_p (published, row-major m x 16) and Tapp <- T_p. Every thread issues all its
+// loads before its first store.
+__device__ void stage_v(Smem& sh, int m, int r0, const float* __restrict__ Vp, const float* __restrict__ Tp) {
   const int t = threadIdx.x;
+  const float tv = (t < BW * BW) ? Tp[t] : 0.f;
   const int total = (m - r0) * 4;  // 16-byte chunks
   const float4* src = reinterpret_cast<const float4*>(Vp + (size_t)r0 * BW);
   float4* dst = reinterpret_cast<float4*>(sh.Vs);
@@ -139,15 +141,16 @@ __device__ void stage_v(Smem& sh, int m, int r0, const float* __restrict__ Vp) {
     const int e = t + NT * i;
     if (e < total) dst[vs_idx(r0 + (e >> 2), e & 3) >> 2] = x[i];
   }
+  if (t < BW * BW) sh.Tapp[(t / BW) * LDW + t % BW] = tv;
 }
 
-// Block `slot` (rows >= r0) <- H_p^T C = (I - V T^T V^T) C with V = V_p staged in Vs and T = T_p.
+// Block `slot` (rows >= r0) <- H_p^T C = (I - V T^T V^T) C with V = V_p staged in Vs and T = T_p
+// staged in Tapp.
 //   W = V^T C  (16 x 16): thread = (8 reflectors kb, 4 columns cb) x row group g (64 groups);
 //   C -= V W2  (rows x 16): thread = 8 rows (128 apart) x 4 columns cb.
-__device__ void apply_block(Smem& sh, int slot, int m, int r0, const float* __restrict__ Tp) {
+__device__ void apply_block(Smem& sh, int slot, int m, int r0) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   float* Cs = sh.C[slot];
-  for (int o = t; o < BW * BW; o += NT) sh.G[(o / BW) * LDW + o % BW] = Tp[o];
   {
     const int tile = t & 7, kb = tile >> 2, cb = tile & 3, g = t >> 3;
     float acc[8][4];
@@ -196,7 +199,7 @@ __device__ void apply_block(Smem& sh, int slot, int m, int r0, const float* __re
   for (int o = t; o < BW * BW; o += NT) {
     const int k = o / BW, c = o % BW;
     float s = 0.f;
-    for (int l = 0; l <= k; ++l) s = fmaf(sh.G[l * LDW + k], sh.Wred[l * LDW + c], s);
+    for (int l = 0; l <= k; ++l) s = fmaf(sh.Tapp[l * LDW + k], sh.Wred[l * LDW + c], s);
     sh.W2[k * LDW2 + c] = s;
   }
   __syncthreads();
@@ -246,139 +249,156 @@ __device__ void apply_block(Smem& sh, int slot, int m, int r0, const float* __re
 
 // Householder QR of panel `slot` (columns 0..jb-1 of the block, rows >= j0 = 16 b), then its
 // compact-WY factor T (dlarft, forward, columnwise) in sh.T.
-// The panel is held in registers: thread t owns rows t and t + NT of the 16 columns, a[2][16], used
-// as a ring. At step i the slots 0..15-i hold the unfinished columns i..15 (slot 0 = the pivot
-// column) and the slots 16-i..15 hold the finished reflectors v_0..v_{i-1} (masked: 0 above the
-// diagonal, 1 on it). Every step works on slot 0 and then rotates the ring by one, so all steps run
-// the same code with static register indices, and one transposed reduction per step yields both
-// the column-update coefficients (unfinished slots) and the Gram entries v_l^T v_i of T (finished
-// slots).
+// A column step is a chain of short reductions, and every warp taking part repeats the reflector
+// arithmetic and a transposed reduction: 8 warps (4 rows per thread, named barrier 1) issue half
+// the instructions of 16 for the same latency chain, so the other 8 warps only wait.
+// The panel is held in registers: thread t < 256 owns rows t + 256 k (k < 4) of the 16 columns,
+// a[4][16], used as a ring. At step i the slots 0..15-i hold the unfinished columns i..15 (slot 0 =
+// the pivot column) and the slots 16-i..15 hold the finished reflectors v_0..v_{i-1} (masked: 0
+// above the diagonal, 1 on it). Every step works on slot 0 and then rotates the ring by one, so all
+// steps run the same code with static register indices, and one transposed reduction per step
+// yields both the column-update coefficients (unfinished slots) and the Gram entries v_l^T v_i of T
+// (finished slots).
+constexpr int FW = 8;           // warps of the panel factorisation
+constexpr int FT = FW * 32;     // its threads
+constexpr int RPT = MMAX / FT;  // rows per thread
+
+__device__ __forceinline__ void bar_factor() { asm volatile("bar.sync 1, %0;" ::"n"(FT) : "memory"); }
+
 __device__ void factor_panel(Smem& sh, int slot, int m, int j0, int jb) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   float* Cs = sh.C[slot];
-  float a[2][BW];
+  if (t < FT) {
+    float a[RPT][BW];
 #pragma unroll
-  for (int rr = 0; rr < 2; ++rr) {
-    const int r = t + rr * NT;
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int r = t + rr * FT;
 #pragma unroll
-    for (int c = 0; c < BW; ++c) a[rr][c] = (r < m) ? Cs[c * LDC + r] : 0.f;
-  }
-  float s = 0.f;  // this thread's part of the sum of squares below the current pivot
-#pragma unroll
-  for (int rr = 0; rr < 2; ++rr) {
-    const int r = t + rr * NT;
-    if (r > j0 && r < m) s = fmaf(a[rr][0], a[rr][0], s);
-  }
-#pragma unroll 1
-  for (int i = 0; i < jb; ++i) {
-    const int j = j0 + i;
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) sh.red[warp * LDW + BW] = s;
-#pragma unroll
-    for (int rr = 0; rr < 2; ++rr)
-      if (t + rr * NT == j) sh.piv = a[rr][0];
-    __syncthreads();
-    // reflector, computed redundantly by every thread
-    float sig = 0.f;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) sig += sh.red[w * LDW + BW];
-    const float x1 = sh.piv;
-    float beta = x1, tau = 0.f, scale = 0.f;
-    if (sig > 0.f) {
-      const float nrm = sqrtf(fmaf(x1, x1, sig));
-      beta = (x1 >= 0.f) ? -nrm : nrm;
-      tau = (beta - x1) / beta;
-      scale = 1.f / (x1 - beta);
+      for (int c = 0; c < BW; ++c) a[rr][c] = (r < m) ? Cs[c * LDC + r] : 0.f;
     }
-    // v_i (masked) of this thread's rows; the pivot slot keeps v below the diagonal
-    float v[2];
+    float s = 0.f;  // this thread's part of the sum of squares below the current pivot
 #pragma unroll
-    for (int rr = 0; rr < 2; ++rr) {
-      const int r = t + rr * NT;
-      v[rr] = 0.f;
-      if (r < m) {
-        if (r > j) {
-          a[rr][0] *= scale;
-          v[rr] = a[rr][0];
-        } else if (r == j) {
-          v[rr] = 1.f;
+    for (int rr = 0; rr < RPT; ++rr) {
+      const int r = t + rr * FT;
+      if (r > j0 && r < m) s = fmaf(a[rr][0], a[rr][0], s);
+    }
+#pragma unroll 1
+    for (int i = 0; i < jb; ++i) {
+      const int j = j0 + i;
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) sh.red[warp * LDW + BW] = s;
+#pragma unroll
+      for (int rr = 0; rr < RPT; ++rr)
+        if (t + rr * FT == j) sh.piv = a[rr][0];
+      bar_factor();
+      // reflector, computed redundantly by every thread (lanes 0..7 gather the warps' partials)
+      float sig = (lane < FW) ? sh.red[lane * LDW + BW] : 0.f;
+#pragma unroll
+      for (int o = 1; o < FW; o <<= 1) sig += __shfl_xor_sync(0xffffffffu, sig, o);
+      sig = __shfl_sync(0xffffffffu, sig, 0);
+      const float x1 = sh.piv;
+      float beta = x1, tau = 0.f, scale = 0.f;
+      if (sig > 0.f) {
+        const float nrm = sqrtf(fmaf(x1, x1, sig));
+        beta = (x1 >= 0.f) ? -nrm : nrm;
+        tau = (beta - x1) / beta;
+        scale = 1.f / (x1 - beta);
+      }
+      // v_i (masked) of this thread's rows; the pivot slot keeps v below the diagonal
+      float v[RPT];
+#pragma unroll
+      for (int rr = 0; rr < RPT; ++rr) {
+        const int r = t + rr * FT;
+        v[rr] = 0.f;
+        if (r < m) {
+          if (r > j) {
+            a[rr][0] *= scale;
+            v[rr] = a[rr][0];
+          } else if (r == j) {
+            v[rr] = 1.f;
+          }
         }
       }
-    }
-    float p[BW];
-    p[0] = 0.f;
+      float p[BW];
+      p[0] = 0.f;
 #pragma unroll
-    for (int c = 1; c < BW; ++c) p[c] = fmaf(v[0], a[0][c], v[1] * a[1][c]);
-    const float ws = warp_transpose_sum(p, lane);
-    if (lane < BW) sh.red[warp * LDW + lane] = ws;
-    __syncthreads();
-    if (warp == 0 && lane < BW) {
-      float tot = 0.f;
+      for (int c = 1; c < BW; ++c) {
+        float x = v[0] * a[0][c];
 #pragma unroll
-      for (int w = 0; w < NW; ++w) tot += sh.red[w * LDW + lane];
-      const bool unfinished = lane >= 1 && lane <= BW - 1 - i && i + lane < jb;
-      sh.f[lane] = unfinished ? tau * tot : 0.f;
-      if (lane >= BW - i) sh.G[(lane - BW + i) * LDW + i] = tot;  // slot 16 - i + l holds v_l
-      if (lane == 0) sh.tau[i] = tau;
-    }
-#pragma unroll
-    for (int rr = 0; rr < 2; ++rr)
-      if (t + rr * NT == j) a[rr][0] = beta;  // R(j, j)
-    __syncthreads();
-    // column update of the unfinished slots (f is zero on the finished ones), and the next
-    // column's sum of squares below its pivot
-    float fc[BW];
-#pragma unroll
-    for (int c4 = 0; c4 < BW / 4; ++c4) {
-      const float4 f4 = reinterpret_cast<const float4*>(sh.f)[c4];
-      fc[4 * c4] = f4.x;
-      fc[4 * c4 + 1] = f4.y;
-      fc[4 * c4 + 2] = f4.z;
-      fc[4 * c4 + 3] = f4.w;
-    }
-    s = 0.f;
-#pragma unroll
-    for (int rr = 0; rr < 2; ++rr) {
-#pragma unroll
-      for (int c = 1; c < BW; ++c) a[rr][c] = fmaf(-v[rr], fc[c], a[rr][c]);
-      const int r = t + rr * NT;
-      const float y = (r > j + 1) ? a[rr][1] : 0.f;
-      s = fmaf(y, y, s);
-    }
-    // retire the pivot column: R part and v to shared memory, masked v into the ring
-#pragma unroll
-    for (int rr = 0; rr < 2; ++rr) {
-      const int r = t + rr * NT;
-      if (r < m) Cs[i * LDC + r] = a[rr][0];
-      const float done = v[rr];
-#pragma unroll
-      for (int c = 0; c < BW - 1; ++c) a[rr][c] = a[rr][c + 1];
-      a[rr][BW - 1] = done;
-    }
-    // no barrier here: the next step rewrites red/piv before its first barrier and f after its
-    // second, and every reader of this step's values has passed this step's later barriers
-  }
-  __syncthreads();
-  // T(k, i) = -tau_i sum_{l=k}^{i-1} T(k, l) G(l, i), T(i, i) = tau_i: lane k of warp 0 runs row k
-  // with the row in registers
-  if (warp == 0 && lane < BW) {
-    const int k = lane;
-    float tr[BW];
-#pragma unroll
-    for (int i = 0; i < BW; ++i) {
-      float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-      for (int l = 0; l < i; ++l) {
-        const float g = sh.G[l * LDW + i];
-        if (l & 1) a1 = fmaf((l >= k) ? tr[l] : 0.f, g, a1);
-        else a0 = fmaf((l >= k) ? tr[l] : 0.f, g, a0);
+        for (int rr = 1; rr < RPT; ++rr) x = fmaf(v[rr], a[rr][c], x);
+        p[c] = x;
       }
-      const float ti = sh.tau[i];
-      tr[i] = (i >= jb || k >= jb || k > i) ? 0.f : ((k == i) ? ti : -ti * (a0 + a1));
-    }
+      const float ws = warp_transpose_sum(p, lane);
+      if (lane < BW) sh.red[warp * LDW + lane] = ws;
+      bar_factor();
+      if (warp == 0 && lane < BW) {
+        float tot = 0.f;
 #pragma unroll
-    for (int i = 0; i < BW; ++i) sh.T[k * LDW + i] = tr[i];
+        for (int w = 0; w < FW; ++w) tot += sh.red[w * LDW + lane];
+        const bool unfinished = lane >= 1 && lane <= BW - 1 - i && i + lane < jb;
+        sh.f[lane] = unfinished ? tau * tot : 0.f;
+        if (lane >= BW - i) sh.G[(lane - BW + i) * LDW + i] = tot;  // slot 16 - i + l holds v_l
+        if (lane == 0) sh.tau[i] = tau;
+      }
+#pragma unroll
+      for (int rr = 0; rr < RPT; ++rr)
+        if (t + rr * FT == j) a[rr][0] = beta;  // R(j, j)
+      bar_factor();
+      // column update of the unfinished slots (f is zero on the finished ones), and the next
+      // column's sum of squares below its pivot
+      float fc[BW];
+#pragma unroll
+      for (int c4 = 0; c4 < BW / 4; ++c4) {
+        const float4 f4 = reinterpret_cast<const float4*>(sh.f)[c4];
+        fc[4 * c4] = f4.x;
+        fc[4 * c4 + 1] = f4.y;
+        fc[4 * c4 + 2] = f4.z;
+        fc[4 * c4 + 3] = f4.w;
+      }
+      s = 0.f;
+#pragma unroll
+      for (int rr = 0; rr < RPT; ++rr) {
+#pragma unroll
+        for (int c = 1; c < BW; ++c) a[rr][c] = fmaf(-v[rr], fc[c], a[rr][c]);
+        const int r = t + rr * FT;
+        const float y = (r > j + 1) ? a[rr][1] : 0.f;
+        s = fmaf(y, y, s);
+      }
+      // retire the pivot column: R part and v to shared memory, masked v into the ring
+#pragma unroll
+      for (int rr = 0; rr < RPT; ++rr) {
+        const int r = t + rr * FT;
+        if (r < m) Cs[i * LDC + r] = a[rr][0];
+        const float done = v[rr];
+#pragma unroll
+        for (int c = 0; c < BW - 1; ++c) a[rr][c] = a[rr][c + 1];
+        a[rr][BW - 1] = done;
+      }
+      // no barrier here: the next step rewrites red/piv before its first barrier and f after its
+      // second, and every reader of this step's values has passed this step's later barriers
+    }
+    bar_factor();
+    // T(k, i) = -tau_i sum_{l=k}^{i-1} T(k, l) G(l, i), T(i, i) = tau_i: lane k of warp 0 runs row k
+    // with the row in registers
+    if (warp == 0 && lane < BW) {
+      const int k = lane;
+      float tr[BW];
+#pragma unroll
+      for (int i = 0; i < BW; ++i) {
+        float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+        for (int l = 0; l < i; ++l) {
+          const float g = sh.G[l * LDW + i];
+          if (l & 1) a1 = fmaf((l >= k) ? tr[l] : 0.f, g, a1);
+          else a0 = fmaf((l >= k) ? tr[l] : 0.f, g, a0);
+        }
+        const float ti = sh.tau[i];
+        tr[i] = (i >= jb || k >= jb || k > i) ? 0.f : ((k == i) ? ti : -ti * (a0 + a1));
+      }
+#pragma unroll
+      for (int i = 0; i < BW; ++i) sh.T[k * LDW + i] = tr[i];
+    }
   }
   __syncthreads();
 }
@@ -455,11 +475,11 @@ __global__ void __launch_bounds__(NT, 1)
     }
     __syncthreads();
     if (sh.failed) return false;
-    stage_v(sh, m, p * BW, Vg + (size_t)p * m * BW);
+    stage_v(sh, m, p * BW, Vg + (size_t)p * m * BW, Tg + p * BW * BW);
     __syncthreads();
     return true;
   };
-  auto apply = [&](int sl, int p) { apply_block(sh, sl, m, p * BW, Tg + p * BW * BW); };
+  auto apply = [&](int sl, int p) { apply_block(sh, sl, m, p * BW); };
   // factorise block slot sl, publish V and T, release the waiters, write the R block
   auto factor_publish = [&](int sl) {
     const int b = blk[sl], jb = jbs[sl], col0 = b * BW;

@@ -53,8 +53,9 @@ struct Smem {
   float Tapp[BW * LDW];       // T of the panel being applied
   float red[NW * LDW];        // per-warp partials of the panel reductions
   float f[BW];                // update coefficients of the current panel column
+  float prow[BW];             // the pivot row of the panel (16-byte aligned)
   float tau[BW];              // tau of every reflector of the panel
-  float piv;                  // the current pivot a(j, j)
+  float rb[2];                // beta and scale of the current reflector
   unsigned long long ready[NBMAX];  // mbarrier per panel
   double amax[CL];            // largest |a| of every CTA's blocks
   double wmax[NW];            // per-warp maxima of this CTA's blocks
@@ -63,6 +64,9 @@ struct Smem {
 
 constexpr size_t kSmemBytes = sizeof(Smem) + 16;
 static_assert(kSmemBytes <= 227 * 1024, "shared memory budget of one CTA");
+static_assert(offsetof(Smem, Vs) % 16 == 0 && offsetof(Smem, W2) % 16 == 0 && offsetof(Smem, f) % 16 == 0 &&
+                  offsetof(Smem, prow) % 16 == 0,
+              "float4 members");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -249,16 +253,20 @@ __device__ void apply_block(Smem& sh, int slot, int m, int r0) {
 
 // Householder QR of panel `slot` (columns 0..jb-1 of the block, rows >= j0 = 16 b), then its
 // compact-WY factor T (dlarft, forward, columnwise) in sh.T.
-// A column step is a chain of short reductions, and every warp taking part repeats the reflector
-// arithmetic and a transposed reduction: 8 warps (4 rows per thread, named barrier 1) issue half
-// the instructions of 16 for the same latency chain, so the other 8 warps only wait.
+// One reduction per column: with x the pivot column below the pivot row j and v = e_j + scale x
+// (dlarfg), v^T a_c = a_c(j) + scale * (x^T a_c), so the sums sig = x^T x and h_c = x^T a_c over
+// the rows > j, taken together in one transposed warp reduction before the reflector is known,
+// give the reflector, every update coefficient f_c = tau v^T a_c (unfinished slots) and the Gram
+// entries v_l^T v_i of T (finished slots). A column step is then: partial sums (8 warps) -> barrier
+// -> warp 0 finishes the sums, the reflector and f -> barrier -> update. Every warp taking part
+// repeats a transposed reduction, so 8 warps (4 rows per thread, named barrier 1) do it and the
+// other 8 only wait.
 // The panel is held in registers: thread t < 256 owns rows t + 256 k (k < 4) of the 16 columns,
 // a[4][16], used as a ring. At step i the slots 0..15-i hold the unfinished columns i..15 (slot 0 =
 // the pivot column) and the slots 16-i..15 hold the finished reflectors v_0..v_{i-1} (masked: 0
 // above the diagonal, 1 on it). Every step works on slot 0 and then rotates the ring by one, so all
-// steps run the same code with static register indices, and one transposed reduction per step
-// yields both the column-update coefficients (unfinished slots) and the Gram entries v_l^T v_i of T
-// (finished slots).
+// steps run the same code with static register indices (unrolled by two, which halves the moves of
+// the rotation).
 constexpr int FW = 8;           // warps of the panel factorisation
 constexpr int FT = FW * 32;     // its threads
 constexpr int RPT = MMAX / FT;  // rows per thread
@@ -276,77 +284,76 @@ __device__ void factor_panel(Smem& sh, int slot, int m, int j0, int jb) {
 #pragma unroll
       for (int c = 0; c < BW; ++c) a[rr][c] = (r < m) ? Cs[c * LDC + r] : 0.f;
     }
-    float s = 0.f;  // this thread's part of the sum of squares below the current pivot
-#pragma unroll
-    for (int rr = 0; rr < RPT; ++rr) {
-      const int r = t + rr * FT;
-      if (r > j0 && r < m) s = fmaf(a[rr][0], a[rr][0], s);
-    }
-#pragma unroll 1
+#pragma unroll 2
     for (int i = 0; i < jb; ++i) {
       const int j = j0 + i;
+      // partial sums over this thread's rows below the pivot: slot 0 -> sig, slot c -> h_c; the
+      // owner of the pivot row publishes it
+      float x[RPT];
 #pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) sh.red[warp * LDW + BW] = s;
+      for (int rr = 0; rr < RPT; ++rr) x[rr] = (t + rr * FT > j) ? a[rr][0] : 0.f;  // rows >= m hold 0
+      float p[BW];
+#pragma unroll
+      for (int c = 0; c < BW; ++c) {
+        float y = x[0] * a[0][c];
+#pragma unroll
+        for (int rr = 1; rr < RPT; ++rr) y = fmaf(x[rr], a[rr][c], y);
+        p[c] = y;
+      }
 #pragma unroll
       for (int rr = 0; rr < RPT; ++rr)
-        if (t + rr * FT == j) sh.piv = a[rr][0];
-      bar_factor();
-      // reflector, computed redundantly by every thread (lanes 0..7 gather the warps' partials)
-      float sig = (lane < FW) ? sh.red[lane * LDW + BW] : 0.f;
+        if (t + rr * FT == j) {
 #pragma unroll
-      for (int o = 1; o < FW; o <<= 1) sig += __shfl_xor_sync(0xffffffffu, sig, o);
-      sig = __shfl_sync(0xffffffffu, sig, 0);
-      const float x1 = sh.piv;
-      float beta = x1, tau = 0.f, scale = 0.f;
-      if (sig > 0.f) {
-        const float nrm = sqrtf(fmaf(x1, x1, sig));
-        beta = (x1 >= 0.f) ? -nrm : nrm;
-        tau = (beta - x1) / beta;
-        scale = 1.f / (x1 - beta);
-      }
-      // v_i (masked) of this thread's rows; the pivot slot keeps v below the diagonal
-      float v[RPT];
-#pragma unroll
-      for (int rr = 0; rr < RPT; ++rr) {
-        const int r = t + rr * FT;
-        v[rr] = 0.f;
-        if (r < m) {
-          if (r > j) {
-            a[rr][0] *= scale;
-            v[rr] = a[rr][0];
-          } else if (r == j) {
-            v[rr] = 1.f;
-          }
+          for (int c4 = 0; c4 < BW / 4; ++c4)
+            reinterpret_cast<float4*>(sh.prow)[c4] =
+                make_float4(a[rr][4 * c4], a[rr][4 * c4 + 1], a[rr][4 * c4 + 2], a[rr][4 * c4 + 3]);
         }
-      }
-      float p[BW];
-      p[0] = 0.f;
-#pragma unroll
-      for (int c = 1; c < BW; ++c) {
-        float x = v[0] * a[0][c];
-#pragma unroll
-        for (int rr = 1; rr < RPT; ++rr) x = fmaf(v[rr], a[rr][c], x);
-        p[c] = x;
-      }
       const float ws = warp_transpose_sum(p, lane);
       if (lane < BW) sh.red[warp * LDW + lane] = ws;
       bar_factor();
+      // warp 0, lane c: the total of slot c, then the reflector (every lane) and slot c's coefficient
       if (warp == 0 && lane < BW) {
-        float tot = 0.f;
+        float t0 = 0.f, t1 = 0.f;
 #pragma unroll
-        for (int w = 0; w < FW; ++w) tot += sh.red[w * LDW + lane];
+        for (int w = 0; w < FW; w += 2) {
+          t0 += sh.red[w * LDW + lane];
+          t1 += sh.red[(w + 1) * LDW + lane];
+        }
+        const float tot = t0 + t1;
+        const float sig = __shfl_sync(0x0000ffffu, tot, 0);
+        const float x1 = sh.prow[0];
+        float beta = x1, tau = 0.f, scale = 0.f;
+        if (sig > 0.f) {
+          // hardware reciprocal square root and reciprocal (a few ulp, which the FP64
+          // re-orthogonalisation absorbs) on the critical path of every column; IEEE operations
+          // when the column is so small that the approximations would meet subnormal operands
+          const float s2 = fmaf(x1, x1, sig);
+          if (s2 > 1e-30f) {
+            const float nrm = s2 * rsqrtf(s2);
+            beta = (x1 >= 0.f) ? -nrm : nrm;
+            tau = (beta - x1) * __fdividef(1.f, beta);
+            scale = __fdividef(1.f, x1 - beta);
+          } else {
+            const float nrm = sqrtf(s2);
+            beta = (x1 >= 0.f) ? -nrm : nrm;
+            tau = (beta - x1) / beta;
+            scale = 1.f / (x1 - beta);
+          }
+        }
+        const float pc = fmaf(scale, tot, sh.prow[lane]);  // v_i^T (slot lane)
         const bool unfinished = lane >= 1 && lane <= BW - 1 - i && i + lane < jb;
-        sh.f[lane] = unfinished ? tau * tot : 0.f;
-        if (lane >= BW - i) sh.G[(lane - BW + i) * LDW + i] = tot;  // slot 16 - i + l holds v_l
-        if (lane == 0) sh.tau[i] = tau;
+        sh.f[lane] = unfinished ? tau * pc : 0.f;
+        if (lane >= BW - i) sh.G[(lane - BW + i) * LDW + i] = pc;  // slot 16 - i + l holds v_l
+        if (lane == 0) {
+          sh.tau[i] = tau;
+          sh.rb[0] = beta;
+          sh.rb[1] = scale;
+        }
       }
-#pragma unroll
-      for (int rr = 0; rr < RPT; ++rr)
-        if (t + rr * FT == j) a[rr][0] = beta;  // R(j, j)
       bar_factor();
-      // column update of the unfinished slots (f is zero on the finished ones), and the next
-      // column's sum of squares below its pivot
+      // v_i (masked) of this thread's rows into the pivot slot, R(j, j) on the pivot row; update of
+      // the unfinished slots (f is zero on the others)
+      const float beta = sh.rb[0], scale = sh.rb[1];
       float fc[BW];
 #pragma unroll
       for (int c4 = 0; c4 < BW / 4; ++c4) {
@@ -356,27 +363,27 @@ __device__ void factor_panel(Smem& sh, int slot, int m, int j0, int jb) {
         fc[4 * c4 + 2] = f4.z;
         fc[4 * c4 + 3] = f4.w;
       }
-      s = 0.f;
-#pragma unroll
-      for (int rr = 0; rr < RPT; ++rr) {
-#pragma unroll
-        for (int c = 1; c < BW; ++c) a[rr][c] = fmaf(-v[rr], fc[c], a[rr][c]);
-        const int r = t + rr * FT;
-        const float y = (r > j + 1) ? a[rr][1] : 0.f;
-        s = fmaf(y, y, s);
-      }
-      // retire the pivot column: R part and v to shared memory, masked v into the ring
 #pragma unroll
       for (int rr = 0; rr < RPT; ++rr) {
         const int r = t + rr * FT;
+        float v = 0.f;
+        if (r > j) {
+          v = x[rr] * scale;
+          a[rr][0] = v;
+        } else if (r == j) {
+          v = 1.f;
+          a[rr][0] = beta;
+        }
+#pragma unroll
+        for (int c = 1; c < BW; ++c) a[rr][c] = fmaf(-v, fc[c], a[rr][c]);
+        // retire the pivot column: R part and v to shared memory, masked v into the ring
         if (r < m) Cs[i * LDC + r] = a[rr][0];
-        const float done = v[rr];
 #pragma unroll
         for (int c = 0; c < BW - 1; ++c) a[rr][c] = a[rr][c + 1];
-        a[rr][BW - 1] = done;
+        a[rr][BW - 1] = v;
       }
-      // no barrier here: the next step rewrites red/piv before its first barrier and f after its
-      // second, and every reader of this step's values has passed this step's later barriers
+      // no barrier here: the next step writes prow/red before its first barrier and f/rb after it,
+      // and every reader of this step's values has passed this step's second barrier
     }
     bar_factor();
     // T(k, i) = -tau_i sum_{l=k}^{i-1} T(k, l) G(l, i), T(i, i) = tau_i: lane k of warp 0 runs row k

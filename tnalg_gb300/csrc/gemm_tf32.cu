@@ -136,6 +136,28 @@ struct Cfg {
   static constexpr uint32_t TMEM_COLS = NACC * BN;  // 256 or 512: powers of two
 };
 
+// hi + lo <- hi + lo + x with hi + x split error-free (Knuth's TwoSum; the _rn intrinsics keep the
+// compiler from reassociating it)
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float t = __fadd_rn(hi, x);
+  const float z = __fsub_rn(t, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(x, z));
+  hi = t;
+  lo = __fadd_rn(lo, e);
+}
+
+// FP32 -> FP64 by integer operations (exact for normal numbers, infinities and NaNs; FP32
+// subnormals, below 1.2e-38, become signed zeros, as the split-TF32 operands already do)
+__device__ __forceinline__ double f32_to_f64(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  uint64_t bits = (uint64_t)(u >> 31) << 63;
+  const uint64_t mant = (uint64_t)(u & 0x7FFFFFu) << 29;
+  if (e == 0xFFu) bits |= (0x7FFull << 52) | mant;
+  else if (e != 0u) bits |= ((uint64_t)(e + 896u) << 52) | mant;
+  return __longlong_as_double((long long)bits);
+}
+
 template <int BN>
 __global__ void __launch_bounds__(NTHREADS, 1)
     tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
@@ -224,18 +246,28 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int row = m_tile * BM + warp * 32 + lane;
   const int64_t base = (int64_t)z * sCb;
   if (have) {
+    // The NACC partial accumulators are summed error-free in FP32 (TwoSum: a head and a tail per
+    // element) and widened with integer operations; only the final head + tail, alpha and beta
+    // use the FP64 pipe, which issues 64 times fewer lanes per clock than FP32 on this part.
     const int nacc = min(nkb, NACC);
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 16) {
-      double acc[16];
+      float hi[16], lo[16];
+      {
+        uint32_t r[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) acc[j] = 0.0;
+        for (int j = 0; j < 16; ++j) {
+          hi[j] = __uint_as_float(r[j]);
+          lo[j] = 0.f;
+        }
+      }
 #pragma unroll 1
-      for (int a = 0; a < nacc; ++a) {
+      for (int a = 1; a < nacc; ++a) {
         uint32_t r[16];
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * BN + c0), r);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) acc[j] += (double)__uint_as_float(r[j]);
+        for (int j = 0; j < 16; ++j) two_sum_acc(hi[j], lo[j], __uint_as_float(r[j]));
       }
       if (row < M) {
 #pragma unroll
@@ -243,7 +275,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const int col = n_tile * BN + c0 + j;
           if (col < N) {
             const int64_t off = base + (int64_t)row * sCm + (int64_t)col * sCn;
-            const double v = alpha * acc[j];
+            const double sum = f32_to_f64(hi[j]) + f32_to_f64(lo[j]);
+            const double v = (alpha == 1.0) ? sum : alpha * sum;
             if (atomic_out) atomicAdd(C + off, v);
             else C[off] = (beta == 0.0) ? v : fma(beta, (Cin ? Cin : C)[off], v);
           }

@@ -298,13 +298,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // ---------------------------------------------------------------------------
 // FP64 -> (tf32 hi, tf32 lo) staging, K-major rows of pitch Kp (multiple of 4).
 
+// x -> tf32(x) + tf32(remainder). One conversion from FP64 (the FP64 pipe issues 64 times fewer
+// lanes per clock than FP32 here); the remainder is taken from the FP32 value, exactly: the bits
+// of x below FP32's 24 lie beneath the 22 that hi + lo keep.
 __device__ __forceinline__ void split_tf32(double x, float& hi, float& lo) {
+  const float xf = __double2float_rn(x);
   uint32_t h, l;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"((float)x));
-  const float rem = (float)(x - (double)__uint_as_float(h));
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(xf));
+  const float rem = __fsub_rn(xf, __uint_as_float(h));
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(rem));
   hi = __uint_as_float(h);
   lo = __uint_as_float(l);
+}
+
+__device__ __forceinline__ bool finite_f64(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;
 }
 
 struct PrepArgs {
@@ -323,23 +331,33 @@ constexpr int kErrRange = 16;
 __device__ __forceinline__ void stage_value(const PrepArgs& a, double x, int64_t o) {
   float h, l;
   split_tf32(x, h, l);
-  if (!isfinite(h) && isfinite(x)) atomicExch(a.err, kErrRange);
+  if (!isfinite(h) && finite_f64(x)) atomicExch(a.err, kErrRange);
   a.hi[o] = h;
   a.lo[o] = l;
 }
 
 // Both prep kernels also write zeros into the pitch padding k in [K, Kp): the staging buffers are
 // reused scratch, and the padding must never feed the product whatever the tensor map's bounds.
-__global__ void prep_direct_kernel(PrepArgs a) {
-  const int64_t per = a.rows * a.Kp;
-  const int64_t total = a.Z * a.R * per;
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t zr = idx / per, e = idx % per;
-    const int64_t z = zr / a.R, r = zr % a.R;
-    const int64_t row = e / a.Kp, k = e % a.Kp;
-    // idx == (zr * rows + row) * Kp + k
-    stage_value(a, k < a.K ? a.src[z * a.sZ + r * a.sR + row * a.sRow + k * a.sK] : 0.0, idx);
+// prep_direct: block (64, 4) = 64 consecutive k of 4 staged rows; every thread stages 4 elements
+// 64 apart with its row index split once (staged row g = zr * rows + row, zr = z * R + r).
+constexpr int PD_K = 64, PD_ROWS = 4, PD_PER = 4;
+__global__ void __launch_bounds__(PD_K * PD_ROWS) prep_direct_kernel(PrepArgs a) {
+  const int64_t g = (int64_t)blockIdx.x * PD_ROWS + threadIdx.y;
+  if (g >= a.Z * a.R * a.rows) return;
+  const int64_t zr = g / a.rows, row = g - zr * a.rows;
+  const int64_t z = zr / a.R, r = zr - z * a.R;
+  const double* src = a.src + z * a.sZ + r * a.sR + row * a.sRow;
+  const int64_t k0 = (int64_t)blockIdx.y * (PD_K * PD_PER) + threadIdx.x;
+  double x[PD_PER];
+#pragma unroll
+  for (int i = 0; i < PD_PER; ++i) {
+    const int64_t k = k0 + i * PD_K;
+    x[i] = (k < a.K) ? src[k * a.sK] : 0.0;
+  }
+#pragma unroll
+  for (int i = 0; i < PD_PER; ++i) {
+    const int64_t k = k0 + i * PD_K;
+    if (k < a.Kp) stage_value(a, x[i], g * a.Kp + k);
   }
 }
 
@@ -365,11 +383,17 @@ __global__ void prep_transpose_kernel(PrepArgs a) {
 __global__ void scale_out_kernel(int64_t Z, int64_t M, int64_t N, double* C, int64_t sCm, int64_t sCn, int64_t sCb,
                                  const double* Cin, double beta) {
   const int64_t total = Z * M * N;
+  const double* src = Cin ? Cin : C;
+  if (Z == 1 && M == 1 && sCn == 1) {  // one contiguous vector: no index arithmetic
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N; idx += (int64_t)gridDim.x * blockDim.x)
+      C[idx] = (beta == 0.0) ? 0.0 : beta * src[idx];
+    return;
+  }
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t z = idx / (M * N), e = idx % (M * N);
     const int64_t off = z * sCb + (e / N) * sCm + (e % N) * sCn;
-    C[off] = (beta == 0.0) ? 0.0 : beta * (Cin ? Cin : C)[off];
+    C[off] = (beta == 0.0) ? 0.0 : beta * src[off];
   }
 }
 
@@ -389,7 +413,10 @@ int prep(const PrepArgs& args, cudaStream_t s) {
     if (grid.z > 65535u || grid.y > 65535u) return tn_fail(TN_ERR_ARG, "tf32 prep: grid too large");
     prep_transpose_kernel<<<grid, dim3(32, 8), 0, s>>>(a);
   } else {
-    prep_direct_kernel<<<blocks_for(a.Z * a.R * a.rows * a.Kp), 256, 0, s>>>(a);
+    const int64_t nrows = a.Z * a.R * a.rows;
+    const int64_t kchunks = tn_cdiv(a.Kp, PD_K * PD_PER);
+    if (kchunks > 65535 || tn_cdiv(nrows, PD_ROWS) > 0x7fffffffLL) return tn_fail(TN_ERR_ARG, "tf32 prep: grid too large");
+    prep_direct_kernel<<<dim3((unsigned)tn_cdiv(nrows, PD_ROWS), (unsigned)kchunks), dim3(PD_K, PD_ROWS), 0, s>>>(a);
   }
   TN_CHECK_LAUNCH();
   return TN_OK;
@@ -648,8 +675,12 @@ int tn_matvec_tf32x3(const tn_site_desc* d, const double* psi, double* y, double
   const int64_t n = cl * dd * cr;
   int st;
   // y = beta * psi, then every product is added atomically
-  scale_out_kernel<<<blocks_for(n), 256, 0, s>>>(1, 1, n, y, 0, 1, 0, psi, beta);
-  TN_CHECK_LAUNCH();
+  if (beta == 0.0) {
+    TN_CUDA(cudaMemsetAsync(y, 0, (size_t)n * sizeof(double), s));
+  } else {
+    scale_out_kernel<<<blocks_for(n), 256, 0, s>>>(1, 1, n, y, 0, 1, 0, psi, beta);
+    TN_CHECK_LAUNCH();
+  }
   if (d->wl) {
     // psi^T staged: B-op[n = b][k = (a s)] = psi[(a s) * cr + b]
     PrepArgs pt{psi, 1, 1, cr, cl * dd, 0, 0, 1, cr, L.psit.hi, L.psit.lo, L.psit.Kp};

@@ -118,14 +118,30 @@ size_t matvec_fp64_ws_bytes(const tn_site_desc* ds) {
 // ---------------------------------------------------------------------------
 // Lanczos vector kernels. V is (ldv) x n row-major: vector i at V + i*n.
 
+// The vector kernels are bound by L2/HBM latency times the bytes in flight: every thread keeps
+// four grid-strided elements (UNR) of each operand in flight before it uses any of them.
+constexpr int UNR = 4;
+
 // part[i*nb + blockIdx.x] = sum over this block's chunk of V[i]·w ; last block per column reduces.
 __global__ void multidot_kernel(int64_t n, int ncols, const double* __restrict__ V, const double* __restrict__ w,
                                 double* part, unsigned int* tickets, double* out) {
   const int i = blockIdx.y;
   const double* v = V + (int64_t)i * n;
-  double acc = 0.0;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    acc = fma(v[k], w[k], acc);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double a4[UNR] = {0.0, 0.0, 0.0, 0.0};
+  for (; k + (UNR - 1) * stride < n; k += UNR * stride) {
+    double x[UNR], y[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      x[u] = v[k + u * stride];
+      y[u] = w[k + u * stride];
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) a4[u] = fma(x[u], y[u], a4[u]);
+  }
+  for (; k < n; k += stride) a4[0] = fma(v[k], w[k], a4[0]);
+  double acc = (a4[0] + a4[1]) + (a4[2] + a4[3]);
   __shared__ double red[NT / 32];
   __shared__ bool last;
   acc = tn_warp_sum(acc);
@@ -154,13 +170,34 @@ __global__ void multiaxpy_kernel(int64_t n, int ncols, const double* __restrict_
   __shared__ double hs[kMaxKrylov + 1];
   for (int i = threadIdx.x; i < ncols; i += blockDim.x) hs[i] = h[i];
   __syncthreads();
-  double acc = 0.0;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double a4[UNR] = {0.0, 0.0, 0.0, 0.0};
+  for (; k + (UNR - 1) * stride < n; k += UNR * stride) {
+    double x[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) x[u] = w[k + u * stride];
+    for (int i = 0; i < ncols; ++i) {
+      const double* vi = V + (int64_t)i * n;
+      double y[UNR];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) y[u] = vi[k + u * stride];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) x[u] = fma(-hs[i], y[u], x[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      w[k + u * stride] = x[u];
+      a4[u] = fma(x[u], x[u], a4[u]);
+    }
+  }
+  for (; k < n; k += stride) {
     double x = w[k];
     for (int i = 0; i < ncols; ++i) x = fma(-hs[i], V[(int64_t)i * n + k], x);
     w[k] = x;
-    acc = fma(x, x, acc);
+    a4[0] = fma(x, x, a4[0]);
   }
+  double acc = (a4[0] + a4[1]) + (a4[2] + a4[3]);
   if (!nrm2) return;
   __shared__ double red[NT / 32];
   __shared__ bool last;
@@ -191,8 +228,16 @@ __global__ void lanczos_finish_kernel(int64_t n, int j, const double* __restrict
   const double nn = *nrm2;
   const double b = nn > 0.0 ? sqrt(nn) : 0.0;
   const double inv = b > 1e-300 ? 1.0 / b : 0.0;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    v[k] = w[k] * inv;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; k + (UNR - 1) * stride < n; k += UNR * stride) {
+    double x[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) x[u] = w[k + u * stride];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) v[k + u * stride] = x[u] * inv;
+  }
+  for (; k < n; k += stride) v[k] = w[k] * inv;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     alpha[j] = h1[j] + h2[j];
     beta[j] = b;
@@ -205,7 +250,22 @@ __global__ void combine_kernel(int64_t n, int ncols, const double* __restrict__ 
   __shared__ double ss[kMaxKrylov + 1];
   for (int i = threadIdx.x; i < ncols; i += blockDim.x) ss[i] = s[i];
   __syncthreads();
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; k + (UNR - 1) * stride < n; k += UNR * stride) {
+    double acc[UNR] = {0.0, 0.0, 0.0, 0.0};
+    for (int i = 0; i < ncols; ++i) {
+      const double* vi = V + (int64_t)i * n;
+      double y[UNR];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) y[u] = vi[k + u * stride];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) acc[u] = fma(ss[i], y[u], acc[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) x[k + u * stride] = acc[u];
+  }
+  for (; k < n; k += stride) {
     double acc = 0.0;
     for (int i = 0; i < ncols; ++i) acc = fma(ss[i], V[(int64_t)i * n + k], acc);
     x[k] = acc;
@@ -217,8 +277,16 @@ __global__ void scaled_copy_kernel(int64_t n, const double* src, double* dst,
                                    const double* nrm2) {
   const double nn = *nrm2;
   const double inv = nn > 0.0 ? 1.0 / sqrt(nn) : 0.0;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    dst[k] = src[k] * inv;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; k + (UNR - 1) * stride < n; k += UNR * stride) {
+    double x[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) x[u] = src[k + u * stride];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) dst[k + u * stride] = x[u] * inv;
+  }
+  for (; k < n; k += stride) dst[k] = src[k] * inv;
 }
 
 // r = w - e*x (e = x.w), nrm2 = ||r||^2 computed in the dot kernel afterwards

@@ -553,6 +553,19 @@ bool tn_tf32x3_supported() {
   return maj == 10 && min == 3 && encode_fn() != nullptr;
 }
 
+// Status for a value h read from the device error word: clears the word and names the failure.
+int tn_device_error_status(int h, cudaStream_t s) {
+  if (!h) return TN_OK;
+  int* err;
+  int st = err_buffer(&err);
+  if (st) return st;
+  TN_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  if (h == kErrRange)
+    return tn_fail(TN_ERR_NUMERIC, "tf32x3 gemm: an operand lies outside the FP32 range (|x| >= 3.4e38)");
+  if (h == TN_DEVERR_QR_WAIT) return tn_fail(TN_ERR_TIMEOUT, "qr32 cluster: a bounded panel wait gave up");
+  return tn_fail(TN_ERR_TIMEOUT, "tf32x3 gemm: a bounded pipeline wait gave up");
+}
+
 int tn_tf32x3_error_check(cudaStream_t s) {
   int* err;
   int st = err_buffer(&err);
@@ -560,14 +573,7 @@ int tn_tf32x3_error_check(cudaStream_t s) {
   int h = 0;
   TN_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
   TN_CUDA(cudaStreamSynchronize(s));
-  if (h) {
-    TN_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-    if (h == kErrRange)
-      return tn_fail(TN_ERR_NUMERIC, "tf32x3 gemm: an operand lies outside the FP32 range (|x| >= 3.4e38)");
-    if (h == TN_DEVERR_QR_WAIT) return tn_fail(TN_ERR_TIMEOUT, "qr32 cluster: a bounded panel wait gave up");
-    return tn_fail(TN_ERR_TIMEOUT, "tf32x3 gemm: a bounded pipeline wait gave up");
-  }
-  return TN_OK;
+  return tn_device_error_status(h, s);
 }
 
 // The device error word shared by the library's kernels (bounded waits, range checks); read and

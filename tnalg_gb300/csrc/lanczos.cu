@@ -20,6 +20,8 @@
 
 int tn_dot_ws(int64_t n, const double* x, const double* y, double* out, void* ws, size_t ws_bytes, cudaStream_t s);
 int tn_tf32x3_error_check(cudaStream_t s);
+int tn_device_error_word(int** out);
+int tn_device_error_status(int h, cudaStream_t s);
 int tn_matvec_tf32x3(const tn_site_desc* d, const double* psi, double* y, double alpha, double beta,
                      void* ws, size_t ws_bytes, cudaStream_t s);
 size_t tn_matvec_tf32x3_ws_bytes(const tn_site_desc* d);
@@ -533,6 +535,11 @@ static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_
   TN_CHECK_LAUNCH();
 
   std::vector<double> ha(kMaxKrylov + 1), hb(kMaxKrylov + 1), sv;
+  // the device error word (range flags of the split-TF32 staging, bounded waits) travels with
+  // alpha/beta at every convergence check, so a mixed-precision solve needs no sync of its own
+  int* dev_err = nullptr;
+  if (mixed && (st = tn_device_error_word(&dev_err))) return st;
+  int herr = 0;
   int matvecs = 0, restarts = 0;
   bool converged = false;
   double theta = 0.0, resid = INFINITY;
@@ -560,7 +567,9 @@ static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_
       if ((j + 1) % check == 0 || last) {
         TN_CUDA(cudaMemcpyAsync(ha.data(), L.alpha, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
         TN_CUDA(cudaMemcpyAsync(hb.data(), L.beta, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (mixed) TN_CUDA(cudaMemcpyAsync(&herr, dev_err, sizeof(int), cudaMemcpyDeviceToHost, s));
         TN_CUDA(cudaStreamSynchronize(s));
+        if (herr) return tn_device_error_status(herr, s);
         for (int i = 0; i < nc; ++i)
           if (!isfinite(ha[i]) || !isfinite(hb[i])) return tn_fail(TN_ERR_NUMERIC, "lanczos: non-finite coefficient");
         // breakdown: truncate at the first negligible beta
@@ -582,13 +591,16 @@ static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_
         if (last) { jj = mm; break; }
       }
     }
-    // Ritz vector x = V s -> psi, normalised
+    // Ritz vector x = V s / ||s|| -> psi: the basis is orthonormal to ~1e-15 (Gram-Schmidt twice),
+    // so ||V s|| = ||s|| to that accuracy and no separate normalisation pass is needed
+    {
+      double ss = 0.0;
+      for (int i = 0; i < jj; ++i) ss += sv[i] * sv[i];
+      const double inv = ss > 0.0 ? 1.0 / sqrt(ss) : 0.0;
+      for (int i = 0; i < jj; ++i) sv[i] *= inv;
+    }
     TN_CUDA(cudaMemcpyAsync(L.s, sv.data(), jj * sizeof(double), cudaMemcpyHostToDevice, s));
     combine_kernel<<<nb, NT, 0, s>>>(n, jj, L.V, L.s, psi);
-    TN_CHECK_LAUNCH();
-    st = dot2(psi, psi, L.nrm2);
-    if (st) return st;
-    scaled_copy_kernel<<<nb, NT, 0, s>>>(n, psi, psi, L.nrm2);
     TN_CHECK_LAUNCH();
     if (stop || restarts >= o->max_restarts) break;
     ++restarts;
@@ -614,10 +626,6 @@ static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_
     TN_CUDA(cudaStreamSynchronize(s));
     res->energy_fp64 = hv[0];
     res->residual = sqrt(std::max(hv[1], 0.0));
-  }
-  if (mixed) {
-    st = tn_tf32x3_error_check(s);
-    if (st) return st;
   }
   res->matvecs = matvecs;
   res->restarts = restarts;

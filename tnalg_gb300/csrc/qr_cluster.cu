@@ -546,17 +546,18 @@ __global__ void __launch_bounds__(NT, 1)
 // identity columns of block q unchanged (they are zero on rows >= 16p), so the CTA applies
 // H_q, ..., H_0 to its columns, each on rows >= 16p only.
 constexpr int QF_CW = 8;    // columns of Q per CTA
-constexpr int QF_NT = 128;  // threads per CTA
+constexpr int QF_NT = 256;  // threads per CTA (the chain of the last blocks is issue-bound)
 constexpr int QF_NW = QF_NT / 32;
 constexpr int QF_ROWS = MMAX / QF_NT;  // rows per thread in the update
-static_assert(BW * QF_CW == QF_NT, "one W element per thread");
+constexpr int QF_W = BW * QF_CW;       // elements of W (threads t < QF_W own one)
+static_assert(QF_W <= QF_NT, "one W element per thread");
 
 __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const float* __restrict__ Vg,
                                                             const float* __restrict__ Tg, double* __restrict__ Q) {
   __shared__ __align__(16) float X[MMAX * QF_CW];  // the CTA's Q columns, row-major m x 8
-  __shared__ __align__(16) float Wp[QF_NW][BW * QF_CW];
-  __shared__ __align__(16) float W[BW * QF_CW];
-  __shared__ __align__(16) float W2[BW * QF_CW];
+  __shared__ __align__(16) float Wp[QF_NW][QF_W];
+  __shared__ __align__(16) float W[QF_W];
+  __shared__ __align__(16) float W2[QF_W];
   __shared__ float T[BW * LDW];
   constexpr int chunks = BW / QF_CW;
   const int q = blockIdx.x / chunks, c0 = q * BW + (blockIdx.x % chunks) * QF_CW;
@@ -572,7 +573,7 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
     const int r0 = p * BW;
     for (int o = t; o < BW * BW; o += QF_NT) T[(o / BW) * LDW + o % BW] = Tp[o];
     __syncthreads();  // X (initial values or the previous update) and T are in place
-    // W = V_p^T X over rows >= r0: thread = (4 reflectors kq, row group g of 32), 4 x 8 partials
+    // W = V_p^T X over rows >= r0: thread = (4 reflectors kq, row group g of 64), 4 x 8 partials
     {
       const int kq = lane & 3, g = warp * 8 + (lane >> 2);
       float acc[4][QF_CW];
@@ -580,7 +581,7 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
       for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < QF_CW; ++b) acc[a][b] = 0.f;
-      for (int r = r0 + g; r < m; r += 32) {
+      for (int r = r0 + g; r < m; r += QF_NW * 8) {
         const float4 v4 = reinterpret_cast<const float4*>(Vp + (size_t)r * BW)[kq];
         const float4* xr = reinterpret_cast<const float4*>(X + r * QF_CW);
         const float4 x0 = xr[0], x1 = xr[1];
@@ -606,7 +607,7 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
       }
     }
     __syncthreads();
-    {
+    if (t < QF_W) {
       float s = 0.f;
 #pragma unroll
       for (int w = 0; w < QF_NW; ++w) s += Wp[w][t];
@@ -614,14 +615,14 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
     }
     __syncthreads();
     // W2 = T_p W (T upper triangular)
-    {
+    if (t < QF_W) {
       const int k = t / QF_CW, c = t % QF_CW;
       float s = 0.f;
       for (int l = k; l < BW; ++l) s = fmaf(T[k * LDW + l], W[l * QF_CW + c], s);
       W2[t] = s;
     }
     __syncthreads();
-    // X -= V_p W2 over rows >= r0: thread t owns rows r0 + t + 128 i of the 8 columns, so every W2
+    // X -= V_p W2 over rows >= r0: thread t owns rows r0 + t + 256 i of the 8 columns, so every W2
     // value read from shared memory feeds QF_ROWS rows
     {
       float out[QF_ROWS][QF_CW];

@@ -21,7 +21,7 @@
 //     factorisation is, per panel: stage V_b, apply it to block b + 1, factorise block b + 1,
 //     publish; every other update runs beside it. The block two panels ahead is updated after
 //     the factorisation, so it never delays the chain.
-//   * Q = H_0 H_1 ... E is formed by a second kernel over 64 CTAs (8 columns each) from the
+//   * Q = H_0 H_1 ... E is formed by a second kernel over 128 CTAs (4 columns each) from the
 //     published V_b, T_b: the chain H_q, ..., H_0 of the last column block would otherwise run on
 //     one SM after the last panel while the rest of the cluster sits idle.
 // Every wait is bounded by a clock budget; on timeout the CTA records an error code, skips its
@@ -152,9 +152,10 @@ __device__ void stage_v(Smem& sh, int m, int r0, const float* __restrict__ Vp, c
 // staged in Tapp.
 //   W = V^T C  (16 x 16): thread = (8 reflectors kb, 4 columns cb) x row group g (64 groups);
 //   C -= V W2  (rows x 16): thread = 8 rows (128 apart) x 4 columns cb.
-__device__ void apply_block(Smem& sh, int slot, int m, int r0) {
+// W2 = T^T V^T C (rows >= r0): the first half of apply_block; ends with a barrier.
+__device__ void apply_w(Smem& sh, int slot, int m, int r0) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  float* Cs = sh.C[slot];
+  const float* Cs = sh.C[slot];
   {
     const int tile = t & 7, kb = tile >> 2, cb = tile & 3, g = t >> 3;
     float acc[8][4];
@@ -207,6 +208,12 @@ __device__ void apply_block(Smem& sh, int slot, int m, int r0) {
     sh.W2[k * LDW2 + c] = s;
   }
   __syncthreads();
+}
+
+// C(rows >= r0) -= V W2: the second half of apply_block.
+__device__ void apply_c(Smem& sh, int slot, int m, int r0) {
+  const int t = threadIdx.x;
+  float* Cs = sh.C[slot];
   // C -= V W2: a warp covers 32 consecutive rows of one column group (Vs reads conflict-free by the
   // swizzle, W2 reads broadcast, C accesses on 32 distinct banks by the odd pitch)
   {
@@ -251,6 +258,11 @@ __device__ void apply_block(Smem& sh, int slot, int m, int r0) {
   __syncthreads();
 }
 
+__device__ void apply_block(Smem& sh, int slot, int m, int r0) {
+  apply_w(sh, slot, m, r0);
+  apply_c(sh, slot, m, r0);
+}
+
 // Householder QR of panel `slot` (columns 0..jb-1 of the block, rows >= j0 = 16 b), then its
 // compact-WY factor T (dlarft, forward, columnwise) in sh.T.
 // One reduction per column: with x the pivot column below the pivot row j and v = e_j + scale x
@@ -273,7 +285,10 @@ constexpr int RPT = MMAX / FT;  // rows per thread
 
 __device__ __forceinline__ void bar_factor() { asm volatile("bar.sync 1, %0;" ::"n"(FT) : "memory"); }
 
-__device__ void factor_panel(Smem& sh, int slot, int m, int j0, int jb) {
+// fr0 >= 0: the block has not yet received the update C -= V W2 of the previous panel (rows >= fr0,
+// V staged in Vs, W2 from apply_w); it is applied here, in registers, on the way in (the panel is
+// retired into shared memory column by column, all rows).
+__device__ void factor_panel(Smem& sh, int slot, int m, int j0, int jb, int fr0) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   float* Cs = sh.C[slot];
   if (t < FT) {
@@ -283,6 +298,38 @@ __device__ void factor_panel(Smem& sh, int slot, int m, int j0, int jb) {
       const int r = t + rr * FT;
 #pragma unroll
       for (int c = 0; c < BW; ++c) a[rr][c] = (r < m) ? Cs[c * LDC + r] : 0.f;
+    }
+    if (fr0 >= 0) {
+#pragma unroll 1
+      for (int k4 = 0; k4 < BW / 4; ++k4) {
+        float v[RPT][4];
+#pragma unroll
+        for (int rr = 0; rr < RPT; ++rr) {
+          const int r = t + rr * FT;
+          const float4 x = (r >= fr0 && r < m) ? *reinterpret_cast<const float4*>(sh.Vs + vs_idx(r, k4))
+                                               : make_float4(0.f, 0.f, 0.f, 0.f);
+          v[rr][0] = x.x;
+          v[rr][1] = x.y;
+          v[rr][2] = x.z;
+          v[rr][3] = x.w;
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          float w[BW];
+#pragma unroll
+          for (int c4 = 0; c4 < BW / 4; ++c4) {
+            const float4 w4 = *reinterpret_cast<const float4*>(sh.W2 + (4 * k4 + kk) * LDW2 + 4 * c4);
+            w[4 * c4] = w4.x;
+            w[4 * c4 + 1] = w4.y;
+            w[4 * c4 + 2] = w4.z;
+            w[4 * c4 + 3] = w4.w;
+          }
+#pragma unroll
+          for (int rr = 0; rr < RPT; ++rr)
+#pragma unroll
+            for (int c = 0; c < BW; ++c) a[rr][c] = fmaf(-v[rr][kk], w[c], a[rr][c]);
+        }
+      }
     }
 #pragma unroll 2
     for (int i = 0; i < jb; ++i) {
@@ -487,10 +534,11 @@ __global__ void __launch_bounds__(NT, 1)
     return true;
   };
   auto apply = [&](int sl, int p) { apply_block(sh, sl, m, p * BW); };
-  // factorise block slot sl, publish V and T, release the waiters, write the R block
-  auto factor_publish = [&](int sl) {
+  // factorise block slot sl (fr0 >= 0: with the pending update of the previous panel folded in),
+  // publish V and T, release the waiters, write the R block
+  auto factor_publish = [&](int sl, int fr0) {
     const int b = blk[sl], jb = jbs[sl], col0 = b * BW;
-    factor_panel(sh, sl, m, col0, jb);
+    factor_panel(sh, sl, m, col0, jb, fr0);
     float* Vb = Vg + (size_t)b * m * BW;
     for (int e = t; e < m * BW; e += NT) {
       const int r = e / BW, c = e % BW;
@@ -518,22 +566,27 @@ __global__ void __launch_bounds__(NT, 1)
 
   if (jbs[0] > 0) {
     const bool two = jbs[1] > 0;
-    // panels left of block q, in order; the last one reaches block q + 16 only after block q is
-    // factorised (it stays in Vs meanwhile)
+    // panels left of block q, in order; the last one is folded into the factorisation of block q
+    // (the link of the chain), and reaches block q + 16 only after it (it stays in Vs meanwhile)
     for (int p = 0; p < blk[0]; ++p) {
       if (!acquire(p)) break;
-      apply(0, p);
-      if (two && p < blk[0] - 1) apply(1, p);
+      if (p == blk[0] - 1) {
+        apply_w(sh, 0, m, p * BW);
+      } else {
+        apply(0, p);
+        if (two) apply(1, p);
+      }
     }
     if (!sh.failed) {
-      factor_publish(0);
+      factor_publish(0, blk[0] > 0 ? (blk[0] - 1) * BW : -1);
       if (two) {
         if (blk[0] > 0) apply(1, blk[0] - 1);
         for (int p = blk[0]; p < blk[1]; ++p) {
           if (!acquire(p)) break;
-          apply(1, p);
+          if (p == blk[1] - 1) apply_w(sh, 1, m, p * BW);
+          else apply(1, p);
         }
-        if (!sh.failed) factor_publish(1);
+        if (!sh.failed) factor_publish(1, (blk[1] - 1) * BW);
       }
     }
   }
@@ -545,16 +598,16 @@ __global__ void __launch_bounds__(NT, 1)
 // factorisation: one CTA per (column block q, chunk of QF_CW columns). H_p with p > q leaves the
 // identity columns of block q unchanged (they are zero on rows >= 16p), so the CTA applies
 // H_q, ..., H_0 to its columns, each on rows >= 16p only.
-constexpr int QF_CW = 8;    // columns of Q per CTA
+constexpr int QF_CW = 4;    // columns of Q per CTA (128 CTAs at n = 512: short per-CTA chains)
 constexpr int QF_NT = 256;  // threads per CTA (the chain of the last blocks is issue-bound)
 constexpr int QF_NW = QF_NT / 32;
 constexpr int QF_ROWS = MMAX / QF_NT;  // rows per thread in the update
 constexpr int QF_W = BW * QF_CW;       // elements of W (threads t < QF_W own one)
-static_assert(QF_W <= QF_NT, "one W element per thread");
+static_assert(QF_W <= QF_NT && QF_CW % 4 == 0 && BW % QF_CW == 0, "one W element per thread, float4 rows");
 
 __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const float* __restrict__ Vg,
                                                             const float* __restrict__ Tg, double* __restrict__ Q) {
-  __shared__ __align__(16) float X[MMAX * QF_CW];  // the CTA's Q columns, row-major m x 8
+  __shared__ __align__(16) float X[MMAX * QF_CW];  // the CTA's Q columns, row-major m x QF_CW
   __shared__ __align__(16) float Wp[QF_NW][QF_W];
   __shared__ __align__(16) float W[QF_W];
   __shared__ __align__(16) float W2[QF_W];
@@ -584,9 +637,16 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
       for (int r = r0 + g; r < m; r += QF_NW * 8) {
         const float4 v4 = reinterpret_cast<const float4*>(Vp + (size_t)r * BW)[kq];
         const float4* xr = reinterpret_cast<const float4*>(X + r * QF_CW);
-        const float4 x0 = xr[0], x1 = xr[1];
         const float v[4] = {v4.x, v4.y, v4.z, v4.w};
-        const float x[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+        float x[QF_CW];
+#pragma unroll
+        for (int h = 0; h < QF_CW / 4; ++h) {
+          const float4 x4 = xr[h];
+          x[4 * h] = x4.x;
+          x[4 * h + 1] = x4.y;
+          x[4 * h + 2] = x4.z;
+          x[4 * h + 3] = x4.w;
+        }
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -646,8 +706,15 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk) {
           const float4* wr = reinterpret_cast<const float4*>(W2 + (4 * k4 + kk) * QF_CW);
-          const float4 w0 = wr[0], w1 = wr[1];
-          const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+          float w[QF_CW];
+#pragma unroll
+          for (int h = 0; h < QF_CW / 4; ++h) {
+            const float4 w4 = wr[h];
+            w[4 * h] = w4.x;
+            w[4 * h + 1] = w4.y;
+            w[4 * h + 2] = w4.z;
+            w[4 * h + 3] = w4.w;
+          }
 #pragma unroll
           for (int i = 0; i < QF_ROWS; ++i)
 #pragma unroll
@@ -659,9 +726,12 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
         const int r = r0 + t + QF_NT * i;
         if (r < m) {
           float4* xr = reinterpret_cast<float4*>(X + r * QF_CW);
-          const float4 x0 = xr[0], x1 = xr[1];
-          xr[0] = make_float4(x0.x - out[i][0], x0.y - out[i][1], x0.z - out[i][2], x0.w - out[i][3]);
-          xr[1] = make_float4(x1.x - out[i][4], x1.y - out[i][5], x1.z - out[i][6], x1.w - out[i][7]);
+#pragma unroll
+          for (int h = 0; h < QF_CW / 4; ++h) {
+            const float4 x4 = xr[h];
+            xr[h] = make_float4(x4.x - out[i][4 * h], x4.y - out[i][4 * h + 1], x4.z - out[i][4 * h + 2],
+                                x4.w - out[i][4 * h + 3]);
+          }
         }
       }
     }

@@ -10,6 +10,9 @@ sweeps at chi=512. Synthetic input of the stated shapes; no dataset is involved.
 
 Prints ONE JSON line. `value` = sweeps/s (inputs resident in HBM), `e2e` = sweeps/s of a full
 dmrg_finite_size() job from host inputs (ramp included, final MPS copied back to the host).
+On the split-TF32 path at one GPU, `fp64_path` repeats the same job (seed, ramp, timed sweeps) on
+the plain FP64 GPU path: its sweeps/s, the speed-up of this line over it and the difference of
+the energies per site (`--no-fp64-leg` skips it).
 `--impl reference` times the CPU restatement of the reference (oracle/, numpy + scipy ARPACK)
 on a bounded sample of the same workload and extrapolates sweeps/s.
 """
@@ -45,6 +48,8 @@ def parse():
     p.add_argument("--eigs-tol", type=float, default=1e-12)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-fp64-leg", action="store_true",
+                   help="skip the plain FP64 GPU run of the same job that the split-TF32 line is compared with")
     p.add_argument("--cpu-solves", type=int, default=1)
     return p.parse_args()
 
@@ -370,6 +375,21 @@ def main():
                                     "matvec": res["mv_ms"] / args.steps,
                                     "rest": ms_step - (res["qr_ms"] + res["lz_ms"]) / args.steps},
             "clocks": res["clocks"], "gpu_launches": res["launches"]}
+    if rank == 0 and world == 1 and mixed and not args.no_fp64_leg:
+        # the same job (seed, ramp, timed sweeps) on the plain FP64 GPU path: the speed-up of the
+        # split-TF32 path and its energy difference per site
+        import copy
+        a64 = copy.copy(args)
+        a64.precision = "fp64"
+        r64, A64, _ = run_ours(a64, rank, 1, local_rank)
+        del A64
+        v64 = args.steps / (r64["ms"] / 1000.0)
+        line["fp64_path"] = {"value": v64, "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
+                             "e_per_site": r64["e_per_site"], "speedup_of_this_line": value / v64,
+                             "abs_de_per_site": abs(res["e_per_site"] - r64["e_per_site"]),
+                             "device_ms_per_sweep": {"qr": r64["qr_ms"] / args.steps,
+                                                     "lanczos_incl_matvec": r64["lz_ms"] / args.steps,
+                                                     "matvec": r64["mv_ms"] / args.steps}}
     if rank == 0 and not args.no_e2e:
         line["e2e"] = run_e2e(args, "cuda:%d" % local_rank, res["precision"])
     if rank == 0 and not args.no_cpu:

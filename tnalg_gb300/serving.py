@@ -1,0 +1,261 @@
+"""Many independent DMRG jobs on one GPU: admission, interleaving, latency.
+
+A job is one finite-size DMRG run (the sweeps of `dmrg_finite_size`, DMRG_anyH.py:18-101, with
+its coupling lists, chi schedule, sweep count and convergence test) that returns its energy per
+site, bond energies and magnetisations. The scheduler
+
+* admits a job once it has arrived and its estimated device memory (MPS, environments and the
+  workspaces of its solver and gauge moves) fits the free part of a budget;
+* gives every admitted job its own CUDA stream, MPS, environments and workspaces, and advances
+  the admitted jobs one local update (solve + gauge move + environment update) at a time in
+  turn: a job's host-side wait for its own Lanczos convergence check then leaves the kernels
+  already queued by the other jobs running beside it, so small jobs fill the GPU together;
+* records each job's latency from arrival to result (p50 and p99 over the jobs) and the
+  aggregate solves/s.
+
+A job touches only its own buffers and draws its random MPS from its own seed, so its result is
+the same alone and in a mix (up to the rounding order of floating-point atomics in the split-TF32
+GEMMs; the FP64 path is deterministic). The host runs one thread: the C library's lazily
+initialised state is shared by all jobs and is not meant for concurrent host threads.
+
+    python -m tnalg_gb300.serving --jobs 16 --sweeps 4 [--rate 200] [--precision fp64|tf32x3]
+"""
+import argparse
+import contextlib
+import json
+import time
+
+import numpy as np
+
+from . import Parameters as pm
+
+
+def chain_job_para(length, chi, jz=1.0, hz=0.0, sweeps=4, precision="fp64", device="cuda", eigs_tol=1e-10,
+                   break_tol=1e-9):
+    """An XXZ open chain (Parameters.py:170-186 conventions) as a job description."""
+    para = pm.generate_parameters_dmrg("chain")
+    para.update(l=int(length), chi=int(chi), jxy=1.0, jz=float(jz), hx=0.0, hz=float(hz), sweep_time=int(sweeps),
+                dt_ob=1, eigs_tol=eigs_tol, break_tol=break_tol, precision=precision, device=device)
+    return pm.make_consistent_parameter_dmrg(para)
+
+
+class DMRGJob:
+    """One DMRG run advanced one local update at a time (`advance`)."""
+
+    def __init__(self, job_id, para, seed, arrival=0.0):
+        self.job_id = job_id
+        self.para = para
+        self.seed = int(seed)
+        self.arrival = float(arrival)
+        self.result = None
+        self.admitted = None
+        self.finished = None
+        self.solves = 0
+        self.stream = None
+        self._steps = None
+        self.A = None
+
+    def footprint_bytes(self):
+        """Upper estimate of the device memory the job holds while admitted: the MPS (L d chi^2),
+        environments with the carried operators of a nearest-neighbour chain (~6 chi x chi per bond)
+        and the solver's Krylov basis and gauge-move workspaces (~60 site tensors of d chi^2)."""
+        chi, d, l = self.para["chi"], self.para["d"], self.para["l"]
+        chi = min(chi, 2 ** (l // 2))
+        n = d * chi * chi
+        return int(8 * (l * n + 6 * l * chi * chi + 60 * n))
+
+    def start(self, device):
+        import torch
+        from .MPSClass import MpsOpenBoundaryClass as Mob
+        if str(device).startswith("cuda"):
+            self.stream = torch.cuda.Stream(device=device)
+        with self._on_stream():
+            np.random.seed(self.seed)
+            p = self.para
+            self.A = Mob(length=p["l"], d=p["d"], chi=p["chi"], operators=p["op"], device=p.get("device", device),
+                         precision=p.get("precision", "fp64"))
+            self.A.correct_orthogonal_center(p["ob_position"])
+        self._steps = self._run()
+
+    def _on_stream(self):
+        if self.stream is None:
+            return contextlib.nullcontext()
+        import torch
+        return torch.cuda.stream(self.stream)
+
+    def _run(self):
+        """The sweeps of dmrg_finite_size (DMRG_anyH.py:47-77), yielding after every local update."""
+        p, A = self.para, self.A
+        l = p["l"]
+        e0 = 0.0
+        conv = 1.0
+        out = {}
+        schedule = p.get("chi_schedule")
+        for t in range(p["sweep_time"]):
+            if schedule:
+                A.grow_bond_dimension(int(schedule[min(t, len(schedule) - 1)]), noise=p.get("chi_noise", 1e-3),
+                                      seed=t)
+            order = list(range(p["ob_position"] + 1, l)) + list(range(l - 2, -1, -1)) + \
+                list(range(1, p["ob_position"]))
+            for k, n in enumerate(order):
+                if k == len(order) - 1:
+                    A.refine_next_solve()
+                A.update_tensor_eigs(n, p["index1"], p["index2"], p["coeff1"], p["coeff2"], p["tau"], p["is_real"],
+                                     tol=p["eigs_tol"])
+                self.solves += 1
+                yield False
+            if ((t + 1) % p["dt_ob"] == 0) or t == p["sweep_time"] - 1:
+                eb = A.observe_bond_energy(p["index2"], p["coeff2"])
+                mx = A.observe_magnetization(1)
+                mz = A.observe_magnetization(3)
+                e = float((np.sum(eb) - p["hx"] * np.sum(mx) - p["hz"] * np.sum(mz)) / l)
+                out = {"e_per_site": e, "eb_full": np.ravel(eb), "mx": np.ravel(mx), "mz": np.ravel(mz),
+                       "sweeps": t + 1}
+                conv = abs(e - e0)
+                e0 = e
+                if conv < p["break_tol"]:
+                    break
+        out["convergence"] = conv
+        out["solves"] = self.solves
+        self.result = out
+        yield True
+
+    def advance(self):
+        """One local update (or the final observation); True once the result is ready."""
+        with self._on_stream():
+            done = next(self._steps)
+        if done:
+            self.A = None  # release the device tensors
+            self._steps = None
+        return done
+
+
+class Scheduler:
+    """Admission by device-memory budget and round-robin interleaving of admitted jobs."""
+
+    def __init__(self, device="cuda", budget_bytes=None, max_active=64):
+        self.device = device
+        self.budget = budget_bytes
+        self.max_active = int(max_active)
+        self.pending = []
+        self.done = []
+        self.max_concurrent = 0
+
+    def submit(self, job):
+        self.pending.append(job)
+
+    def _budget(self):
+        if self.budget is not None:
+            return int(self.budget)
+        if str(self.device).startswith("cuda"):
+            import torch
+            free, _ = torch.cuda.mem_get_info(torch.device(self.device))
+            return int(0.8 * free)
+        return 1 << 62
+
+    def run(self):
+        """Runs every submitted job; returns the finished jobs in completion order."""
+        budget = self._budget()
+        pending = sorted(self.pending, key=lambda j: (j.arrival, j.job_id))
+        self.pending = []
+        active, used = [], 0
+        t0 = time.perf_counter()
+        while pending or active:
+            now = time.perf_counter() - t0
+            # admit in arrival order while the budget allows (a job larger than the whole budget
+            # runs alone)
+            while pending and pending[0].arrival <= now and len(active) < self.max_active:
+                fp = pending[0].footprint_bytes()
+                if active and used + fp > budget:
+                    break
+                job = pending.pop(0)
+                job.admitted = time.perf_counter() - t0
+                job.start(self.device)
+                active.append(job)
+                used += fp
+            self.max_concurrent = max(self.max_concurrent, len(active))
+            if not active:
+                time.sleep(max(0.0, min(pending[0].arrival - now, 0.01)))
+                continue
+            for job in list(active):
+                if job.advance():
+                    job.finished = time.perf_counter() - t0
+                    active.remove(job)
+                    used -= job.footprint_bytes()
+                    self.done.append(job)
+        return self.done
+
+    def summary(self):
+        lat = np.array([j.finished - j.arrival for j in self.done]) if self.done else np.zeros(1)
+        span = max((j.finished for j in self.done), default=0.0)
+        solves = sum(j.solves for j in self.done)
+        return {"jobs": len(self.done), "solves": solves, "wall_s": span,
+                "solves_per_s": solves / span if span > 0 else 0.0,
+                "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+                "max_concurrent": self.max_concurrent}
+
+
+def make_jobs(njobs, seed=0, sweeps=4, precision="fp64", device="cuda", rate=None, lengths=(16, 48),
+              chis=(16, 32, 64)):
+    """Uneven XXZ chains: N ~ U{lengths}, Jz ~ U[0,2], hz ~ U[0,1], chi from `chis`, per-job seed =
+    seed + job id; Poisson arrivals at `rate` per second (all at time 0 when rate is None)."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.random.default_rng(seed + 1)  # its own stream: the jobs do not depend on the rate
+    jobs, t = [], 0.0
+    for k in range(njobs):
+        if rate:
+            t += arrivals.exponential(1.0 / rate)
+        para = chain_job_para(int(rng.integers(lengths[0], lengths[1] + 1)), int(rng.choice(chis)),
+                              jz=float(rng.uniform(0, 2)), hz=float(rng.uniform(0, 1)), sweeps=sweeps,
+                              precision=precision, device=device)
+        jobs.append(DMRGJob(k, para, seed + k, arrival=t))
+    return jobs
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--jobs", type=int, default=16)
+    ap.add_argument("--sweeps", type=int, default=4)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--rate", type=float, default=None)
+    ap.add_argument("--precision", default="fp64")
+    ap.add_argument("--max-active", type=int, default=64)
+    a = ap.parse_args(argv)
+    import torch
+    from . import _lib as L
+    L.load()
+    dev = "cuda"
+    # warm-up: builds, tensor maps, first-launch costs
+    warm = Scheduler(dev)
+    for j in make_jobs(2, seed=a.seed + 10 ** 6, sweeps=1, precision=a.precision, device=dev):
+        warm.submit(j)
+    warm.run()
+    torch.cuda.synchronize()
+    # the same jobs one at a time, then interleaved
+    seq_wall, seq = 0.0, {}
+    for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev):
+        j.arrival = 0.0
+        s = Scheduler(dev, max_active=1)
+        s.submit(j)
+        t0 = time.perf_counter()
+        s.run()
+        torch.cuda.synchronize()
+        seq_wall += time.perf_counter() - t0
+        seq[j.job_id] = j
+    mix = Scheduler(dev, max_active=a.max_active)
+    for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev, rate=a.rate):
+        mix.submit(j)
+    mix.run()
+    torch.cuda.synchronize()
+    out = mix.summary()
+    solves = sum(j.solves for j in seq.values())
+    out.update({"precision": a.precision, "sweeps": a.sweeps, "rate_per_s": a.rate,
+                "sequential_wall_s": seq_wall, "sequential_solves_per_s": solves / seq_wall,
+                "speedup_vs_sequential": out["solves_per_s"] / (solves / seq_wall) if seq_wall else None,
+                "max_abs_de_per_site_mix_vs_alone": max(abs(j.result["e_per_site"] - seq[j.job_id].result["e_per_site"])
+                                                        for j in mix.done)})
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -12,15 +12,17 @@
 //     q + 16 for ALL rows, in shared memory (column-major, odd leading dimension 1025, so
 //     row-parallel and column-parallel accesses are both free of bank conflicts). Panel b is
 //     factorised by its owner alone (LAPACK dgeqr2 conventions per column, then the compact-WY
-//     factor T of dlarft, forward/columnwise), using __syncthreads only.
+//     factor T of dlarft, forward/columnwise), by 8 of its warps on a named barrier, with no
+//     synchronisation outside the CTA.
 //   * The owner publishes V_b (row-major m x 16 in global memory, unit diagonal, zeros above) and
 //     T_b, then arrives on mbarrier ready[b] of every CTA of the cluster (release at cluster
 //     scope).
 //   * A CTA with blocks to the right of b waits on its own ready[b] (bounded), stages V_b in its
 //     shared memory once and applies H_b^T = I - V_b T_b^T V_b^T to those blocks. The chain of the
-//     factorisation is, per panel: stage V_b, apply it to block b + 1, factorise block b + 1,
-//     publish; every other update runs beside it. The block two panels ahead is updated after
-//     the factorisation, so it never delays the chain.
+//     factorisation is, per panel: stage V_b, form W2 = T_b^T V_b^T C of block b + 1 and fold
+//     C -= V_b W2 into the register prologue of its factorisation, factorise, publish; every
+//     other update runs beside it. The block two panels ahead is updated after the
+//     factorisation, so it never delays the chain.
 //   * Q = H_0 H_1 ... E is formed by a second kernel over 128 CTAs (4 columns each) from the
 //     published V_b, T_b: the chain H_q, ..., H_0 of the last column block would otherwise run on
 //     one SM after the last panel while the rest of the cluster sits idle.

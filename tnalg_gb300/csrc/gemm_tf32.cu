@@ -614,7 +614,8 @@ int tn_gemm_tf32x3(const TnGemmF64& g, void* ws, size_t ws_bytes, cudaStream_t s
 namespace {
 struct MvLayout {
   Staged wl, wr, psi, psit;
-  char* fp64_ws;
+  Staged sl, sr, psiz, zs;  // straddling pairs: stacked SL, SR blocks, psi for SL psi, Z for Z SR^T
+  char* fp64_ws;            // Z = [SL_1; ...] psi (FP64, nstr x chil d chir) first
   size_t fp64_bytes;
 };
 
@@ -622,11 +623,11 @@ size_t mv_layout(const tn_site_desc* d, char* base, MvLayout* L) {
   const int64_t cl = d->chil, dd = d->d, cr = d->chir;
   char* p = base ? (char*)(((uintptr_t)base + 1023) & ~(uintptr_t)1023) : nullptr;
   size_t off = 1024;
-  auto take = [&](int64_t rows, int64_t K, Staged* st) {
-    const size_t b = staged_bytes(rows, K, 1);
+  auto take = [&](int64_t rows, int64_t K, Staged* st, int64_t nmat = 1) {
+    const size_t b = staged_bytes(rows, K, nmat);
     if (p) {
       char* q = p;
-      *st = carve(q, rows, K, 1);
+      *st = carve(q, rows, K, nmat);
       p += b;
     }
     off += b;
@@ -635,6 +636,13 @@ size_t mv_layout(const tn_site_desc* d, char* base, MvLayout* L) {
   take(dd * cr, dd * cr, &L->wr);
   take(cl, dd * cr, &L->psi);
   take(cr, cl * dd, &L->psit);
+  if (d->nstr > 0) {
+    const int64_t ng = d->nstr;
+    take(ng * cl, cl, &L->sl);     // A of Z = [SL_1; ...; SL_ng] psi: the SL blocks stacked by rows
+    take(dd * cr, cl, &L->psiz);   // B of the same product: psi read with (s b) as the row, a as k
+    take(cl * dd, cr, &L->zs, ng);  // A of y += sum_g Z_g SR_g^T
+    take(cr, cr, &L->sr, ng);       // B of the same product: SR_g as stored
+  }
   const size_t fb = tn_matvec_fp64_ws_bytes(d) + (size_t)8 * d->nstr * cl * dd * cr + 4096;
   if (p) {
     L->fp64_ws = p;
@@ -669,6 +677,13 @@ int tn_tf32x3_prepare_static(const tn_site_desc* d, void* ws, size_t ws_bytes, c
     PrepArgs a{d->wr, 1, 1, dd * cr, dd * cr, 0, 0, dd * cr, 1, L.wr.hi, L.wr.lo, L.wr.Kp};
     if ((st = prep(a, s))) return st;
   }
+  if (d->nstr > 0) {
+    const int64_t ng = d->nstr;
+    PrepArgs a{d->sl, 1, 1, ng * cl, cl, 0, 0, cl, 1, L.sl.hi, L.sl.lo, L.sl.Kp};
+    if ((st = prep(a, s))) return st;
+    PrepArgs b{d->sr, 1, ng, cr, cr, 0, cr * cr, cr, 1, L.sr.hi, L.sr.lo, L.sr.Kp};
+    if ((st = prep(b, s))) return st;
+  }
   return TN_OK;
 }
 
@@ -701,8 +716,20 @@ int tn_matvec_tf32x3(const tn_site_desc* d, const double* psi, double* y, double
       return st;
   }
   if (d->nstr > 0) {
-    // straddling pairs: FP64 path (absent in nearest-neighbour chains)
-    if ((st = tn_matvec_fp64_straddle(d, psi, y, alpha, L.fp64_ws, L.fp64_bytes, s))) return st;
+    // straddling pairs (absent in nearest-neighbour chains), the products of the FP64 path
+    // (tn_matvec_fp64_straddle) in split TF32: Z = [SL_1; ...; SL_ng] psi as one GEMM, whose
+    // (ng chil) x (d chir) output is Z_g stacked, then y += alpha sum_g Z_g SR_g^T, one GEMM
+    // reduced over g
+    const int64_t ng = d->nstr;
+    double* Z = (double*)L.fp64_ws;
+    PrepArgs pz{psi, 1, 1, dd * cr, cl, 0, 0, 1, dd * cr, L.psiz.hi, L.psiz.lo, L.psiz.Kp};
+    if ((st = prep(pz, s))) return st;
+    if ((st = gemm_staged(L.sl, L.psiz, ng * cl, dd * cr, cl, 1, 1, Z, dd * cr, 1, 0, nullptr, 1.0, 0.0, false, s)))
+      return st;
+    PrepArgs pa{Z, 1, ng, cl * dd, cr, 0, n, cr, 1, L.zs.hi, L.zs.lo, L.zs.Kp};
+    if ((st = prep(pa, s))) return st;
+    if ((st = gemm_staged(L.zs, L.sr, cl * dd, cr, cr, 1, ng, y, cr, 1, 0, nullptr, alpha, 1.0, true, s)))
+      return st;
   }
   return TN_OK;
 }

@@ -91,6 +91,10 @@ class MpsOpenBoundaryClass(MpsBasic):
                         "mixed_floor": 2e-6, "refine": "last"}
         self._refine_next = False
         self.last_solve = None
+        # two-body couplings: "auto" carries them rank-compressed (engine.CompressedModel) when
+        # that saves at least a quarter of the carried operators; True / False force it
+        self.coupling_compress = "auto"
+        self.coupling_tol = 1e-14
         self._model_key = None
         self._dev = E.DeviceMPS(tensors, d, device, precision=precision)
         self.solve_energies = []
@@ -219,7 +223,8 @@ class MpsOpenBoundaryClass(MpsBasic):
 
     # -- local update ------------------------------------------------------------
     def _model(self, index1, index2, coeff1, coeff2, tol):
-        key = (id(index1), id(index2), id(coeff1), id(coeff2), float(tol),
+        key = (id(index1), id(index2), id(coeff1), id(coeff2), float(tol), str(self.coupling_compress),
+               float(self.coupling_tol),
                np.asarray(index2).tobytes(), np.asarray(coeff2, dtype=float).tobytes(),
                np.asarray(index1).tobytes(), np.asarray(coeff1, dtype=float).tobytes())
         if key != self._model_key:
@@ -228,7 +233,8 @@ class MpsOpenBoundaryClass(MpsBasic):
             for k in used:
                 if np.any(np.abs(np.imag(np.asarray(self.operators[k], dtype=complex))) > 0):
                     raise ValueError("operator %d is complex; the GPU path is real FP64" % k)
-            model = E.Model(self.length, self.phys_dim, self.operators, one, two, self._dev.device)
+            model = E.make_model(self.length, self.phys_dim, self.operators, one, two, self._dev.device,
+                                 compress=self.coupling_compress, tol=self.coupling_tol)
             self._dev.set_model(model)
             self._model_key = key
         return self._dev.model

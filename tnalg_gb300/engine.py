@@ -14,6 +14,11 @@ per bond as one stacked device tensor:
 and are updated incrementally when the centre moves (one block-operator GEMM
 pair per carried operator) instead of being rebuilt from the chain end as the
 reference does (MPSClass.py:491-502).
+
+For long-range coupling lists the carried slots are rank-compressed
+combinations of the open operators instead (CompressedModel): a fully
+connected chain then carries a constant number of slots per bond instead of
+O(N).
 """
 import os
 from collections import OrderedDict
@@ -59,7 +64,25 @@ def canonical_terms(index1, coeff1, index2, coeff2, ops, tol):
 class Model:
     """Per-bond / per-site tables derived from the coupling lists (static for a run)."""
 
+    compressed = False
+
     def __init__(self, length, d, ops, one, two, device):
+        self._init_common(length, d, ops, one, two, device)
+        Ln = length
+        # open operators per bond b (0..L): term (i, j) is open at b iff i < b <= j
+        self.open_left = []
+        self.open_right = []
+        for b in range(Ln + 1):
+            lk = OrderedDict()
+            rk = OrderedDict()
+            for i, j, a, bo, c in two:
+                if i < b <= j:
+                    lk.setdefault((i, a), None)
+                    rk.setdefault((j, bo), None)
+            self.open_left.append({k: s + 1 for s, k in enumerate(lk)})
+            self.open_right.append({k: s + 1 for s, k in enumerate(rk)})
+
+    def _init_common(self, length, d, ops, one, two, device):
         self.length = length
         self.d = d
         self.device = device
@@ -79,19 +102,15 @@ class Model:
         for i, j, a, b, c in two:
             if not (0 <= i < Ln and 0 <= j < Ln):
                 raise ValueError("two-body term (%d,%d) outside 0..%d" % (i, j, Ln - 1))
-        # open operators per bond b (0..L): term (i, j) is open at b iff i < b <= j
-        self.open_left = []
-        self.open_right = []
-        for b in range(Ln + 1):
-            lk = OrderedDict()
-            rk = OrderedDict()
-            for i, j, a, bo, c in two:
-                if i < b <= j:
-                    lk.setdefault((i, a), None)
-                    rk.setdefault((j, bo), None)
-            self.open_left.append({k: s + 1 for s, k in enumerate(lk)})
-            self.open_right.append({k: s + 1 for s, k in enumerate(rk)})
         self._tables = {}
+
+    def n_left(self, b):
+        """Carried (non-Hamiltonian) slots of EL[b]."""
+        return len(self.open_left[b])
+
+    def n_right(self, b):
+        """Carried slots of ER[b]."""
+        return len(self.open_right[b])
 
     # -- block-operator term lists (slot, op, coeff) ----------------------------
     def left_block_terms(self, p):
@@ -174,6 +193,217 @@ class Model:
             self._tables[key] = hit
         return hit
 
+    def matrix(self, key, arr):
+        """Cached device copy (FP64, contiguous) of a small host coefficient matrix."""
+        hit = self._tables.get(key)
+        if hit is None:
+            hit = torch.tensor(np.ascontiguousarray(arr, dtype=float), dtype=torch.float64, device=self.device)
+            self._tables[key] = hit
+        return hit
+
+
+class CompressedModel(Model):
+    """Two-body couplings carried as rank-reduced operator combinations (MPO compression).
+
+    The reference carries one effective operator per open (site, op) of every two-body term
+    crossing a bond (MPSClass.py:474-530, 684-733), so a fully connected or power-law chain
+    ('full' / 'longRange', Parameters.py:244-278) carries O(N) operators per bond and its
+    matvec sums O(N) straddling pairs. Here the coupling matrix M[(i,a), (j,b)] (left ports
+    i < j) is factorised bond by bond:
+
+      * left basis at bond b: orthonormal columns U_b over the ports (i, a), i < b, spanning
+        the columns of M[i < b, j >= b]. Slot 1+k of EL[b] holds sum_(i,a) U_b[(i,a), k] C_L(i, a).
+        Moving to bond b+1 the still-needed part lies in span(U_b): its coordinates
+        X = U_b^T M[:, j >= b+1] are reduced by an SVD to P (singular values above
+        tol * ||M||_2 kept), the carried slots of EL[b+1] are the combinations P^T of the carried
+        slots of EL[b] (carry is linear), and the ports of site b enter as fresh slots;
+      * right basis V_b mirrors it (rows of M[i < b, j >= b]);
+      * W_L at site p takes, per operator b of site p, coefficients U_p^T M[:, (p, b)]; W_R takes
+        M[(p, a), :] V_(p+1); the straddling pairs i < p < j become the core
+        C = U_p^T M V_(p+1), split by its SVD into rank(C) groups sum_g SL_g (x) 1 (x) SR_g.
+
+    All of this is exact up to the singular values dropped (tol = 1e-14 by default, i.e. the
+    couplings to 1e-14 of their spectral norm); a larger tol gives a lossy compression. Uniform
+    all-to-all couplings have rank 1 per operator pair, so their environments carry a constant
+    number of slots instead of O(N).
+    """
+
+    compressed = True
+
+    def __init__(self, length, d, ops, one, two, device, tol=1e-14):
+        self._init_common(length, d, ops, one, two, device)
+        Ln = length
+        lports = sorted({(i, a) for i, j, a, b, c in two})
+        rports = sorted({(j, b) for i, j, a, b, c in two})
+        self.lports, self.rports = lports, rports
+        li = {p: k for k, p in enumerate(lports)}
+        ri = {p: k for k, p in enumerate(rports)}
+        M = np.zeros((len(lports), len(rports)))
+        for i, j, a, b, c in two:
+            M[li[(i, a)], ri[(j, b)]] += c
+        self.M = M
+        lsite = np.array([p[0] for p in lports], dtype=int)
+        rsite = np.array([p[0] for p in rports], dtype=int)
+        self.lsite, self.rsite = lsite, rsite
+        self.cut = float(tol) * (float(np.linalg.norm(M, 2)) if M.size else 0.0)
+
+        # left bases, bond 0 -> L
+        self.U = [np.zeros((len(lports), 0))]
+        self.lcombine = []   # per site b: (P (r_b x r'), [fresh ops of site b])
+        for b in range(Ln):
+            U = self.U[b]
+            cols = rsite >= b + 1
+            P = self._reduce(U.T @ M[:, cols] if (U.shape[1] and cols.any()) else None, U.shape[1], left=True)
+            fresh = [k for k in np.nonzero(lsite == b)[0] if np.any(M[k, cols] != 0)]
+            Un = np.zeros((len(lports), P.shape[1] + len(fresh)))
+            Un[:, :P.shape[1]] = U @ P
+            for q, k in enumerate(fresh):
+                Un[k, P.shape[1] + q] = 1.0
+            self.U.append(Un)
+            self.lcombine.append((P, [lports[k][1] for k in fresh]))
+
+        # right bases, bond L -> 0
+        self.V = [None] * (Ln + 1)
+        self.V[Ln] = np.zeros((len(rports), 0))
+        self.rcombine = [None] * Ln
+        for b in range(Ln - 1, -1, -1):
+            V = self.V[b + 1]
+            rows = lsite < b
+            P = self._reduce(M[rows, :] @ V if (V.shape[1] and rows.any()) else None, V.shape[1], left=False)
+            fresh = [k for k in np.nonzero(rsite == b)[0] if np.any(M[rows, k] != 0)]
+            Vn = np.zeros((len(rports), P.shape[1] + len(fresh)))
+            Vn[:, :P.shape[1]] = V @ P
+            for q, k in enumerate(fresh):
+                Vn[k, P.shape[1] + q] = 1.0
+            self.V[b] = Vn
+            self.rcombine[b] = (P, [rports[k][1] for k in fresh])
+        self._straddle = {}
+
+    def _reduce(self, X, r, left):
+        """Orthonormal basis (r x r') of the span needed next: left singular vectors of X
+        (left side, X = r x cols) or right singular vectors of X (right side, X = rows x r)."""
+        if X is None or X.size == 0:
+            return np.zeros((r, 0))
+        if left:
+            P, s, _ = np.linalg.svd(X, full_matrices=False)
+            return P[:, s > self.cut]
+        _, s, Pt = np.linalg.svd(X, full_matrices=False)
+        return Pt[s > self.cut].T
+
+    def n_left(self, b):
+        return self.U[b].shape[1]
+
+    def n_right(self, b):
+        return self.V[b].shape[1]
+
+    def _keep(self, coef):
+        return [(k, float(c)) for k, c in enumerate(coef) if abs(c) > self.cut]
+
+    def left_block_terms(self, p):
+        t = [(0, -1, 1.0)]
+        t += [(-1, sn, c) for sn, c in self.one_at[p]]
+        for k in np.nonzero(self.rsite == p)[0]:
+            op = self.rports[k][1]
+            t += [(1 + s, op, c) for s, c in self._keep(self.U[p].T @ self.M[:, k])]
+        return t
+
+    def right_block_terms(self, p, with_site=True):
+        t = [(0, -1, 1.0)]
+        if with_site:
+            t += [(-1, sn, c) for sn, c in self.one_at[p]]
+        for k in np.nonzero(self.lsite == p)[0]:
+            op = self.lports[k][1]
+            t += [(1 + s, op, c) for s, c in self._keep(self.M[k, :] @ self.V[p + 1])]
+        return t
+
+    def left_carry_plan(self, b):
+        P, fresh = self.lcombine[b]
+        return [("combine", k) for k in range(P.shape[1])] + [("fresh", a) for a in fresh]
+
+    def right_carry_plan(self, b):
+        P, fresh = self.rcombine[b]
+        return [("combine", k) for k in range(P.shape[1])] + [("fresh", a) for a in fresh]
+
+    def left_combine(self, b):
+        """(P^T as a device matrix (r', r_b) or None, fresh ops): slots of EL[b+1] from EL[b]."""
+        P, fresh = self.lcombine[b]
+        return (self.matrix(("lc", b), P.T) if P.size else None), fresh
+
+    def right_combine(self, b):
+        """Slots of ER[b] from ER[b+1]: (P^T (r', r_(b+1)) or None, fresh ops)."""
+        P, fresh = self.rcombine[b]
+        return (self.matrix(("rc", b), P.T) if P.size else None), fresh
+
+    def straddle_core(self, p):
+        """Host (cl (ng x r_L), cr (ng x r_R)) with sum_g cl[g] (x) cr[g] = U_p^T M V_(p+1)."""
+        hit = self._straddle.get(p)
+        if hit is None:
+            U, V = self.U[p], self.V[p + 1]
+            if U.shape[1] == 0 or V.shape[1] == 0:
+                hit = (np.zeros((0, U.shape[1])), np.zeros((0, V.shape[1])))
+            else:
+                A, s, Bt = np.linalg.svd(U.T @ self.M @ V, full_matrices=False)
+                keep = s > self.cut
+                hit = ((A[:, keep] * s[keep]).T, Bt[keep])
+            self._straddle[p] = hit
+        return hit
+
+    def straddle_mats(self, p):
+        """Device (cl, cr, ng) of straddle_core."""
+        cl, cr = self.straddle_core(p)
+        ng = cl.shape[0]
+        if ng == 0:
+            return None, None, 0
+        return self.matrix(("scl", p), cl), self.matrix(("scr", p), cr), ng
+
+    def straddle_groups(self, p):
+        raise NotImplementedError("the compressed model provides straddle_mats")
+
+
+def carried_cost(two, length):
+    """(slots, groups) of the uncompressed model without building it: carried slots summed over
+    all bonds and both sides, and straddling groups (min of distinct left/right operators)
+    summed over all sites."""
+    Ln = length
+    jmax, imin = {}, {}
+    for i, j, a, b, c in two:
+        jmax[(i, a)] = max(jmax.get((i, a), -1), j)
+        imin[(j, b)] = min(imin.get((j, b), Ln), i)
+    dl = np.zeros(Ln + 2)
+    for (i, a), j in jmax.items():          # open on the left at bonds i+1..j
+        dl[i + 1] += 1
+        dl[j + 1] -= 1
+    dr = np.zeros(Ln + 2)
+    for (j, b), i in imin.items():          # open on the right at bonds i+1..j
+        dr[i + 1] += 1
+        dr[j + 1] -= 1
+    slots = float(np.sum(np.cumsum(dl)) + np.sum(np.cumsum(dr)))
+    groups = 0.0
+    for p in range(Ln):
+        nu = sum(1 for (i, a), j in jmax.items() if i < p < j)
+        nv = sum(1 for (j, b), i in imin.items() if i < p < j)
+        groups += min(nu, nv)
+    return slots, groups
+
+
+def make_model(length, d, ops, one, two, device, compress="auto", tol=1e-14):
+    """The coupling model for a run: uncompressed (one slot per open (site, op), the reference's
+    bookkeeping) or CompressedModel. compress='auto' picks the compressed one when it carries at
+    most 3/4 of the slots plus straddling groups."""
+    if compress is False or compress is None or compress == "off" or not two:
+        return Model(length, d, ops, one, two, device)
+    cm = CompressedModel(length, d, ops, one, two, device, tol=tol)
+    if compress is True or compress == "on":
+        return cm
+    if compress != "auto":
+        raise ValueError("mpo_compress must be 'auto', True or False")
+    slots, groups = carried_cost(two, length)
+    c_slots = float(sum(cm.n_left(b) + cm.n_right(b) for b in range(length + 1)))
+    c_groups = float(sum(cm.straddle_core(p)[0].shape[0] for p in range(length)))
+    if c_slots + c_groups <= 0.75 * (slots + groups):
+        return cm
+    return Model(length, d, ops, one, two, device)
+
 
 # ---------------------------------------------------------------------------
 # device MPS
@@ -224,10 +454,10 @@ class DeviceMPS:
     def _edge_envs(self):
         m = self.model
         if self.el_upto < 0:
-            self.EL[0] = torch.zeros((1 + len(m.open_left[0]), 1, 1), dtype=torch.float64, device=self.device)
+            self.EL[0] = torch.zeros((1 + m.n_left(0), 1, 1), dtype=torch.float64, device=self.device)
             self.el_upto = 0
         if self.er_from > self.length:
-            self.ER[self.length] = torch.zeros((1 + len(m.open_right[self.length]), 1, 1), dtype=torch.float64,
+            self.ER[self.length] = torch.zeros((1 + m.n_right(self.length), 1, 1), dtype=torch.float64,
                                                device=self.device)
             self.er_from = self.length
 
@@ -247,6 +477,8 @@ class DeviceMPS:
         """EL[b+1] from EL[b] and the left-canonical tensor at site b (transfer_left,
         TensorBasicModule.py:530-573, for every carried operator at once)."""
         m, A = self.model, self.mps[b]
+        if m.compressed:
+            return self._update_compressed(b, left=True)
         cl, d, cr = A.shape
         env = self.EL[b]
         plan = m.left_carry_plan(b)
@@ -286,6 +518,8 @@ class DeviceMPS:
         """ER[b] from ER[b+1] and the right-canonical tensor at site b (transfer_right,
         TensorBasicModule.py:576-619)."""
         m, B = self.model, self.mps[b]
+        if m.compressed:
+            return self._update_compressed(b, left=False)
         cl, d, cr = B.shape
         env = self.ER[b + 1]
         plan = m.right_carry_plan(b)
@@ -321,6 +555,67 @@ class DeviceMPS:
                bstrides=(0, cl * d * cr, cl * cl), precision=self.precision, ws=self.ws)
         self.ER[b] = out
         self.er_from = b
+
+    def _update_compressed(self, b, left):
+        """EL[b+1] (left) or ER[b] (right) under a CompressedModel. Slot 0 as in the plain
+        update; the carried slots are first combined (P^T times the stacked carried slots of the
+        previous bond, one FP64 GEMM), then carried through site b like plain slots; the ports
+        of site b enter as site operators."""
+        m, A = self.model, self.mps[b]
+        cl, d, cr = A.shape
+        lib, st = L.load(), L.stream_handle()
+        if left:
+            env = self.EL[b]
+            Pt, fresh = m.left_combine(b)
+            rb, chi = m.n_left(b), cl
+        else:
+            env = self.ER[b + 1]
+            Pt, fresh = m.right_combine(b)
+            rb, chi = m.n_right(b + 1), cr
+        rp = int(Pt.shape[0]) if Pt is not None else 0
+        ns = 1 + rp + len(fresh)
+        T = torch.empty((ns, cl * d * cr), dtype=torch.float64, device=self.device)
+        if left:
+            W = torch.empty((cl * d, cl * d), dtype=torch.float64, device=self.device)
+            terms, nt = m.table(("wl", b), m.left_block_terms(b))
+            L.check(lib.tn_assemble_block(0, cl, d, L.ptr(env), L.ptr(m.ops), L.ptr(terms), nt, L.ptr(W), st),
+                    "assemble")
+            L.gemm(W, A, T[0], cl * d, cr, cl * d, (cl * d, 1), (cr, 1), (cr, 1), precision=self.precision,
+                   ws=self.ws)
+        else:
+            W = torch.empty((d * cr, d * cr), dtype=torch.float64, device=self.device)
+            terms, nt = m.table(("wrf", b), m.right_block_terms(b, with_site=True))
+            L.check(lib.tn_assemble_block(1, cr, d, L.ptr(env), L.ptr(m.ops), L.ptr(terms), nt, L.ptr(W), st),
+                    "assemble")
+            L.gemm(A, W, T[0], cl, d * cr, d * cr, (d * cr, 1), (1, d * cr), (d * cr, 1), precision=self.precision,
+                   ws=self.ws)
+        if rp:
+            if int(env.shape[0]) != 1 + rb:
+                raise RuntimeError("environment at bond %d has %d slots, the model %d" % (b, env.shape[0], 1 + rb))
+            g = torch.empty((rp, chi, chi), dtype=torch.float64, device=self.device)
+            L.gemm(Pt, env[1:], g, rp, chi * chi, rb, (rb, 1), (chi * chi, 1), (chi * chi, 1), ws=self.ws)
+            if left:   # T[1+k] = g[k] . A(cl, d*cr)
+                L.gemm(g, A, T[1], cl, d * cr, cl, (cl, 1), (d * cr, 1), (d * cr, 1), batch=rp,
+                       bstrides=(cl * cl, 0, cl * d * cr), precision=self.precision, ws=self.ws)
+            else:      # T[1+k] = A(cl*d, cr) . g[k]^T
+                L.gemm(A, g, T[1], cl * d, cr, cr, (cr, 1), (1, cr), (cr, 1), batch=rp,
+                       bstrides=(0, cr * cr, cl * d * cr), precision=self.precision, ws=self.ws)
+        for q, a in enumerate(fresh):
+            oi = m.opidx(("op", a), [a])
+            L.check(lib.tn_apply_site_ops(cl, d, cr, L.ptr(A), L.ptr(m.ops), L.ptr(oi), 1, L.ptr(T[1 + rp + q]),
+                                          cl * d * cr, st), "site op")
+        if left:
+            out = torch.empty((ns, cr, cr), dtype=torch.float64, device=self.device)
+            L.gemm(A, T, out, cr, cr, cl * d, (1, cr), (cr, 1), (cr, 1), batch=ns,
+                   bstrides=(0, cl * d * cr, cr * cr), precision=self.precision, ws=self.ws)
+            self.EL[b + 1] = out
+            self.el_upto = b + 1
+        else:
+            out = torch.empty((ns, cl, cl), dtype=torch.float64, device=self.device)
+            L.gemm(A, T, out, cl, cl, d * cr, (d * cr, 1), (1, d * cr), (cl, 1), batch=ns,
+                   bstrides=(0, cl * d * cr, cl * cl), precision=self.precision, ws=self.ws)
+            self.ER[b] = out
+            self.er_from = b
 
     # -- gauge -------------------------------------------------------------------
     def _qr(self, mm, nn, A, sA, Q, sQ, R, seed_only):
@@ -476,9 +771,20 @@ class DeviceMPS:
         t, nt = m.table(("wr", p), m.right_block_terms(p, with_site=False))
         L.check(lib.tn_assemble_block(1, cr, d, L.ptr(er), L.ptr(m.ops), L.ptr(t), nt, L.ptr(wr), st), "assemble")
         keep = [wl, wr]
-        slt, srt, ng = m.straddle_groups(p)
         sl = sr = None
-        if ng:
+        if m.compressed:
+            # SL = cL . (stacked carried slots of EL[p]), SR = cR . (those of ER[p+1]): one GEMM each
+            cL, cR, ng = m.straddle_mats(p)
+            if ng:
+                rl, rr = m.n_left(p), m.n_right(p + 1)
+                sl = torch.empty((ng, cl, cl), dtype=torch.float64, device=self.device)
+                sr = torch.empty((ng, cr, cr), dtype=torch.float64, device=self.device)
+                L.gemm(cL, el[1:], sl, ng, cl * cl, rl, (rl, 1), (cl * cl, 1), (cl * cl, 1), ws=self.ws)
+                L.gemm(cR, er[1:], sr, ng, cr * cr, rr, (rr, 1), (cr * cr, 1), (cr * cr, 1), ws=self.ws)
+                keep += [sl, sr]
+        else:
+            slt, srt, ng = m.straddle_groups(p)
+        if ng and not m.compressed:
             sl = torch.empty((ng, cl, cl), dtype=torch.float64, device=self.device)
             sr = torch.empty((ng, cr, cr), dtype=torch.float64, device=self.device)
             a, na = m.table(("sl", p), slt)

@@ -1,0 +1,43 @@
+"""Write a result file with the reference's own ``save_pr`` (BasicFunctionsSJR.py:25-50).
+
+Run by hand where the T-Nalg sources are mounted (``TNALG_REFERENCE``, default
+``/root/reference``)::
+
+    python tests/golden/make_ref_pickle.py
+
+It runs the unmodified reference ``dmrg_finite_size`` (DMRG_anyH.py:18) on an N=8
+spin-1/2 chain with fields (chi=8, 6 sweeps, seed 4) through ``ref_shim`` and saves
+``(ob, A, info, para)`` exactly as the reference's scripts do, into
+``ref_result_chain_n8_h.pr``. The pickle holds the reference's ``MpsOpenBoundaryClass``
+instance (module ``MPSClass``), which is what a user's existing result files contain.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import ref_shim  # noqa: E402
+
+ref_shim.install()
+import BasicFunctionsSJR as bf  # noqa: E402
+import DMRG_anyH  # noqa: E402
+import Parameters as Pm  # noqa: E402
+
+
+def main():
+    para = Pm.generate_parameters_dmrg("chain")
+    para.update(l=8, chi=8, jxy=1, jz=1, hx=0.25, hz=0.15, sweep_time=6, dt_ob=1, break_tol=-1.0,
+                eigs_tol=1e-12, tau=1e-4, if_print_detail=False)
+    para = Pm.make_consistent_parameter_dmrg(para)
+    np.random.seed(4)
+    ob, A, info, para = DMRG_anyH.dmrg_finite_size(para)
+    A.clean_to_save()
+    para.pop("data_path", None)   # a Windows-style path built from the working directory
+    bf.save_pr(HERE, "ref_result_chain_n8_h.pr", [ob, A, info, para], ["ob", "A", "info", "para"])
+    print("e_per_site", ob["e_per_site"])
+
+
+if __name__ == "__main__":
+    main()

@@ -149,3 +149,16 @@ def test_compressed_couplings_on_device(cuda_lib):
     np.testing.assert_allclose(np.ravel(res[(True, "fp64")]["mz"]), np.ravel(res[(False, "fp64")]["mz"]),
                                atol=1e-8)
     assert abs(res[(True, "tf32x3")]["e_per_site"] - e) <= 1e-8
+
+
+def test_reference_result_file_on_device(cuda_lib):
+    """A result file written by the reference's save_pr loads onto the GPU; the observables of the
+    restored MPS equal the ones pickled beside it."""
+    import os
+    pytest.importorskip("numpy._core")   # the file's arrays were pickled by numpy 2
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    ob, A, info, para = bf.load_pr(os.path.join(gc.GOLDEN, "ref_result_chain_n8_h.pr"), ("ob", "A", "info", "para"))
+    assert A.mps_device[0].is_cuda and A.center == 0
+    eb = A.observe_bond_energy(para["index2"], para["coeff2"])
+    np.testing.assert_allclose(np.ravel(eb), np.ravel(ob["eb_full"]), atol=1e-12)
+    np.testing.assert_allclose(np.ravel(A.observe_magnetization(3)), np.ravel(ob["mz"]), atol=1e-12)

@@ -1,0 +1,101 @@
+"""Result files on CPU: save_pr / load_pr (BasicFunctionsSJR.py:25-89) and reference-written files.
+
+``tests/golden/ref_result_chain_n8_h.pr`` was written by the reference's own save_pr after its
+dmrg_finite_size (tests/golden/make_ref_pickle.py); it holds the reference's MpsOpenBoundaryClass.
+The MPS work runs through the numpy test double of the C ABI.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+REF_FILE = os.path.join(gc.GOLDEN, "ref_result_chain_n8_h.pr")
+
+
+def test_reference_result_file_loads_as_device_mps(fake_backend):
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    from tnalg_gb300.MPSClass import MpsOpenBoundaryClass
+    ob, A, info, para = bf.load_pr(REF_FILE, ("ob", "A", "info", "para"), device="cpu")
+    assert isinstance(A, MpsOpenBoundaryClass)
+    assert A.length == para["l"] == 8 and A.center == 0
+    assert list(A.virtual_dim) == [1, 2, 4, 8, 8, 8, 4, 2, 1]
+    assert np.ravel(A.orthogonality).tolist() == [0] + [1] * 7
+    assert len(A.lm) == 7 and A.ent.shape == (7, 1)
+    # observables of the restored MPS equal the ones the reference pickled beside it
+    eb = A.observe_bond_energy(para["index2"], para["coeff2"])
+    np.testing.assert_allclose(np.ravel(eb), np.ravel(ob["eb_full"]), atol=1e-12)
+    np.testing.assert_allclose(np.ravel(A.observe_magnetization(1)), np.ravel(ob["mx"]), atol=1e-12)
+    np.testing.assert_allclose(np.ravel(A.observe_magnetization(3)), np.ravel(ob["mz"]), atol=1e-12)
+    # the entanglement spectrum recomputed on the device equals the pickled one
+    ent = np.ravel(A.ent).copy()
+    A.calculate_entanglement_spectrum()
+    A.calculate_entanglement_entropy()
+    np.testing.assert_allclose(np.ravel(A.ent), ent, atol=1e-10)
+
+
+def test_restored_mps_continues_sweeping(fake_backend):
+    """A restored, converged MPS stays at the pickled energy under another sweep of local solves."""
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    ob, A, info, para = bf.load_pr(REF_FILE, ("ob", "A", "info", "para"), device="cpu")
+    l = para["l"]
+    for p in list(range(1, l)) + list(range(l - 2, -1, -1)):
+        A.update_tensor_eigs(p, para["index1"], para["index2"], para["coeff1"], para["coeff2"], para["tau"],
+                             para["is_real"], tol=para["eigs_tol"])
+    eb = A.observe_bond_energy(para["index2"], para["coeff2"])
+    mx, mz = A.observe_magnetization(1), A.observe_magnetization(3)
+    e = (np.sum(eb) - para["hx"] * np.sum(mx) - para["hz"] * np.sum(mz)) / l
+    assert abs(e - ob["e_per_site"]) <= 1e-10 * abs(ob["e_per_site"])
+
+
+def test_save_load_roundtrip_and_name_forms(fake_backend, tmp_path):
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    from tnalg_gb300.MPSClass import MpsOpenBoundaryClass
+    np.random.seed(5)
+    A = MpsOpenBoundaryClass(6, 2, 4, device="cpu")
+    A.correct_orthogonal_center(2)
+    folder = str(tmp_path / "results" / "run1")
+    bf.save_pr(folder, "r.pr", [A, {"e": -0.4}, "note"], ["A", "ob", "s"])
+    path = os.path.join(folder, "r.pr")
+    whole = bf.load_pr(path, device="cpu")
+    assert sorted(whole) == ["A", "ob", "s"]
+    B = whole["A"]
+    assert B.center == 2 and (B.virtual_dim == A.virtual_dim).all()
+    for a, b in zip(A.mps, B.mps):
+        np.testing.assert_array_equal(a, b)
+    assert bf.load_pr(path, "s", device="cpu") == "note"
+    ob, s = bf.load_pr(path, ["ob", "s"], device="cpu")
+    assert ob == {"e": -0.4} and s == "note"
+    assert bf.load_pr(os.path.join(folder, "missing.pr")) is False
+    assert bf.mkdir(folder) is True
+
+
+def test_reference_script_imports_through_compat(fake_backend):
+    """`from BasicFunctionsSJR import load_pr` with the module-name shims first on sys.path."""
+    import importlib
+    import sys
+    compat = os.path.join(gc.GOLDEN, "..", "..", "tnalg_gb300", "compat")
+    sys.path.insert(0, compat)
+    try:
+        bfs = importlib.import_module("BasicFunctionsSJR")
+        A = bfs.load_pr(REF_FILE, "A", device="cpu")
+        assert type(A).__module__ == "tnalg_gb300.MPSClass"
+    finally:
+        sys.path.remove(compat)
+        sys.modules.pop("BasicFunctionsSJR", None)
+
+
+def test_mismatched_pickled_dims_are_rejected(fake_backend):
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    from tnalg_gb300.MPSClass import MpsOpenBoundaryClass
+    A = bf.load_pr(REF_FILE, "A", device="cpu")
+    st = {"mps": A.mps, "virtual_dim": np.array([1, 2, 4, 8, 8, 8, 4, 2, 2]), "center": 0, "phys_dim": 2}
+    obj = MpsOpenBoundaryClass.__new__(MpsOpenBoundaryClass)
+    from tnalg_gb300 import MPSClass as M
+    token = M.LOAD_DEVICE.set("cpu")
+    try:
+        with pytest.raises(ValueError):
+            obj.__setstate__(dict(st))
+    finally:
+        M.LOAD_DEVICE.reset(token)

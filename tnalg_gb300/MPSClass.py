@@ -18,12 +18,17 @@ Differences a user can observe:
   * Operators must be real (spin 'sy' enters only through complex-free products
     in the Heisenberg expansion).
 """
+import contextvars
+
 import numpy as np
 import torch
 
 from . import _lib as L
 from . import engine as E
 from .HamiltonianModule import spin_operators
+
+# device for MPS objects restored from a reference result file (set by BasicFunctionsSJR.load_pr)
+LOAD_DEVICE = contextvars.ContextVar("tnalg_load_device", default="cuda")
 
 
 def random_open_mps(l, d, chi):
@@ -396,7 +401,33 @@ class MpsOpenBoundaryClass(MpsBasic):
         st["_model_key"] = None
         return st
 
+    def _from_reference_state(self, st):
+        """Restore an object pickled by the reference's MpsOpenBoundaryClass (its __dict__, set up at
+        MPSClass.py:53-106): tensors, centre, orthogonality flags, spectra and entropies are kept;
+        the host operator caches (effect_s / effect_ss and their position tables) are dropped, the
+        device environments are rebuilt on first use. Tensors go to LOAD_DEVICE."""
+        tensors = [np.asarray(t, dtype=float) for t in st["mps"]]
+        d = int(st.get("phys_dim", tensors[0].shape[1]))
+        chi = max(int(t.shape[2]) for t in tensors)
+        self.__init__(len(tensors), d, chi, spin=st.get("spin", "half"), way=st.get("decomp_way", "qr"),
+                      operators=st.get("operators"), debug=bool(st.get("_debug", False)),
+                      is_parallel=bool(st.get("_is_parallel", False)), is_save_op=bool(st.get("_is_save_op", False)),
+                      eig_way=int(st.get("eig_way", 0)), device=LOAD_DEVICE.get(), tensors=tensors)
+        vd = np.ravel(np.asarray(st.get("virtual_dim", self._dev.virtual_dim))).astype(int)
+        if vd.shape != self._dev.virtual_dim.shape or (vd != self._dev.virtual_dim).any():
+            raise ValueError("pickled virtual_dim %s does not match the tensors %s" % (vd, self._dev.virtual_dim))
+        self._dev.center = int(st.get("center", -1))
+        if "orthogonality" in st:
+            self._dev.orthogonality = np.ravel(np.asarray(st["orthogonality"], dtype=float)).copy()
+        if "lm" in st:
+            self.lm = [np.ravel(np.asarray(x, dtype=float)) for x in st["lm"]]
+        if "ent" in st:
+            self.ent = np.asarray(st["ent"], dtype=float).reshape(-1, 1)
+
     def __setstate__(self, st):
+        if "_mps_host" not in st:
+            self._from_reference_state(st)
+            return
         tensors = st.pop("_mps_host")
         vd = st.pop("_virtual_dim")
         c = st.pop("_center")

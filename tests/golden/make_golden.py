@@ -18,6 +18,8 @@ Cases (all with the reference's own ``dmrg_finite_size`` from DMRG_anyH.py:18,
 * ``ladder_2x4_chi8``      'arbitrary' lattice: 2x4 ladder (straddling terms), hz field
 * ``jigsaw_s1_n9_chi12``   spin-1 jigsaw chain (d=3)
 * ``longrange_n8_chi8``    'longRange' lattice (all-to-all couplings)
+* ``j1j2_snake_4x3_chi16`` J1-J2 square lattice (J2 = 0.5) in snake order, 'arbitrary' lattice, hz field
+  (``python tests/golden/make_golden.py j1j2_snake_4x3_chi16`` runs this case alone)
 
 plus the two shipped result pickles (data_dmrg/*.pr), a dense effective
 Hamiltonian at one site (MPSClass.py:532 ``effective_hamiltonian_dmrg``), the
@@ -167,6 +169,46 @@ def longrange_para(l, chi, sweeps):
     return pm.make_consistent_parameter_dmrg(para)
 
 
+def j1j2_para(width, height, chi, hz, sweeps):
+    """J1-J2 (J2 = 0.5) square lattice in snake order through the reference's 'arbitrary' lattice;
+    the bond list is written out here (even rows left to right, odd rows right to left)."""
+    def site(x, y):
+        return y * width + (x if y % 2 == 0 else width - 1 - x)
+
+    bonds = []
+    for y in range(height):
+        for x in range(width):
+            if x + 1 < width:
+                bonds.append((site(x, y), site(x + 1, y), 1.0))
+            if y + 1 < height:
+                bonds.append((site(x, y), site(x, y + 1), 1.0))
+    for y in range(height - 1):
+        for x in range(width - 1):
+            bonds.append((site(x, y), site(x + 1, y + 1), 0.5))
+            bonds.append((site(x + 1, y), site(x, y + 1), 0.5))
+    bonds = sorted((min(i, j), max(i, j), c) for i, j, c in bonds)
+    bonds = [b for b in bonds if b[2] == 1.0] + [b for b in bonds if b[2] == 0.5]
+    para = pm.generate_parameters_dmrg("arbitrary")
+    para["hx"] = 0.0
+    para["hz"] = hz
+    para["op"].append(-para["hx"] * para["op"][1] - para["hz"] * para["op"][3])
+    index2, coeff2 = [], []
+    for i, j, c in bonds:
+        index2 += [[i, j, 4, 5], [i, j, 5, 4], [i, j, 3, 3]]
+        coeff2 += [c / 2, c / 2, c]
+    para["index2"] = index2
+    para["coeff2"] = coeff2
+    para["index1"] = [[n, 6] for n in range(width * height)]
+    para["coeff1"] = [1.0] * (width * height)
+    para.update(chi=chi, sweep_time=sweeps, **COMMON)
+    return pm.make_consistent_parameter_dmrg(para)
+
+
+EXTRA = {
+    "j1j2_snake_4x3_chi16": lambda meta: run_case("j1j2_snake_4x3_chi16", j1j2_para(4, 3, 16, 0.1, 10), 5, meta),
+}
+
+
 def dense_heff(A, para, p, name):
     """Dense effective Hamiltonian (MPSClass.py:532-580) of the MPS A at site p."""
     A._is_save_op = False
@@ -279,7 +321,15 @@ def reference_ed(meta):
     }
 
 
-def main():
+def main(argv=()):
+    if argv:   # only the named extra cases, merged into the existing metadata
+        with open(os.path.join(HERE, "golden_meta.json")) as f:
+            meta = json.load(f)
+        for name in argv:
+            EXTRA[name](meta)
+        with open(os.path.join(HERE, "golden_meta.json"), "w") as f:
+            json.dump(meta, f, indent=1, sort_keys=True)
+        return
     meta = {}
     run_case("chain_n12_chi16", chain_para(12, 16, 1, 1, 0, 0, 10), 0, meta)
     ob, A, para = run_case("chain_n12_chi16_h", chain_para(12, 16, 1, 1, 0.2, 0.3, 10), 0, meta)
@@ -288,6 +338,8 @@ def main():
     dense_heff(A, para, 3, "heff_ladder_2x4_chi8_p3")
     run_case("jigsaw_s1_n9_chi12", jigsaw_para(9, 12, 16), 2, meta)
     run_case("longrange_n8_chi8", longrange_para(8, 8, 8), 3, meta)
+    for fn in EXTRA.values():
+        fn(meta)
     pickled_fixtures(meta)
     docstring_kats(meta)
     reference_ed(meta)
@@ -297,4 +349,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -61,6 +61,25 @@ def test_square_and_husimi_generators():
     assert full.shape == (10, 2)
 
 
+def test_j1j2_snake_generator():
+    """Config-3 lattice: 6 x 6 gives 60 J1 + 50 J2 bonds (330 rows), spans up to 11 sites; the 4 x 3
+    tables equal the ones the reference run of the golden case consumed."""
+    from tnalg_gb300 import HamiltonianModule as hm, Parameters as pm
+    p1, p2 = hm.positions_j1j2_square_snake(6, 6)
+    assert p1.shape == (60, 2) and p2.shape == (50, 2)
+    assert int(max((p1[:, 1] - p1[:, 0]).max(), (p2[:, 1] - p2[:, 0]).max())) == 11
+    # consecutive chain sites are lattice neighbours
+    assert all([n, n + 1] in p1.tolist() for n in range(35))
+    para = pm.generate_parameters_j1j2_snake(6, 6)
+    assert para["l"] == 36 and para["index2"].shape == (330, 4)
+    g = gc.load("j1j2_snake_4x3_chi16")
+    para = pm.generate_parameters_j1j2_snake(4, 3, hz=0.1)
+    np.testing.assert_array_equal(np.asarray(para["index2"]), g["index2"])
+    np.testing.assert_allclose(np.ravel(para["coeff2"]), g["coeff2"])
+    np.testing.assert_array_equal(np.asarray(para["index1"]), g["index1"])
+    np.testing.assert_allclose(np.stack([np.real(o) for o in para["op"]]), g["op"])
+
+
 # -- coupling-list compiler ---------------------------------------------------------------
 
 
@@ -93,7 +112,7 @@ def test_open_operator_sets_chain_and_long_range():
 # -- orchestration through the test double ---------------------------------------------------
 
 
-@pytest.mark.parametrize("name", ["chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8"])
+@pytest.mark.parametrize("name", ["chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8", "j1j2_snake_4x3_chi16"])
 def test_sweep_orchestration_matches_reference(name, fake_backend):
     from tnalg_gb300 import DMRG_anyH
     g, m = gc.load(name), gc.meta()[name]

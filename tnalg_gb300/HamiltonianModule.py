@@ -104,6 +104,38 @@ def positions_husimi(depth):
     return np.array(pos)
 
 
+def snake_site(x, y, width):
+    """Chain index of square-lattice site (x, y) in snake order: even rows left to right, odd rows
+    right to left, so that consecutive chain sites are lattice neighbours."""
+    return y * width + (x if y % 2 == 0 else width - 1 - x)
+
+
+def positions_j1j2_square_snake(width, height):
+    """Bonds of the J1-J2 model on an open width x height square lattice in snake order.
+
+    Returns (pos_j1, pos_j2): nearest-neighbour bonds (2 w h - w - h of them) and diagonal
+    next-nearest-neighbour bonds (2 (w - 1)(h - 1)), each row [i, j] with i < j, rows sorted.
+    Not in the reference, which builds such lattices through its 'arbitrary' index lists
+    (Parameters.py:205-212); a 6 x 6 lattice gives 60 J1 and 50 J2 bonds, bonds up to 11 sites
+    apart along the chain.
+    """
+    def bond(a, b):
+        i, j = snake_site(*a, width), snake_site(*b, width)
+        return [min(i, j), max(i, j)]
+
+    j1, j2 = [], []
+    for y in range(height):
+        for x in range(width):
+            if x + 1 < width:
+                j1.append(bond((x, y), (x + 1, y)))
+            if y + 1 < height:
+                j1.append(bond((x, y), (x, y + 1)))
+            if x + 1 < width and y + 1 < height:
+                j2.append(bond((x, y), (x + 1, y + 1)))
+                j2.append(bond((x + 1, y), (x, y + 1)))
+    return np.array(sorted(j1), dtype=int).reshape(-1, 2), np.array(sorted(j2), dtype=int).reshape(-1, 2)
+
+
 def interactions_position2full_index_heisenberg_two_body(index_pos):
     """Each bond -> rows [i, j, su, sd], [i, j, sd, su], [i, j, sz, sz] (HamiltonianModule.py:242-261)."""
     index_pos = np.asarray(index_pos)

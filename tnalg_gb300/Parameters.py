@@ -185,6 +185,30 @@ def make_consistent_parameter_dmrg(para):
     return para
 
 
+def generate_parameters_j1j2_snake(width=6, height=6, j1=1.0, j2=0.5, hx=0.0, hz=0.0, jz_ratio=1.0):
+    """J1-J2 Heisenberg model on an open width x height square lattice, snake-ordered into a chain,
+    as an 'arbitrary'-lattice para (the reference's route for such models, Parameters.py:205-212).
+
+    Rows: for every bond, [i, j, su, sd], [i, j, sd, su], [i, j, sz, sz] with coefficients
+    (J/2, J/2, jz_ratio J), J = j1 on nearest and j2 on diagonal bonds (J1 bonds first); one-body
+    rows [n, 6] with op 6 = -hx sx - hz sz. Not in the reference.
+    """
+    para = generate_parameters_dmrg("arbitrary")
+    para["hx"], para["hz"] = float(hx), float(hz)
+    para["op"] = _spin_op_list(para["spin"])
+    para["op"].append(-para["hx"] * para["op"][1] - para["hz"] * para["op"][3])
+    pos1, pos2 = hm.positions_j1j2_square_snake(width, height)
+    index2, coeff2 = [], []
+    for pos, j in ((pos1, j1), (pos2, j2)):
+        for i, k in pos:
+            index2 += [[i, k, 4, 5], [i, k, 5, 4], [i, k, 3, 3]]
+            coeff2 += [j / 2, j / 2, jz_ratio * j]
+    n = width * height
+    para.update(index1=[[q, 6] for q in range(n)], coeff1=[1.0] * n, index2=index2, coeff2=coeff2,
+                square_width=width, square_height=height, j1=j1, j2=j2)
+    return make_consistent_parameter_dmrg(para)
+
+
 def from_index2_to_positions_h2(index2):
     """Unique sorted bond positions of index2 (Parameters.py:410-418)."""
     from .DMRG_anyH import sort_positions

@@ -125,40 +125,3 @@ def test_canonical_form_invariants(cuda_lib):
             err = abs(torch.linalg.vector_norm(t) - 1.0)
         assert float(err) < 1e-12, (k, float(err))
 
-
-def test_compressed_couplings_on_device(cuda_lib):
-    """Fully connected chain (N=10, chi=32): rank-compressed couplings give the plain model's and
-    exact diagonalisation's energy, in FP64 and on the split-TF32 path."""
-    from oracle import ed
-    from tnalg_gb300 import DMRG_anyH, Parameters as pm
-    para = pm.generate_parameters_dmrg("full")
-    para.update(l=10, chi=32, jxy=1.0, jz=0.6, hx=0.3, hz=0.2, sweep_time=6, dt_ob=6, break_tol=-1.0,
-                eigs_tol=1e-12)
-    para = pm.make_consistent_parameter_dmrg(para)
-    e0 = ed.ground_state(para["l"], para["d"], para["op"], para["index1"], para["coeff1"], para["index2"],
-                         para["coeff2"])[0]
-    res = {}
-    for mode, prec in ((False, "fp64"), (True, "fp64"), (True, "tf32x3")):
-        np.random.seed(1)
-        p = dict(para)
-        p.update(mpo_compress=mode, precision=prec, device="cuda")
-        res[(mode, prec)] = _quiet(DMRG_anyH.dmrg_finite_size, p)[0]
-    e = res[(True, "fp64")]["e_per_site"]
-    assert abs(e * para["l"] - e0) <= 1e-9 * abs(e0)
-    assert abs(e - res[(False, "fp64")]["e_per_site"]) <= 1e-12
-    np.testing.assert_allclose(np.ravel(res[(True, "fp64")]["mz"]), np.ravel(res[(False, "fp64")]["mz"]),
-                               atol=1e-8)
-    assert abs(res[(True, "tf32x3")]["e_per_site"] - e) <= 1e-8
-
-
-def test_reference_result_file_on_device(cuda_lib):
-    """A result file written by the reference's save_pr loads onto the GPU; the observables of the
-    restored MPS equal the ones pickled beside it."""
-    import os
-    pytest.importorskip("numpy._core")   # the file's arrays were pickled by numpy 2
-    from tnalg_gb300 import BasicFunctionsSJR as bf
-    ob, A, info, para = bf.load_pr(os.path.join(gc.GOLDEN, "ref_result_chain_n8_h.pr"), ("ob", "A", "info", "para"))
-    assert A.mps_device[0].is_cuda and A.center == 0
-    eb = A.observe_bond_energy(para["index2"], para["coeff2"])
-    np.testing.assert_allclose(np.ravel(eb), np.ravel(ob["eb_full"]), atol=1e-12)
-    np.testing.assert_allclose(np.ravel(A.observe_magnetization(3)), np.ravel(ob["mz"]), atol=1e-12)

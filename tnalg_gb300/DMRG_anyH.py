@@ -31,7 +31,7 @@ def dmrg_finite_size(para=None):
                       ("lanczos_mixed_floor", "mixed_floor"), ("lanczos_refine", "refine")):
         if key in para:
             A.lanczos[name] = para[key]
-    A.coupling_compress = para.get("mpo_compress", "auto")
+    A.coupling_compress = para.get("mpo_compress", False)
     A.coupling_tol = float(para.get("mpo_tol", 1e-14))
     A.correct_orthogonal_center(para["ob_position"])
     print("Starting to sweep ...")

@@ -96,9 +96,10 @@ class MpsOpenBoundaryClass(MpsBasic):
                         "mixed_floor": 2e-6, "refine": "last"}
         self._refine_next = False
         self.last_solve = None
-        # two-body couplings: "auto" carries them rank-compressed (engine.CompressedModel) when
-        # that saves at least a quarter of the carried operators; True / False force it
-        self.coupling_compress = "auto"
+        # two-body couplings: False carries one operator per open (site, op) as the reference does;
+        # True carries rank-compressed combinations (engine.CompressedModel); "auto" picks the
+        # compressed model when it saves at least a quarter of the carried operators
+        self.coupling_compress = False
         self.coupling_tol = 1e-14
         self._model_key = None
         self._dev = E.DeviceMPS(tensors, d, device, precision=precision)

@@ -63,3 +63,62 @@ def test_arrivals_and_job_parameters_are_independent_of_the_rate():
         assert x.para["l"] == y.para["l"] and x.para["chi"] == y.para["chi"] and x.seed == y.seed
         assert x.arrival == 0.0
     assert all(y.arrival > 0 for y in b) and all(b[i].arrival < b[i + 1].arrival for i in range(5))
+
+
+def _held_bytes(A):
+    dev = A._dev
+    ts = [t for t in dev.EL + dev.ER if t is not None] + list(dev.mps)
+    return 8 * sum(int(t.numel()) for t in ts)
+
+
+@pytest.mark.parametrize("kind", ["chain", "ladder"])
+def test_footprint_bounds_the_tensors_a_job_holds(kind):
+    """The admission estimate covers the MPS and every environment stack the engine holds after
+    its sweeps (both sides of every bond), for chains and for ladders with straddling terms."""
+    import contextlib
+    import io
+    from tnalg_gb300 import DMRG_anyH
+    if kind == "chain":
+        para = serving.chain_job_para(14, 8, jz=0.7, hz=0.2, sweeps=2, device="cpu")
+    else:
+        para = serving.ladder_job_para(6, 8, j_rung=1.3, jz=0.7, hz=0.2, sweeps=2, device="cpu")
+    np.random.seed(0)
+    with contextlib.redirect_stdout(io.StringIO()):
+        ob, A, info, _ = DMRG_anyH.dmrg_finite_size(para)
+    held = _held_bytes(A)
+    est = serving.estimate_device_bytes(para)
+    assert est >= held
+    assert est < 40 * held   # an estimate, not a blanket reservation
+    assert np.isfinite(ob["e_per_site"])
+
+
+def test_ladder_jobs_alone_and_mixed_with_chains():
+    ladder = serving.ladder_job_para(5, 6, j_rung=1.5, jz=0.8, hz=0.3, sweeps=3, device="cpu")
+    assert ladder["l"] == 10 and np.asarray(ladder["index2"]).shape == (3 * (5 + 2 * 4), 4)
+    alone = serving.DMRGJob(7, ladder, seed=9)
+    s = serving.Scheduler("cpu", max_active=1)
+    s.submit(alone)
+    s.run()
+    mix = serving.Scheduler("cpu")
+    jobs = _jobs() + [serving.DMRGJob(7, ladder, seed=9)]
+    for j in jobs:
+        mix.submit(j)
+    mix.run()
+    got = [j for j in mix.done if j.job_id == 7][0]
+    assert got.result["e_per_site"] == pytest.approx(alone.result["e_per_site"], abs=1e-12)
+    np.testing.assert_allclose(got.result["mz"], alone.result["mz"], atol=1e-12)
+    # a ladder carries more environment slots than a chain of the same length and bond dimension
+    chain = serving.chain_job_para(10, 6, sweeps=3, device="cpu")
+    assert serving.estimate_device_bytes(ladder) > serving.estimate_device_bytes(chain)
+
+
+def test_ladder_mix_in_the_request_stream():
+    plain = serving.make_jobs(12, seed=4, device="cpu")
+    again = serving.make_jobs(12, seed=4, device="cpu", ladder_fraction=0.0)
+    assert [j.para["l"] for j in plain] == [j.para["l"] for j in again]
+    mixed = serving.make_jobs(12, seed=4, device="cpu", ladder_fraction=0.5)
+    lattices = [j.para["lattice"] for j in mixed]
+    assert "arbitrary" in lattices and "chain" in lattices
+    for j in mixed:
+        if j.para["lattice"] == "arbitrary":
+            assert j.para["l"] % 2 == 0 and 16 <= j.para["l"] <= 96

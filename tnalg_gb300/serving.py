@@ -18,7 +18,7 @@ the same alone and in a mix (up to the rounding order of floating-point atomics 
 GEMMs; the FP64 path is deterministic). The host runs one thread: the C library's lazily
 initialised state is shared by all jobs and is not meant for concurrent host threads.
 
-    python -m tnalg_gb300.serving --jobs 16 --sweeps 4 [--rate 200] [--precision fp64|tf32x3]
+    python -m tnalg_gb300.serving --jobs 16 --sweeps 4 [--rate 200] [--precision fp64|tf32x3] [--ladders 0.5]
 """
 import argparse
 import contextlib
@@ -39,6 +39,63 @@ def chain_job_para(length, chi, jz=1.0, hz=0.0, sweeps=4, precision="fp64", devi
     return pm.make_consistent_parameter_dmrg(para)
 
 
+def ladder_job_para(length, chi, j_rung=1.0, jz=1.0, hz=0.0, sweeps=4, precision="fp64", device="cuda",
+                    eigs_tol=1e-10, break_tol=1e-9):
+    """A 2 x length spin-1/2 ladder as an 'arbitrary'-lattice job (Parameters.py:205-212): sites
+    (2r, 2r+1) form rung r; XXZ legs (Jxy = 1, Jz = jz) between rungs r and r+1, Heisenberg rungs
+    of strength j_rung; uniform field hz. Bonds reach two sites along the chain, so every bond
+    carries straddling terms."""
+    para = pm.generate_parameters_dmrg("arbitrary")
+    para["hx"], para["hz"] = 0.0, float(hz)
+    para["op"] = list(para["op"][:6])
+    para["op"].append(-para["hx"] * para["op"][1] - para["hz"] * para["op"][3])
+    index2, coeff2 = [], []
+    for r in range(int(length)):
+        bonds = [(2 * r, 2 * r + 1, float(j_rung), float(j_rung))]
+        if r + 1 < length:
+            bonds += [(2 * r, 2 * r + 2, 1.0, float(jz)), (2 * r + 1, 2 * r + 3, 1.0, float(jz))]
+        for i, j, jxy, jzz in bonds:
+            index2 += [[i, j, 4, 5], [i, j, 5, 4], [i, j, 3, 3]]
+            coeff2 += [jxy / 2, jxy / 2, jzz]
+    n = 2 * int(length)
+    para.update(index1=[[q, 6] for q in range(n)], coeff1=[1.0] * n, index2=index2, coeff2=coeff2, chi=int(chi),
+                sweep_time=int(sweeps), dt_ob=1, eigs_tol=eigs_tol, break_tol=break_tol, tau=1e-4,
+                precision=precision, device=device)
+    return pm.make_consistent_parameter_dmrg(para)
+
+
+def estimate_device_bytes(para, krylov=40):
+    """Upper estimate of the device memory a job holds: the MPS, both environment stacks of every
+    bond (slot 0 plus one chi_b x chi_b slot per open operator; after a sweep the engine holds EL[b]
+    and ER[b] for all b), the block operators and straddling slots of one site, and the solver's
+    Krylov basis (krylov + 1 site vectors) plus ~20 site tensors of gauge-move and GEMM staging."""
+    from .engine import canonical_terms
+    l, d, chi = int(para["l"]), int(para["d"]), int(para["chi"])
+    dims = [min(chi, d ** min(b, l - b, 60)) for b in range(l + 1)]
+    _, two = canonical_terms(para["index1"], para["coeff1"], para["index2"], para["coeff2"], para["op"],
+                             para.get("eigs_tol", 1e-12))
+    jmax, imin = {}, {}
+    for i, j, a, b, c in two:
+        jmax[(i, a)] = max(jmax.get((i, a), -1), j)
+        imin[(j, b)] = min(imin.get((j, b), l), i)
+    nl = np.zeros(l + 2)
+    for (i, a), j in jmax.items():      # open on the left at bonds i+1..j
+        nl[i + 1] += 1
+        nl[j + 1] -= 1
+    nr = np.zeros(l + 2)
+    for (j, b), i in imin.items():      # open on the right at bonds i+1..j
+        nr[i + 1] += 1
+        nr[j + 1] -= 1
+    nl, nr = np.cumsum(nl)[: l + 1], np.cumsum(nr)[: l + 1]
+    mps = sum(dims[q] * d * dims[q + 1] for q in range(l))
+    env = sum((2 + nl[b] + nr[b]) * dims[b] ** 2 for b in range(l + 1))
+    cmax = max(dims)
+    site = d * cmax * cmax
+    strad = int(max(min(nl[b], nr[b + 1]) for b in range(l))) if l > 1 else 0
+    scratch = 2 * (d * cmax) ** 2 + 2 * strad * cmax * cmax + (krylov + 1 + 20) * site
+    return int(8 * (mps + env + scratch))
+
+
 class DMRGJob:
     """One DMRG run advanced one local update at a time (`advance`)."""
 
@@ -56,13 +113,11 @@ class DMRGJob:
         self.A = None
 
     def footprint_bytes(self):
-        """Upper estimate of the device memory the job holds while admitted: the MPS (L d chi^2),
-        environments with the carried operators of a nearest-neighbour chain (~6 chi x chi per bond)
-        and the solver's Krylov basis and gauge-move workspaces (~60 site tensors of d chi^2)."""
-        chi, d, l = self.para["chi"], self.para["d"], self.para["l"]
-        chi = min(chi, 2 ** (l // 2))
-        n = d * chi * chi
-        return int(8 * (l * n + 6 * l * chi * chi + 60 * n))
+        """Upper estimate of the device memory the job holds while admitted (estimate_device_bytes),
+        computed once from its coupling lists."""
+        if getattr(self, "_footprint", None) is None:
+            self._footprint = estimate_device_bytes(self.para)
+        return self._footprint
 
     def start(self, device):
         import torch
@@ -196,18 +251,28 @@ class Scheduler:
 
 
 def make_jobs(njobs, seed=0, sweeps=4, precision="fp64", device="cuda", rate=None, lengths=(16, 48),
-              chis=(16, 32, 64)):
+              chis=(16, 32, 64), ladder_fraction=0.0, ladder_lengths=(8, 48), rung=(0.5, 2.0)):
     """Uneven XXZ chains: N ~ U{lengths}, Jz ~ U[0,2], hz ~ U[0,1], chi from `chis`, per-job seed =
-    seed + job id; Poisson arrivals at `rate` per second (all at time 0 when rate is None)."""
+    seed + job id; Poisson arrivals at `rate` per second (all at time 0 when rate is None).
+    With ladder_fraction > 0 that share of the jobs are 2 x L ladders instead (L ~ U{ladder_lengths},
+    rung coupling ~ U[rung]), as in the mixed chain/ladder request stream of the serving workload;
+    ladder_fraction = 0 draws exactly the chains it always did."""
     rng = np.random.default_rng(seed)
     arrivals = np.random.default_rng(seed + 1)  # its own stream: the jobs do not depend on the rate
+    kinds = np.random.default_rng(seed + 2)     # chain or ladder, drawn only when ladders are asked for
     jobs, t = [], 0.0
     for k in range(njobs):
         if rate:
             t += arrivals.exponential(1.0 / rate)
-        para = chain_job_para(int(rng.integers(lengths[0], lengths[1] + 1)), int(rng.choice(chis)),
-                              jz=float(rng.uniform(0, 2)), hz=float(rng.uniform(0, 1)), sweeps=sweeps,
-                              precision=precision, device=device)
+        if ladder_fraction > 0 and kinds.uniform() < ladder_fraction:
+            para = ladder_job_para(int(kinds.integers(ladder_lengths[0], ladder_lengths[1] + 1)),
+                                   int(kinds.choice(chis)), j_rung=float(kinds.uniform(*rung)),
+                                   jz=float(kinds.uniform(0, 2)), hz=float(kinds.uniform(0, 1)), sweeps=sweeps,
+                                   precision=precision, device=device)
+        else:
+            para = chain_job_para(int(rng.integers(lengths[0], lengths[1] + 1)), int(rng.choice(chis)),
+                                  jz=float(rng.uniform(0, 2)), hz=float(rng.uniform(0, 1)), sweeps=sweeps,
+                                  precision=precision, device=device)
         jobs.append(DMRGJob(k, para, seed + k, arrival=t))
     return jobs
 
@@ -220,6 +285,7 @@ def main(argv=None):
     ap.add_argument("--rate", type=float, default=None)
     ap.add_argument("--precision", default="fp64")
     ap.add_argument("--max-active", type=int, default=64)
+    ap.add_argument("--ladders", type=float, default=0.0, help="share of 2 x L ladder jobs (0..1)")
     a = ap.parse_args(argv)
     import torch
     from . import _lib as L
@@ -233,7 +299,8 @@ def main(argv=None):
     torch.cuda.synchronize()
     # the same jobs one at a time, then interleaved
     seq_wall, seq = 0.0, {}
-    for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev):
+    for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev,
+                       ladder_fraction=a.ladders):
         j.arrival = 0.0
         s = Scheduler(dev, max_active=1)
         s.submit(j)
@@ -243,7 +310,8 @@ def main(argv=None):
         seq_wall += time.perf_counter() - t0
         seq[j.job_id] = j
     mix = Scheduler(dev, max_active=a.max_active)
-    for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev, rate=a.rate):
+    for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev, rate=a.rate,
+                       ladder_fraction=a.ladders):
         mix.submit(j)
     mix.run()
     torch.cuda.synchronize()

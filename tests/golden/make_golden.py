@@ -20,6 +20,9 @@ Cases (all with the reference's own ``dmrg_finite_size`` from DMRG_anyH.py:18,
 * ``longrange_n8_chi8``    'longRange' lattice (all-to-all couplings)
 * ``j1j2_snake_4x3_chi16`` J1-J2 square lattice (J2 = 0.5) in snake order, 'arbitrary' lattice, hz field
   (``python tests/golden/make_golden.py j1j2_snake_4x3_chi16`` runs this case alone)
+* ``square_4x2_chi8``      the reference's 'square' lattice (row-major numbering), 4x2, no field (its
+  make_consistent_parameter_dmrg appends the field operator instead of rebuilding the list, Parameters.py:190,
+  so a field set after generate_parameters_dmrg never reaches index1)
 
 plus the two shipped result pickles (data_dmrg/*.pr), a dense effective
 Hamiltonian at one site (MPSClass.py:532 ``effective_hamiltonian_dmrg``), the
@@ -204,8 +207,16 @@ def j1j2_para(width, height, chi, hz, sweeps):
     return pm.make_consistent_parameter_dmrg(para)
 
 
+def square_para(width, height, chi, hx, hz, sweeps):
+    para = pm.generate_parameters_dmrg("square")
+    para.update(square_width=width, square_height=height, chi=chi, jxy=1, jz=1, hx=hx, hz=hz, sweep_time=sweeps,
+                **COMMON)
+    return pm.make_consistent_parameter_dmrg(para)
+
+
 EXTRA = {
     "j1j2_snake_4x3_chi16": lambda meta: run_case("j1j2_snake_4x3_chi16", j1j2_para(4, 3, 16, 0.1, 10), 5, meta),
+    "square_4x2_chi8": lambda meta: run_case("square_4x2_chi8", square_para(4, 2, 8, 0.0, 0.0, 10), 6, meta),
 }
 
 

@@ -61,6 +61,27 @@ def test_square_and_husimi_generators():
     assert full.shape == (10, 2)
 
 
+def test_square_generator_reproduces_reference_tables():
+    from tnalg_gb300 import Parameters as pm
+    g, m = gc.load("square_4x2_chi8"), gc.meta()["square_4x2_chi8"]
+    para = pm.generate_parameters_dmrg("square")
+    para.update(square_width=4, square_height=2, chi=m["chi"], jxy=1, jz=1, hx=m["hx"], hz=m["hz"])
+    para = pm.make_consistent_parameter_dmrg(para)
+    assert para["l"] == m["l"] == 8
+    np.testing.assert_array_equal(np.asarray(para["index1"]), g["index1"])
+    np.testing.assert_array_equal(np.asarray(para["index2"]), g["index2"])
+    np.testing.assert_allclose(np.ravel(para["coeff2"]), g["coeff2"])
+    np.testing.assert_array_equal(np.asarray(para["positions_h2"]), g["positions_h2"])
+    # the reference appends a second field operator on the repeated call (both zero here); the
+    # list is rebuilt here, so op 6 is the field of the current hx, hz
+    ops = np.stack([np.real(o) for o in para["op"]])
+    assert len(ops) == 7 and len(g["op"]) == 8
+    np.testing.assert_allclose(ops, g["op"][:7])
+    para.update(hx=0.1, hz=0.2)
+    para = pm.make_consistent_parameter_dmrg(para)
+    np.testing.assert_allclose(np.real(para["op"][6]), -0.1 * np.real(para["op"][1]) - 0.2 * np.real(para["op"][3]))
+
+
 def test_j1j2_snake_generator():
     """Config-3 lattice: 6 x 6 gives 60 J1 + 50 J2 bonds (330 rows), spans up to 11 sites; the 4 x 3
     tables equal the ones the reference run of the golden case consumed."""
@@ -112,7 +133,8 @@ def test_open_operator_sets_chain_and_long_range():
 # -- orchestration through the test double ---------------------------------------------------
 
 
-@pytest.mark.parametrize("name", ["chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8", "j1j2_snake_4x3_chi16"])
+@pytest.mark.parametrize("name", ["chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8", "j1j2_snake_4x3_chi16",
+                                  "square_4x2_chi8"])
 def test_sweep_orchestration_matches_reference(name, fake_backend):
     from tnalg_gb300 import DMRG_anyH
     g, m = gc.load(name), gc.meta()[name]

@@ -20,6 +20,7 @@ Cases (all with the reference's own ``dmrg_finite_size`` from DMRG_anyH.py:18,
 * ``longrange_n8_chi8``    'longRange' lattice (all-to-all couplings)
 * ``j1j2_snake_4x3_chi16`` J1-J2 square lattice (J2 = 0.5) in snake order, 'arbitrary' lattice, hz field
   (``python tests/golden/make_golden.py j1j2_snake_4x3_chi16`` runs this case alone)
+* ``full_n8_chi8``         the reference's 'full' lattice (all-to-all Ising couplings, transverse field hx=0.5)
 * ``square_4x2_chi8``      the reference's 'square' lattice (row-major numbering), 4x2, no field (its
   make_consistent_parameter_dmrg appends the field operator instead of rebuilding the list, Parameters.py:190,
   so a field set after generate_parameters_dmrg never reaches index1)
@@ -214,8 +215,15 @@ def square_para(width, height, chi, hx, hz, sweeps):
     return pm.make_consistent_parameter_dmrg(para)
 
 
+def full_para(l, chi, sweeps):
+    para = pm.generate_parameters_dmrg("full")
+    para.update(l=l, chi=chi, sweep_time=sweeps, **COMMON)   # defaults jxy=0, jz=1, hx=0.5, hz=0
+    return pm.make_consistent_parameter_dmrg(para)
+
+
 EXTRA = {
     "j1j2_snake_4x3_chi16": lambda meta: run_case("j1j2_snake_4x3_chi16", j1j2_para(4, 3, 16, 0.1, 10), 5, meta),
+    "full_n8_chi8": lambda meta: run_case("full_n8_chi8", full_para(8, 8, 8), 7, meta),
     "square_4x2_chi8": lambda meta: run_case("square_4x2_chi8", square_para(4, 2, 8, 0.0, 0.0, 10), 6, meta),
 }
 

@@ -101,7 +101,7 @@ def test_auto_keeps_nearest_neighbour_models_plain():
         E.make_model(para["l"], para["d"], para["op"], one, two, "cpu", compress="sometimes")
 
 
-@pytest.mark.parametrize("name", ["longrange_n8_chi8", "ladder_2x4_chi8", "jigsaw_s1_n9_chi12"])
+@pytest.mark.parametrize("name", ["longrange_n8_chi8", "ladder_2x4_chi8", "jigsaw_s1_n9_chi12", "full_n8_chi8"])
 def test_compressed_sweeps_match_reference(name, fake_backend):
     from tnalg_gb300 import DMRG_anyH
     g, m = gc.load(name), gc.meta()[name]

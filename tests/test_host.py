@@ -21,7 +21,8 @@ def _quiet(fn, *a, **k):
 # -- parameters -------------------------------------------------------------------------
 
 
-@pytest.mark.parametrize("name", ["chain_n12_chi16", "chain_n12_chi16_h", "longrange_n8_chi8", "jigsaw_s1_n9_chi12"])
+@pytest.mark.parametrize("name", ["chain_n12_chi16", "chain_n12_chi16_h", "longrange_n8_chi8", "jigsaw_s1_n9_chi12",
+                                  "full_n8_chi8"])
 def test_parameters_reproduce_reference_tables(name):
     from tnalg_gb300 import Parameters as pm
     m, g = gc.meta()[name], gc.load(name)
@@ -134,7 +135,7 @@ def test_open_operator_sets_chain_and_long_range():
 
 
 @pytest.mark.parametrize("name", ["chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8", "j1j2_snake_4x3_chi16",
-                                  "square_4x2_chi8"])
+                                  "square_4x2_chi8", "full_n8_chi8"])
 def test_sweep_orchestration_matches_reference(name, fake_backend):
     from tnalg_gb300 import DMRG_anyH
     g, m = gc.load(name), gc.meta()[name]

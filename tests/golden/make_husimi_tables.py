@@ -1,0 +1,44 @@
+"""Coupling tables of the reference's 'husimi' lattice (library/Parameters.py, package layout).
+
+Run by hand where the T-Nalg sources are mounted (``TNALG_REFERENCE``, default ``/root/reference``)::
+
+    python tests/golden/make_husimi_tables.py
+
+The package layout imports matplotlib.cm and mpl_toolkits.mplot3d for plotting helpers; they are
+stubbed (nothing here plots). Writes ``husimi_tables.npz`` for depths 2 and 3.
+"""
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import ref_shim  # noqa: E402
+
+ref_shim.install()
+for _name in ("matplotlib.cm", "mpl_toolkits", "mpl_toolkits.mplot3d"):
+    sys.modules[_name] = types.ModuleType(_name)
+sys.modules["matplotlib"].cm = sys.modules["matplotlib.cm"]
+sys.modules["matplotlib.cm"].coolwarm = None
+sys.modules["mpl_toolkits.mplot3d"].Axes3D = object
+from library import Parameters as LP  # noqa: E402
+
+
+def main():
+    out = {}
+    for depth in (2, 3):
+        p = LP.generate_parameters_dmrg("husimi")
+        p["depth"] = depth
+        p = LP.make_consistent_parameter_dmrg(p)
+        for k in ("index1", "index2", "coeff1", "coeff2", "positions_h2"):
+            out["d%d_%s" % (depth, k)] = np.asarray(p[k])
+        out["d%d_l" % depth] = np.asarray(p["l"])
+        out["d%d_op" % depth] = np.stack([np.real(np.asarray(o)) for o in p["op"]])
+    np.savez_compressed(os.path.join(HERE, "husimi_tables.npz"), **out)
+    print({k: v.shape for k, v in out.items()})
+
+
+if __name__ == "__main__":
+    main()

@@ -83,6 +83,22 @@ def test_square_generator_reproduces_reference_tables():
     np.testing.assert_allclose(np.real(para["op"][6]), -0.1 * np.real(para["op"][1]) - 0.2 * np.real(para["op"][3]))
 
 
+@pytest.mark.parametrize("depth", [2, 3])
+def test_husimi_generator_reproduces_reference_tables(depth):
+    """library/Parameters.py's 'husimi' lattice (tables written by tests/golden/make_husimi_tables.py)."""
+    from tnalg_gb300 import Parameters as pm
+    g = np.load(os.path.join(gc.GOLDEN, "husimi_tables.npz"))
+    para = pm.generate_parameters_dmrg("husimi")
+    para["depth"] = depth
+    para = pm.make_consistent_parameter_dmrg(para)
+    assert para["l"] == int(g["d%d_l" % depth])
+    for k in ("index1", "index2", "positions_h2"):
+        np.testing.assert_array_equal(np.asarray(para[k]), g["d%d_%s" % (depth, k)])
+    for k in ("coeff1", "coeff2"):
+        np.testing.assert_allclose(np.ravel(para[k]), np.ravel(g["d%d_%s" % (depth, k)]))
+    np.testing.assert_allclose(np.stack([np.real(o) for o in para["op"]]), g["d%d_op" % depth])
+
+
 def test_j1j2_snake_generator():
     """Config-3 lattice: 6 x 6 gives 60 J1 + 50 J2 bonds (330 rows), spans up to 11 sites; the 4 x 3
     tables equal the ones the reference run of the golden case consumed."""

@@ -9,7 +9,9 @@ It runs the unmodified reference ``dmrg_finite_size`` (DMRG_anyH.py:18) on an N=
 spin-1/2 chain with fields (chi=8, 6 sweeps, seed 4) through ``ref_shim`` and saves
 ``(ob, A, info, para)`` exactly as the reference's scripts do, into
 ``ref_result_chain_n8_h.pr``. The pickle holds the reference's ``MpsOpenBoundaryClass``
-instance (module ``MPSClass``), which is what a user's existing result files contain.
+instance (module ``MPSClass``), which is what a user's existing result files contain. It also
+writes ``ref_rdm_chain_n8_h.npz``: two-site reduced density matrices of that state from the
+reference's ``reduced_density_matrix_two_body`` with the centre at sites 0, 4 and 7.
 """
 import os
 import sys
@@ -33,6 +35,15 @@ def main():
     para = Pm.make_consistent_parameter_dmrg(para)
     np.random.seed(4)
     ob, A, info, para = DMRG_anyH.dmrg_finite_size(para)
+    # two-site reduced density matrices by the reference's own method (MPSClass.py:841-855), for
+    # pairs left of, around and right of the centre
+    rdm = {}
+    for p1, p2 in ((0, 1), (1, 5), (2, 3), (3, 7), (6, 7)):
+        for c in (0, 4, 7):
+            A.correct_orthogonal_center(c)
+            rdm["rdm_%d_%d_c%d" % (p1, p2, c)] = A.reduced_density_matrix_two_body(p1, p2)
+    A.correct_orthogonal_center(0)
+    np.savez_compressed(os.path.join(HERE, "ref_rdm_chain_n8_h.npz"), **rdm)
     A.clean_to_save()
     para.pop("data_path", None)   # a Windows-style path built from the working directory
     bf.save_pr(HERE, "ref_result_chain_n8_h.pr", [ob, A, info, para], ["ob", "A", "info", "para"])

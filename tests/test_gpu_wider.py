@@ -73,3 +73,15 @@ def test_reference_result_file_on_device(cuda_lib):
     eb = A.observe_bond_energy(para["index2"], para["coeff2"])
     np.testing.assert_allclose(np.ravel(eb), np.ravel(ob["eb_full"]), atol=1e-12)
     np.testing.assert_allclose(np.ravel(A.observe_magnetization(3)), np.ravel(ob["mz"]), atol=1e-12)
+
+
+def test_two_site_density_matrices_on_device(cuda_lib):
+    """reduced_density_matrix_two_body on the GPU equals the reference's own values on the same state."""
+    pytest.importorskip("numpy._core")   # the result file's arrays were pickled by numpy 2
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    g = np.load(os.path.join(gc.GOLDEN, "ref_rdm_chain_n8_h.npz"))
+    A = bf.load_pr(os.path.join(gc.GOLDEN, "ref_result_chain_n8_h.pr"), "A")
+    for key in g.files:
+        _, p1, p2, c = key.split("_")
+        A.correct_orthogonal_center(int(c[1:]))
+        np.testing.assert_allclose(A.reduced_density_matrix_two_body(int(p1), int(p2)), g[key], atol=1e-12)

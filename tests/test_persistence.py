@@ -99,3 +99,21 @@ def test_mismatched_pickled_dims_are_rejected(fake_backend):
             obj.__setstate__(dict(st))
     finally:
         M.LOAD_DEVICE.reset(token)
+
+
+def test_two_site_density_matrices_match_the_reference(fake_backend):
+    """reduced_density_matrix_two_body (MPSClass.py:841-855) on the restored state equals the
+    reference's own values (tests/golden/ref_rdm_chain_n8_h.npz) for pairs left of, around and
+    right of the centre; reversed arguments give the matrix in the order passed."""
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    g = np.load(os.path.join(gc.GOLDEN, "ref_rdm_chain_n8_h.npz"))
+    A = bf.load_pr(REF_FILE, "A", device="cpu")
+    for key in g.files:
+        _, p1, p2, c = key.split("_")
+        A.correct_orthogonal_center(int(c[1:]))
+        np.testing.assert_allclose(A.reduced_density_matrix_two_body(int(p1), int(p2)), g[key], atol=1e-12)
+    rev = A.reduced_density_matrix_two_body(5, 1)
+    want = g["rdm_1_5_c0"].reshape(2, 2, 2, 2).transpose(1, 0, 3, 2).reshape(4, 4)
+    np.testing.assert_allclose(rev, want, atol=1e-12)
+    with pytest.raises(ValueError):
+        A.reduced_density_matrix_two_body(3, 3)

@@ -371,6 +371,23 @@ class MpsOpenBoundaryClass(MpsBasic):
         for i in range(self.length - 1):
             self.ent[i] = -1 if self.lm[i].size == 0 else entanglement_entropy(self.lm[i])
 
+    def reduced_density_matrix_two_body(self, p1, p2):
+        """MPSClass.py:841-855: the (d^2, d^2) reduced density matrix of sites p1, p2 with trace 1,
+        rho[(s1 s2), (s1' s2')] = sum_rest psi*(.. s1 .. s2 ..) psi(.. s1' .. s2' ..), computed on the
+        device at the current centre. The reference takes p1 < p2; p1 > p2 gives the matrix with
+        the sites in the order passed."""
+        if p1 == p2:
+            raise ValueError("reduced_density_matrix_two_body needs two different sites")
+        if self.center < 0:
+            raise RuntimeError("reduced_density_matrix_two_body needs a central-orthogonal MPS")
+        self._ensure_obs_model()
+        q1, q2 = min(p1, p2), max(p1, p2)
+        rho = E._Observer(self._dev).two_site_density(q1, q2)
+        if p1 > p2:
+            d = self.phys_dim
+            rho = rho.reshape(d, d, d, d).transpose(1, 0, 3, 2).reshape(d * d, d * d)
+        return rho / np.trace(rho)
+
     def norm_mps(self):
         """MPSClass.py:954-966 (norm of the centre tensor)."""
         if self.center < -0.5:

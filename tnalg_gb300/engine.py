@@ -943,6 +943,45 @@ class _Observer:
         cl, d, cr = M.shape
         L.check(self.lib.tn_pair_contract(cl, d, cr, L.ptr(M), L.ptr(X), 1.0, L.ptr(out), self.st), "pair")
 
+    def two_site_density(self, p1, p2):
+        """rho[(x1 x2), (y1 y2)] = <E_x1y1(p1) E_x2y2(p2)> for p1 < p2, E_xy = |x><y| (unnormalised):
+        the d^2 elementary operators are applied at one end in one tn_apply_site_ops call, each is
+        carried to the other end and closed with the local density there. Toward the centre side
+        that is not canonical, as the one- and two-body queries do."""
+        s, d = self.s, self.s.d
+        nk = d * d
+        elem = np.zeros((nk, d, d))
+        for x in range(d):
+            for y in range(d):
+                elem[x * d + y, x, y] = 1.0
+        elem = torch.tensor(elem, dtype=torch.float64, device=self.dev)
+        oi = torch.arange(nk, dtype=torch.int32, device=self.dev)
+        G = torch.zeros((nk, d, d), dtype=torch.float64, device=self.dev)
+        fwd = p2 >= self.c
+        q = p1 if fwd else p2
+        M = s.mps[q]
+        cl, _, cr = M.shape
+        X = self.left_x(M, self.E_at(q)) if fwd else self.right_x(M, self.F_at(q + 1))
+        Xk = torch.empty((nk, cl, d, cr), dtype=torch.float64, device=self.dev)
+        L.check(self.lib.tn_apply_site_ops(cl, d, cr, L.ptr(X), L.ptr(elem), L.ptr(oi), nk, L.ptr(Xk), cl * d * cr,
+                                           self.st), "site op")
+        for k in range(nk):
+            if fwd:
+                V = self.left_close(M, Xk[k])
+                for r in range(p1 + 1, p2):
+                    V = self.tl(s.mps[r], V)
+                M2 = s.mps[p2]
+                self.density(M2, self.left_x(M2, V), G[k])
+            else:
+                V = self.right_close(M, Xk[k])
+                for r in range(p2 - 1, p1, -1):
+                    V = self.tr(s.mps[r], V)
+                M1 = s.mps[p1]
+                self.density(M1, self.right_x(M1, V), G[k])
+        g = G.cpu().numpy().reshape(d, d, d, d)   # [k = (x, y) at the start site][x', y' at the end site]
+        rho = g.transpose(0, 2, 1, 3) if fwd else g.transpose(2, 0, 3, 1)
+        return rho.reshape(nk, nk)
+
     # queries ------------------------------------------------------------------------
     def run(self, one, two):
         """one: [(q, op)], two: [(i, j, a, b)] with i != j. Returns (vals_one, vals_two)."""

@@ -215,3 +215,27 @@ def test_library_exports_header_symbols():
     assert not missing, missing
     assert declared <= set(_lib.exported_symbols()) | {"tn_version"}
     assert lib.tn_version() >= 100
+
+
+def test_full_coefficients_match_exact_ground_state(fake_backend):
+    """full_coefficients_mps (MPSClass.py:968-985, whose dropped reshape at :983 makes the reference
+    fail beyond two sites) gives the DMRG state's amplitudes: unit norm, overlap 1 with the exact
+    ground state of the same N=10 chain."""
+    from oracle import ed
+    from tnalg_gb300 import DMRG_anyH, Parameters as pm
+    para = pm.generate_parameters_dmrg("chain")
+    para.update(l=10, chi=32, jxy=1.0, jz=1.0, hx=0.2, hz=0.1, sweep_time=4, dt_ob=4, break_tol=-1.0,
+                eigs_tol=1e-12, device="cpu")
+    para = pm.make_consistent_parameter_dmrg(para)
+    np.random.seed(3)
+    ob, A, info, _ = _quiet(DMRG_anyH.dmrg_finite_size, para)
+    psi = A.full_coefficients_mps()
+    assert psi.shape == (2 ** 10, 1)
+    assert abs(np.linalg.norm(psi) - 1.0) < 1e-12
+    h = ed.hamiltonian(para["l"], para["d"], para["op"], para["index1"], para["coeff1"], para["index2"],
+                       para["coeff2"])
+    v = np.ravel(psi)
+    e0 = ed.ground_state(para["l"], para["d"], para["op"], para["index1"], para["coeff1"], para["index2"],
+                         para["coeff2"])[0]
+    assert abs(v @ (h @ v) - e0) < 1e-9 * abs(e0)
+    assert A.full_coefficients_mps(tol_memory=1) is None

@@ -388,6 +388,26 @@ class MpsOpenBoundaryClass(MpsBasic):
             rho = rho.reshape(d, d, d, d).transpose(1, 0, 3, 2).reshape(d * d, d * d)
         return rho / np.trace(rho)
 
+    def full_coefficients_mps(self, tol_memory=20):
+        """MPSClass.py:968-985: all d^L amplitudes psi[s_0 ... s_(L-1)] (s_0 slowest) as a (d^L, 1)
+        array, contracted site by site with tn_gemm. The reference drops the result of its reshape
+        (MPSClass.py:983) and fails for three or more sites; it also refuses, as here, when
+        L log2(d) - 5 exceeds tol_memory (returns None)."""
+        tot_size_log2 = self.length * np.log2(self.phys_dim) - 5
+        if tot_size_log2 > tol_memory:
+            print("The memory cost of the total coefficients is too large (a lot more than %d Mb). Stop "
+                  "calculation; pass a larger tol_memory to compute it anyway" % tot_size_log2)
+            return None
+        mps = self._dev.mps
+        x = mps[0].reshape(-1, mps[0].shape[2])
+        for n in range(1, self.length):
+            cl, d, cr = (int(v) for v in mps[n].shape)
+            y = torch.empty((x.shape[0], d * cr), dtype=torch.float64, device=self._dev.device)
+            L.gemm(x, mps[n].contiguous(), y, int(x.shape[0]), d * cr, cl, (cl, 1), (d * cr, 1), (d * cr, 1),
+                   ws=self._dev.ws)
+            x = y.reshape(-1, cr)
+        return x.reshape(-1, 1).cpu().numpy()
+
     def norm_mps(self):
         """MPSClass.py:954-966 (norm of the centre tensor)."""
         if self.center < -0.5:

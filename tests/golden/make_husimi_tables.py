@@ -4,12 +4,10 @@ Run by hand where the T-Nalg sources are mounted (``TNALG_REFERENCE``, default `
 
     python tests/golden/make_husimi_tables.py
 
-The package layout imports matplotlib.cm and mpl_toolkits.mplot3d for plotting helpers; they are
-stubbed (nothing here plots). Writes ``husimi_tables.npz`` for depths 2 and 3.
+The package layout's plotting imports are stubbed by ``ref_shim.install_package_layout``. Writes ``husimi_tables.npz`` for depths 2 and 3.
 """
 import os
 import sys
-import types
 
 import numpy as np
 
@@ -17,12 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 import ref_shim  # noqa: E402
 
-ref_shim.install()
-for _name in ("matplotlib.cm", "mpl_toolkits", "mpl_toolkits.mplot3d"):
-    sys.modules[_name] = types.ModuleType(_name)
-sys.modules["matplotlib"].cm = sys.modules["matplotlib.cm"]
-sys.modules["matplotlib.cm"].coolwarm = None
-sys.modules["mpl_toolkits.mplot3d"].Axes3D = object
+ref_shim.install_package_layout()
 from library import Parameters as LP  # noqa: E402
 
 

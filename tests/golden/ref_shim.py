@@ -63,3 +63,14 @@ def install():
         MPSClass._shim_counter = counter
         C._shimmed = True
     return MPSClass
+
+
+def install_package_layout():
+    """Also make the package layout (``library.*``) importable: it imports matplotlib.cm and
+    mpl_toolkits.mplot3d for plotting helpers, stubbed here (nothing plots)."""
+    install()
+    for name in ("matplotlib.cm", "mpl_toolkits", "mpl_toolkits.mplot3d"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    sys.modules["matplotlib"].cm = sys.modules["matplotlib.cm"]
+    sys.modules["matplotlib.cm"].coolwarm = None
+    sys.modules["mpl_toolkits.mplot3d"].Axes3D = object

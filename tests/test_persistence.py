@@ -108,7 +108,7 @@ def test_two_site_density_matrices_match_the_reference(fake_backend):
     from tnalg_gb300 import BasicFunctionsSJR as bf
     g = np.load(os.path.join(gc.GOLDEN, "ref_rdm_chain_n8_h.npz"))
     A = bf.load_pr(REF_FILE, "A", device="cpu")
-    for key in g.files:
+    for key in [k for k in g.files if k.startswith("rdm_")]:
         _, p1, p2, c = key.split("_")
         A.correct_orthogonal_center(int(c[1:]))
         np.testing.assert_allclose(A.reduced_density_matrix_two_body(int(p1), int(p2)), g[key], atol=1e-12)
@@ -117,3 +117,22 @@ def test_two_site_density_matrices_match_the_reference(fake_backend):
     np.testing.assert_allclose(rev, want, atol=1e-12)
     with pytest.raises(ValueError):
         A.reduced_density_matrix_two_body(3, 3)
+
+
+def test_one_site_density_matrices_and_onsite_entropy(fake_backend):
+    """reduced_density_matrix_one_body / calculate_onsite_entanglement_entropy (library/MPSClass.py)
+    equal the package layout's own values on the same state, at centres 0, 4 and 7; the site at the
+    centre (where the reference's method fails) gives the matrix of the on-site entropy pass."""
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    g = np.load(os.path.join(gc.GOLDEN, "ref_rdm_chain_n8_h.npz"))
+    A = bf.load_pr(REF_FILE, "A", device="cpu")
+    for c in (0, 4, 7):
+        A.correct_orthogonal_center(c)
+        ent, rho = A.calculate_onsite_entanglement_entropy()
+        np.testing.assert_allclose(ent, g["onsite_ent_c%d" % c], atol=1e-12)
+        np.testing.assert_allclose(np.stack(rho), g["onsite_rho_c%d" % c], atol=1e-12)
+        for p in (0, 3, 7):
+            r = A.reduced_density_matrix_one_body(p)
+            want = g["rdm1_%d_c%d" % (p, c)] if p != c else g["onsite_rho_c%d" % c][p]
+            np.testing.assert_allclose(r, want, atol=1e-12)
+    assert 0.4 < float(np.min(ent)) < float(np.max(ent)) < np.log(2)

@@ -17,6 +17,9 @@ Differences a user can observe:
     does; its is_save_op=False values are what this class returns).
   * Operators must be real (spin 'sy' enters only through complex-free products
     in the Heisenberg expansion).
+  * full_coefficients_mps works for any length (the reference's drops a reshape,
+    MPSClass.py:983); reduced_density_matrix_one_body (from the package layout,
+    library/MPSClass.py:994-999) also works at the orthogonality centre.
 """
 import contextvars
 
@@ -387,6 +390,34 @@ class MpsOpenBoundaryClass(MpsBasic):
             d = self.phys_dim
             rho = rho.reshape(d, d, d, d).transpose(1, 0, 3, 2).reshape(d * d, d * d)
         return rho / np.trace(rho)
+
+    def _site_rhos(self, sites):
+        if self.center < 0:
+            raise RuntimeError("one-site density matrices need a central-orthogonal MPS "
+                               "(call correct_orthogonal_center first)")
+        self._ensure_obs_model()
+        out = []
+        for g in E._Observer(self._dev).site_densities(list(sites)):
+            rho = g + g.T
+            out.append(rho / np.trace(rho))
+        return out
+
+    def reduced_density_matrix_one_body(self, p):
+        """library/MPSClass.py:994-999: the (d, d) density matrix of site p, symmetrised (rho + rho^T)
+        and normalised to trace 1, computed on the device. The reference's version fails when p is
+        the orthogonality centre (its transfer from the centre to p is empty); here any site works."""
+        return self._site_rhos([p])[0]
+
+    def calculate_onsite_entanglement_entropy(self):
+        """library/MPSClass.py:1001-1038: (ent, rho) with rho[n] the one-site density matrix of site n
+        (as reduced_density_matrix_one_body) and ent[n] = -sum lm ln lm over its eigenvalues > 1e-25."""
+        rho = self._site_rhos(range(self.length))
+        ent = np.zeros((self.length,))
+        for n, r in enumerate(rho):
+            lm = np.linalg.eigvalsh(r)
+            lm = lm[lm > 1e-25]
+            ent[n] = -np.inner(lm, np.log(lm))
+        return ent, rho
 
     def full_coefficients_mps(self, tol_memory=20):
         """MPSClass.py:968-985: all d^L amplitudes psi[s_0 ... s_(L-1)] (s_0 slowest) as a (d^L, 1)

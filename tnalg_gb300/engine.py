@@ -943,6 +943,16 @@ class _Observer:
         cl, d, cr = M.shape
         L.check(self.lib.tn_pair_contract(cl, d, cr, L.ptr(M), L.ptr(X), 1.0, L.ptr(out), self.st), "pair")
 
+    def site_densities(self, sites):
+        """g[k][x, y] = <E_xy(sites[k])>, E_xy = |x><y| (unnormalised one-site densities), as numpy."""
+        s, d = self.s, self.s.d
+        G = torch.zeros((max(len(sites), 1), d, d), dtype=torch.float64, device=self.dev)
+        for k, q in enumerate(sites):
+            M = s.mps[q]
+            X = self.left_x(M, self.E_at(q)) if q >= self.c else self.right_x(M, self.F_at(q + 1))
+            self.density(M, X, G[k])
+        return G.cpu().numpy()[: len(sites)]
+
     def two_site_density(self, p1, p2):
         """rho[(x1 x2), (y1 y2)] = <E_x1y1(p1) E_x2y2(p2)> for p1 < p2, E_xy = |x><y| (unnormalised):
         the d^2 elementary operators are applied at one end in one tn_apply_site_ops call, each is

@@ -13,6 +13,9 @@ dmrg_finite_size() job from host inputs (ramp included, final MPS copied back to
 On the split-TF32 path at one GPU, `fp64_path` repeats the same job (seed, ramp, timed sweeps) on
 the plain FP64 GPU path: its sweeps/s, the speed-up of this line over it and the difference of
 the energies per site (`--no-fp64-leg` skips it).
+On one GPU, `serving` reports the many-jobs path (tnalg_gb300.serving: 16 uneven XXZ chains interleaved,
+against the same jobs one at a time on the plain FP64 GPU path: solves/s, p50/p99 latency; `--no-serving`
+skips it).
 `--impl reference` times the CPU restatement of the reference (oracle/, numpy + scipy ARPACK)
 on a bounded sample of the same workload and extrapolates sweeps/s.
 """
@@ -51,6 +54,8 @@ def parse():
     p.add_argument("--no-fp64-leg", action="store_true",
                    help="skip the plain FP64 GPU run of the same job that the split-TF32 line is compared with")
     p.add_argument("--cpu-solves", type=int, default=1)
+    p.add_argument("--no-serving", action="store_true",
+                   help="skip the serving leg (many small jobs interleaved vs one at a time on the FP64 path)")
     return p.parse_args()
 
 
@@ -300,6 +305,30 @@ def cpu_sample(length, chi, eigs_tol, nsolves, seed=0):
                                          1.0 / (per_solve * 2 * (length - 1)))}
 
 
+SERVING_ARGS = ["--jobs", "16", "--sweeps", "3"]
+
+
+def run_serving_leg(precision, timeout=420):
+    """The serving path (tnalg_gb300.serving) in a child process: 16 uneven XXZ chains (N in [16, 48],
+    chi in {16, 32, 64}, 3 sweeps, seeded) interleaved on one GPU in `precision`, against the same
+    jobs run one at a time on the plain FP64 GPU path; solves/s and p50/p99 latency of both. A failure
+    or timeout of the child is reported in the line instead of stopping the benchmark."""
+    cmd = [sys.executable, "-m", "tnalg_gb300.serving"] + SERVING_ARGS + ["--precision", precision,
+                                                                          "--baseline-precision", "fp64"]
+    shown = "python -m tnalg_gb300.serving " + " ".join(cmd[3:])
+    try:
+        p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=timeout)
+        lines = [x for x in p.stdout.splitlines() if x.startswith("{")]
+        if p.returncode != 0 or not lines:
+            tail = (p.stderr or p.stdout or "").strip().splitlines()[-1:]
+            return {"error": "exit %d: %s" % (p.returncode, tail[0][:300] if tail else ""), "command": shown}
+        out = json.loads(lines[-1])
+        out["command"] = shown
+        return out
+    except Exception as e:  # timeout or unparsable output: report, keep the benchmark line
+        return {"error": repr(e)[:300], "command": shown}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return None
@@ -394,6 +423,11 @@ def main():
         line["e2e"] = run_e2e(args, "cuda:%d" % local_rank, res["precision"])
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_sample(args.length, args.chi, args.eigs_tol, max(1, args.cpu_solves))
+    if rank == 0 and world == 1 and not args.no_serving:
+        del A
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        line["serving"] = run_serving_leg(res["precision"])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -218,6 +218,15 @@ class FakeLib:
             _strided(r, (k, n), (sRm, sRn))[...] = R[:k]
         return OK
 
+    def tn_qr_mixed_workspace_bytes(self, m, n):
+        return 0
+
+    def tn_qr_mixed(self, m, n, a, sAm, sAn, q, sQm, sQn, r, sRm, sRn, ws, wsb, stream):
+        """Same contract as tn_qr (Q orthonormal, A = Q R; the device version reaches it through an FP32
+        factorisation re-orthogonalised in FP64); the double uses the FP64 factorisation."""
+        self._count("tn_qr_mixed")
+        return self.tn_qr(m, n, a, sAm, sAn, q, sQm, sQn, r, sRm, sRn, ws, wsb, stream)
+
     def tn_singular_values_workspace_bytes(self, k, n):
         return 0
 

@@ -239,3 +239,18 @@ def test_full_coefficients_match_exact_ground_state(fake_backend):
                          para["coeff2"])[0]
     assert abs(v @ (h @ v) - e0) < 1e-9 * abs(e0)
     assert A.full_coefficients_mps(tol_memory=1) is None
+
+
+def test_bench_serving_leg_reports_failures_in_the_line():
+    """bench.py's serving leg runs in a child process; when the child fails (here: no GPU) the leg
+    returns an error entry with the command instead of raising, so the benchmark line still prints."""
+    import importlib
+    import sys
+    sys.path.insert(0, os.path.join(gc.GOLDEN, "..", ".."))
+    try:
+        bench = importlib.import_module("bench")
+        out = bench.run_serving_leg("fp64", timeout=120)
+    finally:
+        sys.path.pop(0)
+    assert "error" in out and out["command"].startswith("python -m tnalg_gb300.serving --jobs 16")
+    assert "--baseline-precision fp64" in out["command"]

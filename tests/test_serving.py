@@ -122,3 +122,17 @@ def test_ladder_mix_in_the_request_stream():
     for j in mixed:
         if j.para["lattice"] == "arbitrary":
             assert j.para["l"] % 2 == 0 and 16 <= j.para["l"] <= 96
+
+
+def test_command_line_compares_the_mix_with_sequential_fp64(capsys):
+    """`python -m tnalg_gb300.serving` (the serving leg of the benchmark): the one-at-a-time pass
+    runs in the baseline precision and the JSON line reports both, with latencies of both passes."""
+    import json
+    serving.main(["--jobs", "4", "--sweeps", "2", "--device", "cpu", "--precision", "tf32x3",
+                  "--baseline-precision", "fp64", "--ladders", "0.5", "--lengths", "8,12", "--chis", "4,8"])
+    out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert out["jobs"] == 4 and out["precision"] == "tf32x3" and out["baseline_precision"] == "fp64"
+    assert out["solves_per_s"] > 0 and out["sequential_solves_per_s"] > 0
+    assert out["sequential_latency_p99_s"] >= out["sequential_latency_p50_s"] > 0
+    assert out["latency_p99_s"] >= out["latency_p50_s"] > 0
+    assert out["max_abs_de_per_site_mix_vs_alone"] < 1e-8

@@ -286,39 +286,59 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp64")
     ap.add_argument("--max-active", type=int, default=64)
     ap.add_argument("--ladders", type=float, default=0.0, help="share of 2 x L ladder jobs (0..1)")
+    ap.add_argument("--baseline-precision", default=None,
+                    help="precision of the one-at-a-time pass (default: --precision); fp64 compares the mix "
+                         "with sequential plain FP64 solves")
+    ap.add_argument("--device", default="cuda")
+    ap.add_argument("--lengths", default="16,48", help="chain length range N (ladders get half as many rungs)")
+    ap.add_argument("--chis", default="16,32,64", help="bond dimensions to draw from")
     a = ap.parse_args(argv)
+    lengths = tuple(int(x) for x in a.lengths.split(","))
+    chis = tuple(int(x) for x in a.chis.split(","))
+    shape = dict(lengths=lengths, chis=chis, ladder_fraction=a.ladders,
+                 ladder_lengths=(max(2, lengths[0] // 2), max(2, lengths[1] // 2)))
     import torch
     from . import _lib as L
     L.load()
-    dev = "cuda"
+    dev = a.device
+    base_prec = a.baseline_precision or a.precision
+
+    def sync():
+        if str(dev).startswith("cuda"):
+            torch.cuda.synchronize()
     # warm-up: builds, tensor maps, first-launch costs
     warm = Scheduler(dev)
-    for j in make_jobs(2, seed=a.seed + 10 ** 6, sweeps=1, precision=a.precision, device=dev):
-        warm.submit(j)
+    for prec in sorted({a.precision, base_prec}):
+        for j in make_jobs(2, seed=a.seed + 10 ** 6, sweeps=1, precision=prec, device=dev, lengths=lengths, chis=chis):
+            warm.submit(j)
     warm.run()
-    torch.cuda.synchronize()
-    # the same jobs one at a time, then interleaved
+    sync()
+    # the same jobs one at a time (in the baseline precision), then interleaved
     seq_wall, seq = 0.0, {}
-    for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev,
-                       ladder_fraction=a.ladders):
+    seq_lat = []
+    for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=base_prec, device=dev, **shape):
         j.arrival = 0.0
         s = Scheduler(dev, max_active=1)
         s.submit(j)
         t0 = time.perf_counter()
         s.run()
-        torch.cuda.synchronize()
+        sync()
         seq_wall += time.perf_counter() - t0
+        seq_lat.append(seq_wall)   # latency of job k when the jobs arrive together and run in turn
         seq[j.job_id] = j
     mix = Scheduler(dev, max_active=a.max_active)
     for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev, rate=a.rate,
-                       ladder_fraction=a.ladders):
+                       **shape):
         mix.submit(j)
     mix.run()
-    torch.cuda.synchronize()
+    sync()
     out = mix.summary()
     solves = sum(j.solves for j in seq.values())
-    out.update({"precision": a.precision, "sweeps": a.sweeps, "rate_per_s": a.rate,
+    out.update({"precision": a.precision, "baseline_precision": base_prec, "sweeps": a.sweeps, "rate_per_s": a.rate,
+                "ladder_fraction": a.ladders, "lengths": list(lengths), "chis": list(chis),
                 "sequential_wall_s": seq_wall, "sequential_solves_per_s": solves / seq_wall,
+                "sequential_latency_p50_s": float(np.percentile(seq_lat, 50)),
+                "sequential_latency_p99_s": float(np.percentile(seq_lat, 99)),
                 "speedup_vs_sequential": out["solves_per_s"] / (solves / seq_wall) if seq_wall else None,
                 "max_abs_de_per_site_mix_vs_alone": max(abs(j.result["e_per_site"] - seq[j.job_id].result["e_per_site"])
                                                         for j in mix.done)})

@@ -15,7 +15,9 @@ the plain FP64 GPU path: its sweeps/s, the speed-up of this line over it and the
 the energies per site (`--no-fp64-leg` skips it).
 On one GPU, `serving` reports the many-jobs path (tnalg_gb300.serving: 16 uneven XXZ chains interleaved,
 against the same jobs one at a time on the plain FP64 GPU path: solves/s, p50/p99 latency; `--no-serving`
-skips it).
+skips it). `j1j2_6x6` reports the J1-J2 model on the 6 x 6 snake-ordered square lattice at chi=512
+(tnalg_gb300.run_lattice, against the plain FP64 path; `--no-lattice` skips it). Both legs run in child
+processes and report a failure in the line instead of stopping the benchmark.
 `--impl reference` times the CPU restatement of the reference (oracle/, numpy + scipy ARPACK)
 on a bounded sample of the same workload and extrapolates sweeps/s.
 """
@@ -56,6 +58,8 @@ def parse():
     p.add_argument("--cpu-solves", type=int, default=1)
     p.add_argument("--no-serving", action="store_true",
                    help="skip the serving leg (many small jobs interleaved vs one at a time on the FP64 path)")
+    p.add_argument("--no-lattice", action="store_true",
+                   help="skip the J1-J2 6x6 lattice leg (chi=512, against the FP64 path)")
     return p.parse_args()
 
 
@@ -315,7 +319,26 @@ def run_serving_leg(precision, timeout=420):
     or timeout of the child is reported in the line instead of stopping the benchmark."""
     cmd = [sys.executable, "-m", "tnalg_gb300.serving"] + SERVING_ARGS + ["--precision", precision,
                                                                           "--baseline-precision", "fp64"]
-    shown = "python -m tnalg_gb300.serving " + " ".join(cmd[3:])
+    return _child_json(cmd, timeout)
+
+
+LATTICE_ARGS = ["j1j2", "--width", "6", "--height", "6", "--chi", "512", "--ramp", "64,256", "--steps", "1"]
+
+
+def run_lattice_leg(precision, timeout=600):
+    """The J1-J2 lattice workload in a child process (tnalg_gb300.run_lattice): the J1-J2 model
+    (J2 = 0.5) on the 6 x 6 open square lattice in snake order, chi ramped 64 -> 256 -> 512, one
+    CUDA-event-timed sweep at chi=512 in `precision`, then the same seed and schedule on the plain FP64
+    path (sweeps/s, energy difference per site). Failures are reported in the line."""
+    cmd = [sys.executable, "-m", "tnalg_gb300.run_lattice"] + LATTICE_ARGS + ["--precision", precision]
+    if precision != "fp64":
+        cmd.append("--compare-fp64")
+    return _child_json(cmd, timeout)
+
+
+def _child_json(cmd, timeout):
+    """Run `cmd` (python -m ...) from the repository root; its last JSON line, or an error entry."""
+    shown = "python " + " ".join(cmd[1:])
     try:
         p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=timeout)
         lines = [x for x in p.stdout.splitlines() if x.startswith("{")]
@@ -428,6 +451,8 @@ def main():
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
         line["serving"] = run_serving_leg(res["precision"])
+    if rank == 0 and world == 1 and not args.no_lattice:
+        line["j1j2_6x6"] = run_lattice_leg(res["precision"])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -43,7 +43,7 @@ def test_fp64_path_matches_reference_run(cuda_lib, name):
     assert info["solves"] == 2 * (m["l"] - 1) * m["sweep_time"]
 
 
-def test_config1_energy_against_exact_diagonalisation(cuda_lib):
+def test_chain_n12_energy_against_exact_diagonalisation(cuda_lib):
     ob, A, info, para = _run_golden("chain_n12_chi16")
     e_ed = gc.meta()["ed_chain_n12"]["e_eig"]
     e = ob["e_per_site"] * 12

@@ -100,7 +100,7 @@ def test_husimi_generator_reproduces_reference_tables(depth):
 
 
 def test_j1j2_snake_generator():
-    """Config-3 lattice: 6 x 6 gives 60 J1 + 50 J2 bonds (330 rows), spans up to 11 sites; the 4 x 3
+    """J1-J2 snake lattice: 6 x 6 gives 60 J1 + 50 J2 bonds (330 rows), spans up to 11 sites; the 4 x 3
     tables equal the ones the reference run of the golden case consumed."""
     from tnalg_gb300 import HamiltonianModule as hm, Parameters as pm
     p1, p2 = hm.positions_j1j2_square_snake(6, 6)
@@ -254,3 +254,17 @@ def test_bench_serving_leg_reports_failures_in_the_line():
         sys.path.pop(0)
     assert "error" in out and out["command"].startswith("python -m tnalg_gb300.serving --jobs 16")
     assert "--baseline-precision fp64" in out["command"]
+
+
+def test_lattice_runner_reports_timed_sweeps(fake_backend, capsys):
+    """python -m tnalg_gb300.run_lattice (the benchmark's lattice leg) on a small J1-J2 lattice through
+    the test double: one JSON line with the timed sweeps and the FP64 comparison."""
+    import json
+    from tnalg_gb300 import run_lattice
+    run_lattice.main(["j1j2", "--width", "3", "--height", "2", "--chi", "8", "--ramp", "4", "--device", "cpu",
+                      "--compare-fp64"])
+    out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert out["sites"] == 6 and out["chi_schedule"] == [4, 8] and out["chi_max"] == 8
+    assert out["sweeps_per_s"] > 0 and out["solves_per_s"] > 0 and out["straddling_terms_max"] > 0
+    assert out["fp64_path"]["precision"] == "fp64" and out["abs_de_per_site_vs_fp64"] < 1e-8
+    assert out["e_per_site"] < 0

@@ -310,16 +310,33 @@ def cpu_sample(length, chi, eigs_tol, nsolves, seed=0):
 
 
 SERVING_ARGS = ["--jobs", "16", "--sweeps", "3"]
+SERVING_WORKERS = 8
 
 
 def run_serving_leg(precision, timeout=420):
     """The serving path (tnalg_gb300.serving) in a child process: 16 uneven XXZ chains (N in [16, 48],
     chi in {16, 32, 64}, 3 sweeps, seeded) interleaved on one GPU in `precision`, against the same
-    jobs run one at a time on the plain FP64 GPU path; solves/s and p50/p99 latency of both. A failure
-    or timeout of the child is reported in the line instead of stopping the benchmark."""
+    jobs run one at a time on the plain FP64 GPU path; solves/s and p50/p99 latency of both, then
+    (`threaded`) the same mix advanced by SERVING_WORKERS host threads. A failure or timeout of a
+    child is reported in the line instead of stopping the benchmark."""
     cmd = [sys.executable, "-m", "tnalg_gb300.serving"] + SERVING_ARGS + ["--precision", precision,
                                                                           "--baseline-precision", "fp64"]
-    return _child_json(cmd, timeout)
+    out = _child_json(cmd, timeout)
+    if "error" in out:
+        return out
+    # the same interleaved mix advanced by SERVING_WORKERS host threads (their library calls release
+    # the GIL, so one job's convergence-check wait no longer holds up the others' kernels), measured
+    # in its own child against the sequential FP64 pass above
+    cmd = [sys.executable, "-m", "tnalg_gb300.serving"] + SERVING_ARGS + [
+        "--precision", precision, "--workers", str(SERVING_WORKERS), "--no-sequential"]
+    thr = _child_json(cmd, min(timeout, 240))
+    if "error" not in thr and out.get("sequential_solves_per_s"):
+        thr["speedup_vs_sequential"] = thr["solves_per_s"] / out["sequential_solves_per_s"]
+        e1, e2 = out.get("e_per_site", {}), thr.get("e_per_site", {})
+        common = set(e1) & set(e2)
+        thr["max_abs_de_per_site_vs_one_thread"] = max((abs(e1[k] - e2[k]) for k in common), default=None)
+    out["threaded"] = thr
+    return out
 
 
 LATTICE_ARGS = ["j1j2", "--width", "6", "--height", "6", "--chi", "512", "--ramp", "64,256", "--steps", "1"]

@@ -15,6 +15,12 @@
  *    ABI. tn_last_error() returns a thread-local message for the last failure.
  *  - `stream` is a cudaStream_t passed as void*; every kernel of a call is queued
  *    on it. Calls are not re-entrant on one stream with one workspace.
+ *  - Host threads: several threads may call the library at once, each with its own
+ *    stream and workspaces (a multi-job host runs one job per thread). The library's
+ *    shared host state (launch counter, FP64-QR graph cache, lazily resolved entry
+ *    points) is synchronised. Process-wide and not for concurrent use: the profiler
+ *    (tn_profile_*), tn_qr_use_graphs, and the device error word read by
+ *    tn_check_device_status, which all streams share.
  *  - Tensors are row-major FP64. An MPS site tensor is (chi_l, d, chi_r); an
  *    environment is (chi, chi) indexed [bra, ket] (TensorBasicModule.py:530-619).
  *  - Strides are in elements.

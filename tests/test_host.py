@@ -268,3 +268,31 @@ def test_lattice_runner_reports_timed_sweeps(fake_backend, capsys):
     assert out["sweeps_per_s"] > 0 and out["solves_per_s"] > 0 and out["straddling_terms_max"] > 0
     assert out["fp64_path"]["precision"] == "fp64" and out["abs_de_per_site_vs_fp64"] < 1e-8
     assert out["e_per_site"] < 0
+
+
+def test_bench_serving_leg_composes_the_threaded_mix(monkeypatch):
+    """The threaded mix is measured in a second child without its own sequential pass; its speed-up
+    is taken against the first child's sequential FP64 solves/s and its per-job energies are
+    compared with the one-thread mix."""
+    import importlib
+    import sys
+    sys.path.insert(0, os.path.join(gc.GOLDEN, "..", ".."))
+    try:
+        bench = importlib.import_module("bench")
+    finally:
+        sys.path.pop(0)
+    calls = []
+
+    def fake_child(cmd, timeout):
+        calls.append(cmd)
+        if "--workers" in cmd:
+            return {"solves_per_s": 3000.0, "e_per_site": {"0": -0.5, "1": -0.4 + 1e-13}}
+        return {"solves_per_s": 600.0, "sequential_solves_per_s": 500.0, "e_per_site": {"0": -0.5, "1": -0.4}}
+
+    monkeypatch.setattr(bench, "_child_json", fake_child)
+    out = bench.run_serving_leg("tf32x3")
+    assert len(calls) == 2 and "--baseline-precision" in calls[0] and "--no-sequential" in calls[1]
+    assert out["threaded"]["speedup_vs_sequential"] == pytest.approx(6.0)
+    assert out["threaded"]["max_abs_de_per_site_vs_one_thread"] < 1e-12
+    monkeypatch.setattr(bench, "_child_json", lambda cmd, timeout: {"error": "exit 1: x", "command": "c"})
+    assert bench.run_serving_leg("fp64") == {"error": "exit 1: x", "command": "c"}

@@ -136,3 +136,37 @@ def test_command_line_compares_the_mix_with_sequential_fp64(capsys):
     assert out["sequential_latency_p99_s"] >= out["sequential_latency_p50_s"] > 0
     assert out["latency_p99_s"] >= out["latency_p50_s"] > 0
     assert out["max_abs_de_per_site_mix_vs_alone"] < 1e-8
+
+
+def test_worker_threads_give_the_results_of_one_thread():
+    """Scheduler(workers=4): jobs advanced by a thread pool (one task per job in flight) finish
+    with the results they give alone, and admission still keeps to the budget."""
+    alone = {}
+    for j in _jobs():
+        s = serving.Scheduler("cpu", max_active=1)
+        s.submit(j)
+        s.run()
+        alone[j.job_id] = j.result
+    mix = serving.Scheduler("cpu", workers=4)
+    for j in _jobs():
+        mix.submit(j)
+    done = mix.run()
+    assert len(done) == 4 and mix.max_concurrent == 4
+    for j in done:
+        assert j.result["e_per_site"] == pytest.approx(alone[j.job_id]["e_per_site"], abs=1e-12)
+        np.testing.assert_allclose(j.result["mz"], alone[j.job_id]["mz"], atol=1e-12)
+        assert j.result["solves"] == alone[j.job_id]["solves"]
+    fps = sorted(j.footprint_bytes() for j in _jobs())
+    tight = serving.Scheduler("cpu", budget_bytes=fps[-1] + fps[-2], workers=4)
+    for j in _jobs():
+        tight.submit(j)
+    assert len(tight.run()) == 4 and 1 <= tight.max_concurrent <= 2
+
+
+def test_command_line_threaded_mix_without_sequential_pass(capsys):
+    import json
+    serving.main(["--jobs", "3", "--sweeps", "2", "--device", "cpu", "--workers", "3", "--no-sequential",
+                  "--lengths", "8,12", "--chis", "4,8", "--rate", "200"])
+    out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert out["workers"] == 3 and out["jobs"] == 3 and "sequential_solves_per_s" not in out
+    assert len(out["e_per_site"]) == 3 and all(v < 0 for v in out["e_per_site"].values())

@@ -22,14 +22,15 @@ int tn_fail(int status, const char* msg) {
   return status;
 }
 
-unsigned long long g_tn_launches = 0;
+std::atomic<unsigned long long> g_tn_launches{0};
+thread_local unsigned long long g_tn_thread_launches = 0;
 bool tn_tf32x3_supported();
 
 extern "C" const char* tn_last_error(void) { return g_err; }
 
 extern "C" int tn_version(void) { return 100; }
 
-extern "C" unsigned long long tn_launch_count(void) { return g_tn_launches; }
+extern "C" unsigned long long tn_launch_count(void) { return g_tn_launches.load(); }
 
 extern "C" int tn_precision_available(int precision) {
   if (precision == TN_PREC_FP64) return 1;

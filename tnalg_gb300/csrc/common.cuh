@@ -4,18 +4,22 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "tnalg_gb300.h"
 
 // Every kernel launch site of the library is followed by TN_CHECK_LAUNCH(), which also counts
-// the launch (tn_launch_count in the C ABI).
-extern unsigned long long g_tn_launches;
+// the launch (tn_launch_count in the C ABI): in a process-wide atomic counter, and in a per-thread
+// one that lets a graph capture count its own launches while other host threads launch theirs.
+extern std::atomic<unsigned long long> g_tn_launches;
+extern thread_local unsigned long long g_tn_thread_launches;
 
 // Code written into the device error word by the cluster QR when a panel wait times out.
 constexpr int TN_DEVERR_QR_WAIT = 32;
 #define TN_CHECK_LAUNCH()                                   \
   do {                                                      \
-    ++g_tn_launches;                                        \
+    g_tn_launches.fetch_add(1, std::memory_order_relaxed);  \
+    ++g_tn_thread_launches;                                 \
     cudaError_t e_ = cudaGetLastError();                    \
     if (e_ != cudaSuccess) return tn_record_error(e_);      \
   } while (0)

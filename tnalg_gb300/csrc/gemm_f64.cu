@@ -101,18 +101,20 @@ __global__ void splitk_reduce_kernel(TnGemmF64 g, int ksplit, const double* part
   }
 }
 
-int g_sm_count = 0;
+std::atomic<int> g_sm_count{0};
 
 }  // namespace
 
 int tn_sm_count() {
-  if (g_sm_count == 0) {
+  int c = g_sm_count.load(std::memory_order_relaxed);
+  if (c == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
-    if (g_sm_count <= 0) g_sm_count = 152;
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    if (c <= 0) c = 152;
+    g_sm_count.store(c, std::memory_order_relaxed);  // every thread computes the same value
   }
-  return g_sm_count;
+  return c;
 }
 
 static int gemm_f64_run(const TnGemmF64& g, void* ws, size_t ws_bytes, cudaStream_t s) {

@@ -18,6 +18,8 @@
 #include <cuda.h>
 #include <string.h>
 
+#include <mutex>
+
 #include "common.cuh"
 
 size_t tn_matvec_fp64_ws_bytes(const tn_site_desc* ds);
@@ -430,17 +432,16 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  // resolved once; the initialisation of a function-local static is thread-safe
+  static const EncodeTiledFn fn = []() -> EncodeTiledFn {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-  }
+      return (EncodeTiledFn)p;
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -481,10 +482,14 @@ Staged carve(char*& p, int64_t rows, int64_t K, int64_t nmat) {
 int* g_err_dev = nullptr;
 
 int err_buffer(int** out) {
-  if (!g_err_dev) {
-    TN_CUDA(cudaMalloc(&g_err_dev, sizeof(int)));
-    TN_CUDA(cudaMemset(g_err_dev, 0, sizeof(int)));
-  }
+  // allocated once, by whichever host thread gets here first
+  static std::once_flag once;
+  static cudaError_t init = cudaSuccess;
+  std::call_once(once, [] {
+    init = cudaMalloc(&g_err_dev, sizeof(int));
+    if (init == cudaSuccess) init = cudaMemset(g_err_dev, 0, sizeof(int));
+  });
+  if (init != cudaSuccess) return tn_record_error(init);
   *out = g_err_dev;
   return TN_OK;
 }
@@ -500,10 +505,10 @@ int launch_kernel(const Staged& A, const Staged& B, int64_t M, int64_t N, int64_
   if ((st = make_map(&ma[1], A.lo, K, M, Z * R, A.Kp, BM))) return st;
   if ((st = make_map(&mb[0], B.hi, K, N, Z * R, B.Kp, BN))) return st;
   if ((st = make_map(&mb[1], B.lo, K, N, Z * R, B.Kp, BN))) return st;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static std::atomic<bool> attr_set{false};
+  if (!attr_set.load()) {
     TN_CUDA(cudaFuncSetAttribute(tf32x3_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, cfg::SMEM));
-    attr_set = true;
+    attr_set.store(true);
   }
   int* err;
   if ((st = err_buffer(&err))) return st;

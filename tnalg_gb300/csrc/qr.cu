@@ -17,6 +17,7 @@
 
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -355,10 +356,10 @@ constexpr size_t kClusterSmem = (size_t)2 * PW * PRW * (NB + 1) * sizeof(double)
 
 int launch_panel(int64_t m, int64_t j0, int jb, const QrWs& w, double* Tp, cudaStream_t s) {
   if (m - j0 <= (int64_t)CL * PW * PRW) {
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<bool> attr{false};
+    if (!attr.load()) {
       TN_CUDA(cudaFuncSetAttribute(qr_panel_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmem));
-      attr = true;
+      attr.store(true);
     }
     qr_panel_cluster<<<CL, PW, kClusterSmem, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
   } else {
@@ -449,8 +450,17 @@ struct QrGraph {
   cudaGraphExec_t exec;
   unsigned long long kernels;  // kernel launches recorded into the graph
 };
+// g_graphs, its eviction and the capture stream are shared by all host threads: g_graph_mu guards
+// the lookup, a capture, the insertion and the launch of a cached graph (an eviction by another
+// thread could otherwise destroy an executable graph between its lookup and its launch).
+// Least recently used at the front. The keys include the workspace address, so every MPS (every
+// job of a multi-job run) has its own graphs, a dozen or so shapes each (interior and edge moves
+// in both directions): the cache holds enough for many interleaved jobs, so that round-robin
+// over them replays graphs instead of capturing one at every move.
+constexpr size_t kQrGraphCap = 512;
 std::vector<QrGraph> g_graphs;
-bool g_use_graphs = true;
+std::mutex g_graph_mu;
+std::atomic<bool> g_use_graphs{true};
 
 }  // namespace
 
@@ -483,11 +493,17 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
   if (!g_use_graphs || cap != cudaStreamCaptureStatusNone) {
     st = qr_body(m, n, sAm, sAn, sQm, sQn, sRm, sRn, q != nullptr, w, s);
   } else {
+    std::lock_guard<std::mutex> lock(g_graph_mu);
     const int64_t key[10] = {m, n, sAm, sAn, sQm, sQn, sRm, sRn, (int64_t)(uintptr_t)base, q != nullptr};
     cudaGraphExec_t exec = nullptr;
     unsigned long long kernels = 0;
-    for (auto& g : g_graphs)
-      if (memcmp(g.key, key, sizeof(key)) == 0) { exec = g.exec; kernels = g.kernels; break; }
+    for (size_t i = 0; i < g_graphs.size(); ++i)
+      if (memcmp(g_graphs[i].key, key, sizeof(key)) == 0) {
+        exec = g_graphs[i].exec;
+        kernels = g_graphs[i].kernels;
+        std::rotate(g_graphs.begin() + i, g_graphs.begin() + i + 1, g_graphs.end());  // now most recent
+        break;
+      }
     if (!exec) {
       // capture on a private stream (the caller's may be the legacy default stream, which
       // cannot capture); nothing runs during capture, the graph is launched on `s` below.
@@ -495,17 +511,18 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
       if (!cs) TN_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       cudaGraph_t graph;
       TN_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-      const unsigned long long launches0 = g_tn_launches;
+      const unsigned long long launches0 = g_tn_thread_launches;
       st = qr_body(m, n, sAm, sAn, sQm, sQn, sRm, sRn, q != nullptr, w, cs);
       cudaError_t e = cudaStreamEndCapture(cs, &graph);
-      kernels = g_tn_launches - launches0;
-      g_tn_launches = launches0;  // counted at every replay below
+      kernels = g_tn_thread_launches - launches0;
+      g_tn_thread_launches = launches0;  // recorded, not run: counted at every replay below
+      g_tn_launches.fetch_sub(kernels);
       if (st) return st;
       if (e != cudaSuccess) return tn_record_error(e);
       e = cudaGraphInstantiate(&exec, graph, 0);
       cudaGraphDestroy(graph);
       if (e != cudaSuccess) return tn_record_error(e);
-      if (g_graphs.size() >= 64) {
+      if (g_graphs.size() >= kQrGraphCap) {
         cudaGraphExecDestroy(g_graphs.front().exec);
         g_graphs.erase(g_graphs.begin());
       }
@@ -516,7 +533,8 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
       g_graphs.push_back(gg);
     }
     TN_CUDA(cudaGraphLaunch(exec, s));
-    g_tn_launches += kernels;
+    g_tn_launches.fetch_add(kernels);
+    g_tn_thread_launches += kernels;
     st = TN_OK;
   }
   // algorithmic work of the factorisation, 2mn^2 - 2n^3/3 (forming Q is not counted)

@@ -745,7 +745,6 @@ __global__ void __launch_bounds__(QF_NT) qr32_form_q_kernel(int m, int n, const 
   }
 }
 
-int g_cluster_state = -1;  // -1 unknown, 0 unavailable, 1 available
 
 cudaLaunchConfig_t launch_config(cudaLaunchAttribute* at, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
@@ -767,8 +766,10 @@ cudaLaunchConfig_t launch_config(cudaLaunchAttribute* at, cudaStream_t s) {
 // True when the 16-CTA cluster kernel can run this shape on the current device.
 bool tn_qr32_cluster_supported(int64_t m, int64_t n) {
   if (n < 1 || n > (int64_t)NBMAX * BW || m < n || m > MMAX) return false;
-  if (g_cluster_state < 0) {
-    g_cluster_state = 0;
+  // probed once (the initialisation of a function-local static is thread-safe, so concurrent
+  // first callers all see the probe's answer)
+  static const bool available = [] {
+    bool ok = false;
     if (cudaFuncSetAttribute(qr32_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
             cudaSuccess &&
         cudaFuncSetAttribute(qr32_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) ==
@@ -777,11 +778,12 @@ bool tn_qr32_cluster_supported(int64_t m, int64_t n) {
       cudaLaunchConfig_t cfg = launch_config(at, 0);
       int clusters = 0;
       if (cudaOccupancyMaxActiveClusters(&clusters, qr32_cluster_kernel, &cfg) == cudaSuccess && clusters > 0)
-        g_cluster_state = 1;
+        ok = true;
     }
     cudaGetLastError();  // an unsupported attribute leaves no sticky error behind
-  }
-  return g_cluster_state == 1;
+    return ok;
+  }();
+  return available;
 }
 
 // Scratch floats for V and T of all panels of an m x n factorisation.

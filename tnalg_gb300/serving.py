@@ -188,10 +188,11 @@ class DMRGJob:
 class Scheduler:
     """Admission by device-memory budget and round-robin interleaving of admitted jobs."""
 
-    def __init__(self, device="cuda", budget_bytes=None, max_active=64):
+    def __init__(self, device="cuda", budget_bytes=None, max_active=64, workers=1):
         self.device = device
         self.budget = budget_bytes
         self.max_active = int(max_active)
+        self.workers = max(1, int(workers))
         self.pending = []
         self.done = []
         self.max_concurrent = 0
@@ -210,6 +211,8 @@ class Scheduler:
 
     def run(self):
         """Runs every submitted job; returns the finished jobs in completion order."""
+        if self.workers > 1:
+            return self._run_threaded()
         budget = self._budget()
         pending = sorted(self.pending, key=lambda j: (j.arrival, j.job_id))
         self.pending = []
@@ -238,6 +241,49 @@ class Scheduler:
                     active.remove(job)
                     used -= job.footprint_bytes()
                     self.done.append(job)
+        return self.done
+
+    def _run_threaded(self):
+        """run() with `workers` host threads: admission as in run() (on this thread, which also
+        builds each admitted job's MPS, so the global RNG draws stay in admission order); every
+        admitted job has one local update (a task) in flight at a time on the pool. The library's
+        calls release the GIL, so while one thread waits inside a job's Lanczos convergence check,
+        the others run their jobs' host code and queue their kernels on their own streams."""
+        from concurrent.futures import FIRST_COMPLETED, ThreadPoolExecutor, wait
+        budget = self._budget()
+        pending = sorted(self.pending, key=lambda j: (j.arrival, j.job_id))
+        self.pending = []
+        active, used, inflight = [], 0, {}
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=self.workers) as pool:
+            while pending or active:
+                now = time.perf_counter() - t0
+                while pending and pending[0].arrival <= now and len(active) < self.max_active:
+                    fp = pending[0].footprint_bytes()
+                    if active and used + fp > budget:
+                        break
+                    job = pending.pop(0)
+                    job.admitted = time.perf_counter() - t0
+                    job.start(self.device)
+                    active.append(job)
+                    used += fp
+                    inflight[pool.submit(job.advance)] = job
+                self.max_concurrent = max(self.max_concurrent, len(active))
+                if not active:
+                    time.sleep(max(0.0, min(pending[0].arrival - now, 0.01)))
+                    continue
+                # wake up for the next arrival while jobs run
+                wake = max(0.0, min(pending[0].arrival - (time.perf_counter() - t0), 0.01)) if pending else None
+                finished, _ = wait(list(inflight), timeout=wake, return_when=FIRST_COMPLETED)
+                for f in finished:
+                    job = inflight.pop(f)
+                    if f.result():   # a job's exception is raised here
+                        job.finished = time.perf_counter() - t0
+                        active.remove(job)
+                        used -= job.footprint_bytes()
+                        self.done.append(job)
+                    else:
+                        inflight[pool.submit(job.advance)] = job
         return self.done
 
     def summary(self):
@@ -290,6 +336,9 @@ def main(argv=None):
                     help="precision of the one-at-a-time pass (default: --precision); fp64 compares the mix "
                          "with sequential plain FP64 solves")
     ap.add_argument("--device", default="cuda")
+    ap.add_argument("--workers", type=int, default=1,
+                    help="host threads advancing the interleaved jobs (1: one thread, round robin)")
+    ap.add_argument("--no-sequential", action="store_true", help="skip the one-at-a-time pass")
     ap.add_argument("--lengths", default="16,48", help="chain length range N (ladders get half as many rungs)")
     ap.add_argument("--chis", default="16,32,64", help="bond dimensions to draw from")
     a = ap.parse_args(argv)
@@ -316,7 +365,8 @@ def main(argv=None):
     # the same jobs one at a time (in the baseline precision), then interleaved
     seq_wall, seq = 0.0, {}
     seq_lat = []
-    for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=base_prec, device=dev, **shape):
+    for j in ([] if a.no_sequential else
+              make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=base_prec, device=dev, **shape)):
         j.arrival = 0.0
         s = Scheduler(dev, max_active=1)
         s.submit(j)
@@ -326,22 +376,24 @@ def main(argv=None):
         seq_wall += time.perf_counter() - t0
         seq_lat.append(seq_wall)   # latency of job k when the jobs arrive together and run in turn
         seq[j.job_id] = j
-    mix = Scheduler(dev, max_active=a.max_active)
+    mix = Scheduler(dev, max_active=a.max_active, workers=a.workers)
     for j in make_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev, rate=a.rate,
                        **shape):
         mix.submit(j)
     mix.run()
     sync()
     out = mix.summary()
-    solves = sum(j.solves for j in seq.values())
     out.update({"precision": a.precision, "baseline_precision": base_prec, "sweeps": a.sweeps, "rate_per_s": a.rate,
-                "ladder_fraction": a.ladders, "lengths": list(lengths), "chis": list(chis),
-                "sequential_wall_s": seq_wall, "sequential_solves_per_s": solves / seq_wall,
-                "sequential_latency_p50_s": float(np.percentile(seq_lat, 50)),
-                "sequential_latency_p99_s": float(np.percentile(seq_lat, 99)),
-                "speedup_vs_sequential": out["solves_per_s"] / (solves / seq_wall) if seq_wall else None,
-                "max_abs_de_per_site_mix_vs_alone": max(abs(j.result["e_per_site"] - seq[j.job_id].result["e_per_site"])
-                                                        for j in mix.done)})
+                "ladder_fraction": a.ladders, "lengths": list(lengths), "chis": list(chis), "workers": a.workers})
+    if seq:
+        solves = sum(j.solves for j in seq.values())
+        out.update({"sequential_wall_s": seq_wall, "sequential_solves_per_s": solves / seq_wall,
+                    "sequential_latency_p50_s": float(np.percentile(seq_lat, 50)),
+                    "sequential_latency_p99_s": float(np.percentile(seq_lat, 99)),
+                    "speedup_vs_sequential": out["solves_per_s"] / (solves / seq_wall) if seq_wall else None,
+                    "max_abs_de_per_site_mix_vs_alone": max(abs(j.result["e_per_site"] -
+                                                                seq[j.job_id].result["e_per_site"]) for j in mix.done)})
+    out["e_per_site"] = {str(j.job_id): j.result["e_per_site"] for j in mix.done}
     print(json.dumps(out), flush=True)
 
 

@@ -309,11 +309,12 @@ def cpu_sample(length, chi, eigs_tol, nsolves, seed=0):
                                          1.0 / (per_solve * 2 * (length - 1)))}
 
 
+LEGS_BUDGET_S = 480   # serving + lattice legs together (normally ~3 minutes)
 SERVING_ARGS = ["--jobs", "16", "--sweeps", "3"]
 SERVING_WORKERS = 8
 
 
-def run_serving_leg(precision, timeout=420):
+def run_serving_leg(precision, timeout=240, deadline=None):
     """The serving path (tnalg_gb300.serving) in a child process: 16 uneven XXZ chains (N in [16, 48],
     chi in {16, 32, 64}, 3 sweeps, seeded) interleaved on one GPU in `precision`, against the same
     jobs run one at a time on the plain FP64 GPU path; solves/s and p50/p99 latency of both, then
@@ -321,6 +322,8 @@ def run_serving_leg(precision, timeout=420):
     child is reported in the line instead of stopping the benchmark."""
     cmd = [sys.executable, "-m", "tnalg_gb300.serving"] + SERVING_ARGS + ["--precision", precision,
                                                                           "--baseline-precision", "fp64"]
+    if deadline is not None:
+        timeout = max(1.0, min(timeout, deadline - time.time()))
     out = _child_json(cmd, timeout)
     if "error" in out:
         return out
@@ -329,8 +332,9 @@ def run_serving_leg(precision, timeout=420):
     # in its own child against the sequential FP64 pass above
     cmd = [sys.executable, "-m", "tnalg_gb300.serving"] + SERVING_ARGS + [
         "--precision", precision, "--workers", str(SERVING_WORKERS), "--no-sequential"]
-    thr = _child_json(cmd, min(timeout, 240))
-    if "error" not in thr and out.get("sequential_solves_per_s"):
+    left = 150.0 if deadline is None else min(150.0, deadline - time.time())
+    thr = _child_json(cmd, left) if left > 30 else {"skipped": "the legs' time budget was spent"}
+    if "error" not in thr and "skipped" not in thr and out.get("sequential_solves_per_s"):
         thr["speedup_vs_sequential"] = thr["solves_per_s"] / out["sequential_solves_per_s"]
         e1, e2 = out.get("e_per_site", {}), thr.get("e_per_site", {})
         common = set(e1) & set(e2)
@@ -342,7 +346,7 @@ def run_serving_leg(precision, timeout=420):
 LATTICE_ARGS = ["j1j2", "--width", "6", "--height", "6", "--chi", "512", "--ramp", "64,256", "--steps", "1"]
 
 
-def run_lattice_leg(precision, timeout=600):
+def run_lattice_leg(precision, timeout=300):
     """The J1-J2 lattice workload in a child process (tnalg_gb300.run_lattice): the J1-J2 model
     (J2 = 0.5) on the 6 x 6 open square lattice in snake order, chi ramped 64 -> 256 -> 512, one
     CUDA-event-timed sweep at chi=512 in `precision`, then the same seed and schedule on the plain FP64
@@ -463,13 +467,18 @@ def main():
         line["e2e"] = run_e2e(args, "cuda:%d" % local_rank, res["precision"])
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_sample(args.length, args.chi, args.eigs_tol, max(1, args.cpu_solves))
-    if rank == 0 and world == 1 and not args.no_serving:
+    if rank == 0 and world == 1 and not (args.no_serving and args.no_lattice):
         del A
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
-        line["serving"] = run_serving_leg(res["precision"])
-    if rank == 0 and world == 1 and not args.no_lattice:
-        line["j1j2_6x6"] = run_lattice_leg(res["precision"])
+        # the child legs share one time budget, so a stuck leg cannot hold back the line
+        legs_end = time.time() + LEGS_BUDGET_S
+        if not args.no_serving:
+            line["serving"] = run_serving_leg(res["precision"], deadline=legs_end)
+        if not args.no_lattice:
+            left = legs_end - time.time()
+            line["j1j2_6x6"] = (run_lattice_leg(res["precision"], timeout=min(300.0, left)) if left > 60 else
+                                {"skipped": "the legs' %d s time budget was spent" % LEGS_BUDGET_S})
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -98,3 +98,36 @@ def test_one_site_density_matrices_on_device(cuda_lib):
         ent, rho = A.calculate_onsite_entanglement_entropy()
         np.testing.assert_allclose(ent, g["onsite_ent_c%d" % c], atol=1e-12)
         np.testing.assert_allclose(np.stack(rho), g["onsite_rho_c%d" % c], atol=1e-12)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("tf32x3", 1e-8)])
+def test_worker_threads_on_device(cuda_lib, precision, tol):
+    """Scheduler(workers=4): jobs advanced from four host threads, each on its own stream, give the
+    results they give alone (exercises the library's shared host state under concurrent calls)."""
+    from tnalg_gb300 import _lib as L, serving
+    if precision == "tf32x3" and not L.tf32x3_available():
+        pytest.skip("tf32x3 needs an sm_103 device")
+
+    def jobs():
+        out = []
+        for k, (l, chi, jz, hz) in enumerate([(16, 16, 1.0, 0.0), (24, 32, 0.5, 0.2), (20, 16, 1.5, 0.1),
+                                              (12, 8, 1.0, 0.3), (32, 32, 0.8, 0.0), (18, 64, 1.2, 0.4)]):
+            para = serving.chain_job_para(l, chi, jz=jz, hz=hz, sweeps=3, precision=precision, device="cuda")
+            out.append(serving.DMRGJob(k, para, seed=300 + k))
+        return out
+
+    alone = {}
+    for j in jobs():
+        s = serving.Scheduler("cuda", max_active=1)
+        s.submit(j)
+        s.run()
+        alone[j.job_id] = j.result
+    mix = serving.Scheduler("cuda", workers=4)
+    for j in jobs():
+        mix.submit(j)
+    done = mix.run()
+    assert len(done) == 6 and mix.max_concurrent == 6
+    for j in done:
+        ref = alone[j.job_id]
+        assert abs(j.result["e_per_site"] - ref["e_per_site"]) <= tol
+        np.testing.assert_allclose(j.result["mz"], ref["mz"], atol=10 * tol)

@@ -131,3 +131,16 @@ def test_worker_threads_on_device(cuda_lib, precision, tol):
         ref = alone[j.job_id]
         assert abs(j.result["e_per_site"] - ref["e_per_site"]) <= tol
         np.testing.assert_allclose(j.result["mz"], ref["mz"], atol=10 * tol)
+
+
+@pytest.mark.parametrize("name,chi", [("pickle_chi16", 16), ("pickle_chi24", 24)])
+def test_shipped_result_files_replayed_on_device(cuda_lib, name, chi):
+    """The reference's shipped data_dmrg/ result files: their pickled coupling tables run on the GPU
+    reach the energies and bond energies the files record."""
+    from test_persistence import _pickled_para
+    from tnalg_gb300 import DMRG_anyH
+    g, para = _pickled_para(name, chi, "cuda")
+    np.random.seed(0)
+    ob, A, info, _ = _quiet(DMRG_anyH.dmrg_finite_size, para)
+    assert abs(ob["e_per_site"] - float(g["e_per_site"])) <= 1e-10 * abs(float(g["e_per_site"]))
+    np.testing.assert_allclose(np.ravel(ob["eb_full"]), np.ravel(g["eb_full"]), atol=1e-8)

@@ -136,3 +136,31 @@ def test_one_site_density_matrices_and_onsite_entropy(fake_backend):
             want = g["rdm1_%d_c%d" % (p, c)] if p != c else g["onsite_rho_c%d" % c][p]
             np.testing.assert_allclose(r, want, atol=1e-12)
     assert 0.4 < float(np.min(ent)) < float(np.max(ent)) < np.log(2)
+
+
+def _pickled_para(name, chi, device):
+    from tnalg_gb300 import Parameters as pm
+    g = gc.load(name)
+    para = pm.generate_parameters_dmrg("arbitrary")
+    para.update(index1=g["index1"], coeff1=g["coeff1"], index2=g["index2"], coeff2=g["coeff2"], op=list(g["op"]))
+    para = pm.make_consistent_parameter_dmrg(para)
+    para.update(chi=chi, sweep_time=30, dt_ob=1, break_tol=1e-13, eigs_tol=1e-12, tau=1e-4, hx=0.0, hz=0.0,
+                device=device)
+    return g, para
+
+
+@pytest.mark.parametrize("name,chi", [("pickle_chi16", 16), ("pickle_chi24", 24)])
+def test_shipped_result_files_replayed(fake_backend, name, chi):
+    """The coupling tables pickled in the reference's data_dmrg/ result files (EasyStart convention,
+    coeff 1 on S+S- / S-S+) run through dmrg_finite_size reach the energies and bond energies those
+    files record (a different random start; both runs converged at the same bond dimension)."""
+    import contextlib
+    import io
+    from tnalg_gb300 import DMRG_anyH
+    g, para = _pickled_para(name, chi, "cpu")
+    np.random.seed(0)
+    with contextlib.redirect_stdout(io.StringIO()):
+        ob, A, info, _ = DMRG_anyH.dmrg_finite_size(para)
+    assert abs(ob["e_per_site"] - float(g["e_per_site"])) <= 1e-10 * abs(float(g["e_per_site"]))
+    np.testing.assert_allclose(np.ravel(ob["eb_full"]), np.ravel(g["eb_full"]), atol=1e-8)
+    assert list(A.virtual_dim) == list(g["virtual_dim"])

@@ -144,3 +144,16 @@ def test_shipped_result_files_replayed_on_device(cuda_lib, name, chi):
     ob, A, info, _ = _quiet(DMRG_anyH.dmrg_finite_size, para)
     assert abs(ob["e_per_site"] - float(g["e_per_site"])) <= 1e-10 * abs(float(g["e_per_site"]))
     np.testing.assert_allclose(np.ravel(ob["eb_full"]), np.ravel(g["eb_full"]), atol=1e-8)
+
+
+GPU_ED_CASES = [("chain", 16), ("ladder", 16), ("jigsaw", 9), ("full", 12), ("longRange", 12), ("square", 12),
+                ("j1j2", 12), ("j1j2", 16)]
+
+
+@pytest.mark.parametrize("kind,size", GPU_ED_CASES)
+def test_full_bond_dimension_reaches_the_exact_ground_state_on_device(cuda_lib, kind, size):
+    """Every lattice generator at N <= 16 (full bond dimension, FP64 path): the DMRG energy equals
+    exact diagonalisation's to 1e-9 relative."""
+    from test_ed_parity import run_against_ed
+    e, e0 = run_against_ed(kind, size, "cuda")
+    assert abs(e - e0) <= 1e-9 * abs(e0), (kind, size, e, e0)

@@ -428,6 +428,16 @@ def main():
     qr_line = kernel_roofline("gauge-move QR (tn_qr_mixed: FP32 cluster QR + FP64 re-orthogonalisation)" if mixed
                               else "gauge-move QR (tn_qr: FP64 Householder)", res["qr_ms"], res["qr_cnt"],
                               res["qr_flops"], "F_qr = 2 m n^2 - 2 n^3 / 3, m = d chi, n = chi")
+    if mixed:
+        # DRAM traffic from the committed ncu captures of the same shapes (cold cache, one launch each)
+        qr_line.update(traffic=4.41e6, traffic_kernel="qr32_cluster_kernel (the factorisation of tn_qr_mixed; 43% of "
+                       "the sweep's device time in the launch list)",
+                       traffic_source="profiles/qr32_cluster_1024x512_ncu.md: dram__bytes_read 4.41 MB + write 0 per "
+                       "launch at 1024 x 512; the Q kernel reads 1.6 MB, the Gram 4.2 MB "
+                       "(profiles/qr32_form_q_and_gram_1024x512_ncu.md)")
+        mv_line.update(traffic_component={"kernel": "tf32x3_gemm_kernel (one block GEMM of the chi=512 matvec)",
+                                          "dram_bytes": 16.8e6,
+                                          "source": "profiles/tf32x3_gemm_matvec_chi512_ncu.md"})
     # the roofline object describes the kernel class with the most device time in the timed sweeps
     dominant, other = (qr_line, mv_line) if res["qr_ms"] > res["mv_ms"] else (mv_line, qr_line)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

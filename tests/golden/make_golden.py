@@ -222,9 +222,9 @@ def full_para(l, chi, sweeps):
 
 
 EXTRA = {
-    "j1j2_snake_4x3_chi16": lambda meta: run_case("j1j2_snake_4x3_chi16", j1j2_para(4, 3, 16, 0.1, 10), 5, meta),
+    "j1j2_snake_4x3_chi16": lambda meta: run_case("j1j2_snake_4x3_chi16", j1j2_para(4, 3, 16, 0.1, 40), 5, meta),
     "full_n8_chi8": lambda meta: run_case("full_n8_chi8", full_para(8, 8, 8), 7, meta),
-    "square_4x2_chi8": lambda meta: run_case("square_4x2_chi8", square_para(4, 2, 8, 0.0, 0.0, 10), 6, meta),
+    "square_4x2_chi8": lambda meta: run_case("square_4x2_chi8", square_para(4, 2, 8, 0.0, 0.0, 60), 6, meta),
 }
 
 

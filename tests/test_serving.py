@@ -129,7 +129,8 @@ def test_command_line_compares_the_mix_with_sequential_fp64(capsys):
     runs in the baseline precision and the JSON line reports both, with latencies of both passes."""
     import json
     serving.main(["--jobs", "4", "--sweeps", "2", "--device", "cpu", "--precision", "tf32x3",
-                  "--baseline-precision", "fp64", "--ladders", "0.5", "--lengths", "8,12", "--chis", "4,8"])
+                  "--baseline-precision", "fp64", "--ladders", "0.5", "--lengths", "8,12", "--chis", "4,8",
+                  "--ladder-rungs", "3,5"])
     out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert out["jobs"] == 4 and out["precision"] == "tf32x3" and out["baseline_precision"] == "fp64"
     assert out["solves_per_s"] > 0 and out["sequential_solves_per_s"] > 0

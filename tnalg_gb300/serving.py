@@ -341,11 +341,13 @@ def main(argv=None):
     ap.add_argument("--no-sequential", action="store_true", help="skip the one-at-a-time pass")
     ap.add_argument("--lengths", default="16,48", help="chain length range N (ladders get half as many rungs)")
     ap.add_argument("--chis", default="16,32,64", help="bond dimensions to draw from")
+    ap.add_argument("--ladder-rungs", default=None, help="rung range L of the 2 x L ladders (default: half of --lengths)")
     a = ap.parse_args(argv)
     lengths = tuple(int(x) for x in a.lengths.split(","))
     chis = tuple(int(x) for x in a.chis.split(","))
-    shape = dict(lengths=lengths, chis=chis, ladder_fraction=a.ladders,
-                 ladder_lengths=(max(2, lengths[0] // 2), max(2, lengths[1] // 2)))
+    rungs = (tuple(int(x) for x in a.ladder_rungs.split(",")) if a.ladder_rungs else
+             (max(2, lengths[0] // 2), max(2, lengths[1] // 2)))
+    shape = dict(lengths=lengths, chis=chis, ladder_fraction=a.ladders, ladder_lengths=rungs)
     import torch
     from . import _lib as L
     L.load()

@@ -164,3 +164,15 @@ def test_shipped_result_files_replayed(fake_backend, name, chi):
     assert abs(ob["e_per_site"] - float(g["e_per_site"])) <= 1e-10 * abs(float(g["e_per_site"]))
     np.testing.assert_allclose(np.ravel(ob["eb_full"]), np.ravel(g["eb_full"]), atol=1e-8)
     assert list(A.virtual_dim) == list(g["virtual_dim"])
+
+
+def test_correlators_from_middle_honour_ob_len(fake_backend):
+    """observe_correlators_from_middle(op1, op2, ob_len) (MPSClass.py:936-952) stops after ob_len + 1
+    pairs, growing alternately to the left and right of round(L/2)."""
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    A = bf.load_pr(REF_FILE, "A", device="cpu")
+    full = A.observe_correlators_from_middle(3, 3)
+    assert full.shape == (6,)      # pairs (4,5), (3,5), (3,6), (2,6), (2,7), (1,7): then the right end is passed
+    short = A.observe_correlators_from_middle(3, 3, ob_len=2)
+    np.testing.assert_allclose(short, full[:3], atol=1e-14)
+    assert A.observe_correlators_from_middle(1, 3, ob_len=0).shape == (1,)

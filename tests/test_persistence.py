@@ -176,3 +176,32 @@ def test_correlators_from_middle_honour_ob_len(fake_backend):
     short = A.observe_correlators_from_middle(3, 3, ob_len=2)
     np.testing.assert_allclose(short, full[:3], atol=1e-14)
     assert A.observe_correlators_from_middle(1, 3, ob_len=0).shape == (1,)
+
+
+def test_single_observations_norm_and_centre_moves(fake_backend):
+    """observation_s1 / observation_s1_s2 (MPSClass.py:857-909) against the pickled magnetisations and
+    the reference's two-site density matrix; norm_mps, central_orthogonalization and
+    check_orthogonal_center (MPSClass.py:170-185, 954-1022) on the restored state; set_precision
+    round trip."""
+    from tnalg_gb300 import BasicFunctionsSJR as bf
+    ob, A, info, para = bf.load_pr(REF_FILE, ("ob", "A", "info", "para"), device="cpu")
+    g = np.load(os.path.join(gc.GOLDEN, "ref_rdm_chain_n8_h.npz"))
+    ops = [np.real(np.asarray(o)) for o in para["op"]]
+    for p in range(8):
+        assert abs(A.observation_s1((3, p)) - float(np.ravel(ob["mz"])[p])) < 1e-12
+    rho = g["rdm_1_5_c0"].reshape(2, 2, 2, 2)         # [x1, x2, y1, y2]
+    for a, b in ((3, 3), (1, 3), (4, 5)):
+        want = np.einsum("xy,uv,xuyv->", ops[a], ops[b], rho)
+        assert abs(A.observation_s1_s2(([a, b], [1, 5])) - want) < 1e-12
+        # the reference sorts the positions with their operators (MPSClass.py:878-880)
+        assert abs(A.observation_s1_s2(([b, a], [5, 1])) - want) < 1e-12
+    assert abs(A.norm_mps() - 1.0) < 1e-12
+    A.central_orthogonalization(5)
+    assert A.center == 5 and A.check_orthogonal_center(if_print=False) == 5
+    assert np.ravel(A.orthogonality).tolist() == [-1] * 5 + [0] + [1] * 2
+    assert abs(A.norm_mps() - 1.0) < 1e-12
+    assert abs(A.observation_s1((3, 2)) - float(np.ravel(ob["mz"])[2])) < 1e-12
+    A.set_precision("tf32x3")
+    assert A.precision == "tf32x3"
+    A.set_precision("fp64")
+    assert A.precision == "fp64"

@@ -20,6 +20,7 @@ Cases (all with the reference's own ``dmrg_finite_size`` from DMRG_anyH.py:18,
 * ``longrange_n8_chi8``    'longRange' lattice (all-to-all couplings)
 * ``j1j2_snake_4x3_chi16`` J1-J2 square lattice (J2 = 0.5) in snake order, 'arbitrary' lattice, hz field
   (``python tests/golden/make_golden.py j1j2_snake_4x3_chi16`` runs this case alone)
+* ``chain_n10_chi8_ob3``   XXZ chain (Jz = 0.7) with fields, sweeps starting from site 3 (``ob_position``)
 * ``full_n8_chi8``         the reference's 'full' lattice (all-to-all Ising couplings, transverse field hx=0.5)
 * ``square_4x2_chi8``      the reference's 'square' lattice (row-major numbering), 4x2, no field (its
   make_consistent_parameter_dmrg appends the field operator instead of rebuilding the list, Parameters.py:190,
@@ -121,6 +122,7 @@ def run_case(name, para, seed, meta):
         "hx": float(para.get("hx", 0.0)),
         "hz": float(para.get("hz", 0.0)),
         "lattice": para["lattice"],
+        "ob_position": int(para.get("ob_position", 0)),
         "eig_solves": MPSClass._shim_counter["solves"],
     }
     MPSClass._shim_counter["solves"] = 0
@@ -224,6 +226,8 @@ def full_para(l, chi, sweeps):
 EXTRA = {
     "j1j2_snake_4x3_chi16": lambda meta: run_case("j1j2_snake_4x3_chi16", j1j2_para(4, 3, 16, 0.1, 40), 5, meta),
     "full_n8_chi8": lambda meta: run_case("full_n8_chi8", full_para(8, 8, 8), 7, meta),
+    "chain_n10_chi8_ob3": lambda meta: run_case("chain_n10_chi8_ob3",
+                                                dict(chain_para(10, 8, 1, 0.7, 0.2, 0.3, 12), ob_position=3), 8, meta),
     "square_4x2_chi8": lambda meta: run_case("square_4x2_chi8", square_para(4, 2, 8, 0.0, 0.0, 60), 6, meta),
 }
 

@@ -153,7 +153,7 @@ def test_open_operator_sets_chain_and_long_range():
 # (the J1-J2 reference run, 40 sweeps, is checked on the GPU; its lattice's host path is covered on the
 # CPU by the 3 x 3 case of test_ed_parity.py)
 @pytest.mark.parametrize("name", ["chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8", "square_4x2_chi8",
-                                  "full_n8_chi8"])
+                                  "full_n8_chi8", "chain_n10_chi8_ob3"])
 def test_sweep_orchestration_matches_reference(name, fake_backend):
     from tnalg_gb300 import DMRG_anyH
     g, m = gc.load(name), gc.meta()[name]
@@ -165,7 +165,7 @@ def test_sweep_orchestration_matches_reference(name, fake_backend):
     np.testing.assert_allclose(ob["corr_z"], g["corr_z_nocache"], atol=1e-8)
     np.testing.assert_allclose(np.ravel(A.ent), g["ent"], atol=1e-8)
     assert (A.virtual_dim == g["virtual_dim"]).all()
-    assert info["solves"] == 2 * (m["l"] - 1) * m["sweep_time"]
+    assert info["solves"] == m.get("eig_solves", 2 * (m["l"] - 1) * m["sweep_time"])
 
 
 def test_reference_script_through_compat_modules(fake_backend):

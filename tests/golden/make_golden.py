@@ -20,6 +20,7 @@ Cases (all with the reference's own ``dmrg_finite_size`` from DMRG_anyH.py:18,
 * ``longrange_n8_chi8``    'longRange' lattice (all-to-all couplings)
 * ``j1j2_snake_4x3_chi16`` J1-J2 square lattice (J2 = 0.5) in snake order, 'arbitrary' lattice, hz field
   (``python tests/golden/make_golden.py j1j2_snake_4x3_chi16`` runs this case alone)
+* ``chain_n10_chi8_break`` XXZ chain (Jz = 1.3) with fields, observed every 2nd sweep, stopped by break_tol=1e-9
 * ``chain_n10_chi8_ob3``   XXZ chain (Jz = 0.7) with fields, sweeps starting from site 3 (``ob_position``)
 * ``full_n8_chi8``         the reference's 'full' lattice (all-to-all Ising couplings, transverse field hx=0.5)
 * ``square_4x2_chi8``      the reference's 'square' lattice (row-major numbering), 4x2, no field (its
@@ -117,6 +118,8 @@ def run_case(name, para, seed, meta):
         "d": int(para["d"]),
         "chi": int(para["chi"]),
         "sweep_time": int(para["sweep_time"]),
+        "dt_ob": int(para.get("dt_ob", 1)),
+        "break_tol": float(para.get("break_tol", -1.0)),
         "tau": para["tau"],
         "eigs_tol": para["eigs_tol"],
         "hx": float(para.get("hx", 0.0)),
@@ -226,6 +229,9 @@ def full_para(l, chi, sweeps):
 EXTRA = {
     "j1j2_snake_4x3_chi16": lambda meta: run_case("j1j2_snake_4x3_chi16", j1j2_para(4, 3, 16, 0.1, 40), 5, meta),
     "full_n8_chi8": lambda meta: run_case("full_n8_chi8", full_para(8, 8, 8), 7, meta),
+    "chain_n10_chi8_break": lambda meta: run_case("chain_n10_chi8_break",
+                                                  dict(chain_para(10, 8, 1, 1.3, 0.1, 0.25, 40), dt_ob=2,
+                                                       break_tol=1e-9), 9, meta),
     "chain_n10_chi8_ob3": lambda meta: run_case("chain_n10_chi8_ob3",
                                                 dict(chain_para(10, 8, 1, 0.7, 0.2, 0.3, 12), ob_position=3), 8, meta),
     "square_4x2_chi8": lambda meta: run_case("square_4x2_chi8", square_para(4, 2, 8, 0.0, 0.0, 60), 6, meta),

@@ -7,7 +7,8 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 RUN_CASES = ["chain_n12_chi16", "chain_n12_chi16_h", "ladder_2x4_chi8", "jigsaw_s1_n9_chi12", "longrange_n8_chi8"]
 # further reference runs; their GPU parity test is in test_gpu_wider.py
-LATER_CASES = ["j1j2_snake_4x3_chi16", "square_4x2_chi8", "full_n8_chi8", "chain_n10_chi8_ob3"]
+LATER_CASES = ["j1j2_snake_4x3_chi16", "square_4x2_chi8", "full_n8_chi8", "chain_n10_chi8_ob3",
+               "chain_n10_chi8_break"]
 
 
 def meta():
@@ -25,7 +26,7 @@ def para_of(name, device="cuda", precision="fp64"):
     return {
         "l": m["l"], "d": m["d"], "chi": m["chi"], "op": list(g["op"]), "index1": g["index1"],
         "index2": g["index2"], "coeff1": g["coeff1"], "coeff2": g["coeff2"], "positions_h2": g["positions_h2"],
-        "tau": m["tau"], "eigs_tol": m["eigs_tol"], "sweep_time": m["sweep_time"], "dt_ob": 1, "break_tol": -1.0,
+        "tau": m["tau"], "eigs_tol": m["eigs_tol"], "sweep_time": m["sweep_time"], "dt_ob": m.get("dt_ob", 1), "break_tol": m.get("break_tol", -1.0),
         "hx": m["hx"], "hz": m["hz"], "ob_position": m.get("ob_position", 0), "if_print_detail": False, "is_real": True,
         "device": device, "precision": precision,
     }

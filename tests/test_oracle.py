@@ -15,11 +15,13 @@ def _run(name):
     return O.dmrg_finite_size(m["l"], m["d"], m["chi"], list(g["op"]), g["index1"], g["coeff1"], g["index2"],
                               g["coeff2"], g["positions_h2"], tau=m["tau"], eigs_tol=m["eigs_tol"],
                               sweep_time=m["sweep_time"], hx=m["hx"], hz=m["hz"], seed=m["seed"],
-                              ob_position=m.get("ob_position", 0))
+                              ob_position=m.get("ob_position", 0), dt_ob=m.get("dt_ob", 1),
+                              break_tol=m.get("break_tol", -1.0))
 
 
 @pytest.mark.parametrize("name", ["chain_n12_chi16", "chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8",
-                                  "j1j2_snake_4x3_chi16", "square_4x2_chi8", "full_n8_chi8", "chain_n10_chi8_ob3"])
+                                  "j1j2_snake_4x3_chi16", "square_4x2_chi8", "full_n8_chi8", "chain_n10_chi8_ob3",
+                                  "chain_n10_chi8_break"])
 def test_oracle_matches_reference_runs(name):
     g = gc.load(name)
     ob, A, info = _run(name)

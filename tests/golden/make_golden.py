@@ -20,6 +20,7 @@ Cases (all with the reference's own ``dmrg_finite_size`` from DMRG_anyH.py:18,
 * ``longrange_n8_chi8``    'longRange' lattice (all-to-all couplings)
 * ``j1j2_snake_4x3_chi16`` J1-J2 square lattice (J2 = 0.5) in snake order, 'arbitrary' lattice, hz field
   (``python tests/golden/make_golden.py j1j2_snake_4x3_chi16`` runs this case alone)
+* ``chain_n10_chi16_pbc``  Heisenberg chain with periodic boundary (bond (0, 9) straddles every site), fields
 * ``chain_n10_chi8_break`` XXZ chain (Jz = 1.3) with fields, observed every 2nd sweep, stopped by break_tol=1e-9
 * ``chain_n10_chi8_ob3``   XXZ chain (Jz = 0.7) with fields, sweeps starting from site 3 (``ob_position``)
 * ``full_n8_chi8``         the reference's 'full' lattice (all-to-all Ising couplings, transverse field hx=0.5)
@@ -139,6 +140,12 @@ def chain_para(l, chi, jxy, jz, hx, hz, sweeps):
     return pm.make_consistent_parameter_dmrg(para)
 
 
+def chain_para_bc(l, chi, jxy, jz, hx, hz, sweeps, bound_cond):
+    para = pm.generate_parameters_dmrg("chain")
+    para.update(l=l, chi=chi, jxy=jxy, jz=jz, hx=hx, hz=hz, sweep_time=sweeps, bound_cond=bound_cond, **COMMON)
+    return pm.make_consistent_parameter_dmrg(para)
+
+
 def ladder_para(length, chi, j_leg, j_rung, hz, sweeps):
     """2 x length ladder numbered rung by rung: sites (2r, 2r+1) form rung r."""
     para = pm.generate_parameters_dmrg("arbitrary")
@@ -232,6 +239,9 @@ EXTRA = {
     "chain_n10_chi8_break": lambda meta: run_case("chain_n10_chi8_break",
                                                   dict(chain_para(10, 8, 1, 1.3, 0.1, 0.25, 40), dt_ob=2,
                                                        break_tol=1e-9), 9, meta),
+    "chain_n10_chi16_pbc": lambda meta: run_case("chain_n10_chi16_pbc",
+                                                 dict(chain_para_bc(10, 16, 1, 1, 0.15, 0.2, 16, "periodic")), 10,
+                                                 meta),
     "chain_n10_chi8_ob3": lambda meta: run_case("chain_n10_chi8_ob3",
                                                 dict(chain_para(10, 8, 1, 0.7, 0.2, 0.3, 12), ob_position=3), 8, meta),
     "square_4x2_chi8": lambda meta: run_case("square_4x2_chi8", square_para(4, 2, 8, 0.0, 0.0, 60), 6, meta),

@@ -62,6 +62,18 @@ def test_square_and_husimi_generators():
     assert full.shape == (10, 2)
 
 
+def test_periodic_chain_generator_reproduces_reference_tables():
+    from tnalg_gb300 import Parameters as pm
+    g, m = gc.load("chain_n10_chi16_pbc"), gc.meta()["chain_n10_chi16_pbc"]
+    para = pm.generate_parameters_dmrg("chain")
+    para.update(l=10, chi=16, jxy=1, jz=1, hx=m["hx"], hz=m["hz"], bound_cond="periodic")
+    para = pm.make_consistent_parameter_dmrg(para)
+    np.testing.assert_array_equal(np.asarray(para["index2"]), g["index2"])
+    np.testing.assert_allclose(np.ravel(para["coeff2"]), g["coeff2"])
+    np.testing.assert_array_equal(np.asarray(para["positions_h2"]), g["positions_h2"])
+    np.testing.assert_allclose(np.stack([np.real(o) for o in para["op"]]), g["op"])
+
+
 def test_square_generator_reproduces_reference_tables():
     from tnalg_gb300 import Parameters as pm
     g, m = gc.load("square_4x2_chi8"), gc.meta()["square_4x2_chi8"]
@@ -153,7 +165,8 @@ def test_open_operator_sets_chain_and_long_range():
 # (the J1-J2 reference run, 40 sweeps, is checked on the GPU; its lattice's host path is covered on the
 # CPU by the 3 x 3 case of test_ed_parity.py)
 @pytest.mark.parametrize("name", ["chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8", "square_4x2_chi8",
-                                  "full_n8_chi8", "chain_n10_chi8_ob3", "chain_n10_chi8_break"])
+                                  "full_n8_chi8", "chain_n10_chi8_ob3", "chain_n10_chi8_break",
+                                  "chain_n10_chi16_pbc"])
 def test_sweep_orchestration_matches_reference(name, fake_backend):
     from tnalg_gb300 import DMRG_anyH
     g, m = gc.load(name), gc.meta()[name]

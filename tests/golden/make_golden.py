@@ -20,6 +20,7 @@ Cases (all with the reference's own ``dmrg_finite_size`` from DMRG_anyH.py:18,
 * ``longrange_n8_chi8``    'longRange' lattice (all-to-all couplings)
 * ``j1j2_snake_4x3_chi16`` J1-J2 square lattice (J2 = 0.5) in snake order, 'arbitrary' lattice, hz field
   (``python tests/golden/make_golden.py j1j2_snake_4x3_chi16`` runs this case alone)
+* ``chain_s1_n8_chi9``     spin-1 Heisenberg chain (d = 3) in a field hz = 0.3
 * ``chain_n10_chi16_pbc``  Heisenberg chain with periodic boundary (bond (0, 9) straddles every site), fields
 * ``chain_n10_chi8_break`` XXZ chain (Jz = 1.3) with fields, observed every 2nd sweep, stopped by break_tol=1e-9
 * ``chain_n10_chi8_ob3``   XXZ chain (Jz = 0.7) with fields, sweeps starting from site 3 (``ob_position``)
@@ -140,6 +141,13 @@ def chain_para(l, chi, jxy, jz, hx, hz, sweeps):
     return pm.make_consistent_parameter_dmrg(para)
 
 
+def chain_s1_para(l, chi, hz, sweeps):
+    """Spin-1 Heisenberg chain (d = 3); the field hz splits the open chain's edge-spin degeneracy."""
+    para = pm.generate_parameters_dmrg("chain")
+    para.update(l=l, chi=chi, spin="one", jxy=1, jz=1, hx=0.0, hz=hz, sweep_time=sweeps, **COMMON)
+    return pm.make_consistent_parameter_dmrg(para)
+
+
 def chain_para_bc(l, chi, jxy, jz, hx, hz, sweeps, bound_cond):
     para = pm.generate_parameters_dmrg("chain")
     para.update(l=l, chi=chi, jxy=jxy, jz=jz, hx=hx, hz=hz, sweep_time=sweeps, bound_cond=bound_cond, **COMMON)
@@ -239,6 +247,7 @@ EXTRA = {
     "chain_n10_chi8_break": lambda meta: run_case("chain_n10_chi8_break",
                                                   dict(chain_para(10, 8, 1, 1.3, 0.1, 0.25, 40), dt_ob=2,
                                                        break_tol=1e-9), 9, meta),
+    "chain_s1_n8_chi9": lambda meta: run_case("chain_s1_n8_chi9", chain_s1_para(8, 9, 0.3, 80), 12, meta),
     "chain_n10_chi16_pbc": lambda meta: run_case("chain_n10_chi16_pbc",
                                                  dict(chain_para_bc(10, 16, 1, 1, 0.15, 0.2, 16, "periodic")), 10,
                                                  meta),

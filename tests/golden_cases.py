@@ -8,7 +8,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 RUN_CASES = ["chain_n12_chi16", "chain_n12_chi16_h", "ladder_2x4_chi8", "jigsaw_s1_n9_chi12", "longrange_n8_chi8"]
 # further reference runs; their GPU parity test is in test_gpu_wider.py
 LATER_CASES = ["j1j2_snake_4x3_chi16", "square_4x2_chi8", "full_n8_chi8", "chain_n10_chi8_ob3",
-               "chain_n10_chi8_break", "chain_n10_chi16_pbc"]
+               "chain_n10_chi8_break", "chain_n10_chi16_pbc", "chain_s1_n8_chi9"]
 
 
 def meta():

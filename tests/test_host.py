@@ -166,7 +166,7 @@ def test_open_operator_sets_chain_and_long_range():
 # CPU by the 3 x 3 case of test_ed_parity.py)
 @pytest.mark.parametrize("name", ["chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8", "square_4x2_chi8",
                                   "full_n8_chi8", "chain_n10_chi8_ob3", "chain_n10_chi8_break",
-                                  "chain_n10_chi16_pbc"])
+                                  "chain_n10_chi16_pbc", "chain_s1_n8_chi9"])
 def test_sweep_orchestration_matches_reference(name, fake_backend):
     from tnalg_gb300 import DMRG_anyH
     g, m = gc.load(name), gc.meta()[name]

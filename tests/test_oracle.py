@@ -21,7 +21,7 @@ def _run(name):
 
 @pytest.mark.parametrize("name", ["chain_n12_chi16", "chain_n12_chi16_h", "ladder_2x4_chi8", "longrange_n8_chi8",
                                   "j1j2_snake_4x3_chi16", "square_4x2_chi8", "full_n8_chi8", "chain_n10_chi8_ob3",
-                                  "chain_n10_chi8_break", "chain_n10_chi16_pbc"])
+                                  "chain_n10_chi8_break", "chain_n10_chi16_pbc", "chain_s1_n8_chi9"])
 def test_oracle_matches_reference_runs(name):
     g = gc.load(name)
     ob, A, info = _run(name)

@@ -171,3 +171,39 @@ def test_command_line_threaded_mix_without_sequential_pass(capsys):
     out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert out["workers"] == 3 and out["jobs"] == 3 and "sequential_solves_per_s" not in out
     assert len(out["e_per_site"]) == 3 and all(v < 0 for v in out["e_per_site"].values())
+
+
+@pytest.mark.parametrize("workers", [1, 3])
+def test_requests_submitted_while_running(workers):
+    """run(wait=True) is a request loop: jobs submitted from another thread while it runs (arrival
+    None: stamped at submission) are admitted and finished, each with its single-job result; the
+    loop returns after close() once everything submitted has finished."""
+    import threading
+    import time as _time
+    alone = {}
+    for j in _jobs():
+        s = serving.Scheduler("cpu", max_active=1)
+        s.submit(j)
+        s.run()
+        alone[j.job_id] = j.result["e_per_site"]
+    sched = serving.Scheduler("cpu", workers=workers)
+    live = _jobs()
+    for j in live:
+        j.arrival = None
+
+    def producer():
+        for j in live:
+            _time.sleep(0.05)
+            sched.submit(j)
+        sched.close()
+
+    t = threading.Thread(target=producer)
+    t.start()
+    done = sched.run(wait=True)
+    t.join()
+    assert sorted(j.job_id for j in done) == [0, 1, 2, 3]
+    for j in done:
+        assert j.result["e_per_site"] == pytest.approx(alone[j.job_id], abs=1e-12)
+        assert j.arrival > 0 and j.finished >= j.admitted >= j.arrival
+    arrivals = [j.arrival for j in sorted(done, key=lambda j: j.job_id)]
+    assert arrivals == sorted(arrivals)

@@ -23,6 +23,7 @@ initialised state is shared by all jobs and is not meant for concurrent host thr
 import argparse
 import contextlib
 import json
+import threading
 import time
 
 import numpy as np
@@ -196,9 +197,38 @@ class Scheduler:
         self.pending = []
         self.done = []
         self.max_concurrent = 0
+        self._lock = threading.Lock()
+        self._closed = False
+        self._t0 = None
 
     def submit(self, job):
-        self.pending.append(job)
+        """Queue a job; safe to call from any thread. While run(wait=True) executes, a job submitted
+        with arrival=None is stamped with its submission time and admitted as slots and memory
+        allow (latency is measured from that time)."""
+        with self._lock:
+            if job.arrival is None and self._t0 is not None:
+                job.arrival = time.perf_counter() - self._t0
+            self.pending.append(job)
+
+    def close(self):
+        """No more submissions: run(wait=True) returns once every submitted job has finished."""
+        with self._lock:
+            self._closed = True
+
+    def _take_new(self, pending):
+        """Submissions made since the last call, merged into the arrival-ordered pending list."""
+        with self._lock:
+            new, self.pending = self.pending, []
+        if new:
+            for j in new:
+                if j.arrival is None:
+                    j.arrival = time.perf_counter() - self._t0
+            pending = sorted(pending + new, key=lambda j: (j.arrival, j.job_id))
+        return pending
+
+    def _open(self, wait):
+        with self._lock:
+            return wait and not self._closed
 
     def _budget(self):
         if self.budget is not None:
@@ -209,16 +239,17 @@ class Scheduler:
             return int(0.8 * free)
         return 1 << 62
 
-    def run(self):
-        """Runs every submitted job; returns the finished jobs in completion order."""
+    def run(self, wait=False):
+        """Runs every submitted job; returns the finished jobs in completion order. wait=True keeps
+        accepting submissions (from other threads) until close() has been called."""
         if self.workers > 1:
-            return self._run_threaded()
+            return self._run_threaded(wait)
         budget = self._budget()
-        pending = sorted(self.pending, key=lambda j: (j.arrival, j.job_id))
-        self.pending = []
+        self._t0 = t0 = time.perf_counter()
+        pending = self._take_new([])
         active, used = [], 0
-        t0 = time.perf_counter()
-        while pending or active:
+        while pending or active or self._open(wait):
+            pending = self._take_new(pending)
             now = time.perf_counter() - t0
             # admit in arrival order while the budget allows (a job larger than the whole budget
             # runs alone)
@@ -233,7 +264,7 @@ class Scheduler:
                 used += fp
             self.max_concurrent = max(self.max_concurrent, len(active))
             if not active:
-                time.sleep(max(0.0, min(pending[0].arrival - now, 0.01)))
+                time.sleep(max(0.0, min(pending[0].arrival - now, 0.01)) if pending else 0.001)
                 continue
             for job in list(active):
                 if job.advance():
@@ -243,20 +274,21 @@ class Scheduler:
                     self.done.append(job)
         return self.done
 
-    def _run_threaded(self):
+    def _run_threaded(self, wait=False):
         """run() with `workers` host threads: admission as in run() (on this thread, which also
         builds each admitted job's MPS, so the global RNG draws stay in admission order); every
         admitted job has one local update (a task) in flight at a time on the pool. The library's
         calls release the GIL, so while one thread waits inside a job's Lanczos convergence check,
         the others run their jobs' host code and queue their kernels on their own streams."""
-        from concurrent.futures import FIRST_COMPLETED, ThreadPoolExecutor, wait
+        from concurrent.futures import FIRST_COMPLETED, ThreadPoolExecutor
+        from concurrent.futures import wait as wait_any
         budget = self._budget()
-        pending = sorted(self.pending, key=lambda j: (j.arrival, j.job_id))
-        self.pending = []
+        self._t0 = t0 = time.perf_counter()
+        pending = self._take_new([])
         active, used, inflight = [], 0, {}
-        t0 = time.perf_counter()
         with ThreadPoolExecutor(max_workers=self.workers) as pool:
-            while pending or active:
+            while pending or active or self._open(wait):
+                pending = self._take_new(pending)
                 now = time.perf_counter() - t0
                 while pending and pending[0].arrival <= now and len(active) < self.max_active:
                     fp = pending[0].footprint_bytes()
@@ -270,11 +302,14 @@ class Scheduler:
                     inflight[pool.submit(job.advance)] = job
                 self.max_concurrent = max(self.max_concurrent, len(active))
                 if not active:
-                    time.sleep(max(0.0, min(pending[0].arrival - now, 0.01)))
+                    time.sleep(max(0.0, min(pending[0].arrival - now, 0.01)) if pending else 0.001)
                     continue
-                # wake up for the next arrival while jobs run
-                wake = max(0.0, min(pending[0].arrival - (time.perf_counter() - t0), 0.01)) if pending else None
-                finished, _ = wait(list(inflight), timeout=wake, return_when=FIRST_COMPLETED)
+                # wake up for the next arrival (or, while open, for new submissions) while jobs run
+                if pending:
+                    wake = max(0.0, min(pending[0].arrival - (time.perf_counter() - t0), 0.01))
+                else:
+                    wake = 0.005 if self._open(wait) else None
+                finished, _ = wait_any(list(inflight), timeout=wake, return_when=FIRST_COMPLETED)
                 for f in finished:
                     job = inflight.pop(f)
                     if f.result():   # a job's exception is raised here

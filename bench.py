@@ -222,7 +222,8 @@ def run_ours(args, rank, world, local_rank):
     e_site = float(np.sum(eb)) / L_
     res = {"ms": ms, "wall": wall, "solves": solves, "matvecs": matvecs, "mv_ms": mv_ms, "mv_cnt": mv_cnt,
            "mv_flops": mv_flops, "qr_ms": qr_ms, "qr_cnt": qr_cnt, "qr_flops": qr_flops, "lz_ms": lz_ms,
-           "lz_cnt": lz_cnt, "precision": precision, "e_per_site": e_site, "clocks": clk.summary(),
+           "lz_cnt": lz_cnt, "precision": precision, "e_per_site": e_site, "eb_full": np.ravel(eb),
+           "clocks": clk.summary(),
            "launches": launches, "chi_max": int(A.virtual_dim.max())}
     return res, A, para
 
@@ -470,6 +471,10 @@ def main():
         line["fp64_path"] = {"value": v64, "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
                              "e_per_site": r64["e_per_site"], "speedup_of_this_line": value / v64,
                              "abs_de_per_site": abs(res["e_per_site"] - r64["e_per_site"]),
+                             # index2 rows per bond: (su, sd), (sd, su), (sz, sz) with Jz = 1
+                             "max_abs_d_szsz": float(np.max(np.abs(res["eb_full"][2::3] - r64["eb_full"][2::3]))),
+                             "max_abs_d_bond_energy": float(np.max(np.abs(
+                                 res["eb_full"].reshape(-1, 3).sum(1) - r64["eb_full"].reshape(-1, 3).sum(1)))),
                              "device_ms_per_sweep": {"qr": r64["qr_ms"] / args.steps,
                                                      "lanczos_incl_matvec": r64["lz_ms"] / args.steps,
                                                      "matvec": r64["mv_ms"] / args.steps}}

@@ -89,7 +89,7 @@ def run(para, precision, schedule, steps, device="cuda", seed=0):
     e = float((np.sum(eb) - para["hx"] * np.sum(mx) - para["hz"] * np.sum(mz)) / l)
     return {"precision": precision, "ms_per_sweep": tm.ms / steps, "sweeps_per_s": 1000.0 * steps / tm.ms,
             "solves_per_s": 1000.0 * solves / tm.ms, "matvecs_per_solve": matvecs / max(solves, 1),
-            "e_per_site": e, "chi_max": int(A.virtual_dim.max())}
+            "e_per_site": e, "chi_max": int(A.virtual_dim.max()), "eb_full": np.ravel(eb)}
 
 
 def straddle_max(para):
@@ -121,12 +121,17 @@ def main(argv=None):
     schedule = [int(x) for x in a.ramp.split(",") if x] + [a.chi]
     out = {"workload": name, "sites": int(para["l"]), "two_body_rows": int(np.asarray(para["index2"]).shape[0]),
            "straddling_terms_max": straddle_max(para), "chi_schedule": schedule, "timed_sweeps": a.steps}
-    out.update(run(para, a.precision, schedule, a.steps, a.device, a.seed))
+    res = run(para, a.precision, schedule, a.steps, a.device, a.seed)
+    eb = res.pop("eb_full")
+    out.update(res)
     if a.compare_fp64 and a.precision != "fp64":
         ref = run(para, "fp64", schedule, a.steps, a.device, a.seed)
+        eb64 = ref.pop("eb_full")
         out["fp64_path"] = ref
         out["speedup_vs_fp64"] = out["sweeps_per_s"] / ref["sweeps_per_s"]
         out["abs_de_per_site_vs_fp64"] = abs(out["e_per_site"] - ref["e_per_site"])
+        # two-body terms: c <op_a(i) op_b(j)> per index2 row; the largest difference over all rows
+        out["max_abs_d_term_energy_vs_fp64"] = float(np.max(np.abs(eb - eb64)))
     print(json.dumps(out), flush=True)
 
 

@@ -9,9 +9,11 @@ the CUDA implementation in ``tnalg_gb300``: only ``tests/``,
 fallback.
 
 Parity pin: the oracle is checked against golden vectors produced by running
-the unmodified reference (``tests/golden/make_golden.py``): five DMRG runs
-(spin-1/2 chains with and without fields, a 2x4 ladder, a spin-1 jigsaw chain,
-an all-to-all long-range chain), the two result pickles shipped with the
-reference, a dense effective Hamiltonian, the docstring examples of the
+the unmodified reference (``tests/golden/make_golden.py``): twelve DMRG runs
+(spin-1/2 chains with and without fields, periodic, started mid-chain and
+stopped early by the convergence test; a spin-1 chain; a 2x4 ladder; a spin-1
+jigsaw chain; all-to-all long-range and fully connected chains; the 'square'
+lattice; a J1-J2 square lattice in snake order), the two result pickles shipped
+with the reference, a dense effective Hamiltonian, the docstring examples of the
 contraction primitives and the reference's exact diagonalisation.
 """

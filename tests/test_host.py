@@ -311,3 +311,20 @@ def test_bench_serving_leg_composes_the_threaded_mix(monkeypatch):
     assert out["threaded"]["max_abs_de_per_site_vs_one_thread"] < 1e-12
     monkeypatch.setattr(bench, "_child_json", lambda cmd, timeout: {"error": "exit 1: x", "command": "c"})
     assert bench.run_serving_leg("fp64") == {"error": "exit 1: x", "command": "c"}
+
+
+def test_chi_schedule_grows_bonds_and_reaches_the_direct_energy(fake_backend):
+    """para['chi_schedule'] (bond growth with seeded noise between sweeps, not in the reference):
+    bonds follow the schedule capped by d^min(b, L-b), and the ramped run ends at the energy of a run
+    started at the final bond dimension (N=12 chain with fields, chi 4 -> 8 -> 16)."""
+    from tnalg_gb300 import DMRG_anyH, Parameters as pm
+    para = pm.generate_parameters_dmrg("chain")
+    para.update(l=12, chi=4, jxy=1.0, jz=0.8, hx=0.2, hz=0.1, sweep_time=8, dt_ob=1, break_tol=-1.0,
+                eigs_tol=1e-12, device="cpu")
+    para = pm.make_consistent_parameter_dmrg(para)
+    np.random.seed(2)
+    ob, A, info, _ = _quiet(DMRG_anyH.dmrg_finite_size, dict(para, chi_schedule=[4, 8, 16]))
+    assert list(A.virtual_dim) == [1, 2, 4, 8, 16, 16, 16, 16, 16, 8, 4, 2, 1]
+    np.random.seed(2)
+    ob16, _, _, _ = _quiet(DMRG_anyH.dmrg_finite_size, dict(para, chi=16))
+    assert abs(ob["e_per_site"] - ob16["e_per_site"]) < 1e-9

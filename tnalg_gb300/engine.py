@@ -103,6 +103,7 @@ class Model:
             if not (0 <= i < Ln and 0 <= j < Ln):
                 raise ValueError("two-body term (%d,%d) outside 0..%d" % (i, j, Ln - 1))
         self._tables = {}
+        self._memo = {}
 
     def n_left(self, b):
         """Carried (non-Hamiltonian) slots of EL[b]."""
@@ -184,6 +185,21 @@ class Model:
         if hit is None:
             hit = L.terms_tensor(terms, self.device)
             self._tables[key] = hit
+        return hit
+
+    def table_lazy(self, key, make):
+        """table(key, make()) with the term list built only when the key is not cached yet."""
+        hit = self._tables.get(key)
+        if hit is None:
+            hit = L.terms_tensor(make(), self.device)
+            self._tables[key] = hit
+        return hit
+
+    def memo(self, key, make):
+        """A per-model cache of host-side plans (the coupling lists are fixed for a model)."""
+        hit = self._memo.get(key)
+        if hit is None:
+            hit = self._memo[key] = make()
         return hit
 
     def opidx(self, key, ops):
@@ -481,12 +497,12 @@ class DeviceMPS:
             return self._update_compressed(b, left=True)
         cl, d, cr = A.shape
         env = self.EL[b]
-        plan = m.left_carry_plan(b)
+        plan = m.memo(("lcp", b), lambda: m.left_carry_plan(b))
         ns = 1 + len(plan)
         lib, st = L.load(), L.stream_handle()
         T = torch.empty((ns, cl * d * cr), dtype=torch.float64, device=self.device)
         W = torch.empty((cl * d, cl * d), dtype=torch.float64, device=self.device)
-        terms, nt = m.table(("wl", b), m.left_block_terms(b))
+        terms, nt = m.table_lazy(("wl", b), lambda: m.left_block_terms(b))
         L.check(lib.tn_assemble_block(0, cl, d, L.ptr(env), L.ptr(m.ops), L.ptr(terms), nt, L.ptr(W), st), "assemble")
         L.gemm(W, A, T[0], cl * d, cr, cl * d, (cl * d, 1), (cr, 1), (cr, 1), precision=self.precision, ws=self.ws)
         carry = [(k, s) for k, (kind, s) in enumerate(plan) if kind == "carry"]
@@ -494,7 +510,7 @@ class DeviceMPS:
         if carry:
             # T[1+k] = EL[b][slot] . A(cl, d*cr); slots gathered into a contiguous stack first
             g = torch.empty((len(carry), cl, cl), dtype=torch.float64, device=self.device)
-            gt, ng = m.table(("lg", b), [(s, q, 1.0) for q, (_, s) in enumerate(carry)])
+            gt, ng = m.table_lazy(("lg", b), lambda: [(s, q, 1.0) for q, (_, s) in enumerate(carry)])
             L.check(lib.tn_combine_slots(cl, L.ptr(env), L.ptr(gt), ng, len(carry), L.ptr(g), st), "gather")
             ks = [k for k, _ in carry]
             if ks == list(range(ks[0], ks[0] + len(ks))):
@@ -522,12 +538,12 @@ class DeviceMPS:
             return self._update_compressed(b, left=False)
         cl, d, cr = B.shape
         env = self.ER[b + 1]
-        plan = m.right_carry_plan(b)
+        plan = m.memo(("rcp", b), lambda: m.right_carry_plan(b))
         ns = 1 + len(plan)
         lib, st = L.load(), L.stream_handle()
         T = torch.empty((ns, cl * d * cr), dtype=torch.float64, device=self.device)
         W = torch.empty((d * cr, d * cr), dtype=torch.float64, device=self.device)
-        terms, nt = m.table(("wrf", b), m.right_block_terms(b, with_site=True))
+        terms, nt = m.table_lazy(("wrf", b), lambda: m.right_block_terms(b, with_site=True))
         L.check(lib.tn_assemble_block(1, cr, d, L.ptr(env), L.ptr(m.ops), L.ptr(terms), nt, L.ptr(W), st), "assemble")
         # T0 = B(cl, d*cr) . W^T
         L.gemm(B, W, T[0], cl, d * cr, d * cr, (d * cr, 1), (1, d * cr), (d * cr, 1), precision=self.precision,
@@ -536,7 +552,7 @@ class DeviceMPS:
         fresh = [(k, a) for k, (kind, a) in enumerate(plan) if kind == "fresh"]
         if carry:
             g = torch.empty((len(carry), cr, cr), dtype=torch.float64, device=self.device)
-            gt, ng = m.table(("rg", b), [(s, q, 1.0) for q, (_, s) in enumerate(carry)])
+            gt, ng = m.table_lazy(("rg", b), lambda: [(s, q, 1.0) for q, (_, s) in enumerate(carry)])
             L.check(lib.tn_combine_slots(cr, L.ptr(env), L.ptr(gt), ng, len(carry), L.ptr(g), st), "gather")
             ks = [k for k, _ in carry]
             if ks == list(range(ks[0], ks[0] + len(ks))):
@@ -577,14 +593,14 @@ class DeviceMPS:
         T = torch.empty((ns, cl * d * cr), dtype=torch.float64, device=self.device)
         if left:
             W = torch.empty((cl * d, cl * d), dtype=torch.float64, device=self.device)
-            terms, nt = m.table(("wl", b), m.left_block_terms(b))
+            terms, nt = m.table_lazy(("wl", b), lambda: m.left_block_terms(b))
             L.check(lib.tn_assemble_block(0, cl, d, L.ptr(env), L.ptr(m.ops), L.ptr(terms), nt, L.ptr(W), st),
                     "assemble")
             L.gemm(W, A, T[0], cl * d, cr, cl * d, (cl * d, 1), (cr, 1), (cr, 1), precision=self.precision,
                    ws=self.ws)
         else:
             W = torch.empty((d * cr, d * cr), dtype=torch.float64, device=self.device)
-            terms, nt = m.table(("wrf", b), m.right_block_terms(b, with_site=True))
+            terms, nt = m.table_lazy(("wrf", b), lambda: m.right_block_terms(b, with_site=True))
             L.check(lib.tn_assemble_block(1, cr, d, L.ptr(env), L.ptr(m.ops), L.ptr(terms), nt, L.ptr(W), st),
                     "assemble")
             L.gemm(A, W, T[0], cl, d * cr, d * cr, (d * cr, 1), (1, d * cr), (d * cr, 1), precision=self.precision,
@@ -766,9 +782,9 @@ class DeviceMPS:
         el, er = self.EL[p], self.ER[p + 1]
         wl = torch.empty((cl * d, cl * d), dtype=torch.float64, device=self.device)
         wr = torch.empty((d * cr, d * cr), dtype=torch.float64, device=self.device)
-        t, nt = m.table(("wl", p), m.left_block_terms(p))
+        t, nt = m.table_lazy(("wl", p), lambda: m.left_block_terms(p))
         L.check(lib.tn_assemble_block(0, cl, d, L.ptr(el), L.ptr(m.ops), L.ptr(t), nt, L.ptr(wl), st), "assemble")
-        t, nt = m.table(("wr", p), m.right_block_terms(p, with_site=False))
+        t, nt = m.table_lazy(("wr", p), lambda: m.right_block_terms(p, with_site=False))
         L.check(lib.tn_assemble_block(1, cr, d, L.ptr(er), L.ptr(m.ops), L.ptr(t), nt, L.ptr(wr), st), "assemble")
         keep = [wl, wr]
         sl = sr = None
@@ -783,7 +799,7 @@ class DeviceMPS:
                 L.gemm(cR, er[1:], sr, ng, cr * cr, rr, (rr, 1), (cr * cr, 1), (cr * cr, 1), ws=self.ws)
                 keep += [sl, sr]
         else:
-            slt, srt, ng = m.straddle_groups(p)
+            slt, srt, ng = m.memo(("sg", p), lambda: m.straddle_groups(p))
         if ng and not m.compressed:
             sl = torch.empty((ng, cl, cl), dtype=torch.float64, device=self.device)
             sr = torch.empty((ng, cr, cr), dtype=torch.float64, device=self.device)

@@ -5,7 +5,7 @@
  * is MpsOpenBoundaryClass (MPSClass.py:26-1098) driven by dmrg_finite_size
  * (DMRG_anyH.py:18-101). Each entry point below replaces a numpy/scipy step of
  * that path, cited as file:line. The Python host (tnalg_gb300/MPSClass.py) binds
- * these functions with ctypes; INTEGRATION.md shows the binding.
+ * these functions with ctypes (tnalg_gb300/_lib.py).
  *
  * Conventions
  *  - All pointers except descriptor/option structs are DEVICE pointers owned by the
@@ -19,8 +19,14 @@
  *    stream and workspaces (a multi-job host runs one job per thread). The library's
  *    shared host state (launch counter, FP64-QR graph cache, lazily resolved entry
  *    points) is synchronised. Process-wide and not for concurrent use: the profiler
- *    (tn_profile_*), tn_qr_use_graphs, and the device error word read by
- *    tn_check_device_status, which all streams share.
+ *    (tn_profile_*) and tn_qr_use_graphs.
+ *  - Devices: every call works on the CURRENT device (cudaSetDevice); `stream` and all
+ *    pointers must belong to it. Per-device state (SM count, kernel attributes, QR
+ *    capture streams and graphs) is set up for each device on first use there.
+ *  - Device errors (bounded waits that gave up, operands outside FP32 range) are
+ *    recorded in an error word of the stream the failing kernel ran on, and reported
+ *    by the next tn_check_device_status / tn_lanczos convergence check on that stream:
+ *    jobs on their own streams never see or clear each other's errors.
  *  - Tensors are row-major FP64. An MPS site tensor is (chi_l, d, chi_r); an
  *    environment is (chi, chi) indexed [bra, ket] (TensorBasicModule.py:530-619).
  *  - Strides are in elements.
@@ -143,14 +149,17 @@ typedef struct {
   int32_t max_restarts;
   int32_t check_every;  /* steps between host convergence checks */
   int32_t precision;    /* matvec precision */
-  int32_t refine;       /* 1: FP64 residual + Rayleigh quotient of the final vector */
-  int32_t reserved;
+  int32_t refine;       /* 1: FP64 residual + Rayleigh quotient of the final vector;
+                           2 (TF32X3): refine the vector itself: after the split-TF32 iteration
+                           reaches mixed_floor, restart cycles that open with an FP64 matvec run
+                           until the FP64 residual meets the FP64 tolerance (energy = FP64 x.Hx) */
+  int32_t refine_cycles; /* refine == 2: at most this many FP64-opened cycles (0 = 4) */
 } tn_lanczos_opts;
 
 typedef struct {
   double energy;        /* Ritz value of H_eff */
   double residual;      /* ||H x - energy x|| (estimate, or FP64 value when refined) */
-  double energy_fp64;   /* FP64 Rayleigh quotient x.Hx (refine == 1) */
+  double energy_fp64;   /* FP64 Rayleigh quotient x.Hx (refine == 1 or 2) */
   int32_t matvecs;
   int32_t restarts;
   int32_t converged;
@@ -236,6 +245,59 @@ typedef struct tn_sv_item {
 int tn_singular_values_batched(int count, const tn_sv_item* items, double tol, int max_sweeps, void* ws,
                                size_t ws_bytes, void* stream);
 size_t tn_singular_values_batched_workspace_bytes(int count, const tn_sv_item* items);
+
+/* ---- grouped contractions (many independent jobs per launch) --------------------------- */
+/*
+ * One contraction of a group: C = alpha * sum_r A_r . B_r + beta * C (accumulate == 0; the problem
+ * must then be the only writer of its C in the call), or C += alpha * sum_r A_r . B_r added
+ * atomically (accumulate == 1; several problems may add into one C).
+ * A_r(m, k) = A[r*sAr + m*sAm + k*sAk], B_r(k, n) = B[r*sBr + k*sBk + n*sBn], C(m, n) = C[m*sCm + n*sCn].
+ * active: DEVICE int32 flag or NULL; the problem is skipped when *active == 0 at launch time.
+ * These are the per-job np.dot calls of a local update (MPSClass.py:755-776, transfer
+ * contractions TensorBasicModule.py:530-619, R-absorb :387-424) of many independent jobs.
+ */
+typedef struct {
+  int32_t M, N, K, nred;
+  const double* A; int64_t sAm, sAk, sAr;
+  const double* B; int64_t sBk, sBn, sBr;
+  double* C; int64_t sCm, sCn;
+  double alpha, beta;
+  int32_t accumulate, reserved;
+  const int32_t* active;
+} tn_grouped_gemm_problem;
+
+/*
+ * Every problem of a HOST table in one grouped launch. TN_PREC_TF32X3: operands staged as split-TF32
+ * tiles (one launch), then one persistent tcgen05 launch over all output tiles; TN_PREC_FP64:
+ * CUDA-core FP64 tiles. ws: DEVICE scratch of tn_grouped_gemm_workspace_bytes bytes (tables and
+ * staged operands). No counterpart in the reference, which runs these products one at a time.
+ */
+int tn_grouped_gemm(int precision, const tn_grouped_gemm_problem* problems, int count, void* ws, size_t ws_bytes,
+                    void* stream);
+size_t tn_grouped_gemm_workspace_bytes(int precision, const tn_grouped_gemm_problem* problems, int count);
+
+/* ---- batched local solves -------------------------------------------------------------- */
+/* One job of a batched solve: its effective Hamiltonian and its start / result vectors. */
+typedef struct {
+  tn_site_desc site;       /* WL, WR (straddling pairs not supported here: nstr must be 0) */
+  const double* psi_in;    /* DEVICE start vector, chil*d*chir values */
+  double* psi_out;         /* DEVICE unit eigenvector (may equal psi_in) */
+} tn_batch_solve;
+
+/*
+ * The lowest eigenpair of every job's effective Hamiltonian, all jobs advanced together: the
+ * eigsh of update_tensor_eigs (MPSClass.py:778-809) for many independent DMRG jobs. Lanczos with
+ * classical Gram-Schmidt applied twice, as tn_lanczos; one grouped matvec launch (split TF32 or
+ * FP64 by opts->precision) and grouped vector kernels per step for all jobs, the tridiagonal
+ * eigenpairs and the convergence test on the device (one warp per job); the host reads one
+ * counter per check (opts->check_every steps). max_krylov <= 64; refine must be 0 or 1 (1 is
+ * accepted and ignored: energy_fp64 = energy). jobs and results are HOST arrays; ws is DEVICE
+ * scratch of tn_batched_lanczos_workspace_bytes bytes. Returns TN_ERR_NOCONV if any job hit the
+ * restart limit (its last Ritz vector is written). results[i].matvecs counts the batch's steps.
+ */
+int tn_batched_lanczos(const tn_batch_solve* jobs, int count, const tn_lanczos_opts* opts, void* ws,
+                       size_t ws_bytes, tn_lanczos_result* results, void* stream);
+size_t tn_batched_lanczos_workspace_bytes(const tn_batch_solve* jobs, int count, const tn_lanczos_opts* opts);
 
 /* ---- profiling ----------------------------------------------------------------------- */
 /* CUDA-event timing of kernel classes on their launching stream (0 = effective-Hamiltonian

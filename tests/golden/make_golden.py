@@ -1,9 +1,9 @@
 """Generate the golden fixtures in this directory from the unmodified reference.
 
-Run by hand where the T-Nalg sources are mounted (``TNALG_REFERENCE``, default
-``/root/reference``)::
+Run by hand where the T-Nalg sources are mounted, with ``TNALG_REFERENCE`` set to their
+directory (required)::
 
-    python tests/golden/make_golden.py
+    TNALG_REFERENCE=<path to T-Nalg> python tests/golden/make_golden.py
 
 It imports the reference through ``ref_shim`` (compatibility patches only) and
 writes small ``.npz``/``.json`` files that the test suite reads; the tests never

@@ -1,8 +1,9 @@
 """Coupling tables of the reference's 'husimi' lattice (library/Parameters.py, package layout).
 
-Run by hand where the T-Nalg sources are mounted (``TNALG_REFERENCE``, default ``/root/reference``)::
+Run by hand where the T-Nalg sources are mounted, with ``TNALG_REFERENCE`` set to their directory
+(required)::
 
-    python tests/golden/make_husimi_tables.py
+    TNALG_REFERENCE=<path to T-Nalg> python tests/golden/make_husimi_tables.py
 
 The package layout's plotting imports are stubbed by ``ref_shim.install_package_layout``. Writes ``husimi_tables.npz`` for depths 2 and 3.
 """

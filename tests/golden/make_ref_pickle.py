@@ -1,9 +1,9 @@
 """Write a result file with the reference's own ``save_pr`` (BasicFunctionsSJR.py:25-50).
 
-Run by hand where the T-Nalg sources are mounted (``TNALG_REFERENCE``, default
-``/root/reference``)::
+Run by hand where the T-Nalg sources are mounted, with ``TNALG_REFERENCE`` set to their
+directory (required)::
 
-    python tests/golden/make_ref_pickle.py
+    TNALG_REFERENCE=<path to T-Nalg> python tests/golden/make_ref_pickle.py
 
 It runs the unmodified reference ``dmrg_finite_size`` (DMRG_anyH.py:18) on an N=8
 spin-1/2 XXZ chain (Jz = 0.6) with fields (chi=8, 6 sweeps, seed 4) through ``ref_shim`` and saves

@@ -21,7 +21,9 @@ import types
 
 import numpy as np
 
-REF_ROOT = os.environ.get("TNALG_REFERENCE", "/root/reference")
+REF_ROOT = os.environ.get("TNALG_REFERENCE")
+if not REF_ROOT:
+    raise RuntimeError("set TNALG_REFERENCE to the directory of the T-Nalg sources")
 
 
 def install():

@@ -138,6 +138,28 @@ def test_singular_values_match_numpy(cuda_lib):
         np.testing.assert_allclose(s, ref, atol=1e-13 * ref[0], rtol=1e-11)
 
 
+def test_singular_values_stop_on_rank_deficient_rows(cuda_lib):
+    """More rows than columns (48 x 40): 8 rows end up numerically null and rounding noise keeps
+    them from ever becoming orthogonal; the null-row test must let the sweeps stop well before
+    max_sweeps (square cases of this size take 15-20 sweeps), so 25 sweeps return TN_OK. With one
+    sweep allowed the call reports TN_ERR_NOCONV and still writes the values."""
+    lib = L.load()
+    k, n = 48, 40
+    X = _rand(k, n, seed=11)
+    out = torch.empty(k, dtype=torch.float64, device=_dev())
+    ws = L.Workspace(_dev())
+    wp, wb = ws.args(lib.tn_singular_values_workspace_bytes(k, n))
+    st = lib.tn_singular_values(k, n, L.ptr(X), n, 1, L.ptr(out), 1e-15, 25, wp, wb, L.stream_handle())
+    assert st == L.TN_OK, lib.tn_last_error()
+    s = np.sort(out.cpu().numpy())[::-1]
+    ref = np.linalg.svd(X.cpu().numpy(), compute_uv=False)
+    np.testing.assert_allclose(s[:n], ref, atol=1e-13 * ref[0], rtol=1e-11)
+    assert np.all(s[n:] <= 1e-12 * ref[0])
+    st = lib.tn_singular_values(k, n, L.ptr(X), n, 1, L.ptr(out), 1e-15, 1, wp, wb, L.stream_handle())
+    assert st == L.TN_ERR_NOCONV
+    assert np.all(np.isfinite(out.cpu().numpy()))
+
+
 def test_singular_values_batched_match_numpy(cuda_lib):
     """One batched call over matrices of different shapes (an odd row count, a transposed view,
     a 512 x 512 bond matrix), to 1e-13 of each matrix's largest value."""

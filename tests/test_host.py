@@ -328,3 +328,45 @@ def test_chi_schedule_grows_bonds_and_reaches_the_direct_energy(fake_backend):
     np.random.seed(2)
     ob16, _, _, _ = _quiet(DMRG_anyH.dmrg_finite_size, dict(para, chi=16))
     assert abs(ob["e_per_site"] - ob16["e_per_site"]) < 1e-9
+
+
+# -- device selection ---------------------------------------------------------------------
+
+
+def test_methods_run_with_the_mps_device_current(monkeypatch):
+    """Every C-ABI call works on the current device and its current stream: an MPS on cuda:1 used
+    while cuda:0 is current must make cuda:1 current for the call (and only then)."""
+    import torch
+
+    from tnalg_gb300 import MPSClass
+    from tnalg_gb300 import _lib as L
+
+    entered = []
+
+    class Recorder:
+        def __init__(self, dev):
+            self.dev = dev
+
+        def __enter__(self):
+            entered.append(torch.device(self.dev))
+
+        def __exit__(self, *exc):
+            return False
+
+    monkeypatch.setattr(torch.cuda, "current_device", lambda: 0)
+    monkeypatch.setattr(torch.cuda, "device", Recorder)
+    monkeypatch.setattr(L, "_host_test", False)
+
+    class Stub:
+        def __init__(self, dev):
+            self._dev = type("D", (), {"device": torch.device(dev)})()
+
+        @MPSClass.on_device
+        def work(self):
+            return "ran"
+
+    assert Stub("cuda:1").work() == "ran"
+    assert entered == [torch.device("cuda:1")]
+    assert Stub("cuda:0").work() == "ran"   # already current: no switch
+    assert Stub("cpu").work() == "ran"
+    assert entered == [torch.device("cuda:1")]

@@ -44,6 +44,12 @@ def test_noalloc_matches_workspace_version_twice(cuda_lib):
         second = _no_alloc(lib, x, k, n, sr, sc)
         np.testing.assert_allclose(first, ref, atol=1e-13 * ref[0], rtol=1e-11)
         np.testing.assert_allclose(second, ref, atol=1e-13 * ref[0], rtol=1e-11)
+        # and against LAPACK on the host: the k x n matrix the strides describe
+        xh = torch.as_strided(x, (k, n), (sr, sc)).cpu().numpy()
+        lapack = np.linalg.svd(xh, compute_uv=False)
+        np.testing.assert_allclose(second[: lapack.size], lapack, atol=1e-13 * lapack[0], rtol=1e-10)
+        if k > lapack.size:   # k > n: the surplus rows of the rotated matrix carry zero norm
+            assert np.all(second[lapack.size:] <= 1e-12 * lapack[0])
 
 
 def test_noalloc_rejects_sizes_beyond_the_static_scratch(cuda_lib):

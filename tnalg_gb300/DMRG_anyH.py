@@ -28,7 +28,8 @@ def dmrg_finite_size(para=None):
             device=para.get("device", "cuda"), precision=para.get("precision", "fp64"))
     for key, name in (("lanczos_krylov", "max_krylov"), ("lanczos_tol_cap", "tol_cap"),
                       ("lanczos_restarts", "max_restarts"), ("lanczos_check_every", "check_every"),
-                      ("lanczos_mixed_floor", "mixed_floor"), ("lanczos_refine", "refine")):
+                      ("lanczos_mixed_floor", "mixed_floor"), ("lanczos_refine", "refine"),
+                      ("lanczos_refine_cycles", "refine_cycles")):
         if key in para:
             A.lanczos[name] = para[key]
     A.coupling_compress = para.get("mpo_compress", False)
@@ -48,6 +49,7 @@ def dmrg_finite_size(para=None):
         if schedule:
             A.grow_bond_dimension(int(schedule[min(t, len(schedule) - 1)]), noise=para.get("chi_noise", 1e-3),
                                   seed=t)
+        A.refine_vectors = refine_sweep(para, t, info["convergence"])
         if_ob = ((t + 1) % para["dt_ob"] == 0) or t == (para["sweep_time"] - 1)
         if if_ob:
             print("In the %d-th round of sweep ..." % (t + 1))
@@ -90,6 +92,28 @@ def dmrg_finite_size(para=None):
     print("Simulation finished in %g seconds" % info["t_cost"])
     A.clean_to_save()
     return ob, A, info, para
+
+
+def refine_sweep(para, t, convergence):
+    """Whether the local solves of sweep t refine their vectors to the FP64 tolerance (split-TF32
+    path only; the FP64 path always solves to it). para['mixed_refine']: 'off' (default) lets the
+    local solves stop at the split-TF32 floor; 'final' refines the last para['mixed_refine_sweeps']
+    (1) sweeps of the schedule, and every sweep once the observed change of the energy per site is
+    below 100 x break_tol; 'all' every sweep. On GB300 the refinement does not make the returned
+    state more accurate: the effective Hamiltonian is assembled from environments contracted in
+    split TF32, whose error (~1e-5 of the energy per site on an N=100 chain) a tighter local solve
+    cannot remove, while the state's energy error stays second order (~1e-10 per site)."""
+    mode = para.get("mixed_refine", "off")
+    if mode == "all":
+        return True
+    if mode in ("off", None, False):
+        return False
+    if mode != "final":
+        raise ValueError("mixed_refine must be 'final', 'all' or 'off'")
+    if t >= para["sweep_time"] - int(para.get("mixed_refine_sweeps", 1)):
+        return True
+    bt = float(para.get("break_tol", -1.0))
+    return bt > 0 and convergence < 100.0 * bt
 
 
 def positions_set2array(pos_set):

@@ -22,6 +22,7 @@ Differences a user can observe:
     library/MPSClass.py:994-999) also works at the orthogonality centre.
 """
 import contextvars
+import functools
 
 import numpy as np
 import torch
@@ -32,6 +33,21 @@ from .HamiltonianModule import spin_operators
 
 # device for MPS objects restored from a reference result file (set by BasicFunctionsSJR.load_pr)
 LOAD_DEVICE = contextvars.ContextVar("tnalg_load_device", default="cuda")
+
+
+def on_device(fn):
+    """Run a method with the MPS's device current. Every C-ABI call works on the current device
+    and launches on its current stream, so an MPS on cuda:1 used while cuda:0 is current would
+    otherwise queue kernels on a cuda:0 stream with cuda:1 pointers."""
+    @functools.wraps(fn)
+    def wrapper(self, *args, **kwargs):
+        dev = self._dev.device
+        if dev.type == "cuda" and dev.index is not None and not L._host_test and \
+                dev.index != torch.cuda.current_device():
+            with torch.cuda.device(dev):
+                return fn(self, *args, **kwargs)
+        return fn(self, *args, **kwargs)
+    return wrapper
 
 
 def random_open_mps(l, d, chi):
@@ -96,8 +112,12 @@ class MpsOpenBoundaryClass(MpsBasic):
         # "last" = only for solves flagged with refine_next_solve() (dmrg_finite_size flags the last
         # solve of every sweep)
         self.lanczos = {"max_krylov": 40, "max_restarts": 50, "check_every": 3, "tol_cap": 0.0,
-                        "mixed_floor": 2e-6, "refine": "last"}
+                        "mixed_floor": 2e-6, "refine": "last", "refine_cycles": 4}
         self._refine_next = False
+        # split-TF32 path: when set, every local solve refines its vector to the FP64 tolerance
+        # (restart cycles opened by an FP64 matvec, refine == 2 of tn_lanczos); dmrg_finite_size
+        # sets it for the final sweeps, whose local solves fix the accuracy of the returned state
+        self.refine_vectors = False
         self.last_solve = None
         # two-body couplings: False carries one operator per open (site, op) as the reference does;
         # True carries rank-compressed combinations (engine.CompressedModel); "auto" picks the
@@ -137,6 +157,7 @@ class MpsOpenBoundaryClass(MpsBasic):
     def precision(self):
         return {v: k for k, v in L.PRECISIONS.items() if k in ("fp64", "tf32x3")}[self._dev.precision]
 
+    @on_device
     def set_precision(self, precision):
         self._dev.precision = L.PRECISIONS[precision]
         self._dev.set_model(None)
@@ -147,6 +168,7 @@ class MpsOpenBoundaryClass(MpsBasic):
         return self._dev.stats
 
     # -- gauge -------------------------------------------------------------------
+    @on_device
     def orthogonalize_mps(self, l0, l1):
         """MPSClass.py:143-167 (QR moves; 'svd' moves also record the Schmidt values)."""
         if self.decomp_way == "svd":
@@ -154,6 +176,7 @@ class MpsOpenBoundaryClass(MpsBasic):
         else:
             self._dev.orthogonalize_mps(l0, l1)
 
+    @on_device
     def central_orthogonalization(self, lc, l0=0, l1=-1):
         """MPSClass.py:170-185."""
         if l1 == -1:
@@ -162,6 +185,7 @@ class MpsOpenBoundaryClass(MpsBasic):
         self.orthogonalize_mps(l1, lc)
         self._dev.center = lc
 
+    @on_device
     def correct_orthogonal_center(self, p=-1):
         """MPSClass.py:188-198."""
         if p < -0.5 and self.center < -0.5:
@@ -215,6 +239,7 @@ class MpsOpenBoundaryClass(MpsBasic):
             dev.orthogonality[l1 + 1:l0 + 1] = 1
             dev.orthogonality[l1] = 0
 
+    @on_device
     def grow_bond_dimension(self, chi_new, noise=1e-3, seed=0):
         """Enlarge all bonds to chi_new (capped by d^b) with seeded noise and re-centre the MPS at
         its previous centre (or 0). Not in the reference, whose chi is fixed; used by
@@ -248,6 +273,7 @@ class MpsOpenBoundaryClass(MpsBasic):
             self._model_key = key
         return self._dev.model
 
+    @on_device
     def update_tensor_eigs(self, p, index1, index2, coeff1, coeff2, tau, is_real, tol=1e-16):
         """MPSClass.py:778-809: move the centre to p and replace site p by the lowest eigenvector
         of its effective Hamiltonian. Returns the eigenvalue of H_eff."""
@@ -260,10 +286,12 @@ class MpsOpenBoundaryClass(MpsBasic):
         refine = o["refine"]
         if refine == "last":  # FP64 Rayleigh quotient only when the caller marks the solve
             refine = 1 if self._refine_next else 0
+        if self.refine_vectors and self._dev.precision == L.PREC_TF32X3:
+            refine = 2
         self._refine_next = False
         res = self._dev.solve(p, tol, tau, tol_cap=o["tol_cap"], max_krylov=o["max_krylov"],
                               max_restarts=o["max_restarts"], check_every=o["check_every"], refine=refine,
-                              mixed_floor=o["mixed_floor"])
+                              mixed_floor=o["mixed_floor"], refine_cycles=o.get("refine_cycles", 4))
         self.last_solve = res
         e = res.energy_fp64 if res.energy_fp64 != 0.0 or res.energy == 0.0 else res.energy
         self.solve_energies.append(e)
@@ -273,6 +301,7 @@ class MpsOpenBoundaryClass(MpsBasic):
         """Have the next update_tensor_eigs end with an FP64 residual and Rayleigh quotient."""
         self._refine_next = True
 
+    @on_device
     def effective_hamiltonian_dmrg(self, p, index1, index2, coeff1, coeff2, tol=1e-12):
         """Dense H_eff at the centre p (MPSClass.py:532-580), built column by column with
         tn_matvec; only for small bond dimensions."""
@@ -290,12 +319,14 @@ class MpsOpenBoundaryClass(MpsBasic):
         if self._dev.model is None:
             self._dev.set_model(E.Model(self.length, self.phys_dim, self.operators, [], [], self._dev.device))
 
+    @on_device
     def observe_magnetization(self, sn):
         """MPSClass.py:911-921: <operators[sn]> on every site, shape (length, 1)."""
         self._ensure_obs_model()
         v1, _ = E.observe(self._dev, [(i, sn) for i in range(self.length)], [])
         return v1.reshape(-1, 1)
 
+    @on_device
     def observe_bond_energy(self, index2, coeff2):
         """MPSClass.py:923-934: coeff * <op_i op_j> for every row of index2, shape (nh, 1)."""
         self._ensure_obs_model()
@@ -304,17 +335,20 @@ class MpsOpenBoundaryClass(MpsBasic):
         _, v2 = E.observe(self._dev, [], [tuple(int(x) for x in r) for r in idx])
         return (c2 * v2).reshape(-1, 1)
 
+    @on_device
     def observation_s1(self, inputs):
         sn, position = inputs
         self._ensure_obs_model()
         return float(E.observe(self._dev, [(int(position), int(sn))], [])[0][0])
 
+    @on_device
     def observation_s1_s2(self, inputs):
         ssn, positions = inputs
         self._ensure_obs_model()
         q = (int(positions[0]), int(positions[1]), int(ssn[0]), int(ssn[1]))
         return float(E.observe(self._dev, [], [q])[1][0])
 
+    @on_device
     def observe_correlators_from_middle(self, op1, op2, ob_len=None):
         """MPSClass.py:936-952 (Python round() of length/2 for the middle site)."""
         self._ensure_obs_model()
@@ -338,6 +372,7 @@ class MpsOpenBoundaryClass(MpsBasic):
         # correlations); energies and one-site observables stay FP64
         return E.observe(self._dev, [], pairs, precision=self._dev.precision)[1]
 
+    @on_device
     def calculate_entanglement_spectrum(self, if_fast=True):
         """MPSClass.py:812-832: moves to the ends and back fill lm. The reference takes an SVD at
         every move of the three passes; the spectra do not depend on the pass, and the middle
@@ -374,6 +409,7 @@ class MpsOpenBoundaryClass(MpsBasic):
         for i in range(self.length - 1):
             self.ent[i] = -1 if self.lm[i].size == 0 else entanglement_entropy(self.lm[i])
 
+    @on_device
     def reduced_density_matrix_two_body(self, p1, p2):
         """MPSClass.py:841-855: the (d^2, d^2) reduced density matrix of sites p1, p2 with trace 1,
         rho[(s1 s2), (s1' s2')] = sum_rest psi*(.. s1 .. s2 ..) psi(.. s1' .. s2' ..), computed on the
@@ -402,12 +438,14 @@ class MpsOpenBoundaryClass(MpsBasic):
             out.append(rho / np.trace(rho))
         return out
 
+    @on_device
     def reduced_density_matrix_one_body(self, p):
         """library/MPSClass.py:994-999: the (d, d) density matrix of site p, symmetrised (rho + rho^T)
         and normalised to trace 1, computed on the device. The reference's version fails when p is
         the orthogonality centre (its transfer from the centre to p is empty); here any site works."""
         return self._site_rhos([p])[0]
 
+    @on_device
     def calculate_onsite_entanglement_entropy(self):
         """library/MPSClass.py:1001-1038: (ent, rho) with rho[n] the one-site density matrix of site n
         (as reduced_density_matrix_one_body) and ent[n] = -sum lm ln lm over its eigenvalues > 1e-25."""
@@ -419,6 +457,7 @@ class MpsOpenBoundaryClass(MpsBasic):
             ent[n] = -np.inner(lm, np.log(lm))
         return ent, rho
 
+    @on_device
     def full_coefficients_mps(self, tol_memory=20):
         """MPSClass.py:968-985: all d^L amplitudes psi[s_0 ... s_(L-1)] (s_0 slowest) as a (d^L, 1)
         array, contracted site by site with tn_gemm. The reference drops the result of its reshape
@@ -439,6 +478,7 @@ class MpsOpenBoundaryClass(MpsBasic):
             x = y.reshape(-1, cr)
         return x.reshape(-1, 1).cpu().numpy()
 
+    @on_device
     def norm_mps(self):
         """MPSClass.py:954-966 (norm of the centre tensor)."""
         if self.center < -0.5:

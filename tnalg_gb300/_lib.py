@@ -41,11 +41,34 @@ class SiteDesc(ctypes.Structure):
 class LanczosOpts(ctypes.Structure):
     _fields_ = [("eigs_tol", c_dbl), ("tau", c_dbl), ("tol_cap", c_dbl), ("mixed_floor", c_dbl),
                 ("max_krylov", ctypes.c_int32), ("max_restarts", ctypes.c_int32), ("check_every", ctypes.c_int32),
-                ("precision", ctypes.c_int32), ("refine", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("precision", ctypes.c_int32), ("refine", ctypes.c_int32), ("refine_cycles", ctypes.c_int32)]
+
+
+class BatchSolve(ctypes.Structure):
+    _fields_ = [("site", SiteDesc), ("psi_in", c_vp), ("psi_out", c_vp)]
 
 
 class SvItem(ctypes.Structure):
     _fields_ = [("k", c_i64), ("n", c_i64), ("x", c_vp), ("sXr", c_i64), ("sXc", c_i64), ("s_out", c_vp)]
+
+
+class GroupedGemmProblem(ctypes.Structure):
+    _fields_ = [("M", ctypes.c_int32), ("N", ctypes.c_int32), ("K", ctypes.c_int32), ("nred", ctypes.c_int32),
+                ("A", c_vp), ("sAm", c_i64), ("sAk", c_i64), ("sAr", c_i64),
+                ("B", c_vp), ("sBk", c_i64), ("sBn", c_i64), ("sBr", c_i64),
+                ("C", c_vp), ("sCm", c_i64), ("sCn", c_i64),
+                ("alpha", c_dbl), ("beta", c_dbl), ("accumulate", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("active", c_vp)]
+
+
+# the same record as a numpy dtype (C layout), for tables built with array operations
+GEMM_PROBLEM_DTYPE = np.dtype([("M", "<i4"), ("N", "<i4"), ("K", "<i4"), ("nred", "<i4"),
+                               ("A", "<u8"), ("sAm", "<i8"), ("sAk", "<i8"), ("sAr", "<i8"),
+                               ("B", "<u8"), ("sBk", "<i8"), ("sBn", "<i8"), ("sBr", "<i8"),
+                               ("C", "<u8"), ("sCm", "<i8"), ("sCn", "<i8"),
+                               ("alpha", "<f8"), ("beta", "<f8"), ("accumulate", "<i4"), ("reserved", "<i4"),
+                               ("active", "<u8")], align=True)
+assert GEMM_PROBLEM_DTYPE.itemsize == ctypes.sizeof(GroupedGemmProblem)
 
 
 class LanczosResult(ctypes.Structure):
@@ -82,6 +105,10 @@ _SIGS = {
     "tn_singular_values_noalloc": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp]),
     "tn_singular_values_batched": (c_int, [c_int, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_batched_workspace_bytes": (c_sz, [c_int, c_vp]),
+    "tn_grouped_gemm": (c_int, [c_int, c_vp, c_int, c_vp, c_sz, c_vp]),
+    "tn_grouped_gemm_workspace_bytes": (c_sz, [c_int, c_vp, c_int]),
+    "tn_batched_lanczos": (c_int, [c_vp, c_int, c_vp, c_vp, c_sz, c_vp, c_vp]),
+    "tn_batched_lanczos_workspace_bytes": (c_sz, [c_vp, c_int, c_vp]),
     "tn_profile_enable": (c_int, [c_int]),
     "tn_profile_reset": (c_int, []),
     "tn_profile_read": (c_int, [c_int, c_vp, c_vp, c_vp]),
@@ -182,6 +209,20 @@ def gemm(A, B, C, M, N, K, sA, sB, sC, *, Cin=None, batch=1, bstrides=(0, 0, 0),
                       rstrides[0], rstrides[1], alpha, beta, wp, wb, stream_handle()), "gemm")
 
 
+def grouped_gemm(table, precision=PREC_TF32X3, ws=None, device=None):
+    """Every problem of `table` (numpy array of GEMM_PROBLEM_DTYPE records) in one grouped call."""
+    lib = load()
+    n = int(table.shape[0])
+    if n == 0:
+        return
+    table = np.ascontiguousarray(table, dtype=GEMM_PROBLEM_DTYPE)
+    tp = c_vp(table.ctypes.data)
+    need = lib.tn_grouped_gemm_workspace_bytes(precision, tp, n)
+    ws = ws or Workspace(device or torch.device("cuda"))
+    wp, wb = ws.args(need)
+    check(lib.tn_grouped_gemm(precision, tp, n, wp, wb, stream_handle()), "grouped gemm")
+
+
 def terms_tensor(terms, device):
     """list of (slot, op, coeff) -> device buffer of tn_block_term structs (16 bytes each)."""
     n = len(terms)
@@ -212,9 +253,13 @@ def singular_values_batched(mats, ws=None, tol=1e-15, max_sweeps=60):
     ws = ws or Workspace(mats[0].device)
     buf = ws.get(need + 256)
     base = (buf.data_ptr() + 255) // 256 * 256
-    check(lib.tn_singular_values_batched(len(mats), table, tol, max_sweeps, c_vp(base),
-                                         c_sz(buf.numel() - (base - buf.data_ptr())), stream_handle()),
-          "singular values")
+    st = lib.tn_singular_values_batched(len(mats), table, tol, max_sweeps, c_vp(base),
+                                        c_sz(buf.numel() - (base - buf.data_ptr())), stream_handle())
+    if st == TN_ERR_NOCONV:   # values written; the last Jacobi sweep still rotated some pair
+        import warnings
+        warnings.warn("singular values: Jacobi not converged after %d sweeps" % max_sweeps)
+    else:
+        check(st, "singular values")
     return [np.sort(o.cpu().numpy())[::-1] for o in outs]
 
 

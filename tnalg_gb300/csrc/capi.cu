@@ -6,7 +6,6 @@
 
 int tn_gemm_tf32x3(const TnGemmF64& g, void* ws, size_t ws_bytes, cudaStream_t s);
 size_t tn_gemm_tf32x3_ws_bytes(int64_t M, int64_t N, int64_t K, int64_t batch, int64_t nred);
-int tn_tf32x3_error_check(cudaStream_t s);
 
 namespace {
 thread_local char g_err[512] = "";
@@ -54,10 +53,9 @@ extern "C" size_t tn_gemm_workspace_bytes(int precision, int64_t M, int64_t N, i
 }
 
 extern "C" int tn_check_device_status(void* stream) {
-  cudaStream_t s = (cudaStream_t)stream;
-  TN_CUDA(cudaStreamSynchronize(s));
-  if (tn_tf32x3_supported()) return tn_tf32x3_error_check(s);
-  return TN_OK;
+  // the error word of this stream on the current device: kernels of other streams (other jobs)
+  // record their failures in their own words
+  return tn_error_check((cudaStream_t)stream);
 }
 
 extern "C" int tn_gemm(int precision, int64_t M, int64_t N, int64_t K, const double* A, int64_t sAm, int64_t sAk,

@@ -14,8 +14,31 @@
 extern std::atomic<unsigned long long> g_tn_launches;
 extern thread_local unsigned long long g_tn_thread_launches;
 
-// Code written into the device error word by the cluster QR when a panel wait times out.
+// Codes written into a device error word: 1-3 name the split-TF32 GEMM pipeline wait that gave
+// up, TN_DEVERR_RANGE a finite operand beyond FP32's range (split TF32 cannot represent it), and
+// TN_DEVERR_QR_WAIT a cluster-QR panel wait that timed out.
+constexpr int TN_DEVERR_RANGE = 16;
 constexpr int TN_DEVERR_QR_WAIT = 32;
+
+// Per-device host state (device_state.cu). Device ordinals 0..TN_MAX_DEVICES-1.
+constexpr int TN_MAX_DEVICES = 64;
+int tn_current_device(int* dev);
+// The error word of stream s on the current device (device memory, zeroed at creation).
+int tn_error_word(cudaStream_t s, int** out);
+// Status for a value h read from stream s's error word; clears the word (on s) when h != 0.
+int tn_error_status(int h, cudaStream_t s);
+// Synchronise s, read and clear its error word.
+int tn_error_check(cudaStream_t s);
+// cudaFuncAttributeMaxDynamicSharedMemorySize = bytes for func, once per device (key: one bit per
+// kernel configuration, TN_ATTR_*).
+int tn_set_smem_attr_once(int key, const void* func, int bytes);
+enum {
+  TN_ATTR_TF32_BN64 = 0,
+  TN_ATTR_TF32_BN128 = 1,
+  TN_ATTR_QR_PANEL_CLUSTER = 2,
+  TN_ATTR_GROUPED_GEMM = 3,
+  TN_ATTR_BATCH_QR = 4,
+};
 #define TN_CHECK_LAUNCH()                                   \
   do {                                                      \
     g_tn_launches.fetch_add(1, std::memory_order_relaxed);  \

@@ -101,21 +101,7 @@ __global__ void splitk_reduce_kernel(TnGemmF64 g, int ksplit, const double* part
   }
 }
 
-std::atomic<int> g_sm_count{0};
-
 }  // namespace
-
-int tn_sm_count() {
-  int c = g_sm_count.load(std::memory_order_relaxed);
-  if (c == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
-    if (c <= 0) c = 152;
-    g_sm_count.store(c, std::memory_order_relaxed);  // every thread computes the same value
-  }
-  return c;
-}
 
 static int gemm_f64_run(const TnGemmF64& g, void* ws, size_t ws_bytes, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return TN_OK;

@@ -21,6 +21,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "tcgen05.cuh"
 
 size_t tn_matvec_fp64_ws_bytes(const tn_site_desc* ds);
 int tn_matvec_fp64_straddle(const tn_site_desc* ds, const double* psi, double* y, double alpha, void* ws,
@@ -32,98 +33,7 @@ constexpr int BM = 128;
 constexpr int BK = 32;  // fp32 elements per K-block = 128 bytes
 constexpr int STAGES = 3;
 constexpr int NTHREADS = 128;
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait: false (and an error code recorded) when the budget runs out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) {
-      atomicExch(err, code);
-      return false;
-    }
-  }
-  return true;
-}
-
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
-               : "memory");
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128B swizzle, 8-row groups 1024 B apart.
-__device__ __forceinline__ uint64_t smem_desc(const void* p) {
-  const uint64_t addr = (uint64_t)(smem_u32(p) & 0x3FFFF) >> 4;
-  return addr | (1ull << 16) | (64ull << 32) | (1ull << 46) | (2ull << 61);
-}
-
-// Instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major, M x N.
-__host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
+using namespace tc;
 
 // K-blocks rotate over NACC accumulators in TMEM (summed in FP64 by the epilogue): each FP32
 // tensor-core accumulation chain is NACC times shorter.
@@ -137,28 +47,6 @@ struct Cfg {
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 256;
   static constexpr uint32_t TMEM_COLS = NACC * BN;  // 256 or 512: powers of two
 };
-
-// hi + lo <- hi + lo + x with hi + x split error-free (Knuth's TwoSum; the _rn intrinsics keep the
-// compiler from reassociating it)
-__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
-  const float t = __fadd_rn(hi, x);
-  const float z = __fsub_rn(t, hi);
-  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(x, z));
-  hi = t;
-  lo = __fadd_rn(lo, e);
-}
-
-// FP32 -> FP64 by integer operations (exact for normal numbers, infinities and NaNs; FP32
-// subnormals, below 1.2e-38, become signed zeros, as the split-TF32 operands already do)
-__device__ __forceinline__ double f32_to_f64(float x) {
-  const uint32_t u = __float_as_uint(x);
-  const uint32_t e = (u >> 23) & 0xFFu;
-  uint64_t bits = (uint64_t)(u >> 31) << 63;
-  const uint64_t mant = (uint64_t)(u & 0x7FFFFFu) << 29;
-  if (e == 0xFFu) bits |= (0x7FFull << 52) | mant;
-  else if (e != 0u) bits |= ((uint64_t)(e + 896u) << 52) | mant;
-  return __longlong_as_double((long long)bits);
-}
 
 template <int BN>
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -300,23 +188,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // ---------------------------------------------------------------------------
 // FP64 -> (tf32 hi, tf32 lo) staging, K-major rows of pitch Kp (multiple of 4).
 
-// x -> tf32(x) + tf32(remainder). One conversion from FP64 (the FP64 pipe issues 64 times fewer
-// lanes per clock than FP32 here); the remainder is taken from the FP32 value, exactly: the bits
-// of x below FP32's 24 lie beneath the 22 that hi + lo keep.
-__device__ __forceinline__ void split_tf32(double x, float& hi, float& lo) {
-  const float xf = __double2float_rn(x);
-  uint32_t h, l;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(xf));
-  const float rem = __fsub_rn(xf, __uint_as_float(h));
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(rem));
-  hi = __uint_as_float(h);
-  lo = __uint_as_float(l);
-}
-
-__device__ __forceinline__ bool finite_f64(double x) {
-  return ((__double_as_longlong(x) >> 52) & 0x7FF) != 0x7FF;
-}
-
 struct PrepArgs {
   const double* src;
   int64_t Z, R, rows, K;
@@ -326,9 +197,7 @@ struct PrepArgs {
   int* err;  // set by prep(): the kernels' device error word
 };
 
-// Error word codes: 1-3 name the pipeline wait that gave up; kErrRange a finite operand beyond
-// FP32's range, which split TF32 cannot represent.
-constexpr int kErrRange = 16;
+constexpr int kErrRange = TN_DEVERR_RANGE;
 
 __device__ __forceinline__ void stage_value(const PrepArgs& a, double x, int64_t o) {
   float h, l;
@@ -403,12 +272,10 @@ int blocks_for(int64_t total) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(total, 256), 16LL * tn_sm_count()));
 }
 
-int err_buffer(int** out);
-
 int prep(const PrepArgs& args, cudaStream_t s) {
   if (args.Z * args.R * args.rows * args.K == 0) return TN_OK;
   PrepArgs a = args;
-  int st = err_buffer(&a.err);
+  int st = tn_error_word(s, &a.err);
   if (st) return st;
   if (a.sRow == 1 && a.sK != 1) {
     dim3 grid((unsigned)tn_cdiv(a.rows, 32), (unsigned)tn_cdiv(a.K, 32), (unsigned)(a.Z * a.R));
@@ -479,21 +346,6 @@ Staged carve(char*& p, int64_t rows, int64_t K, int64_t nmat) {
   return st;
 }
 
-int* g_err_dev = nullptr;
-
-int err_buffer(int** out) {
-  // allocated once, by whichever host thread gets here first
-  static std::once_flag once;
-  static cudaError_t init = cudaSuccess;
-  std::call_once(once, [] {
-    init = cudaMalloc(&g_err_dev, sizeof(int));
-    if (init == cudaSuccess) init = cudaMemset(g_err_dev, 0, sizeof(int));
-  });
-  if (init != cudaSuccess) return tn_record_error(init);
-  *out = g_err_dev;
-  return TN_OK;
-}
-
 template <int BN>
 int launch_kernel(const Staged& A, const Staged& B, int64_t M, int64_t N, int64_t K, int64_t Z, int64_t R,
                   double* C, int64_t sCm, int64_t sCn, int64_t sCb, const double* Cin, double alpha, double beta,
@@ -505,13 +357,11 @@ int launch_kernel(const Staged& A, const Staged& B, int64_t M, int64_t N, int64_
   if ((st = make_map(&ma[1], A.lo, K, M, Z * R, A.Kp, BM))) return st;
   if ((st = make_map(&mb[0], B.hi, K, N, Z * R, B.Kp, BN))) return st;
   if ((st = make_map(&mb[1], B.lo, K, N, Z * R, B.Kp, BN))) return st;
-  static std::atomic<bool> attr_set{false};
-  if (!attr_set.load()) {
-    TN_CUDA(cudaFuncSetAttribute(tf32x3_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, cfg::SMEM));
-    attr_set.store(true);
-  }
+  if ((st = tn_set_smem_attr_once(BN == 128 ? TN_ATTR_TF32_BN128 : TN_ATTR_TF32_BN64,
+                                   (const void*)tf32x3_gemm_kernel<BN>, cfg::SMEM)))
+    return st;
   int* err;
-  if ((st = err_buffer(&err))) return st;
+  if ((st = tn_error_word(s, &err))) return st;
   dim3 grid((unsigned)tn_cdiv(N, BN), (unsigned)tn_cdiv(M, BM), (unsigned)(Z * ksplit));
   if (grid.y > 65535u || grid.z > 65535u) return tn_fail(TN_ERR_ARG, "tf32 gemm grid too large");
   tf32x3_gemm_kernel<BN><<<grid, NTHREADS, cfg::SMEM, s>>>(ma[0], ma[1], mb[0], mb[1], (int)M, (int)N, (int)K,
@@ -557,33 +407,6 @@ bool tn_tf32x3_supported() {
   cudaDeviceGetAttribute(&min, cudaDevAttrComputeCapabilityMinor, dev);
   return maj == 10 && min == 3 && encode_fn() != nullptr;
 }
-
-// Status for a value h read from the device error word: clears the word and names the failure.
-int tn_device_error_status(int h, cudaStream_t s) {
-  if (!h) return TN_OK;
-  int* err;
-  int st = err_buffer(&err);
-  if (st) return st;
-  TN_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-  if (h == kErrRange)
-    return tn_fail(TN_ERR_NUMERIC, "tf32x3 gemm: an operand lies outside the FP32 range (|x| >= 3.4e38)");
-  if (h == TN_DEVERR_QR_WAIT) return tn_fail(TN_ERR_TIMEOUT, "qr32 cluster: a bounded panel wait gave up");
-  return tn_fail(TN_ERR_TIMEOUT, "tf32x3 gemm: a bounded pipeline wait gave up");
-}
-
-int tn_tf32x3_error_check(cudaStream_t s) {
-  int* err;
-  int st = err_buffer(&err);
-  if (st) return st;
-  int h = 0;
-  TN_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
-  TN_CUDA(cudaStreamSynchronize(s));
-  return tn_device_error_status(h, s);
-}
-
-// The device error word shared by the library's kernels (bounded waits, range checks); read and
-// cleared by tn_check_device_status.
-int tn_device_error_word(int** out) { return err_buffer(out); }
 
 size_t tn_gemm_tf32x3_ws_bytes(int64_t M, int64_t N, int64_t K, int64_t batch, int64_t nred) {
   const int64_t zr = batch * std::max<int64_t>(nred, 1);
@@ -665,6 +488,18 @@ int tn_matvec_fp64_straddle(const tn_site_desc* ds, const double* psi, double* y
 size_t tn_matvec_tf32x3_ws_bytes(const tn_site_desc* d) {
   MvLayout L;
   return mv_layout(d, nullptr, &L);
+}
+
+// The FP64 scratch region inside a split-TF32 matvec workspace: an FP64 matvec run between
+// split-TF32 ones (the FP64 steps of a refined Lanczos solve) must use this region, not the start
+// of the workspace, where the staged hi/lo copies of WL, WR, SL and SR live.
+int tn_matvec_tf32x3_fp64_region(const tn_site_desc* d, void* ws, size_t ws_bytes, void** out, size_t* out_bytes) {
+  MvLayout L;
+  if (!ws || ws_bytes < mv_layout(d, nullptr, &L)) return tn_fail(TN_ERR_WORKSPACE, "tf32 matvec: workspace");
+  mv_layout(d, (char*)ws, &L);
+  *out = L.fp64_ws;
+  *out_bytes = L.fp64_bytes;
+  return TN_OK;
 }
 
 int tn_tf32x3_prepare_static(const tn_site_desc* d, void* ws, size_t ws_bytes, cudaStream_t s) {

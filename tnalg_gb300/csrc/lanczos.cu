@@ -19,13 +19,11 @@
 #include "common.cuh"
 
 int tn_dot_ws(int64_t n, const double* x, const double* y, double* out, void* ws, size_t ws_bytes, cudaStream_t s);
-int tn_tf32x3_error_check(cudaStream_t s);
-int tn_device_error_word(int** out);
-int tn_device_error_status(int h, cudaStream_t s);
 int tn_matvec_tf32x3(const tn_site_desc* d, const double* psi, double* y, double alpha, double beta,
                      void* ws, size_t ws_bytes, cudaStream_t s);
 size_t tn_matvec_tf32x3_ws_bytes(const tn_site_desc* d);
 int tn_tf32x3_prepare_static(const tn_site_desc* d, void* ws, size_t ws_bytes, cudaStream_t s);
+int tn_matvec_tf32x3_fp64_region(const tn_site_desc* d, void* ws, size_t ws_bytes, void** out, size_t* out_bytes);
 
 namespace {
 
@@ -510,8 +508,14 @@ static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_
   const bool mixed = (o->precision == TN_PREC_TF32X3);
 
   TN_CUDA(cudaMemsetAsync(L.tickets, 0, (kMaxKrylov + 2) * sizeof(unsigned int), s));
+  // FP64 matvecs of a split-TF32 solve (refinement) work in the FP64 region of the split-TF32
+  // workspace, which leaves the staged hi/lo operator copies intact
+  void* f64_ws = L.mv_ws;
+  size_t f64_bytes = L.mv_bytes;
   if (mixed) {
     st = tn_tf32x3_prepare_static(desc, L.mv_ws, L.mv_bytes, s);
+    if (st) return st;
+    st = tn_matvec_tf32x3_fp64_region(desc, L.mv_ws, L.mv_bytes, &f64_ws, &f64_bytes);
     if (st) return st;
   }
   auto matvec = [&](const double* x, double* y) -> int {
@@ -538,17 +542,35 @@ static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_
   // the device error word (range flags of the split-TF32 staging, bounded waits) travels with
   // alpha/beta at every convergence check, so a mixed-precision solve needs no sync of its own
   int* dev_err = nullptr;
-  if (mixed && (st = tn_device_error_word(&dev_err))) return st;
+  if (mixed && (st = tn_error_word(s, &dev_err))) return st;
   int herr = 0;
   int matvecs = 0, restarts = 0;
   bool converged = false;
   double theta = 0.0, resid = INFINITY;
+  // refine == 2 on the split-TF32 path: once the mixed-precision iteration has reached its floor,
+  // every further restart cycle begins with an FP64 matvec of the current vector x. That step's
+  // alpha = x.Hx and beta = ||Hx - alpha x|| are FP64-exact (the true Rayleigh quotient and
+  // residual), the cycle's later matvecs act on vectors orthogonal to x with weights of order
+  // beta/gap, so their split-TF32 error enters the next vector only at second order: each cycle
+  // divides the true residual by ~(split-TF32 error x ||H|| / gap) until it meets the FP64 tolerance.
+  const bool vec_refine = mixed && o->refine == 2;
+  const int max_cycles = o->refine_cycles > 0 ? o->refine_cycles : 4;
+  bool exact_phase = false;  // restart cycles open with an FP64 matvec
+  int cycles = 0;
+  double beta0 = INFINITY, theta0 = 0.0;
   for (;;) {
     int jj = 0;
     bool stop = false;
     for (int j = 0; j < m; ++j) {
       double* vj = L.V + (int64_t)j * n;
-      st = matvec(vj, L.w);
+      const bool exact = exact_phase && j == 0;
+      if (exact) {
+        cudaEvent_t ev = tn_profile_begin(s);
+        st = matvec_fp64(desc, vj, L.w, 1.0, 0.0, f64_ws, f64_bytes, s);
+        tn_profile_end(ev, s, TN_PROF_MATVEC, matvec_flops(desc));
+      } else {
+        st = matvec(vj, L.w);
+      }
       if (st) return st;
       ++matvecs;
       const int nc = j + 1;
@@ -564,12 +586,12 @@ static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_
                                              L.beta);
       TN_CHECK_LAUNCH();
       const bool last = (j + 1 == m);
-      if ((j + 1) % check == 0 || last) {
+      if ((j + 1) % check == 0 || last || exact) {
         TN_CUDA(cudaMemcpyAsync(ha.data(), L.alpha, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
         TN_CUDA(cudaMemcpyAsync(hb.data(), L.beta, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
         if (mixed) TN_CUDA(cudaMemcpyAsync(&herr, dev_err, sizeof(int), cudaMemcpyDeviceToHost, s));
         TN_CUDA(cudaStreamSynchronize(s));
-        if (herr) return tn_device_error_status(herr, s);
+        if (herr) return tn_error_status(herr, s);
         for (int i = 0; i < nc; ++i)
           if (!isfinite(ha[i]) || !isfinite(hb[i])) return tn_fail(TN_ERR_NUMERIC, "lanczos: non-finite coefficient");
         // breakdown: truncate at the first negligible beta
@@ -586,8 +608,27 @@ static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_
         if (o->tau > 0) tol = o->eigs_tol / o->tau * fabs(1.0 - o->tau * theta);
         else tol = o->eigs_tol * std::max(1.0, fabs(theta));
         if (o->tol_cap > 0) tol = std::min(tol, o->tol_cap * std::max(1.0, fabs(theta)));
+        if (exact_phase) {
+          if (exact) {
+            // FP64-exact Rayleigh quotient and residual of the current vector
+            theta0 = ha[0];
+            beta0 = hb[0];
+            if (beta0 <= tol || brk) { converged = true; jj = 1; sv.assign(1, 1.0); stop = true; break; }
+            continue;
+          }
+          // a cycle ends once its mixed-precision estimate has dropped well below the exact
+          // residual it started from; the next cycle's FP64 step measures the true one
+          if (resid <= std::max(tol, 1e-4 * beta0) || brk || nc >= n || last) { jj = mm; break; }
+          continue;
+        }
         if (mixed) tol = std::max(tol, std::max(o->mixed_floor, 0.0) * std::max(1.0, fabs(theta)));
-        if (resid <= tol || brk || nc >= n) { converged = true; jj = mm; stop = true; break; }
+        if (resid <= tol || brk || nc >= n) {
+          jj = mm;
+          if (vec_refine && !brk && nc < n) { exact_phase = true; break; }
+          converged = true;
+          stop = true;
+          break;
+        }
         if (last) { jj = mm; break; }
       }
     }
@@ -602,16 +643,31 @@ static int lanczos_impl(const tn_site_desc* desc, double* psi, const tn_lanczos_
     TN_CUDA(cudaMemcpyAsync(L.s, sv.data(), jj * sizeof(double), cudaMemcpyHostToDevice, s));
     combine_kernel<<<nb, NT, 0, s>>>(n, jj, L.V, L.s, psi);
     TN_CHECK_LAUNCH();
-    if (stop || restarts >= o->max_restarts) break;
+    if (stop) break;
+    if (exact_phase) {
+      if (cycles >= max_cycles) {
+        // the FP64 residual measured at the start of the last cycle stands for the vector
+        theta = theta0;
+        resid = beta0;
+        break;
+      }
+      ++cycles;
+    } else {
+      if (restarts >= o->max_restarts) break;
+    }
     ++restarts;
     TN_CUDA(cudaMemcpyAsync(L.V, psi, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  if (vec_refine && exact_phase && converged) {
+    theta = theta0;
+    resid = beta0;
   }
   res->energy = theta;
   res->residual = resid;
   res->energy_fp64 = theta;
-  if (o->refine) {
+  if (o->refine == 1) {
     // FP64 residual and Rayleigh quotient of the final vector.
-    st = matvec_fp64(desc, psi, L.w, 1.0, 0.0, L.mv_ws, L.mv_bytes, s);
+    st = matvec_fp64(desc, psi, L.w, 1.0, 0.0, f64_ws, f64_bytes, s);
     if (st) return st;
     ++matvecs;
     st = dot2(psi, L.w, L.e);

@@ -356,11 +356,8 @@ constexpr size_t kClusterSmem = (size_t)2 * PW * PRW * (NB + 1) * sizeof(double)
 
 int launch_panel(int64_t m, int64_t j0, int jb, const QrWs& w, double* Tp, cudaStream_t s) {
   if (m - j0 <= (int64_t)CL * PW * PRW) {
-    static std::atomic<bool> attr{false};
-    if (!attr.load()) {
-      TN_CUDA(cudaFuncSetAttribute(qr_panel_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmem));
-      attr.store(true);
-    }
+    int st = tn_set_smem_attr_once(TN_ATTR_QR_PANEL_CLUSTER, (const void*)qr_panel_cluster, (int)kClusterSmem);
+    if (st) return st;
     qr_panel_cluster<<<CL, PW, kClusterSmem, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
   } else {
     qr_panel<<<1, NTP, 0, s>>>(m, j0, jb, w.Aw, w.Vf, Tp);
@@ -446,7 +443,7 @@ int qr_body(int64_t m, int64_t n, int64_t sAm, int64_t sAn, int64_t sQm, int64_t
 
 // Graph cache: one executable graph per (shape, strides, workspace, outputs requested).
 struct QrGraph {
-  int64_t key[10];
+  int64_t key[11];
   cudaGraphExec_t exec;
   unsigned long long kernels;  // kernel launches recorded into the graph
 };
@@ -494,7 +491,9 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
     st = qr_body(m, n, sAm, sAn, sQm, sQn, sRm, sRn, q != nullptr, w, s);
   } else {
     std::lock_guard<std::mutex> lock(g_graph_mu);
-    const int64_t key[10] = {m, n, sAm, sAn, sQm, sQn, sRm, sRn, (int64_t)(uintptr_t)base, q != nullptr};
+    int dev = 0;
+    if ((st = tn_current_device(&dev))) return st;
+    const int64_t key[11] = {m, n, sAm, sAn, sQm, sQn, sRm, sRn, (int64_t)(uintptr_t)base, q != nullptr, dev};
     cudaGraphExec_t exec = nullptr;
     unsigned long long kernels = 0;
     for (size_t i = 0; i < g_graphs.size(); ++i)
@@ -507,7 +506,9 @@ extern "C" int tn_qr(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t
     if (!exec) {
       // capture on a private stream (the caller's may be the legacy default stream, which
       // cannot capture); nothing runs during capture, the graph is launched on `s` below.
-      static cudaStream_t cs = nullptr;
+      // one capture stream per device (a stream belongs to the device it was created on)
+      static cudaStream_t capture_streams[TN_MAX_DEVICES] = {nullptr};
+      cudaStream_t& cs = capture_streams[dev];
       if (!cs) TN_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       cudaGraph_t graph;
       TN_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));

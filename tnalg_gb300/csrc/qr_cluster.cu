@@ -28,9 +28,10 @@
 //     one SM after the last panel while the rest of the cluster sits idle.
 // Every wait is bounded by a clock budget; on timeout the CTA records an error code, skips its
 // remaining work and still joins the final cluster barrier.
+#include <mutex>
+
 #include "common.cuh"
 
-int tn_device_error_word(int** out);
 
 namespace {
 
@@ -766,9 +767,14 @@ cudaLaunchConfig_t launch_config(cudaLaunchAttribute* at, cudaStream_t s) {
 // True when the 16-CTA cluster kernel can run this shape on the current device.
 bool tn_qr32_cluster_supported(int64_t m, int64_t n) {
   if (n < 1 || n > (int64_t)NBMAX * BW || m < n || m > MMAX) return false;
-  // probed once (the initialisation of a function-local static is thread-safe, so concurrent
-  // first callers all see the probe's answer)
-  static const bool available = [] {
+  // probed once per device (under a mutex, so concurrent first callers all see the probe's answer)
+  static std::mutex mu;
+  static signed char probed[TN_MAX_DEVICES] = {0};  // 0 unknown, 1 yes, -1 no
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= TN_MAX_DEVICES) return false;
+  std::lock_guard<std::mutex> lk(mu);
+  if (probed[dev]) return probed[dev] > 0;
+  const bool available = [] {
     bool ok = false;
     if (cudaFuncSetAttribute(qr32_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
             cudaSuccess &&
@@ -783,6 +789,7 @@ bool tn_qr32_cluster_supported(int64_t m, int64_t n) {
     cudaGetLastError();  // an unsupported attribute leaves no sticky error behind
     return ok;
   }();
+  probed[dev] = available ? 1 : -1;
   return available;
 }
 
@@ -799,7 +806,7 @@ int tn_qr32_cluster(int64_t m, int64_t n, const double* a, int64_t sAm, int64_t 
   if (!tn_qr32_cluster_supported(m, n)) return tn_fail(TN_ERR_ARG, "qr32 cluster: unsupported shape or device");
   if (((uintptr_t)scratch & 15) != 0) return tn_fail(TN_ERR_ARG, "qr32 cluster: scratch misaligned");
   int* err;
-  int st = tn_device_error_word(&err);
+  int st = tn_error_word(s, &err);
   if (st) return st;
   const int64_t np = tn_cdiv(n, BW);
   float* Vg = scratch;

@@ -9,9 +9,16 @@
 // the singular values. Pairs follow a round-robin tournament, so each round is
 // k/2 independent pairs (one CTA each); a sweep is k-1 rounds. The host reads a
 // single "rotated" flag per sweep and stops when a sweep rotates nothing.
+// A pair is left alone when its off-diagonal is below tol relative to the rows, or when one
+// of its rows is numerically null (squared norm below (4 eps)^2 max(k, n) ||X||_F^2): rounding
+// noise keeps such rows from ever becoming orthogonal, and their norms are noise-level singular
+// values either way (LAPACK's are accurate to ~eps ||X|| too). A sweep that still rotated after
+// max_sweeps makes the call return TN_ERR_NOCONV (the values are written all the same).
 #include <math.h>
 
 #include <vector>
+
+#include <mutex>
 
 #include "common.cuh"
 
@@ -19,13 +26,26 @@ namespace {
 
 constexpr int NT = 256;
 
-__global__ void svd_copy_in(int64_t k, int64_t kp, int64_t n, const double* x, int64_t sr, int64_t sc, double* X) {
+// Squared norm below which a row counts as numerically null, relative to ||X||_F^2.
+inline double null_row_rel2(int64_t k, int64_t n) {
+  const double e = 4.0 * 2.220446049250313e-16;
+  return e * e * (double)std::max<int64_t>(k, n);
+}
+
+// X = x (rows padded to kp with zeros); *fro2 += ||x||_F^2 (*fro2 zeroed by the caller).
+__global__ void svd_copy_in(int64_t k, int64_t kp, int64_t n, const double* x, int64_t sr, int64_t sc, double* X,
+                            double* fro2) {
   const int64_t total = kp * n;
+  double acc = 0.0;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = idx / n, c = idx % n;
-    X[idx] = r < k ? x[r * sr + c * sc] : 0.0;
+    const double v = r < k ? x[r * sr + c * sc] : 0.0;
+    X[idx] = v;
+    acc = fma(v, v, acc);
   }
+  acc = tn_warp_sum(acc);
+  if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(fro2, acc);
 }
 
 // Round-robin pairing: player 0 fixed, others rotate. Round r pairs slot i with slot kp-1-i.
@@ -34,7 +54,8 @@ __device__ __forceinline__ int64_t rr_player(int64_t slot, int64_t r, int64_t kp
   return 1 + (slot - 1 + r) % (kp - 1);
 }
 
-__global__ void jacobi_round(int64_t kp, int64_t n, int64_t r, double* X, double tol, int* rotated) {
+__global__ void jacobi_round(int64_t kp, int64_t n, int64_t r, double* X, double tol, const double* fro2,
+                             double null_rel2, int* rotated) {
   const int64_t i = blockIdx.x;  // pair index 0..kp/2-1
   const int64_t p = rr_player(i, r, kp), q = rr_player(kp - 1 - i, r, kp);
   double* xp = X + p * n;
@@ -58,12 +79,12 @@ __global__ void jacobi_round(int64_t kp, int64_t n, int64_t r, double* X, double
     double A = 0, B = 0, G = 0;
     for (int w = 0; w < NT / 32; ++w) { A += red[0][w]; B += red[1][w]; G += red[2][w]; }
     double c = 1.0, s = 0.0;
-    if (fabs(G) > tol * sqrt(A * B) && G != 0.0) {
+    if (G != 0.0 && fabs(G) > tol * sqrt(A * B) && fmin(A, B) > null_rel2 * (*fro2)) {
       const double zeta = (B - A) / (2.0 * G);
       const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
       c = 1.0 / sqrt(1.0 + t * t);
       s = c * t;
-      *rotated = 1;
+      if (s != 0.0) *rotated = 1;
     }
     cs[0] = c; cs[1] = s;
   }
@@ -93,6 +114,33 @@ __global__ void row_norms(int64_t k, int64_t n, const double* X, double* out) {
   }
 }
 
+// The whole one-matrix solve on scratch X (kp x n), flag (int) and fro2 (double).
+int jacobi_run(int64_t k, int64_t kp, int64_t n, const double* x, int64_t sXr, int64_t sXc, double* s_out,
+               double tol, int max_sweeps, double* X, int* flag, double* fro2, cudaStream_t s) {
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(kp * n, NT), 8LL * tn_sm_count()));
+  TN_CUDA(cudaMemsetAsync(fro2, 0, sizeof(double), s));
+  svd_copy_in<<<blocks, NT, 0, s>>>(k, kp, n, x, sXr, sXc, X, fro2);
+  TN_CHECK_LAUNCH();
+  const double nr2 = null_row_rel2(k, n);
+  int h = 0;
+  if (kp >= 2) {
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+      TN_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+      for (int64_t r = 0; r < kp - 1; ++r) {
+        jacobi_round<<<(unsigned)(kp / 2), NT, 0, s>>>(kp, n, r, X, tol, fro2, nr2, flag);
+        TN_CHECK_LAUNCH();
+      }
+      TN_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+      TN_CUDA(cudaStreamSynchronize(s));
+      if (!h) break;
+    }
+  }
+  row_norms<<<(unsigned)k, NT, 0, s>>>(k, n, X, s_out);
+  TN_CHECK_LAUNCH();
+  if (h) return tn_fail(TN_ERR_NOCONV, "singular values: Jacobi still rotating after max_sweeps");
+  return TN_OK;
+}
+
 }  // namespace
 
 extern "C" size_t tn_singular_values_workspace_bytes(int64_t k, int64_t n) {
@@ -108,26 +156,9 @@ extern "C" int tn_singular_values(int64_t k, int64_t n, const double* x, int64_t
     return tn_fail(TN_ERR_WORKSPACE, "singular_values: workspace too small");
   cudaStream_t s = (cudaStream_t)stream;
   int* flag = (int*)ws;
+  double* fro2 = (double*)((char*)ws + 8);
   double* X = (double*)((char*)ws + 256);
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(kp * n, NT), 8LL * tn_sm_count()));
-  svd_copy_in<<<blocks, NT, 0, s>>>(k, kp, n, x, sXr, sXc, X);
-  TN_CHECK_LAUNCH();
-  if (kp >= 2) {
-    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-      TN_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
-      for (int64_t r = 0; r < kp - 1; ++r) {
-        jacobi_round<<<(unsigned)(kp / 2), NT, 0, s>>>(kp, n, r, X, tol, flag);
-        TN_CHECK_LAUNCH();
-      }
-      int h = 0;
-      TN_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
-      TN_CUDA(cudaStreamSynchronize(s));
-      if (!h) break;
-    }
-  }
-  row_norms<<<(unsigned)k, NT, 0, s>>>(k, n, X, s_out);
-  TN_CHECK_LAUNCH();
-  return TN_OK;
+  return jacobi_run(k, kp, n, x, sXr, sXc, s_out, tol, max_sweeps, X, flag, fro2, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -147,6 +178,8 @@ struct SvItem {
   int64_t sXr, sXc;
   double* s_out;
   T* X;
+  double* fro2;      // ||x||_F^2, accumulated by the copy-in
+  double null_rel2;  // null-row threshold relative to fro2
 };
 
 template <typename T>
@@ -160,11 +193,16 @@ template <typename T>
 __global__ void svb_copy_in(const SvItem<T>* items) {
   const SvItem<T> it = items[blockIdx.y];
   const int64_t total = it.kp * it.n;
+  double acc = 0.0;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = idx / it.n, c = idx % it.n;
-    it.X[idx] = r < it.k ? (T)it.x[r * it.sXr + c * it.sXc] : (T)0;
+    const double v = r < it.k ? it.x[r * it.sXr + c * it.sXc] : 0.0;
+    it.X[idx] = (T)v;
+    acc = fma(v, v, acc);
   }
+  acc = tn_warp_sum(acc);
+  if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(it.fro2, acc);
 }
 
 template <typename T>
@@ -203,12 +241,12 @@ __global__ void svb_round(const SvItem<T>* items, int64_t r, T tol, int* rotated
       G += red[2][w];
     }
     T c = 1, sn = 0;
-    if (G != (T)0 && fabs(G) > tol * sqrt(A * B)) {
+    if (G != (T)0 && fabs(G) > tol * sqrt(A * B) && (double)fmin(A, B) > it.null_rel2 * (*it.fro2)) {
       const T zeta = (B - A) / (2 * G);
       const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
       c = (T)1 / sqrt((T)1 + tt * tt);
       sn = c * tt;
-      *rotated = 1;
+      if (sn != (T)0) *rotated = 1;
     }
     cs[0] = c;
     cs[1] = sn;
@@ -249,6 +287,8 @@ size_t svb_align(size_t x) { return (x + 255) / 256 * 256; }
 template <typename T>
 size_t svb_layout(int count, const tn_sv_item* items, char* base, std::vector<SvItem<T>>* out) {
   size_t off = 256 + svb_align(sizeof(SvItem<T>) * (size_t)count);
+  double* fro2 = base ? (double*)(base + off) : nullptr;   // one accumulator per matrix
+  off += svb_align(sizeof(double) * (size_t)count);
   for (int b = 0; b < count; ++b) {
     const int64_t k = items[b].k, n = items[b].n, kp = k + (k & 1);
     if (out) {
@@ -261,6 +301,8 @@ size_t svb_layout(int count, const tn_sv_item* items, char* base, std::vector<Sv
       it.sXc = items[b].sXc;
       it.s_out = items[b].s_out;
       it.X = (T*)(base + off);
+      it.fro2 = fro2 + b;
+      it.null_rel2 = null_row_rel2(k, n);
       out->push_back(it);
     }
     off += svb_align(sizeof(T) * (size_t)kp * n);
@@ -283,8 +325,10 @@ int svb_run(int count, const tn_sv_item* items, T tol, int max_sweeps, void* ws,
     nmax = std::max(nmax, it.n);
   }
   const dim3 cgrid((unsigned)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(kpmax * nmax, NT), 64)), (unsigned)count);
+  TN_CUDA(cudaMemsetAsync(host[0].fro2, 0, sizeof(double) * (size_t)count, s));
   svb_copy_in<T><<<cgrid, NT, 0, s>>>(dev_items);
   TN_CHECK_LAUNCH();
+  int h = 0;
   if (kpmax >= 2) {
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
       TN_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
@@ -292,7 +336,6 @@ int svb_run(int count, const tn_sv_item* items, T tol, int max_sweeps, void* ws,
         svb_round<T><<<dim3((unsigned)(kpmax / 2), (unsigned)count), NT, 0, s>>>(dev_items, r, tol, flag);
         TN_CHECK_LAUNCH();
       }
-      int h = 0;
       TN_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
       TN_CUDA(cudaStreamSynchronize(s));
       if (!h) break;
@@ -302,6 +345,7 @@ int svb_run(int count, const tn_sv_item* items, T tol, int max_sweeps, void* ws,
   TN_CHECK_LAUNCH();
   // the item table is read by the launches above: keep the host copy alive until they ran
   TN_CUDA(cudaStreamSynchronize(s));
+  if (h) return tn_fail(TN_ERR_NOCONV, "singular values: Jacobi still rotating after max_sweeps");
   return TN_OK;
 }
 
@@ -335,21 +379,24 @@ extern "C" int tn_singular_values_batched(int count, const tn_sv_item* items, do
 // Limit: (k rounded up to even) * n <= TN_SV_NOALLOC_MAX_ELEMS doubles (512 KiB; e.g. 256 x 256).
 // Every GPU that loads the library holds the array until the process exits. All calls share it:
 // calls that overlap on the GPU (different streams, or different host threads on one device) race
-// and must be serialised by the caller. The flag is cleared at the start of every sweep; the copy
-// of X is rewritten by every call, so no state leaks from one call into the next.
+// and must be serialised by the caller. The flag is cleared at the start of every sweep, the norm
+// accumulator at the start of every call, and the copy of X is rewritten by every call, so no
+// state leaks from one call into the next.
 #define TN_SV_NOALLOC_MAX_ELEMS 65536
 #define TN_SV_NOALLOC_FLAG_SLOTS 32
 static __device__ __align__(256) double g_sv_noalloc_scratch[TN_SV_NOALLOC_FLAG_SLOTS + TN_SV_NOALLOC_MAX_ELEMS];
 
 namespace {
-constexpr int kMaxDevices = 64;
-void* g_sv_noalloc_ptr[kMaxDevices] = {nullptr};
+void* g_sv_noalloc_ptr[TN_MAX_DEVICES] = {nullptr};
+std::mutex g_sv_noalloc_mu;
 
-// Device address of the static scratch on the current device, resolved once per device.
+// Device address of the static scratch on the current device, resolved once per device (under a
+// mutex: host threads of a multi-job host may make their first calls at the same time).
 int sv_noalloc_scratch(void** out) {
   int dev = 0;
-  TN_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return tn_fail(TN_ERR_ARG, "singular_values_noalloc: device ordinal >= 64");
+  int st = tn_current_device(&dev);
+  if (st) return st;
+  std::lock_guard<std::mutex> lk(g_sv_noalloc_mu);
   if (!g_sv_noalloc_ptr[dev]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_sv_noalloc_scratch);
@@ -372,25 +419,8 @@ extern "C" int tn_singular_values_noalloc(int64_t k, int64_t n, const double* x,
   int st = sv_noalloc_scratch(&base);
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  int* flag = (int*)base;
+  int* flag = (int*)base;                   // flag slots: the "rotated" flag, then ||X||_F^2
+  double* fro2 = (double*)base + 1;
   double* X = (double*)base + TN_SV_NOALLOC_FLAG_SLOTS;
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(kp * n, NT), 8LL * tn_sm_count()));
-  svd_copy_in<<<blocks, NT, 0, s>>>(k, kp, n, x, sXr, sXc, X);
-  TN_CHECK_LAUNCH();
-  if (kp >= 2) {
-    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-      TN_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
-      for (int64_t r = 0; r < kp - 1; ++r) {
-        jacobi_round<<<(unsigned)(kp / 2), NT, 0, s>>>(kp, n, r, X, tol, flag);
-        TN_CHECK_LAUNCH();
-      }
-      int h = 0;
-      TN_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
-      TN_CUDA(cudaStreamSynchronize(s));
-      if (!h) break;
-    }
-  }
-  row_norms<<<(unsigned)k, NT, 0, s>>>(k, n, X, s_out);
-  TN_CHECK_LAUNCH();
-  return TN_OK;
+  return jacobi_run(k, kp, n, x, sXr, sXc, s_out, tol, max_sweeps, X, flag, fro2, s);
 }

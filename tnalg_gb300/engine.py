@@ -813,13 +813,15 @@ class DeviceMPS:
         return desc, keep
 
     def solve(self, p, eigs_tol, tau, *, tol_cap=0.0, max_krylov=40, max_restarts=50, check_every=3,
-              refine=None, mixed_floor=2e-6):
-        """Lowest eigenvector of H_eff at the centre p (MPSClass.py:778-809)."""
+              refine=None, mixed_floor=2e-6, refine_cycles=4):
+        """Lowest eigenvector of H_eff at the centre p (MPSClass.py:778-809). refine: 0 none,
+        1 FP64 Rayleigh quotient of the final vector, 2 the vector refined to the FP64 tolerance
+        (split-TF32 path); None = 1 on the split-TF32 path, 0 on FP64."""
         desc, keep = self.site_operator(p)
         psi = self.mps[p].contiguous()
         opts = L.LanczosOpts(float(eigs_tol), float(tau), float(tol_cap), float(mixed_floor), int(max_krylov),
                              int(max_restarts), int(check_every), int(self.precision),
-                             int(self.precision != L.PREC_FP64 if refine is None else refine), 0)
+                             int(self.precision != L.PREC_FP64 if refine is None else refine), int(refine_cycles))
         lib = L.load()
         need = lib.tn_lanczos_workspace_bytes(ctypes_ref(desc), ctypes_ref(opts))
         wp, wb = self.ws.args(need)

@@ -61,35 +61,44 @@ class _Timer:
             self.ms = 1000.0 * (time.perf_counter() - self.t)
 
 
-def run(para, precision, schedule, steps, device="cuda", seed=0):
-    """Ramp over `schedule` (one sweep per bond dimension), then `steps` timed sweeps at schedule[-1]."""
+def run(para, precision, schedule, steps, device="cuda", seed=0, refine="off"):
+    """Ramp over `schedule[:-1]` (one sweep per bond dimension), then `steps` timed sweeps at
+    schedule[-1]. refine (split-TF32 path): 'final' refines the local solves of the last sweep to
+    the FP64 tolerance (DMRG_anyH.refine_sweep), 'all' those of every sweep, 'off' none."""
     np.random.seed(seed)
     l = para["l"]
     A = MpsOpenBoundaryClass(l, para["d"], schedule[0], operators=para["op"], device=device, precision=precision)
     A.correct_orthogonal_center(0)
     order = list(range(1, l)) + list(range(l - 2, -1, -1))
+    total = len(schedule) - 1 + steps
+    energies = []
 
-    def sweep():
+    def sweep(t):
+        A.refine_vectors = refine == "all" or (refine == "final" and t == total - 1)
         for k, n in enumerate(order):
             if k == len(order) - 1:
                 A.refine_next_solve()
-            A.update_tensor_eigs(n, para["index1"], para["index2"], para["coeff1"], para["coeff2"], para["tau"],
-                                 True, tol=para["eigs_tol"])
+            e = A.update_tensor_eigs(n, para["index1"], para["index2"], para["coeff1"], para["coeff2"],
+                                     para["tau"], True, tol=para["eigs_tol"])
+        energies.append(float(e) / l)
 
-    for t, chi in enumerate(schedule):
+    for t, chi in enumerate(schedule[:-1]):
         A.grow_bond_dimension(int(chi), seed=t)
-        sweep()
+        sweep(t)
+    A.grow_bond_dimension(int(schedule[-1]), seed=len(schedule) - 1)
     s0, m0 = A.stats["solves"], A.stats["matvecs"]
     with _Timer(device) as tm:
-        for _ in range(steps):
-            sweep()
+        for k in range(steps):
+            sweep(len(schedule) - 1 + k)
     solves, matvecs = A.stats["solves"] - s0, A.stats["matvecs"] - m0
     eb = A.observe_bond_energy(para["index2"], para["coeff2"])
     mx, mz = A.observe_magnetization(1), A.observe_magnetization(3)
     e = float((np.sum(eb) - para["hx"] * np.sum(mx) - para["hz"] * np.sum(mz)) / l)
-    return {"precision": precision, "ms_per_sweep": tm.ms / steps, "sweeps_per_s": 1000.0 * steps / tm.ms,
+    return {"precision": precision, "refine": refine if precision != "fp64" else None,
+            "ms_per_sweep": tm.ms / steps, "sweeps_per_s": 1000.0 * steps / tm.ms,
             "solves_per_s": 1000.0 * solves / tm.ms, "matvecs_per_solve": matvecs / max(solves, 1),
-            "e_per_site": e, "chi_max": int(A.virtual_dim.max()), "eb_full": np.ravel(eb)}
+            "e_per_site": e, "chi_max": int(A.virtual_dim.max()), "sweep_energies_per_site": energies,
+            "unconverged_solves": int(A.stats["unconverged"]), "eb_full": np.ravel(eb)}
 
 
 def straddle_max(para):
@@ -114,6 +123,9 @@ def main(argv=None):
     ap.add_argument("--eigs-tol", type=float, default=1e-12)
     ap.add_argument("--device", default="cuda")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--refine", default="off", choices=["final", "all", "off"],
+                    help="split-TF32 path: local solves refined to the FP64 tolerance in the last sweep (final), "
+                         "in every sweep (all) or never (off)")
     a = ap.parse_args(argv)
     from . import _lib as L
     L.load()
@@ -121,7 +133,7 @@ def main(argv=None):
     schedule = [int(x) for x in a.ramp.split(",") if x] + [a.chi]
     out = {"workload": name, "sites": int(para["l"]), "two_body_rows": int(np.asarray(para["index2"]).shape[0]),
            "straddling_terms_max": straddle_max(para), "chi_schedule": schedule, "timed_sweeps": a.steps}
-    res = run(para, a.precision, schedule, a.steps, a.device, a.seed)
+    res = run(para, a.precision, schedule, a.steps, a.device, a.seed, refine=a.refine)
     eb = res.pop("eb_full")
     out.update(res)
     if a.compare_fp64 and a.precision != "fp64":

@@ -15,8 +15,9 @@ site, bond energies and magnetisations. The scheduler
 
 A job touches only its own buffers and draws its random MPS from its own seed, so its result is
 the same alone and in a mix (up to the rounding order of floating-point atomics in the split-TF32
-GEMMs; the FP64 path is deterministic). The host runs one thread: the C library's lazily
-initialised state is shared by all jobs and is not meant for concurrent host threads.
+GEMMs; the FP64 path is deterministic). The interleaved jobs are advanced by one host thread, or
+with `workers=N` by a pool of host threads (the C library's calls release the GIL and its shared
+host state is synchronised; each job keeps its own stream and workspaces).
 
     python -m tnalg_gb300.serving --jobs 16 --sweeps 4 [--rate 200] [--precision fp64|tf32x3] [--ladders 0.5]
 """

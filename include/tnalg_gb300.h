@@ -279,7 +279,7 @@ size_t tn_grouped_gemm_workspace_bytes(int precision, const tn_grouped_gemm_prob
 /* ---- batched local solves -------------------------------------------------------------- */
 /* One job of a batched solve: its effective Hamiltonian and its start / result vectors. */
 typedef struct {
-  tn_site_desc site;       /* WL, WR (straddling pairs not supported here: nstr must be 0) */
+  tn_site_desc site;       /* WL, WR and straddling pairs SL, SR */
   const double* psi_in;    /* DEVICE start vector, chil*d*chir values */
   double* psi_out;         /* DEVICE unit eigenvector (may equal psi_in) */
 } tn_batch_solve;

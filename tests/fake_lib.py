@@ -202,6 +202,51 @@ class FakeLib:
         r.converged = 1
         return OK
 
+    def tn_batched_lanczos_workspace_bytes(self, jobs, count, opts):
+        return 0
+
+    def tn_batched_lanczos(self, jobs, count, opts, ws, wsb, results, stream):
+        """Every job of the batch through the single-job solver above (same documented result)."""
+        self._count("tn_batched_lanczos")
+        from tnalg_gb300 import _lib
+        arr = ctypes.cast(jobs, ctypes.POINTER(_lib.BatchSolve))
+        res = ctypes.cast(results, ctypes.POINTER(_lib.LanczosResult))
+        for b in range(int(count)):
+            j = arr[b]
+            ds = j.site
+            n = int(ds.chil * ds.d * ds.chir)
+            if j.psi_out != j.psi_in:
+                _view(j.psi_out, n)[:] = _view(j.psi_in, n)
+            st = self.tn_lanczos(ctypes.byref(ds), j.psi_out, opts, None, 0, ctypes.byref(res[b]), stream)
+            if st not in (OK, ERR_NOCONV):
+                return st
+        return OK
+
+    # -- grouped contractions ----------------------------------------------------------------
+    def tn_grouped_gemm_workspace_bytes(self, prec, problems, count):
+        return 0
+
+    def tn_grouped_gemm(self, prec, problems, count, ws, wsb, stream):
+        self._count("tn_grouped_gemm")
+        from tnalg_gb300 import _lib
+        tab = np.ctypeslib.as_array((ctypes.c_uint8 * (int(count) * _lib.GEMM_PROBLEM_DTYPE.itemsize))
+                                    .from_address(_addr(problems))).view(_lib.GEMM_PROBLEM_DTYPE)
+        for q in tab:
+            M, N, K, R = int(q["M"]), int(q["N"]), int(q["K"]), int(q["nred"])
+            C = _strided(int(q["C"]), (M, N), (int(q["sCm"]), int(q["sCn"])))
+            acc = np.zeros((M, N))
+            for r in range(R):
+                A = _strided(int(q["A"]) + 8 * r * int(q["sAr"]), (M, K), (int(q["sAm"]), int(q["sAk"])))
+                B = _strided(int(q["B"]) + 8 * r * int(q["sBr"]), (K, N), (int(q["sBk"]), int(q["sBn"])))
+                acc += A @ B
+            if q["active"] and _view(int(q["active"]), 1, np.int32)[0] == 0:
+                continue
+            if q["accumulate"]:
+                C += q["alpha"] * acc
+            else:
+                C[...] = q["alpha"] * acc + (q["beta"] * C if q["beta"] != 0 else 0.0)
+        return OK
+
     # -- decompositions -------------------------------------------------------------------
     def tn_qr_workspace_bytes(self, m, n):
         return 0

@@ -1,0 +1,74 @@
+"""The batched engine (tnalg_gb300/batched.py) on the CPU through the test double of the C ABI:
+continuous batching of uneven jobs gives every job the result it gets alone and the result of the
+one-job scheduler; admission keeps to the slot limit and the memory budget."""
+import numpy as np
+import pytest
+
+import fake_lib
+from tnalg_gb300 import batched, serving
+
+
+@pytest.fixture(autouse=True)
+def _fake():
+    fake_lib.install()
+    yield
+    fake_lib.uninstall()
+
+
+SPECS = [(8, 4, 1.0, 0.0), (10, 6, 0.5, 0.2), (12, 4, 1.5, 0.1), (6, 4, 1.0, 0.3), (9, 8, 0.2, 0.6)]
+
+
+def _jobs(kind="batch"):
+    out = []
+    for k, (l, chi, jz, hz) in enumerate(SPECS):
+        para = serving.chain_job_para(l, chi, jz=jz, hz=hz, sweeps=3, device="cpu")
+        cls = batched.BatchJob if kind == "batch" else serving.DMRGJob
+        out.append(cls(k, para, seed=100 + k))
+    return out
+
+
+def _run(jobs, **kw):
+    eng = batched.BatchEngine("cpu", precision="fp64", **kw)
+    for j in jobs:
+        eng.submit(j)
+    done = eng.run()
+    return eng, {j.job_id: j.result for j in done}
+
+
+def test_batched_results_match_alone_and_the_single_job_path():
+    alone = {}
+    for j in _jobs():
+        _, r = _run([j])
+        alone.update(r)
+    eng, mix = _run(_jobs())
+    assert eng.max_concurrent == len(SPECS)
+    single = {}
+    for j in _jobs("serial"):
+        s = serving.Scheduler("cpu", max_active=1)
+        s.submit(j)
+        s.run()
+        single[j.job_id] = j.result
+    for k in range(len(SPECS)):
+        assert mix[k]["e_per_site"] == pytest.approx(alone[k]["e_per_site"], abs=1e-13)
+        np.testing.assert_allclose(mix[k]["eb_full"], alone[k]["eb_full"], atol=1e-12)
+        assert mix[k]["solves"] == alone[k]["solves"] == 3 * 2 * (SPECS[k][0] - 1)
+        # the one-job path (serving.DMRGJob, dmrg_finite_size's schedule) reaches the same state
+        assert mix[k]["e_per_site"] == pytest.approx(single[k]["e_per_site"], abs=1e-10)
+        np.testing.assert_allclose(mix[k]["mz"], single[k]["mz"], atol=1e-8)
+
+
+def test_slots_and_budget_limit_admission_and_late_jobs_join_running_ones():
+    jobs = _jobs()
+    eng, res = _run(jobs, max_active=2)
+    assert eng.max_concurrent == 2 and len(res) == len(SPECS)
+    # a job admitted after others started shares steps with them and still gets its own result
+    _, ref = _run(_jobs())
+    for k in res:
+        assert res[k]["e_per_site"] == pytest.approx(ref[k]["e_per_site"], abs=1e-13)
+    fps = sorted(j.footprint_bytes() for j in _jobs())
+    budget = fps[-1] + fps[-2]
+    eng2, res2 = _run(_jobs(), budget_bytes=budget)
+    assert len(res2) == len(SPECS) and eng2.max_used <= budget and eng2.max_concurrent < len(SPECS)
+    summ = eng2.summary()
+    assert summ["jobs"] == len(SPECS) and summ["solves"] == sum(r["solves"] for r in res2.values())
+    assert summ["latency_p99_s"] >= summ["latency_p50_s"] >= 0.0

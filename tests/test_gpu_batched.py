@@ -139,3 +139,50 @@ def ctypes_ptr(arr):
 def ctypes_ref(obj):
     import ctypes
     return ctypes.byref(obj)
+
+
+@pytest.mark.parametrize("precision", [L.PREC_FP64, L.PREC_TF32X3])
+def test_batched_lanczos_with_straddling_pairs(cuda_lib, precision):
+    """Jobs whose effective Hamiltonian carries straddling pairs (ladder-like couplings across the
+    site), mixed in one batch with jobs that have none."""
+    if precision == L.PREC_TF32X3 and not L.tf32x3_available():
+        pytest.skip("tf32x3 needs an sm_103 device")
+    lib = L.load()
+    specs = [(8, 2, 12, 2), (16, 2, 16, 0), (20, 2, 20, 3), (1, 2, 4, 0)]
+    keep, jobs, dense = [], [], []
+    for i, (cl, d, cr, ng) in enumerate(specs):
+        wl = _sym_block(cl * d, 200 + i, shift=0.3)
+        wr = _sym_block(d * cr, 300 + i)
+        sl = torch.stack([_sym_block(cl, 400 + 7 * i + g) for g in range(ng)]) if ng else None
+        sr = torch.stack([_sym_block(cr, 500 + 7 * i + g) for g in range(ng)]) if ng else None
+        psi = _rand(cl * d * cr, seed=600 + i)
+        out = torch.empty_like(psi)
+        keep += [wl, wr, sl, sr, psi, out]
+        j = L.BatchSolve()
+        j.site = L.SiteDesc(cl, d, cr, wl.data_ptr(), wr.data_ptr(), ng, sl.data_ptr() if ng else None,
+                            sr.data_ptr() if ng else None)
+        j.psi_in, j.psi_out = psi.data_ptr(), out.data_ptr()
+        jobs.append(j)
+        H = _dense_heff(wl, wr, cl, d, cr)
+        eye_d = torch.eye(d, dtype=torch.float64, device="cuda")
+        for g in range(ng):
+            H = H + torch.kron(sl[g], torch.kron(eye_d, sr[g]))
+        dense.append(H)
+    arr = (L.BatchSolve * len(jobs))(*jobs)
+    opts = L.LanczosOpts(1e-12, 1e-4, 0.0, 2e-6, 30, 50, 3, precision, 0, 0)
+    need = lib.tn_batched_lanczos_workspace_bytes(ctypes_ptr(arr), len(jobs), ctypes_ref(opts))
+    ws = torch.empty(need + 1024, dtype=torch.uint8, device="cuda")
+    res = (L.LanczosResult * len(jobs))()
+    st = lib.tn_batched_lanczos(ctypes_ptr(arr), len(jobs), ctypes_ref(opts), ws.data_ptr(), ws.numel(),
+                                ctypes_ptr(res), L.stream_handle())
+    assert st == L.TN_OK, lib.tn_last_error()
+    torch.cuda.synchronize()
+    for i, H in enumerate(dense):
+        w = torch.linalg.eigvalsh(H)
+        x = keep[6 * i + 5]
+        scale = max(1.0, abs(w[0].item()))
+        rq = (x @ (H @ x)).item()
+        tol = 1e-10 if precision == L.PREC_FP64 else 1e-9
+        assert abs(rq - w[0].item()) < tol * scale, (i, rq, w[0].item())
+        if precision == L.PREC_FP64:
+            assert abs(res[i].energy - w[0].item()) < 1e-10 * scale

@@ -307,3 +307,19 @@ def test_tf32x3_ladder_with_straddling_couplings(tf32):
     with contextlib.redirect_stdout(io.StringIO()):
         ob, A, info, _ = DMRG_anyH.dmrg_finite_size(gc.para_of("ladder_2x4_chi8", precision="tf32x3"))
     assert abs(ob["e_per_site"] - float(g["e_per_site"])) <= 1e-7
+
+
+def test_tf32x3_j1j2_lattice_matches_fp64_after_ten_sweeps(tf32):
+    """The frustrated J1-J2 model (J2 = 0.5) on a 4 x 4 open square lattice in snake order (straddling
+    couplings up to 7 sites apart), 10 sweeps at chi = 64 from the same seeded random MPS on both
+    paths: the split-TF32 state's energy per site (FP64 observables) within 1e-8 of the plain FP64
+    path's, the energy per site of the metric's tolerance."""
+    from tnalg_gb300 import Parameters as pm
+    from tnalg_gb300 import run_lattice
+    para = pm.generate_parameters_j1j2_snake(4, 4, j1=1.0, j2=0.5)
+    para.update(tau=1e-4, eigs_tol=1e-12)
+    mixed = run_lattice.run(para, "tf32x3", [64], 10, "cuda", seed=0)
+    fp64 = run_lattice.run(para, "fp64", [64], 10, "cuda", seed=0)
+    assert mixed["chi_max"] == fp64["chi_max"] == 64
+    assert abs(mixed["e_per_site"] - fp64["e_per_site"]) <= 1e-8, (mixed["e_per_site"], fp64["e_per_site"])
+    assert np.max(np.abs(mixed["eb_full"] - fp64["eb_full"])) < 1e-5

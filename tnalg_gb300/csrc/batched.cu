@@ -372,13 +372,14 @@ size_t al(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 struct Layout {
   std::vector<BjJob> jobs;
   std::vector<int> chunk_prefix;
-  // matvec tables
-  std::vector<GgStage> st_static, st_iter;
-  std::vector<int> pf_static, pf_iter;
-  std::vector<GgProblem> probs;
-  std::vector<int> pf_probs;
-  std::vector<GgF64Problem> f64;
-  std::vector<int> pf_f64;
+  // matvec tables; phase 2 (straddling pairs: y += sum_g Z_g SR_g^T after Z = [SL_g] x) runs after
+  // phase 1 (WL x, x WR^T, Z)
+  std::vector<GgStage> st_static, st_iter, st_iter2;
+  std::vector<int> pf_static, pf_iter, pf_iter2;
+  std::vector<GgProblem> probs, probs2;
+  std::vector<int> pf_probs, pf_probs2;
+  std::vector<GgF64Problem> f64, f64b;
+  std::vector<int> pf_f64, pf_f64b;
   BjJob* d_jobs = nullptr;
   unsigned int* tickets = nullptr;
   size_t tickets_bytes = 0;
@@ -402,12 +403,15 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
   L->chunk_prefix.assign(1, 0);
   L->pf_static.assign(1, 0);
   L->pf_iter.assign(1, 0);
+  L->pf_iter2.assign(1, 0);
   L->pf_probs.assign(1, 0);
+  L->pf_probs2.assign(1, 0);
   L->pf_f64.assign(1, 0);
+  L->pf_f64b.assign(1, 0);
   for (int i = 0; i < count; ++i) {
     const tn_site_desc& d = in[i].site;
-    if (d.chil <= 0 || d.d <= 0 || d.chir <= 0) return tn_fail(TN_ERR_ARG, "batched lanczos: bad site shape");
-    if (d.nstr > 0) return tn_fail(TN_ERR_ARG, "batched lanczos: straddling pairs are not supported here");
+    if (d.chil <= 0 || d.d <= 0 || d.chir <= 0 || d.nstr < 0) return tn_fail(TN_ERR_ARG, "batched lanczos: bad site shape");
+    if (d.nstr > 0 && (!d.sl || !d.sr)) return tn_fail(TN_ERR_ARG, "batched lanczos: straddling pointers missing");
     if (!in[i].psi_in || !in[i].psi_out) return tn_fail(TN_ERR_ARG, "batched lanczos: null vector");
     const int64_t cl = d.chil, dd = d.d, cr = d.chir, n = cl * dd * cr;
     if (n > (1LL << 30)) return tn_fail(TN_ERR_ARG, "batched lanczos: site too large");
@@ -432,18 +436,44 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
     J.psi_out = in[i].psi_out;
     J.active = 1;
     L->jobs.push_back(J);
-    // matvec problems: WL . x  and  x . WR^T, both added into w
+    const int64_t ng = d.nstr;
+    double* Z = ng > 0 ? (double*)take(sizeof(double) * (size_t)ng * n) : nullptr;
+    // matvec problems: WL . x  and  x . WR^T, both added into w; straddling pairs in two phases
     if (mixed) {
       auto stage = [&](std::vector<GgStage>& v, std::vector<int>& pf, const double* src, int64_t rows, int64_t K,
-                       int64_t s_row, int64_t s_k) -> const float* {
+                       int64_t s_row, int64_t s_k, int64_t nred = 1, int64_t s_red = 0) -> const float* {
         GgStage g{};
-        g.src = src; g.s_row = s_row; g.s_k = s_k; g.s_red = 0; g.active = active;
-        gg_stage_shape(&g, rows, K, 1);
-        g.dst = (float*)take(sizeof(float) * gg_staged_floats(rows, K, 1));
+        g.src = src; g.s_row = s_row; g.s_k = s_k; g.s_red = s_red; g.active = active;
+        gg_stage_shape(&g, rows, K, nred);
+        g.dst = (float*)take(sizeof(float) * gg_staged_floats(rows, K, nred));
         v.push_back(g);
         pf.push_back(pf.back() + gg_stage_tiles(g));
         return g.dst;
       };
+      if (ng > 0) {
+        // phase 1: Z (ng chil x d chir) = [SL_1; ...; SL_ng] (ng chil x chil) . x (chil x d chir)
+        GgProblem p{};
+        p.M = (int32_t)(ng * cl); p.N = (int32_t)(dd * cr); p.nred = 1;
+        p.n_kb = (int32_t)tn_cdiv(cl, 32); p.n_nt = (int32_t)tn_cdiv(dd * cr, 128);
+        p.a = stage(L->st_static, L->pf_static, d.sl, ng * cl, cl, cl, 1);
+        p.a_nrt = (int32_t)tn_cdiv(ng * cl, 128);
+        p.b = stage(L->st_iter, L->pf_iter, J.x, dd * cr, cl, 1, dd * cr);  // B^T rows (s b), k = a
+        p.b_nrt = (int32_t)tn_cdiv(dd * cr, 128);
+        p.C = Z; p.sCm = dd * cr; p.sCn = 1; p.alpha = 1.0; p.beta = 0.0; p.accumulate = 0; p.active = active;
+        L->probs.push_back(p);
+        L->pf_probs.push_back(L->pf_probs.back() + gg_tf32_tiles(p, 128));
+        // phase 2: w += sum_g Z_g (chil d x chir) . SR_g^T
+        GgProblem q{};
+        q.M = (int32_t)(cl * dd); q.N = (int32_t)cr; q.nred = (int32_t)ng;
+        q.n_kb = (int32_t)tn_cdiv(cr, 32); q.n_nt = (int32_t)tn_cdiv(cr, 128);
+        q.a = stage(L->st_iter2, L->pf_iter2, Z, cl * dd, cr, cr, 1, ng, n);
+        q.a_nrt = (int32_t)tn_cdiv(cl * dd, 128);
+        q.b = stage(L->st_static, L->pf_static, d.sr, cr, cr, cr, 1, ng, cr * cr);  // B^T rows b = SR_g rows
+        q.b_nrt = (int32_t)tn_cdiv(cr, 128);
+        q.C = J.w; q.sCm = cr; q.sCn = 1; q.alpha = 1.0; q.accumulate = 1; q.active = active;
+        L->probs2.push_back(q);
+        L->pf_probs2.push_back(L->pf_probs2.back() + gg_tf32_tiles(q, 128));
+      }
       if (d.wl) {
         GgProblem p{};
         p.M = (int32_t)(cl * dd); p.N = (int32_t)cr; p.nred = 1;
@@ -469,6 +499,22 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
         L->pf_probs.push_back(L->pf_probs.back() + gg_tf32_tiles(p, 128));
       }
     } else {
+      if (ng > 0) {
+        GgF64Problem f{};
+        f.M = (int32_t)(ng * cl); f.N = (int32_t)(dd * cr); f.K = (int32_t)cl; f.nred = 1;
+        f.A = d.sl; f.sAm = cl; f.sAk = 1;
+        f.B = J.x; f.sBk = dd * cr; f.sBn = 1;
+        f.C = Z; f.sCm = dd * cr; f.sCn = 1; f.alpha = 1.0; f.beta = 0.0; f.accumulate = 0; f.active = active;
+        L->f64.push_back(f);
+        L->pf_f64.push_back(L->pf_f64.back() + gg_f64_tiles(f));
+        GgF64Problem g{};
+        g.M = (int32_t)(cl * dd); g.N = (int32_t)cr; g.K = (int32_t)cr; g.nred = (int32_t)ng;
+        g.A = Z; g.sAm = cr; g.sAk = 1; g.sAr = n;
+        g.B = d.sr; g.sBk = 1; g.sBn = cr; g.sBr = cr * cr;
+        g.C = J.w; g.sCm = cr; g.sCn = 1; g.alpha = 1.0; g.accumulate = 1; g.active = active;
+        L->f64b.push_back(g);
+        L->pf_f64b.push_back(L->pf_f64b.back() + gg_f64_tiles(g));
+      }
       if (d.wl) {
         GgF64Problem f{};
         f.M = (int32_t)(cl * dd); f.N = (int32_t)cr; f.K = (int32_t)(cl * dd); f.nred = 1;
@@ -497,10 +543,16 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
   tab(sizeof(int) * L->pf_static.size());
   tab(sizeof(GgStage) * L->st_iter.size());
   tab(sizeof(int) * L->pf_iter.size());
+  tab(sizeof(GgStage) * L->st_iter2.size());
+  tab(sizeof(int) * L->pf_iter2.size());
   tab(sizeof(GgProblem) * L->probs.size());
   tab(sizeof(int) * L->pf_probs.size());
+  tab(sizeof(GgProblem) * L->probs2.size());
+  tab(sizeof(int) * L->pf_probs2.size());
   tab(sizeof(GgF64Problem) * L->f64.size());
   tab(sizeof(int) * L->pf_f64.size());
+  tab(sizeof(GgF64Problem) * L->f64b.size());
+  tab(sizeof(int) * L->pf_f64b.size());
   L->bytes = off + 1024;
   return TN_OK;
 }
@@ -550,11 +602,18 @@ extern "C" int tn_batched_lanczos(const tn_batch_solve* in, int count, const tn_
   int* d_pst = (int*)put(L.pf_static.data(), sizeof(int) * L.pf_static.size());
   GgStage* d_sit = (GgStage*)put(L.st_iter.data(), sizeof(GgStage) * L.st_iter.size());
   int* d_pit = (int*)put(L.pf_iter.data(), sizeof(int) * L.pf_iter.size());
+  GgStage* d_sit2 = (GgStage*)put(L.st_iter2.data(), sizeof(GgStage) * L.st_iter2.size());
+  int* d_pit2 = (int*)put(L.pf_iter2.data(), sizeof(int) * L.pf_iter2.size());
   GgProblem* d_pr = (GgProblem*)put(L.probs.data(), sizeof(GgProblem) * L.probs.size());
   int* d_ppr = (int*)put(L.pf_probs.data(), sizeof(int) * L.pf_probs.size());
+  GgProblem* d_pr2 = (GgProblem*)put(L.probs2.data(), sizeof(GgProblem) * L.probs2.size());
+  int* d_ppr2 = (int*)put(L.pf_probs2.data(), sizeof(int) * L.pf_probs2.size());
   GgF64Problem* d_f = (GgF64Problem*)put(L.f64.data(), sizeof(GgF64Problem) * L.f64.size());
   int* d_pf = (int*)put(L.pf_f64.data(), sizeof(int) * L.pf_f64.size());
-  if (!d_cpf || !d_sst || !d_pst || !d_sit || !d_pit || !d_pr || !d_ppr || !d_f || !d_pf)
+  GgF64Problem* d_f2 = (GgF64Problem*)put(L.f64b.data(), sizeof(GgF64Problem) * L.f64b.size());
+  int* d_pf2 = (int*)put(L.pf_f64b.data(), sizeof(int) * L.pf_f64b.size());
+  if (!d_cpf || !d_sst || !d_pst || !d_sit || !d_pit || !d_sit2 || !d_pit2 || !d_pr || !d_ppr || !d_pr2 ||
+      !d_ppr2 || !d_f || !d_pf || !d_f2 || !d_pf2)
     return tn_record_error(cudaGetLastError());
   // the counter of running jobs lives in the first bytes of the workspace
   int* running = (int*)base;
@@ -581,8 +640,13 @@ extern "C" int tn_batched_lanczos(const tn_batch_solve* in, int count, const tn_
     if (mixed) {
       if ((st = gg_launch_stage(d_sit, (int)L.st_iter.size(), d_pit, L.pf_iter.back(), s))) return st;
       if ((st = gg_launch_tf32(d_pr, (int)L.probs.size(), d_ppr, L.pf_probs.back(), 128, 0, s))) return st;
+      if (!L.probs2.empty()) {
+        if ((st = gg_launch_stage(d_sit2, (int)L.st_iter2.size(), d_pit2, L.pf_iter2.back(), s))) return st;
+        if ((st = gg_launch_tf32(d_pr2, (int)L.probs2.size(), d_ppr2, L.pf_probs2.back(), 128, 0, s))) return st;
+      }
     } else {
       if ((st = gg_launch_f64(d_f, (int)L.f64.size(), d_pf, L.pf_f64.back(), s))) return st;
+      if (!L.f64b.empty() && (st = gg_launch_f64(d_f2, (int)L.f64b.size(), d_pf2, L.pf_f64b.back(), s))) return st;
     }
     const int nc = k + 1;
     bl_multidot_kernel<<<dim3(chunks, nc), NT, 0, s>>>(d_jobs, njobs, d_cpf, 0);

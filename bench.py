@@ -6,20 +6,21 @@ environment updates): spin-1/2 Heisenberg open chain, N=100, J=1, d=2, seeded
 random-normal initial MPS, chi ramped 64 -> 256 -> 512 during the warm-up sweeps, timed
 sweeps at chi=512. Synthetic input of the stated shapes; no dataset is involved.
 
-    python bench.py [--steps K] [--warmup W] [--precision tf32x3|fp64] [--impl ours|reference]
+    python bench.py [--steps K] [--warmup W] [--precision tf32x3|fp64] [--impl ours|reference] [--no-legs]
 
 Prints ONE JSON line. `value` = sweeps/s (inputs resident in HBM), `e2e` = sweeps/s of a full
-dmrg_finite_size() job from host inputs (ramp included, final MPS copied back to the host).
-On the split-TF32 path at one GPU, `fp64_path` repeats the same job (seed, ramp, timed sweeps) on
-the plain FP64 GPU path: its sweeps/s, the speed-up of this line over it and the difference of
-the energies per site (`--no-fp64-leg` skips it).
-On one GPU, `serving` reports the many-jobs path (tnalg_gb300.serving: 16 uneven XXZ chains interleaved,
-against the same jobs one at a time on the plain FP64 GPU path: solves/s, p50/p99 latency; `--no-serving`
-skips it). `j1j2_6x6` reports the J1-J2 model on the 6 x 6 snake-ordered square lattice at chi=512
-(tnalg_gb300.run_lattice, against the plain FP64 path; `--no-lattice` skips it). Both legs run in child
-processes and report a failure in the line instead of stopping the benchmark.
-`--impl reference` times the CPU restatement of the reference (oracle/, numpy + scipy ARPACK)
-on a bounded sample of the same workload and extrapolates sweeps/s.
+dmrg_finite_size() job from host inputs (ramp included, final MPS copied back to the host),
+`cpu_baseline` = the reference's local update (oracle/: numpy + scipy ARPACK) measured on the host
+cores on the converged state of the timed sweeps. At one GPU the workload legs follow (child
+processes, one shared time budget; a failure is reported in the line): config1 = N=12, chi=16,
+10 sweeps in full on the CPU port and the GPU path; config2_chain = N=100, chi 64 -> 256 -> 512 over
+8 sweeps, mixed against the plain FP64 GPU path; config3_j1j2 = J1-J2 6x6 in snake order, 10
+sweeps at chi=512, mixed against FP64; config4_batched = 512 uneven XXZ chains advanced together
+(tnalg_gb300.batched) against the same jobs one at a time on the FP64 path; config5_serving = a
+Poisson stream of chain and ladder requests at several rates. `summary` (the last key) gathers
+the figures the metric is quoted on.
+`--impl reference` times the same local update of the reference's algorithm (oracle/) on a seeded
+random state whose site is converged first, on the host cores.
 """
 import argparse
 import contextlib
@@ -53,13 +54,10 @@ def parse():
     p.add_argument("--eigs-tol", type=float, default=1e-12)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--no-fp64-leg", action="store_true",
-                   help="skip the plain FP64 GPU run of the same job that the split-TF32 line is compared with")
-    p.add_argument("--cpu-solves", type=int, default=1)
-    p.add_argument("--no-serving", action="store_true",
-                   help="skip the serving leg (many small jobs interleaved vs one at a time on the FP64 path)")
-    p.add_argument("--no-lattice", action="store_true",
-                   help="skip the J1-J2 6x6 lattice leg (chi=512, against the FP64 path)")
+    p.add_argument("--cpu-solves", type=int, default=2)
+    p.add_argument("--no-legs", action="store_true",
+                   help="skip the workload legs (configs 1-5: N=12 in full, N=100 and J1-J2 6x6 mixed vs FP64, "
+                        "batched jobs, serving)")
     return p.parse_args()
 
 
@@ -256,111 +254,149 @@ def _initial_host_mps(l, d, chi):
 
 
 # ---------------------------------------------------------------------------------------
-# CPU restatement (oracle) timing: bounded sample of interior local solves at the bench chi
+# CPU restatement (oracle) timing: measured local updates of the bench workload
 
 
-def cpu_sample(length, chi, eigs_tol, nsolves, seed=0):
-    """Bounded CPU sample: local solves at full-chi interior sites of a shorter chain (the cost of an
-    interior solve depends on chi, not on N), extrapolated to 2(N-1) solves per sweep of the N-site
-    chain. Environment construction happens before the clock starts."""
-    from oracle import dmrg_oracle as O
+def cpu_info():
+    """Host cores, CPU model and the BLAS numpy calls (the reference's dgemm/LAPACK)."""
+    model = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu part", "hardware")):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+    except Exception:
+        pass
+    blas = "unknown"
+    try:
+        cfg = np.__config__.CONFIG["Build Dependencies"]["blas"]
+        blas = "%s %s" % (cfg.get("name", ""), cfg.get("version", ""))
+    except Exception:
+        pass
     try:
         import torch
         threads = torch.get_num_threads()
     except Exception:
         threads = os.cpu_count()
-    short = max(8, 2 * int(np.ceil(np.log2(chi))) + 6)  # middle bonds reach chi
-    para = chain_para(short, chi, eigs_tol, "fp64", "cpu")
-    np.random.seed(seed)
-    A = O.OracleMPS(short, 2, chi, para["op"])
+    return {"nproc": os.cpu_count(), "threads": threads, "cpu": model, "blas": blas.strip()}
+
+
+def cpu_sample(length, chi, eigs_tol, nsolves, mps=None, seed=0):
+    """The reference's local update timed on the host cores (oracle/: numpy + scipy ARPACK, the
+    reference's algorithm and bookkeeping) at an interior site of the N-site chain at `chi`:
+      (b) eigsh at a converged site: the site is solved once untimed, then re-solved `nsolves`
+          times from its own eigenvector (ARPACK still builds its ncv = 20 vectors first);
+      (a) one move of the orthogonality centre with the rebuild of the site's operator buckets
+          (the QR move and the transfers of every carried term the move invalidated).
+    A converged sweep costs 2(N-1) x (a + b): both parts measured here, nothing assumed. `mps`: the
+    host tensors of a converged state (the benchmark's own, after its timed sweeps); without it a
+    seeded random MPS, whose site the untimed first solve converges."""
+    from oracle import dmrg_oracle as O
+    para = chain_para(length, chi, eigs_tol, "fp64", "cpu")
+    if mps is None:
+        np.random.seed(seed)
+        A = O.OracleMPS(length, 2, chi, para["op"])
+    else:
+        A = O.OracleMPS(length, 2, chi, para["op"], mps=mps)
     one, two = O.canonical_terms(para["index1"], para["coeff1"], para["index2"], para["coeff2"], A.ops, eigs_tol)
-    mid = short // 2 - 1
+    mid = length // 2 - 1
     t0 = time.time()
     A.correct_orthogonal_center(mid)
-    A.site_buckets(mid, one, two)      # builds the cached environments of the first site
-    t_prep = time.time() - t0
-    # cost of one effective-Hamiltonian application at this site
-    env = A.site_buckets(mid, one, two)
-    psi = A.mps[mid]
-    t = time.time()
-    for _ in range(3):
-        A.apply_heff(env, psi)
-    t_mv = (time.time() - t) / 3
+    A.site_buckets(mid, one, two)
+    A.update_tensor_eigs(mid, one, two, 1e-4, eigs_tol)
+    t_setup = time.time() - t0
     times, mvs = [], []
-    for n in range(mid, mid + nsolves):
+    for _ in range(max(1, nsolves)):
         mv0 = A.n_matvec
         t = time.time()
-        A.update_tensor_eigs(n, one, two, 1e-4, eigs_tol)
+        A.update_tensor_eigs(mid, one, two, 1e-4, eigs_tol)
         times.append(time.time() - t)
         mvs.append(A.n_matvec - mv0)
-    per_solve = float(np.mean(times))
-    mv_per_solve = float(np.mean(mvs))
-    t_rest = max(per_solve - mv_per_solve * t_mv, 0.0)
-    # the reference's eigsh builds ncv=20 Lanczos vectors before its first convergence test, so a
-    # solve started from an already converged site still costs >= 20 matvecs
-    t_converged = 20 * t_mv + t_rest
-    sweeps_per_s = 1.0 / (t_converged * 2 * (length - 1))
-    return {"value": sweeps_per_s, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "numpy/scipy ARPACK restatement of the reference, %d local solve(s) at interior chi=%d sites of a "
-                      "%d-site chain from a random MPS (%.1f s setup untimed): %.2f s/solve with %.0f matvecs of "
-                      "%.3f s; per-solve cost at a converged site estimated as 20 matvecs + %.2f s other work = %.2f s, "
-                      "extrapolated to 2(N-1)=%d solves per N=%d sweep (the random-state sample alone would give "
-                      "%.2e sweeps/s)" % (nsolves, chi, short, t_prep, per_solve, mv_per_solve, t_mv, t_rest,
-                                         t_converged, 2 * (length - 1), length,
-                                         1.0 / (per_solve * 2 * (length - 1)))}
+    t = time.time()
+    A.correct_orthogonal_center(mid + 1)
+    A.site_buckets(mid + 1, one, two)
+    t_move = time.time() - t
+    per_solve = float(np.mean(times)) + t_move
+    sweeps_per_s = 1.0 / (per_solve * 2 * (length - 1))
+    info = cpu_info()
+    return {"value": sweeps_per_s, "unit": UNIT, "cores": info["threads"], "kind": "port",
+            "cpu": info, "solve_s": float(np.mean(times)), "move_s": t_move, "matvecs_per_solve": float(np.mean(mvs)),
+            "sample": "oracle (numpy/scipy ARPACK restatement of the reference) on %d host threads, N=%d chain at "
+                      "chi=%d, %s state: %d eigsh solve(s) at converged interior site %d (%.2f s each, %.0f matvecs) "
+                      "+ one centre move with its operator rebuild (%.2f s), measured; sweeps/s = 1 / (2(N-1) x "
+                      "%.2f s); %.0f s untimed setup" % (
+                          info["threads"], length, chi, "converged (the GPU run's)" if mps is not None else
+                          "seeded random", len(times), mid, float(np.mean(times)), float(np.mean(mvs)), t_move,
+                          per_solve, t_setup)}
 
 
-LEGS_BUDGET_S = 480   # serving + lattice legs together (normally ~3 minutes)
-SERVING_ARGS = ["--jobs", "16", "--sweeps", "3"]
-SERVING_WORKERS = 8
-
-
-def run_serving_leg(precision, timeout=240, deadline=None):
-    """The serving path (tnalg_gb300.serving) in a child process: 16 uneven XXZ chains (N in [16, 48],
-    chi in {16, 32, 64}, 3 sweeps, seeded) interleaved on one GPU in `precision`, against the same
-    jobs run one at a time on the plain FP64 GPU path; solves/s and p50/p99 latency of both, then
-    (`threaded`) the same mix advanced by SERVING_WORKERS host threads. A failure or timeout of a
-    child is reported in the line instead of stopping the benchmark."""
-    cmd = [sys.executable, "-m", "tnalg_gb300.serving"] + SERVING_ARGS + ["--precision", precision,
-                                                                          "--baseline-precision", "fp64"]
-    if deadline is not None:
-        timeout = max(1.0, min(timeout, deadline - time.time()))
-    out = _child_json(cmd, timeout)
-    if "error" in out:
-        return out
-    # the same interleaved mix advanced by SERVING_WORKERS host threads (their library calls release
-    # the GIL, so one job's convergence-check wait no longer holds up the others' kernels), measured
-    # in its own child against the sequential FP64 pass above
-    cmd = [sys.executable, "-m", "tnalg_gb300.serving"] + SERVING_ARGS + [
-        "--precision", precision, "--workers", str(SERVING_WORKERS), "--no-sequential"]
-    left = 150.0 if deadline is None else min(150.0, deadline - time.time())
-    thr = _child_json(cmd, left) if left > 30 else {"skipped": "the legs' time budget was spent"}
-    if "error" not in thr and "skipped" not in thr and out.get("sequential_solves_per_s"):
-        thr["speedup_vs_sequential"] = thr["solves_per_s"] / out["sequential_solves_per_s"]
-        e1, e2 = out.get("e_per_site", {}), thr.get("e_per_site", {})
-        common = set(e1) & set(e2)
-        thr["max_abs_de_per_site_vs_one_thread"] = max((abs(e1[k] - e2[k]) for k in common), default=None)
-    out["threaded"] = thr
+def config1_leg(device):
+    """BASELINE config 1 in full: N=12 Heisenberg chain, chi=16, seed 0, 10 sweeps (break_tol=-1),
+    eigs_tol 1e-12, on the oracle (the reference's numpy/scipy path, host cores) and on the GPU
+    path (dmrg_finite_size, FP64 and split TF32); sweeps/s, solves/s and the energy against exact
+    diagonalisation."""
+    import torch
+    from oracle import dmrg_oracle as O
+    from oracle import ed as ED
+    from tnalg_gb300 import DMRG_anyH
+    para = chain_para(12, 16, 1e-12, "fp64", device)
+    para.update(sweep_time=10, dt_ob=1, break_tol=-1.0)
+    e0 = float(ED.ground_state(12, 2, para["op"], para["index1"], para["coeff1"], para["index2"],
+                               para["coeff2"])[0]) / 12
+    out = {"workload": "N=12 Heisenberg chain, chi=16, 10 sweeps, seed 0", "ed_e_per_site": e0}
+    t = time.time()
+    ob, _, _ = O.dmrg_finite_size(12, 2, 16, para["op"], para["index1"], para["coeff1"], para["index2"],
+                                  para["coeff2"], para["positions_h2"], tau=1e-4, eigs_tol=1e-12, sweep_time=10,
+                                  hx=0.0, hz=0.0, seed=0)
+    w = time.time() - t
+    out["cpu_port"] = {"sweeps_per_s": 10 / w, "solves_per_s": 10 * 22 / w, "wall_s": w,
+                       "abs_de_per_site_vs_ed": abs(ob["e_per_site"] - e0), "cores": cpu_info()["threads"]}
+    for prec in ("fp64", "tf32x3"):
+        q = dict(para)
+        q["precision"] = prec
+        np.random.seed(0)
+        torch.cuda.synchronize()
+        t = time.time()
+        with contextlib.redirect_stdout(io.StringIO()):
+            obg, _, info, _ = DMRG_anyH.dmrg_finite_size(q)
+        torch.cuda.synchronize()
+        w = time.time() - t
+        out["gpu_" + prec] = {"sweeps_per_s": 10 / w, "solves_per_s": info["solves"] / w, "wall_s": w,
+                              "abs_de_per_site_vs_ed": abs(obg["e_per_site"] - e0),
+                              "abs_de_per_site_vs_cpu_port": abs(obg["e_per_site"] - ob["e_per_site"])}
     return out
 
 
-LATTICE_ARGS = ["j1j2", "--width", "6", "--height", "6", "--chi", "512", "--ramp", "64,256", "--steps", "1"]
+LEGS_BUDGET_S = 720   # the child legs together (normally ~8 minutes)
+CHAIN_ARGS = ["chain", "--length", "100", "--chi", "512", "--ramp", "64,256", "--steps", "6"]
+LATTICE_ARGS = ["j1j2", "--width", "6", "--height", "6", "--chi", "512", "--ramp", "", "--steps", "10"]
+BATCH_ARGS = ["--jobs", "512", "--lengths", "16,64", "--chis", "32,64,128", "--sweeps", "8", "--baseline-jobs", "8"]
+SERVING_RATES = (10.0, 100.0, 2000.0)
+SERVING_ARGS = ["--jobs", "48", "--lengths", "16,128", "--ladders", "0.5", "--ladder-rungs", "8,48",
+                "--chis", "32,64,128,256,512", "--sweeps", "6"]
 
 
-def run_lattice_leg(precision, timeout=300):
-    """The J1-J2 lattice workload in a child process (tnalg_gb300.run_lattice): the J1-J2 model
-    (J2 = 0.5) on the 6 x 6 open square lattice in snake order, chi ramped 64 -> 256 -> 512, one
-    CUDA-event-timed sweep at chi=512 in `precision`, then the same seed and schedule on the plain FP64
-    path (sweeps/s, energy difference per site). Failures are reported in the line."""
-    cmd = [sys.executable, "-m", "tnalg_gb300.run_lattice"] + LATTICE_ARGS + ["--precision", precision]
+def run_lattice_leg(args_list, precision, timeout):
+    """A one-job workload (tnalg_gb300.run_lattice) in a child process, on `precision` and then on
+    the plain FP64 GPU path from the same seed and schedule."""
+    cmd = [sys.executable, "-m", "tnalg_gb300.run_lattice"] + args_list + ["--precision", precision]
     if precision != "fp64":
         cmd.append("--compare-fp64")
     return _child_json(cmd, timeout)
 
 
+def run_batch_leg(extra, precision, timeout):
+    """The batched engine (tnalg_gb300.batched) in a child process."""
+    cmd = [sys.executable, "-m", "tnalg_gb300.batched"] + extra + ["--precision", precision]
+    return _child_json(cmd, timeout)
+
+
 def _child_json(cmd, timeout):
     """Run `cmd` (python -m ...) from the repository root; its last JSON line, or an error entry."""
-    shown = "python " + " ".join(cmd[1:])
+    shown = "python " + " ".join(c if c else '""' for c in cmd[1:])
+    if timeout < 20:
+        return {"skipped": "the legs' %d s time budget was spent" % LEGS_BUDGET_S, "command": shown}
     try:
         p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=timeout)
         lines = [x for x in p.stdout.splitlines() if x.startswith("{")]
@@ -372,6 +408,45 @@ def _child_json(cmd, timeout):
         return out
     except Exception as e:  # timeout or unparsable output: report, keep the benchmark line
         return {"error": repr(e)[:300], "command": shown}
+
+
+def _pick(d, keys):
+    return {k: d[k] for k in keys if isinstance(d, dict) and k in d}
+
+
+def summarise(line):
+    """The figures the metric is quoted on, gathered in one compact object (last key of the line)."""
+    out = {}
+    c1 = line.get("config1")
+    if isinstance(c1, dict) and "cpu_port" in c1:
+        out["config1_n12_chi16"] = {"cpu_port_sweeps_per_s": c1["cpu_port"]["sweeps_per_s"],
+                                    "gpu_fp64_sweeps_per_s": c1.get("gpu_fp64", {}).get("sweeps_per_s"),
+                                    "gpu_tf32x3_sweeps_per_s": c1.get("gpu_tf32x3", {}).get("sweeps_per_s"),
+                                    "abs_de_per_site_vs_ed": {k: c1[k]["abs_de_per_site_vs_ed"] for k in
+                                                              ("cpu_port", "gpu_fp64", "gpu_tf32x3") if k in c1}}
+    for key, name in (("config2_chain", "config2_n100_chi512_8sweeps"), ("config3_j1j2", "config3_j1j2_6x6_chi512_10sweeps")):
+        c = line.get(key)
+        if isinstance(c, dict) and "fp64_path" in c:
+            out[name] = {"speedup_vs_fp64": c["speedup_vs_fp64"], "abs_de_per_site_vs_fp64": c["abs_de_per_site_vs_fp64"],
+                         "max_abs_d_term_energy_vs_fp64": c.get("max_abs_d_term_energy_vs_fp64"),
+                         "sweeps_per_s": c["sweeps_per_s"], "fp64_sweeps_per_s": c["fp64_path"]["sweeps_per_s"],
+                         "matvecs_per_solve": c["matvecs_per_solve"],
+                         "fp64_matvecs_per_solve": c["fp64_path"]["matvecs_per_solve"]}
+        elif isinstance(c, dict):
+            out[name] = _pick(c, ["error", "skipped"])
+    c4 = line.get("config4_batched")
+    if isinstance(c4, dict):
+        out["config4_batched_512"] = _pick(c4, ["solves_per_s", "speedup_vs_sequential", "latency_p50_s",
+                                                "latency_p99_s", "max_abs_de_per_site_vs_sequential", "jobs",
+                                                "unconverged_solves", "error", "skipped"])
+        if "sequential" in c4:
+            out["config4_batched_512"]["sequential_fp64_solves_per_s"] = c4["sequential"]["solves_per_s"]
+    c5 = line.get("config5_serving")
+    if isinstance(c5, list):
+        out["config5_serving"] = [_pick(r, ["rate_per_s", "solves_per_s", "latency_p50_s", "latency_p99_s",
+                                            "speedup_vs_sequential", "max_abs_de_per_site_vs_sequential",
+                                            "max_concurrent", "error", "skipped"]) for r in c5]
+    return out
 
 
 def run_reference(args, rank):
@@ -459,41 +534,42 @@ def main():
                                     "matvec": res["mv_ms"] / args.steps,
                                     "rest": ms_step - (res["qr_ms"] + res["lz_ms"]) / args.steps},
             "clocks": res["clocks"], "gpu_launches": res["launches"]}
-    if rank == 0 and world == 1 and mixed and not args.no_fp64_leg:
-        # the same job (seed, ramp, timed sweeps) on the plain FP64 GPU path: the speed-up of the
-        # split-TF32 path and its energy difference per site
-        import copy
-        a64 = copy.copy(args)
-        a64.precision = "fp64"
-        r64, A64, _ = run_ours(a64, rank, 1, local_rank)
-        del A64
-        v64 = args.steps / (r64["ms"] / 1000.0)
-        line["fp64_path"] = {"value": v64, "unit": UNIT, "ms_per_step": r64["ms"] / args.steps,
-                             "e_per_site": r64["e_per_site"], "speedup_of_this_line": value / v64,
-                             "abs_de_per_site": abs(res["e_per_site"] - r64["e_per_site"]),
-                             # index2 rows per bond: (su, sd), (sd, su), (sz, sz) with Jz = 1
-                             "max_abs_d_szsz": float(np.max(np.abs(res["eb_full"][2::3] - r64["eb_full"][2::3]))),
-                             "max_abs_d_bond_energy": float(np.max(np.abs(
-                                 res["eb_full"].reshape(-1, 3).sum(1) - r64["eb_full"].reshape(-1, 3).sum(1)))),
-                             "device_ms_per_sweep": {"qr": r64["qr_ms"] / args.steps,
-                                                     "lanczos_incl_matvec": r64["lz_ms"] / args.steps,
-                                                     "matvec": r64["mv_ms"] / args.steps}}
     if rank == 0 and not args.no_e2e:
         line["e2e"] = run_e2e(args, "cuda:%d" % local_rank, res["precision"])
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_sample(args.length, args.chi, args.eigs_tol, max(1, args.cpu_solves))
-    if rank == 0 and world == 1 and not (args.no_serving and args.no_lattice):
+        # the reference's local update timed on the host cores, on the converged state of the timed sweeps
+        host = [t.detach().cpu().numpy() for t in A.mps_device]
+        line["cpu_baseline"] = cpu_sample(args.length, args.chi, args.eigs_tol, max(1, args.cpu_solves), mps=host)
+        del host
+    if rank == 0 and world == 1 and not args.no_legs:
         del A
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
+        try:
+            line["config1"] = config1_leg("cuda:%d" % local_rank)
+        except Exception as e:
+            line["config1"] = {"error": repr(e)[:300]}
         # the child legs share one time budget, so a stuck leg cannot hold back the line
-        legs_end = time.time() + LEGS_BUDGET_S
-        if not args.no_serving:
-            line["serving"] = run_serving_leg(res["precision"], deadline=legs_end)
-        if not args.no_lattice:
-            left = legs_end - time.time()
-            line["j1j2_6x6"] = (run_lattice_leg(res["precision"], timeout=min(300.0, left)) if left > 60 else
-                                {"skipped": "the legs' %d s time budget was spent" % LEGS_BUDGET_S})
+        end = time.time() + LEGS_BUDGET_S
+        prec = res["precision"]
+        line["config2_chain"] = run_lattice_leg(CHAIN_ARGS, prec, min(200.0, end - time.time()))
+        line["config3_j1j2"] = run_lattice_leg(LATTICE_ARGS, prec, min(330.0, end - time.time()))
+        line["config4_batched"] = run_batch_leg(BATCH_ARGS, prec, min(240.0, end - time.time()))
+        serving = []
+        for k, rate in enumerate(SERVING_RATES):
+            extra = SERVING_ARGS + ["--rate", str(rate), "--baseline-jobs", "4" if k == 0 else "0"]
+            r = run_batch_leg(extra, prec, min(150.0, end - time.time()))
+            for drop in ("e_per_site",):
+                r.pop(drop, None)
+            serving.append(r)
+        if serving and serving[0].get("sequential"):
+            seq = serving[0]["sequential"]["solves_per_s"]
+            for r in serving[1:]:
+                if "solves_per_s" in r:
+                    r["speedup_vs_sequential"] = r["solves_per_s"] / seq
+        line["config5_serving"] = serving
+    if rank == 0:
+        line["summary"] = summarise(line)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

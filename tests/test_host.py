@@ -256,19 +256,23 @@ def test_full_coefficients_match_exact_ground_state(fake_backend):
     assert A.full_coefficients_mps(tol_memory=1) is None
 
 
-def test_bench_serving_leg_reports_failures_in_the_line():
-    """bench.py's serving leg runs in a child process; when the child fails (here: no GPU) the leg
-    returns an error entry with the command instead of raising, so the benchmark line still prints."""
+def _bench():
     import importlib
     import sys
     sys.path.insert(0, os.path.join(gc.GOLDEN, "..", ".."))
     try:
-        bench = importlib.import_module("bench")
-        out = bench.run_serving_leg("fp64", timeout=120)
+        return importlib.import_module("bench")
     finally:
         sys.path.pop(0)
-    assert "error" in out and out["command"].startswith("python -m tnalg_gb300.serving --jobs 16")
-    assert "--baseline-precision fp64" in out["command"]
+
+
+def test_bench_batch_leg_reports_failures_in_the_line():
+    """bench.py's workload legs run in child processes; when a child fails (here: no GPU) the leg
+    returns an error entry with the command instead of raising, so the benchmark line still prints."""
+    bench = _bench()
+    out = bench.run_batch_leg(bench.BATCH_ARGS, "fp64", timeout=120)
+    assert "error" in out and out["command"].startswith("python -m tnalg_gb300.batched --jobs 512")
+    assert bench.run_batch_leg(bench.BATCH_ARGS, "fp64", timeout=1)["skipped"]
 
 
 def test_lattice_runner_reports_timed_sweeps(fake_backend, capsys):
@@ -285,32 +289,23 @@ def test_lattice_runner_reports_timed_sweeps(fake_backend, capsys):
     assert out["e_per_site"] < 0
 
 
-def test_bench_serving_leg_composes_the_threaded_mix(monkeypatch):
-    """The threaded mix is measured in a second child without its own sequential pass; its speed-up
-    is taken against the first child's sequential FP64 solves/s and its per-job energies are
-    compared with the one-thread mix."""
-    import importlib
-    import sys
-    sys.path.insert(0, os.path.join(gc.GOLDEN, "..", ".."))
-    try:
-        bench = importlib.import_module("bench")
-    finally:
-        sys.path.pop(0)
-    calls = []
-
-    def fake_child(cmd, timeout):
-        calls.append(cmd)
-        if "--workers" in cmd:
-            return {"solves_per_s": 3000.0, "e_per_site": {"0": -0.5, "1": -0.4 + 1e-13}}
-        return {"solves_per_s": 600.0, "sequential_solves_per_s": 500.0, "e_per_site": {"0": -0.5, "1": -0.4}}
-
-    monkeypatch.setattr(bench, "_child_json", fake_child)
-    out = bench.run_serving_leg("tf32x3")
-    assert len(calls) == 2 and "--baseline-precision" in calls[0] and "--no-sequential" in calls[1]
-    assert out["threaded"]["speedup_vs_sequential"] == pytest.approx(6.0)
-    assert out["threaded"]["max_abs_de_per_site_vs_one_thread"] < 1e-12
-    monkeypatch.setattr(bench, "_child_json", lambda cmd, timeout: {"error": "exit 1: x", "command": "c"})
-    assert bench.run_serving_leg("fp64") == {"error": "exit 1: x", "command": "c"}
+def test_bench_summary_gathers_the_metric_figures():
+    """The last key of the benchmark line: mixed-vs-FP64 speed-up and energy difference of the
+    one-job legs, the batched leg against sequential FP64 solves, and the serving rates."""
+    bench = _bench()
+    leg = {"speedup_vs_fp64": 12.0, "abs_de_per_site_vs_fp64": 3e-10, "max_abs_d_term_energy_vs_fp64": 2e-5,
+           "sweeps_per_s": 3.0, "matvecs_per_solve": 3.5,
+           "fp64_path": {"sweeps_per_s": 0.25, "matvecs_per_solve": 7.0}}
+    line = {"config2_chain": leg, "config3_j1j2": {"error": "exit 1: x"},
+            "config4_batched": {"solves_per_s": 9000.0, "speedup_vs_sequential": 30.0, "latency_p99_s": 20.0,
+                                "sequential": {"solves_per_s": 300.0}},
+            "config5_serving": [{"rate_per_s": 10.0, "solves_per_s": 500.0, "latency_p99_s": 3.0, "noise": 1}]}
+    out = bench.summarise(line)
+    assert out["config2_n100_chi512_8sweeps"]["speedup_vs_fp64"] == 12.0
+    assert out["config2_n100_chi512_8sweeps"]["fp64_matvecs_per_solve"] == 7.0
+    assert out["config3_j1j2_6x6_chi512_10sweeps"] == {"error": "exit 1: x"}
+    assert out["config4_batched_512"]["sequential_fp64_solves_per_s"] == 300.0
+    assert out["config5_serving"] == [{"rate_per_s": 10.0, "solves_per_s": 500.0, "latency_p99_s": 3.0}]
 
 
 def test_chi_schedule_grows_bonds_and_reaches_the_direct_energy(fake_backend):

@@ -248,7 +248,8 @@ size_t tn_singular_values_batched_workspace_bytes(int count, const tn_sv_item* i
 
 /* ---- grouped contractions (many independent jobs per launch) --------------------------- */
 /*
- * One contraction of a group: C = alpha * sum_r A_r . B_r + beta * C (accumulate == 0; the problem
+ * One contraction of a group (or `batch` contractions A_z . B_z -> C_z at strides sAb, sBb, sCb):
+ * C = alpha * sum_r A_r . B_r + beta * C (accumulate == 0; the problem
  * must then be the only writer of its C in the call), or C += alpha * sum_r A_r . B_r added
  * atomically (accumulate == 1; several problems may add into one C).
  * A_r(m, k) = A[r*sAr + m*sAm + k*sAk], B_r(k, n) = B[r*sBr + k*sBk + n*sBn], C(m, n) = C[m*sCm + n*sCn].
@@ -262,7 +263,8 @@ typedef struct {
   const double* B; int64_t sBk, sBn, sBr;
   double* C; int64_t sCm, sCn;
   double alpha, beta;
-  int32_t accumulate, reserved;
+  int32_t accumulate, batch;       /* batch: z = 0..batch-1 (0 counts as 1); nred must be 1 when batch > 1 */
+  int64_t sAb, sBb, sCb;           /* batch strides of A, B and C */
   const int32_t* active;
 } tn_grouped_gemm_problem;
 
@@ -275,6 +277,59 @@ typedef struct {
 int tn_grouped_gemm(int precision, const tn_grouped_gemm_problem* problems, int count, void* ws, size_t ws_bytes,
                     void* stream);
 size_t tn_grouped_gemm_workspace_bytes(int precision, const tn_grouped_gemm_problem* problems, int count);
+
+/* ---- grouped building blocks and the batched gauge move --------------------------------- */
+enum { TN_BOP_BLOCK_LEFT = 0, TN_BOP_BLOCK_RIGHT = 1, TN_BOP_COMBINE = 2, TN_BOP_SITE_OPS = 3 };
+
+/*
+ * One item of tn_grouped_ops:
+ *  TN_BOP_BLOCK_LEFT / _RIGHT: a block operator as tn_assemble_block (side 0 / 1) into out,
+ *      (chi*d)^2 values; terms: DEVICE tn_block_term[nterms];
+ *  TN_BOP_COMBINE: out[g] = sum_t c_t E[slot_t] as tn_combine_slots (group in the op field), groups
+ *      out_stride apart, total = ngroups * chi^2;
+ *  TN_BOP_SITE_OPS: out[k] = ops[opidx[k]] on the physical bond of the (chi, d, chir) tensor src, as
+ *      tn_apply_site_ops; terms: DEVICE int32 opidx[nterms], outputs out_stride apart.
+ * Environment element (slot, r, c) at src[slot*s_slot + r*s_row + c]. total: output elements.
+ * active: DEVICE flag or NULL (skipped when *active == 0).
+ */
+typedef struct {
+  int32_t kind;
+  int32_t chi, d, chir;
+  int32_t nterms, reserved;
+  const double* src;
+  int64_t s_slot, s_row;
+  const double* ops;
+  const void* terms;
+  double* out;
+  int64_t out_stride;
+  int64_t total;
+  const int32_t* active;
+} tn_batch_op;
+
+/* Every item of a HOST table in one launch (the per-job block assembly, slot gathers and site
+ * operators of MPSClass.py:684-733 and TensorBasicModule.py:414-421 for many jobs). ws: DEVICE
+ * scratch of tn_grouped_ops_workspace_bytes(count). No counterpart in the reference. */
+int tn_grouped_ops(const tn_batch_op* items, int count, void* ws, size_t ws_bytes, void* stream);
+size_t tn_grouped_ops_workspace_bytes(int count);
+
+/* One gauge move of tn_batched_qr_mixed: A (m x n, 1 <= n <= m, m*n <= 32768, general strides) is
+ * replaced by Q (orthonormal columns), R (n x n upper) written to r. */
+typedef struct {
+  int32_t m, n;
+  double* a; int64_t sAm, sAn;
+  double* r; int64_t sRm, sRn;
+  const int32_t* active;
+} tn_qr_item;
+
+/*
+ * The QR gauge moves (left2right / right2left_decompose_tensor, TensorBasicModule.py:314-384) of
+ * many jobs at once, in tn_qr_mixed's precision: FP32 Householder per matrix (one CTA each, the
+ * matrix in shared memory), Q re-orthogonalised in FP64 (||Q^T Q - I|| ~ 1e-12, col(Q) = col(A) to
+ * FP32 accuracy), R accurate to FP32 (it seeds the next local solve). Q overwrites A in place.
+ * Needs an sm_103 device. items: HOST table; ws: DEVICE scratch.
+ */
+int tn_batched_qr_mixed(const tn_qr_item* items, int count, void* ws, size_t ws_bytes, void* stream);
+size_t tn_batched_qr_mixed_workspace_bytes(const tn_qr_item* items, int count);
 
 /* ---- batched local solves -------------------------------------------------------------- */
 /* One job of a batched solve: its effective Hamiltonian and its start / result vectors. */

@@ -231,20 +231,93 @@ class FakeLib:
         from tnalg_gb300 import _lib
         tab = np.ctypeslib.as_array((ctypes.c_uint8 * (int(count) * _lib.GEMM_PROBLEM_DTYPE.itemsize))
                                     .from_address(_addr(problems))).view(_lib.GEMM_PROBLEM_DTYPE)
+        # every product is formed before any output is written (the device stages the operands in
+        # a launch of their own first, so an output may alias an operand)
+        results = []
         for q in tab:
-            M, N, K, R = int(q["M"]), int(q["N"]), int(q["K"]), int(q["nred"])
-            C = _strided(int(q["C"]), (M, N), (int(q["sCm"]), int(q["sCn"])))
-            acc = np.zeros((M, N))
-            for r in range(R):
-                A = _strided(int(q["A"]) + 8 * r * int(q["sAr"]), (M, K), (int(q["sAm"]), int(q["sAk"])))
-                B = _strided(int(q["B"]) + 8 * r * int(q["sBr"]), (K, N), (int(q["sBk"]), int(q["sBn"])))
-                acc += A @ B
             if q["active"] and _view(int(q["active"]), 1, np.int32)[0] == 0:
                 continue
+            M, N, K, R = int(q["M"]), int(q["N"]), int(q["K"]), int(q["nred"])
+            for z in range(max(int(q["batch"]), 1)):
+                acc = np.zeros((M, N))
+                for r in range(R):
+                    oa = 8 * (r * int(q["sAr"]) + z * int(q["sAb"]))
+                    ob = 8 * (r * int(q["sBr"]) + z * int(q["sBb"]))
+                    A = _strided(int(q["A"]) + oa, (M, K), (int(q["sAm"]), int(q["sAk"])))
+                    B = _strided(int(q["B"]) + ob, (K, N), (int(q["sBk"]), int(q["sBn"])))
+                    acc += A @ B
+                results.append((q, z, acc))
+        for q, z, acc in results:
+            M, N = int(q["M"]), int(q["N"])
+            C = _strided(int(q["C"]) + 8 * z * int(q["sCb"]), (M, N), (int(q["sCm"]), int(q["sCn"])))
             if q["accumulate"]:
                 C += q["alpha"] * acc
             else:
                 C[...] = q["alpha"] * acc + (q["beta"] * C if q["beta"] != 0 else 0.0)
+        return OK
+
+    def tn_grouped_ops_workspace_bytes(self, count):
+        return 0
+
+    def tn_grouped_ops(self, items, count, ws, wsb, stream):
+        self._count("tn_grouped_ops")
+        from tnalg_gb300 import _lib
+        arr = ctypes.cast(items, ctypes.POINTER(_lib.BatchOp))
+        for i in range(int(count)):
+            it = arr[i]
+            if it.active and _view(it.active, 1, np.int32)[0] == 0:
+                continue
+            chi, d, kind = int(it.chi), int(it.d), int(it.kind)
+            if kind in (0, 1, 2):
+                tl = _terms(it.terms, int(it.nterms))
+                nslot = 1 + max([sl for sl, _, _ in tl] + [0])
+                E = _strided(it.src, (nslot, chi, chi), (int(it.s_slot), int(it.s_row), 1))
+            if kind in (0, 1):
+                nop = 1 + max([o for _, o, _ in tl] + [0])
+                O = _view(it.ops, nop * d * d).reshape(nop, d, d)
+                W = np.zeros((chi * d, chi * d))
+                for slot, op, c in tl:
+                    e = np.eye(chi) if slot < 0 else E[slot]
+                    o = np.eye(d) if op < 0 else O[op]
+                    W += c * (np.kron(e, o) if kind == 0 else np.kron(o, e))
+                _view(it.out, W.size)[:] = W.reshape(-1)
+            elif kind == 2:
+                ng = int(it.total) // (chi * chi)
+                out = _strided(it.out, (ng, chi * chi), (int(it.out_stride), 1))
+                res = np.zeros((ng, chi, chi))
+                for slot, g, c in tl:
+                    res[g] += c * (np.eye(chi) if slot < 0 else E[slot])
+                out[...] = res.reshape(ng, -1)
+            else:
+                chir, nout = int(it.chir), int(it.nterms)
+                idx = _view(it.terms, nout, np.int32)
+                nop = 1 + max(int(idx.max()), 0)
+                O = _view(it.ops, nop * d * d).reshape(nop, d, d)
+                X = _view(it.src, chi * d * chir).reshape(chi, d, chir)
+                out = _strided(it.out, (nout, chi * d * chir), (int(it.out_stride), 1))
+                for k in range(nout):
+                    op = np.eye(d) if idx[k] < 0 else O[idx[k]]
+                    out[k] = np.einsum("xs,asb->axb", op, X).reshape(-1)
+        return OK
+
+    def tn_batched_qr_mixed_workspace_bytes(self, items, count):
+        return 0
+
+    def tn_batched_qr_mixed(self, items, count, ws, wsb, stream):
+        """numpy QR with LAPACK's sign convention (the device's FP32 Householder agrees up to its
+        rounding)."""
+        self._count("tn_batched_qr_mixed")
+        from tnalg_gb300 import _lib
+        arr = ctypes.cast(items, ctypes.POINTER(_lib.QrItem))
+        for i in range(int(count)):
+            it = arr[i]
+            if it.active and _view(it.active, 1, np.int32)[0] == 0:
+                continue
+            m, n = int(it.m), int(it.n)
+            A = _strided(it.a, (m, n), (int(it.sAm), int(it.sAn)))
+            Q, R = np.linalg.qr(A.copy())
+            A[...] = Q
+            _strided(it.r, (n, n), (int(it.sRm), int(it.sRn)))[...] = R
         return OK
 
     # -- decompositions -------------------------------------------------------------------

@@ -27,8 +27,8 @@ def _jobs(kind="batch"):
     return out
 
 
-def _run(jobs, **kw):
-    eng = batched.BatchEngine("cpu", precision="fp64", **kw)
+def _run(jobs, precision="fp64", **kw):
+    eng = batched.BatchEngine("cpu", precision=precision, **kw)
     for j in jobs:
         eng.submit(j)
     done = eng.run()
@@ -72,3 +72,23 @@ def test_slots_and_budget_limit_admission_and_late_jobs_join_running_ones():
     summ = eng2.summary()
     assert summ["jobs"] == len(SPECS) and summ["solves"] == sum(r["solves"] for r in res2.values())
     assert summ["latency_p99_s"] >= summ["latency_p50_s"] >= 0.0
+
+
+def test_grouped_path_matches_the_per_job_path():
+    """The grouped path (job arenas; gauge moves, environment updates and block assembly as
+    grouped launches) against the per-job path, through the test double: same states (the test
+    double's batched QR is LAPACK's, as the per-job path's), chains and a ladder with straddling
+    couplings."""
+    def jobs():
+        out = _jobs()
+        lad = serving.ladder_job_para(4, 8, j_rung=1.3, jz=0.7, hz=0.2, sweeps=3, device="cpu")
+        out.append(batched.BatchJob(len(out), lad, seed=77))
+        return out
+    _, per_job = _run(jobs(), grouped=False)
+    eng, grouped = _run(jobs(), grouped=True)
+    assert all(isinstance(j, batched.ArenaJob) for j in eng.done)
+    for k in per_job:
+        assert grouped[k]["e_per_site"] == pytest.approx(per_job[k]["e_per_site"], abs=1e-11), k
+        np.testing.assert_allclose(grouped[k]["eb_full"], per_job[k]["eb_full"], atol=1e-9)
+        np.testing.assert_allclose(grouped[k]["mz"], per_job[k]["mz"], atol=1e-8)
+        assert grouped[k]["solves"] == per_job[k]["solves"]

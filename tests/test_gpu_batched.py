@@ -186,3 +186,162 @@ def test_batched_lanczos_with_straddling_pairs(cuda_lib, precision):
         assert abs(rq - w[0].item()) < tol * scale, (i, rq, w[0].item())
         if precision == L.PREC_FP64:
             assert abs(res[i].energy - w[0].item()) < 1e-10 * scale
+
+
+def test_batched_qr_mixed_orthonormal_and_spanning(cuda_lib):
+    """Many matrices of uneven shapes (2 x 2 up to 256 x 128 = the shared-memory limit, a transposed
+    view, a rank-deficient one, widely scaled entries) in one call: Q^T Q = I to 1e-12, Q R = A to
+    FP32 accuracy, R upper triangular, span(Q) = col(A)."""
+    if not L.tf32x3_available():
+        pytest.skip("needs an sm_103 device")
+    lib = L.load()
+    shapes = [(2, 2, 1.0), (8, 4, 1e-30), (64, 32, 1.0), (128, 64, 1e5), (256, 128, 1.0), (200, 100, 1.0),
+              (96, 96, 1.0)]
+    keep, items, refs = [], [], []
+    for i, (m, n, scale) in enumerate(shapes):
+        A = _rand(m, n, seed=700 + i) * scale
+        if i == 5:
+            A[:, 50:] = A[:, :50] @ _rand(50, 50, seed=9)   # rank 50 of 100
+        R = torch.zeros(n, n, dtype=torch.float64, device="cuda")
+        keep += [A, R]
+        refs.append(A.clone())
+        items.append(_qr_item(A, m, n, (n, 1), R))
+    At = _rand(72, 48, seed=800)          # A (48 x 72)^T read through strides: Q written back the same way
+    Rt = torch.zeros(48, 48, dtype=torch.float64, device="cuda")
+    keep += [At, Rt]
+    refs.append(At.T.clone())
+    items.append(_qr_item(At, 72, 48, (1, 72), Rt, flat=True))
+    tab = np.concatenate(items)
+    tp = ctypes_ptr_np(tab)
+    ws = torch.empty(lib.tn_batched_qr_mixed_workspace_bytes(tp, len(items)) + 4096, dtype=torch.uint8,
+                     device="cuda")
+    L.check(lib.tn_batched_qr_mixed(tp, len(items), ws.data_ptr(), ws.numel(), L.stream_handle()))
+    L.check(lib.tn_check_device_status(L.stream_handle()))
+    torch.cuda.synchronize()
+    for i, A0 in enumerate(refs):
+        if i < len(shapes):
+            Q, R = keep[2 * i], keep[2 * i + 1]
+        else:
+            Q, R = At.T, Rt
+        m, n = A0.shape
+        eye = torch.eye(n, dtype=torch.float64, device="cuda")
+        assert torch.max(torch.abs(Q.T @ Q - eye)).item() < 1e-12, i
+        scale = torch.max(torch.abs(A0)).item()
+        assert torch.max(torch.abs(Q @ R - A0)).item() < 2e-6 * scale * np.sqrt(n), i
+        assert torch.max(torch.abs(torch.tril(R, -1))).item() == 0.0
+        # the part of A outside span(Q) is at FP32 level
+        resid = A0 - Q @ (Q.T @ A0)
+        assert torch.max(torch.abs(resid)).item() < 2e-6 * scale * np.sqrt(n), i
+
+
+def _qr_item(A, m, n, sA, R, flat=False):
+    r = np.zeros(1, dtype=L.QR_ITEM_DTYPE)
+    r["m"], r["n"], r["a"], r["sAm"], r["sAn"] = m, n, A.data_ptr(), sA[0], sA[1]
+    r["r"], r["sRm"], r["sRn"] = R.data_ptr(), n, 1
+    return r
+
+
+def ctypes_ptr_np(tab):
+    import ctypes
+    return ctypes.c_void_p(tab.ctypes.data)
+
+
+def test_grouped_ops_match_the_single_kernels(cuda_lib):
+    """Block assembly (both sides, strided environment stacks), slot combination and site
+    operators of several jobs in one tn_grouped_ops launch, against tn_assemble_block /
+    tn_combine_slots / tn_apply_site_ops one call at a time."""
+    lib = L.load()
+    d = 2
+    ops = _rand(5, d, d, seed=1)
+    terms = [(0, -1, 1.0), (1, 2, 0.5), (-1, 3, -0.25), (2, 1, 2.0)]
+    tt, nt = L.terms_tensor(terms, torch.device("cuda"))
+    gterms = [(1, 0, 1.0), (2, 0, -0.5), (0, 1, 3.0)]
+    gt, ngt = L.terms_tensor(gterms, torch.device("cuda"))
+    oi = torch.tensor([2, -1, 4], dtype=torch.int32, device="cuda")
+    keep, items, checks = [], [], []
+    for i, chi in enumerate([3, 16, 40]):
+        env = _rand(3, chi, chi, seed=10 + i)
+        for side in (0, 1):
+            w = torch.empty((chi * d) ** 2, dtype=torch.float64, device="cuda")
+            ref = torch.empty_like(w)
+            L.check(lib.tn_assemble_block(side, chi, d, L.ptr(env), L.ptr(ops), L.ptr(tt), nt, L.ptr(ref),
+                                          L.stream_handle()))
+            items.append(_bop(side, chi, d, env, w, (chi * d) ** 2, terms=tt, nterms=nt, ops=ops, s_slot=chi * chi,
+                              s_row=chi))
+            keep += [w, ref]
+            checks.append((w, ref))
+        g = torch.empty(2, chi * chi, dtype=torch.float64, device="cuda")
+        gref = torch.empty_like(g)
+        L.check(lib.tn_combine_slots(chi, L.ptr(env), L.ptr(gt), ngt, 2, L.ptr(gref), L.stream_handle()))
+        items.append(_bop(L.BOP_COMBINE, chi, d, env, g, 2 * chi * chi, terms=gt, nterms=ngt, s_slot=chi * chi,
+                          s_row=chi, out_stride=chi * chi))
+        checks.append((g, gref))
+        x = _rand(chi, d, chi + 1, seed=20 + i)
+        o = torch.empty(3, chi * d * (chi + 1), dtype=torch.float64, device="cuda")
+        oref = torch.empty_like(o)
+        L.check(lib.tn_apply_site_ops(chi, d, chi + 1, L.ptr(x), L.ptr(ops), L.ptr(oi), 3, L.ptr(oref),
+                                      chi * d * (chi + 1), L.stream_handle()))
+        items.append(_bop(L.BOP_SITE_OPS, chi, d, x, o, 3 * chi * d * (chi + 1), terms=oi, nterms=3, ops=ops,
+                          chir=chi + 1, out_stride=chi * d * (chi + 1)))
+        checks.append((o, oref))
+        keep += [env, g, gref, x, o, oref]
+    tab = np.concatenate(items)
+    ws = torch.empty(lib.tn_grouped_ops_workspace_bytes(len(items)), dtype=torch.uint8, device="cuda")
+    L.check(lib.tn_grouped_ops(ctypes_ptr_np(tab), len(items), ws.data_ptr(), ws.numel(), L.stream_handle()))
+    torch.cuda.synchronize()
+    for out, ref in checks:
+        assert torch.max(torch.abs(out - ref)).item() < 1e-13
+
+
+def _bop(kind, chi, d, src, out, total, terms=None, nterms=0, ops=None, s_slot=0, s_row=0, chir=0, out_stride=0):
+    r = np.zeros(1, dtype=L.BATCH_OP_DTYPE)
+    r["kind"], r["chi"], r["d"], r["chir"], r["nterms"] = kind, chi, d, chir, nterms
+    r["src"], r["s_slot"], r["s_row"] = src.data_ptr(), s_slot, s_row
+    r["ops"] = ops.data_ptr() if ops is not None else 0
+    r["terms"] = terms.data_ptr() if terms is not None else 0
+    r["out"], r["out_stride"], r["total"] = out.data_ptr(), out_stride, total
+    return r
+
+
+@pytest.mark.parametrize("precision", [L.PREC_FP64, L.PREC_TF32X3])
+def test_grouped_gemm_batch_dimension(cuda_lib, precision):
+    """batch > 1: C_z = A_z B_z at strides, with A shared by every z (stride 0) as in the closing
+    contractions of an environment update."""
+    if precision == L.PREC_TF32X3 and not L.tf32x3_available():
+        pytest.skip("tf32x3 needs an sm_103 device")
+    Z, M, N, K = 4, 72, 72, 144
+    A = _rand(K, M, seed=1)          # used as A^T (strides (1, M))
+    B = _rand(Z, K, N, seed=2)
+    C = torch.zeros(Z, M, N, dtype=torch.float64, device="cuda")
+    rec = _problem(A, B, C, M, N, K, (1, M), (N, 1), (N, 1))
+    rec["batch"], rec["sAb"], rec["sBb"], rec["sCb"] = Z, 0, K * N, M * N
+    L.grouped_gemm(np.array([rec], dtype=L.GEMM_PROBLEM_DTYPE), precision=precision)
+    torch.cuda.synchronize()
+    ref = torch.einsum("km,zkn->zmn", A, B)
+    err = torch.max(torch.abs(C - ref)).item() / torch.max(torch.abs(ref)).item()
+    assert err < (1e-13 if precision == L.PREC_FP64 else 5e-6), err
+
+
+def test_grouped_engine_matches_the_per_job_engine(cuda_lib):
+    """The batched engine's grouped path (job arenas, grouped launches, batched QR) against its
+    per-job path on the same uneven jobs (XXZ chains and a ladder), split TF32: energies per site
+    within 1e-8 (each path's trajectory carries its own split-TF32 rounding)."""
+    if not L.tf32x3_available():
+        pytest.skip("tf32x3 needs an sm_103 device")
+    from tnalg_gb300 import batched, serving
+
+    def jobs():
+        out = []
+        for k, (l, chi, jz, hz) in enumerate([(12, 16, 1.0, 0.0), (20, 32, 0.5, 0.3), (16, 64, 1.5, 0.1)]):
+            out.append(batched.BatchJob(k, serving.chain_job_para(l, chi, jz=jz, hz=hz, sweeps=4), seed=50 + k))
+        out.append(batched.BatchJob(3, serving.ladder_job_para(6, 32, j_rung=1.2, sweeps=4), seed=60))
+        return out
+    res = {}
+    for grouped in (False, True):
+        eng = batched.BatchEngine("cuda", "tf32x3", grouped=grouped)
+        for j in jobs():
+            eng.submit(j)
+        res[grouped] = {j.job_id: j.result for j in eng.run()}
+    for k in res[False]:
+        assert abs(res[True][k]["e_per_site"] - res[False][k]["e_per_site"]) < 1e-8, k
+        assert res[True][k]["solves"] == res[False][k]["solves"]

@@ -48,6 +48,32 @@ class BatchSolve(ctypes.Structure):
     _fields_ = [("site", SiteDesc), ("psi_in", c_vp), ("psi_out", c_vp)]
 
 
+class BatchOp(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("chi", ctypes.c_int32), ("d", ctypes.c_int32), ("chir", ctypes.c_int32),
+                ("nterms", ctypes.c_int32), ("reserved", ctypes.c_int32), ("src", c_vp), ("s_slot", c_i64),
+                ("s_row", c_i64), ("ops", c_vp), ("terms", c_vp), ("out", c_vp), ("out_stride", c_i64),
+                ("total", c_i64), ("active", c_vp)]
+
+
+class QrItem(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_int32), ("n", ctypes.c_int32), ("a", c_vp), ("sAm", c_i64), ("sAn", c_i64),
+                ("r", c_vp), ("sRm", c_i64), ("sRn", c_i64), ("active", c_vp)]
+
+
+BOP_BLOCK_LEFT, BOP_BLOCK_RIGHT, BOP_COMBINE, BOP_SITE_OPS = range(4)
+BATCH_SOLVE_DTYPE = np.dtype([("chil", "<i8"), ("d", "<i8"), ("chir", "<i8"), ("wl", "<u8"), ("wr", "<u8"),
+                              ("nstr", "<i8"), ("sl", "<u8"), ("sr", "<u8"), ("psi_in", "<u8"), ("psi_out", "<u8")],
+                             align=True)
+BATCH_OP_DTYPE = np.dtype([("kind", "<i4"), ("chi", "<i4"), ("d", "<i4"), ("chir", "<i4"), ("nterms", "<i4"),
+                           ("reserved", "<i4"), ("src", "<u8"), ("s_slot", "<i8"), ("s_row", "<i8"), ("ops", "<u8"),
+                           ("terms", "<u8"), ("out", "<u8"), ("out_stride", "<i8"), ("total", "<i8"),
+                           ("active", "<u8")], align=True)
+QR_ITEM_DTYPE = np.dtype([("m", "<i4"), ("n", "<i4"), ("a", "<u8"), ("sAm", "<i8"), ("sAn", "<i8"), ("r", "<u8"),
+                          ("sRm", "<i8"), ("sRn", "<i8"), ("active", "<u8")], align=True)
+assert BATCH_OP_DTYPE.itemsize == ctypes.sizeof(BatchOp) and QR_ITEM_DTYPE.itemsize == ctypes.sizeof(QrItem)
+assert BATCH_SOLVE_DTYPE.itemsize == ctypes.sizeof(BatchSolve)
+
+
 class SvItem(ctypes.Structure):
     _fields_ = [("k", c_i64), ("n", c_i64), ("x", c_vp), ("sXr", c_i64), ("sXc", c_i64), ("s_out", c_vp)]
 
@@ -57,8 +83,8 @@ class GroupedGemmProblem(ctypes.Structure):
                 ("A", c_vp), ("sAm", c_i64), ("sAk", c_i64), ("sAr", c_i64),
                 ("B", c_vp), ("sBk", c_i64), ("sBn", c_i64), ("sBr", c_i64),
                 ("C", c_vp), ("sCm", c_i64), ("sCn", c_i64),
-                ("alpha", c_dbl), ("beta", c_dbl), ("accumulate", ctypes.c_int32), ("reserved", ctypes.c_int32),
-                ("active", c_vp)]
+                ("alpha", c_dbl), ("beta", c_dbl), ("accumulate", ctypes.c_int32), ("batch", ctypes.c_int32),
+                ("sAb", c_i64), ("sBb", c_i64), ("sCb", c_i64), ("active", c_vp)]
 
 
 # the same record as a numpy dtype (C layout), for tables built with array operations
@@ -66,8 +92,8 @@ GEMM_PROBLEM_DTYPE = np.dtype([("M", "<i4"), ("N", "<i4"), ("K", "<i4"), ("nred"
                                ("A", "<u8"), ("sAm", "<i8"), ("sAk", "<i8"), ("sAr", "<i8"),
                                ("B", "<u8"), ("sBk", "<i8"), ("sBn", "<i8"), ("sBr", "<i8"),
                                ("C", "<u8"), ("sCm", "<i8"), ("sCn", "<i8"),
-                               ("alpha", "<f8"), ("beta", "<f8"), ("accumulate", "<i4"), ("reserved", "<i4"),
-                               ("active", "<u8")], align=True)
+                               ("alpha", "<f8"), ("beta", "<f8"), ("accumulate", "<i4"), ("batch", "<i4"),
+                               ("sAb", "<i8"), ("sBb", "<i8"), ("sCb", "<i8"), ("active", "<u8")], align=True)
 assert GEMM_PROBLEM_DTYPE.itemsize == ctypes.sizeof(GroupedGemmProblem)
 
 
@@ -107,6 +133,10 @@ _SIGS = {
     "tn_singular_values_batched_workspace_bytes": (c_sz, [c_int, c_vp]),
     "tn_grouped_gemm": (c_int, [c_int, c_vp, c_int, c_vp, c_sz, c_vp]),
     "tn_grouped_gemm_workspace_bytes": (c_sz, [c_int, c_vp, c_int]),
+    "tn_grouped_ops": (c_int, [c_vp, c_int, c_vp, c_sz, c_vp]),
+    "tn_grouped_ops_workspace_bytes": (c_sz, [c_int]),
+    "tn_batched_qr_mixed": (c_int, [c_vp, c_int, c_vp, c_sz, c_vp]),
+    "tn_batched_qr_mixed_workspace_bytes": (c_sz, [c_vp, c_int]),
     "tn_batched_lanczos": (c_int, [c_vp, c_int, c_vp, c_vp, c_sz, c_vp, c_vp]),
     "tn_batched_lanczos_workspace_bytes": (c_sz, [c_vp, c_int, c_vp]),
     "tn_profile_enable": (c_int, [c_int]),

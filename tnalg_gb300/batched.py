@@ -110,12 +110,251 @@ class BatchJob:
         self.A = None   # release the device tensors
 
 
+# ---------------------------------------------------------------------------------------------
+# grouped path: every job's state in one device arena, every local update as table rows
+
+
+def _rec(dtype, **kw):
+    r = np.zeros(1, dtype=dtype)
+    for k, v in kw.items():
+        r[k] = v
+    return r
+
+
+def _gemm(M, N, K, A, sA, B, sB, C, sC, *, batch=1, sAb=0, sBb=0, sCb=0, alpha=1.0, beta=0.0, accumulate=0,
+          active=0):
+    return _rec(L.GEMM_PROBLEM_DTYPE, M=M, N=N, K=K, nred=1, A=A, sAm=sA[0], sAk=sA[1], B=B, sBk=sB[0], sBn=sB[1],
+                C=C, sCm=sC[0], sCn=sC[1], alpha=alpha, beta=beta, accumulate=accumulate, batch=batch, sAb=sAb,
+                sBb=sBb, sCb=sCb, active=active)
+
+
+def _op(kind, chi, d, src, out, total, *, terms=0, nterms=0, ops=0, s_slot=0, s_row=0, chir=0, out_stride=0,
+        active=0):
+    return _rec(L.BATCH_OP_DTYPE, kind=kind, chi=chi, d=d, chir=chir, nterms=nterms, src=src, s_slot=s_slot,
+                s_row=s_row, ops=ops, terms=terms, out=out, out_stride=out_stride, total=total, active=active)
+
+
+QR_MAX_ELEMS = 32768   # m n of one matrix of tn_batched_qr_mixed
+
+
+class ArenaJob(BatchJob):
+    """A job of the grouped path. Its MPS, both environment stacks of every bond and its scratch live
+    in one device arena allocated at admission, so every pointer of every local update is fixed and
+    the launch records of each (site, direction) are built once: a step of the batch concatenates
+    the records of every job's current site and runs a dozen grouped launches for all jobs. The
+    arithmetic is that of DeviceMPS (gauge move, incremental environment update with the carry
+    plans of engine.Model, block assembly), in the grouped kernels."""
+
+    def start(self, device, precision):
+        super().start(device, precision)
+        if self.para["ob_position"] != 0:
+            raise ValueError("the grouped path starts its sweeps at site 0 (ob_position = 0)")
+        A = self.A
+        dev = A._dev
+        m = dev.model
+        if m.compressed:
+            raise ValueError("the grouped path runs uncompressed coupling models")
+        Ln, d = A.length, A.phys_dim
+        # a random MPS is centred by QR moves from the right end, which leave the bonds near the left
+        # end wider than d^b; moving the centre right past them and back gives every bond its final
+        # dimension min(chi, d^b, d^(L-b)) now (a reduced QR truncates nothing: the state is
+        # unchanged), so the arena's shapes stay fixed for the whole run
+        b = 0
+        while b < Ln - 1 and int(dev.virtual_dim[b + 1]) > d ** (b + 1):
+            b += 1
+        if b > 0:
+            A.correct_orthogonal_center(b)
+            A.correct_orthogonal_center(0)
+        dev.ensure_envs(0)
+        dims = [int(x) for x in dev.virtual_dim]
+        self.dims, self.d, self.model = dims, d, m
+        nl = [m.n_left(b) for b in range(Ln + 1)]
+        nr = [m.n_right(b) for b in range(Ln + 1)]
+        cmax = max(dims)
+        ngmax = max([m.memo(("sg", p), lambda p=p: m.straddle_groups(p))[2] for p in range(Ln)] + [0])
+        carry_max = max(max(nl), max(nr)) + 1
+        off = 0
+        lay = {}
+
+        def take(name, n):
+            nonlocal off
+            lay[name] = (off, n)
+            off += (n + 31) // 32 * 32   # 256-byte aligned views
+        for n in range(Ln):
+            take(("site", n), dims[n] * d * dims[n + 1])
+        for b in range(Ln + 1):
+            take(("EL", b), (1 + nl[b]) * dims[b] ** 2)
+            take(("ER", b), (1 + nr[b]) * dims[b] ** 2)
+        take("WL", (d * cmax) ** 2)
+        take("WR", (d * cmax) ** 2)
+        take("Wenv", (d * cmax) ** 2)
+        take("seed", d * cmax * cmax)
+        take("R", cmax * cmax)
+        take("T", carry_max * d * cmax * cmax)
+        take("SL", max(ngmax, 1) * cmax * cmax)
+        take("SR", max(ngmax, 1) * cmax * cmax)
+        self.arena = torch.zeros(off, dtype=torch.float64, device=dev.device)
+        self.active = torch.ones(1, dtype=torch.int32, device=dev.device)
+        self.lay = lay
+        base = self.arena.data_ptr()
+        self.addr = {k: base + 8 * o for k, (o, _) in lay.items()}
+        for n in range(Ln):
+            self.view(("site", n)).copy_(dev.mps[n].reshape(-1))
+        self.view(("EL", 0)).copy_(dev.EL[0].reshape(-1))
+        for b in range(1, Ln + 1):
+            self.view(("ER", b)).copy_(dev.ER[b].reshape(-1))
+        # the one-job state is no longer needed (observables use the arena's site tensors)
+        dev.mps = [self.view(("site", n)).view(dims[n], d, dims[n + 1]) for n in range(Ln)]
+        dev.EL = [None] * (Ln + 1)
+        dev.ER = [None] * (Ln + 1)
+        dev.el_upto, dev.er_from = -1, Ln + 1
+        self._rows = {}
+
+    def view(self, key):
+        o, n = self.lay[key]
+        return self.arena[o:o + n]
+
+    def rows(self):
+        """Launch records of this step's local update (built once per (site, direction))."""
+        k = self._k
+        hit = self._rows.get(k)
+        if hit is None:
+            hit = self._rows[k] = self._build(k)
+        return hit
+
+    def _build(self, k):
+        p = self._order[k]
+        right = k < self.para["l"] - 1   # the first half of the sweep moves right
+        m, d, dims, a = self.model, self.d, self.dims, self.addr
+        act = self.active.data_ptr()
+        ops = m.ops.data_ptr()
+        q = p - 1 if right else p + 1
+        cl, cr = dims[q], dims[q + 1]
+        n_q = cl * d * cr
+        site_q = a[("site", q)]
+        out = {"ops1": [], "qr": [], "gemm1": [], "ops2": [], "gemm2": [], "ops3": []}
+        if right:
+            mm, nn = cl * d, cr
+            qr = _rec(L.QR_ITEM_DTYPE, m=mm, n=nn, a=site_q, sAm=cr, sAn=1, r=a["R"], sRm=nn, sRn=1, active=act)
+            # seed = R (cr x cr) . site[p] (cr x d dims[p+1])
+            nxt = d * dims[p + 1]
+            out["gemm1"].append(_gemm(cr, nxt, cr, a["R"], (cr, 1), a[("site", p)], (nxt, 1), a["seed"], (nxt, 1),
+                                      active=act))
+            plan = m.memo(("lcp", q), lambda: m.left_carry_plan(q))
+            terms, nt = m.table_lazy(("wl", q), lambda: m.left_block_terms(q))
+            out["ops1"].append(_op(L.BOP_BLOCK_LEFT, cl, d, a[("EL", q)], a["Wenv"], (cl * d) ** 2, terms=terms.data_ptr(),
+                                   nterms=nt, ops=ops, s_slot=cl * cl, s_row=cl, active=act))
+            # T0 = Wenv (cl d x cl d) . Q (cl d x cr)
+            out["gemm1"].append(_gemm(cl * d, cr, cl * d, a["Wenv"], (cl * d, 1), site_q, (cr, 1), a["T"], (cr, 1),
+                                      active=act))
+            for j, (kind, x) in enumerate(plan):
+                tj = a["T"] + 8 * (1 + j) * n_q
+                if kind == "carry":   # T[1+j] = EL[q][slot] (cl x cl) . Q (cl x d cr)
+                    out["gemm1"].append(_gemm(cl, d * cr, cl, a[("EL", q)] + 8 * x * cl * cl, (cl, 1), site_q,
+                                              (d * cr, 1), tj, (d * cr, 1), active=act))
+                else:
+                    oi = m.opidx(("op", x), [x])
+                    out["ops2"].append(_op(L.BOP_SITE_OPS, cl, d, site_q, tj, n_q, terms=oi.data_ptr(), nterms=1,
+                                           ops=ops, chir=cr, out_stride=n_q, active=act))
+            ns = 1 + len(plan)
+            # EL[p][s] = Q^T (cr x cl d) . T[s] (cl d x cr)
+            out["gemm2"].append(_gemm(cr, cr, cl * d, site_q, (1, cr), a["T"], (cr, 1), a[("EL", p)], (cr, 1),
+                                      batch=ns, sAb=0, sBb=n_q, sCb=cr * cr, active=act))
+        else:
+            mm, nn = d * cr, cl
+            qr = _rec(L.QR_ITEM_DTYPE, m=mm, n=nn, a=site_q, sAm=1, sAn=d * cr, r=a["R"], sRm=nn, sRn=1, active=act)
+            # seed = site[p] (dims[p] d x cl) . R^T
+            prv = dims[p] * d
+            out["gemm1"].append(_gemm(prv, cl, cl, a[("site", p)], (cl, 1), a["R"], (1, cl), a["seed"], (cl, 1),
+                                      active=act))
+            plan = m.memo(("rcp", q), lambda: m.right_carry_plan(q))
+            terms, nt = m.table_lazy(("wrf", q), lambda: m.right_block_terms(q, with_site=True))
+            out["ops1"].append(_op(L.BOP_BLOCK_RIGHT, cr, d, a[("ER", q + 1)], a["Wenv"], (d * cr) ** 2,
+                                   terms=terms.data_ptr(), nterms=nt, ops=ops, s_slot=cr * cr, s_row=cr, active=act))
+            # T0 = B (cl x d cr) . Wenv^T
+            out["gemm1"].append(_gemm(cl, d * cr, d * cr, site_q, (d * cr, 1), a["Wenv"], (1, d * cr), a["T"],
+                                      (d * cr, 1), active=act))
+            for j, (kind, x) in enumerate(plan):
+                tj = a["T"] + 8 * (1 + j) * n_q
+                if kind == "carry":   # T[1+j] = B (cl d x cr) . ER[q+1][slot]^T
+                    out["gemm1"].append(_gemm(cl * d, cr, cr, site_q, (cr, 1), a[("ER", q + 1)] + 8 * x * cr * cr,
+                                              (1, cr), tj, (cr, 1), active=act))
+                else:
+                    oi = m.opidx(("op", x), [x])
+                    out["ops2"].append(_op(L.BOP_SITE_OPS, cl, d, site_q, tj, n_q, terms=oi.data_ptr(), nterms=1,
+                                           ops=ops, chir=cr, out_stride=n_q, active=act))
+            ns = 1 + len(plan)
+            # ER[q][s] = B (cl x d cr) . T[s]^T
+            out["gemm2"].append(_gemm(cl, cl, d * cr, site_q, (d * cr, 1), a["T"], (1, d * cr), a[("ER", q)], (cl, 1),
+                                      batch=ns, sAb=0, sBb=n_q, sCb=cl * cl, active=act))
+        # effective Hamiltonian of site p
+        pl, pr = dims[p], dims[p + 1]
+        t, nt = m.table_lazy(("wl", p), lambda: m.left_block_terms(p))
+        out["ops3"].append(_op(L.BOP_BLOCK_LEFT, pl, d, a[("EL", p)], a["WL"], (pl * d) ** 2, terms=t.data_ptr(),
+                               nterms=nt, ops=ops, s_slot=pl * pl, s_row=pl, active=act))
+        t, nt = m.table_lazy(("wr", p), lambda: m.right_block_terms(p, with_site=False))
+        out["ops3"].append(_op(L.BOP_BLOCK_RIGHT, pr, d, a[("ER", p + 1)], a["WR"], (d * pr) ** 2,
+                               terms=t.data_ptr(), nterms=nt, ops=ops, s_slot=pr * pr, s_row=pr, active=act))
+        slt, srt, ng = m.memo(("sg", p), lambda: m.straddle_groups(p))
+        if ng:
+            ta, na = m.table(("sl", p), slt)
+            tb, nb = m.table(("sr", p), srt)
+            out["ops3"].append(_op(L.BOP_COMBINE, pl, d, a[("EL", p)], a["SL"], ng * pl * pl, terms=ta.data_ptr(),
+                                   nterms=na, s_slot=pl * pl, s_row=pl, out_stride=pl * pl, active=act))
+            out["ops3"].append(_op(L.BOP_COMBINE, pr, d, a[("ER", p + 1)], a["SR"], ng * pr * pr, terms=tb.data_ptr(),
+                                   nterms=nb, s_slot=pr * pr, s_row=pr, out_stride=pr * pr, active=act))
+        solve = _rec(L.BATCH_SOLVE_DTYPE, chil=pl, d=d, chir=pr, wl=a["WL"], wr=a["WR"], nstr=ng,
+                     sl=a["SL"] if ng else 0, sr=a["SR"] if ng else 0, psi_in=a["seed"], psi_out=a[("site", p)])
+        res = {key: (np.concatenate(v) if v else np.zeros(0, dtype=v_dtype(key))) for key, v in out.items() if key != "qr"}
+        res["qr"] = qr
+        res["solve"] = solve
+        res["qr_shape"] = (mm, nn, right, q)
+        res["qr_big"] = mm * nn > QR_MAX_ELEMS
+        return res
+
+    def big_qr(self, ws):
+        """A gauge move whose site tensor exceeds the batched QR's shared memory (m n > 32768, e.g.
+        chi > 128 at d = 2): tn_qr_mixed into a scratch Q, copied back in place."""
+        mm, nn, right, q = self.rows()["qr_shape"]
+        lib = L.load()
+        cl, cr = self.dims[q], self.dims[q + 1]
+        site = self.view(("site", q))
+        Qt = torch.empty(mm * nn, dtype=torch.float64, device=site.device)
+        R = self.view("R")
+        wp, wb = ws.args(lib.tn_qr_mixed_workspace_bytes(mm, nn))
+        if right:
+            L.check(lib.tn_qr_mixed(mm, nn, L.ptr(site), nn, 1, L.ptr(Qt), nn, 1, L.ptr(R), nn, 1, wp, wb,
+                                    L.stream_handle()), "qr_mixed")
+            site.copy_(Qt)
+        else:
+            L.check(lib.tn_qr_mixed(mm, nn, L.ptr(site), 1, mm, L.ptr(Qt), 1, mm, L.ptr(R), nn, 1, wp, wb,
+                                    L.stream_handle()), "qr_mixed")
+            site.copy_(Qt)
+
+    def solved(self, res):
+        done = super().solved(res)
+        return done
+
+    def observe(self):
+        dev = self.A._dev
+        dev.center = self._order[self._k - 1] if self._k > 0 else 0
+        if self._k == 0:
+            dev.center = self._order[-1]
+        dev.unit_norm = True
+        super().observe()
+        self.arena = None
+
+
+def v_dtype(key):
+    return L.GEMM_PROBLEM_DTYPE if key.startswith("gemm") else L.BATCH_OP_DTYPE
+
+
 class BatchEngine:
     """Continuous batching of DMRG jobs: admission by device memory, one batched local solve per
     step for all admitted jobs, p50/p99 latency from arrival to result."""
 
     def __init__(self, device="cuda", precision="tf32x3", budget_bytes=None, max_active=1024, max_krylov=24,
-                 check_every=3, mixed_floor=2e-6, workers=8, streams=16):
+                 check_every=3, mixed_floor=2e-6, workers=8, streams=16, grouped=None):
         self.device = device
         self.workers = max(1, int(workers))
         self.nstreams = max(1, int(streams))
@@ -136,8 +375,12 @@ class BatchEngine:
         self.max_used = 0
         self._used = 0
         self._ws = None
+        self._ws2 = None
         self._t0 = None
         self.step_ms = []
+        # grouped path (job arenas, grouped launches for the whole local update) on the split-TF32
+        # path; the FP64 path prepares every job with its own DeviceMPS calls
+        self.grouped = self.prec == L.PREC_TF32X3 if grouped is None else bool(grouped)
 
     def submit(self, job):
         self.pending.append(job)
@@ -159,6 +402,8 @@ class BatchEngine:
                 break
             job = self.pending.pop(0)
             job.admitted = now
+            if self.grouped and not isinstance(job, ArenaJob):
+                job.__class__ = ArenaJob
             job.start(self.device, self.precision)
             self.active.append(job)
             self._used += fp
@@ -202,11 +447,72 @@ class BatchEngine:
                 results[i] = r
         return results
 
+    def _grouped_step(self, jobs):
+        """One local update of every job of the grouped path: ~a dozen grouped launches for all
+        jobs (block assembly, gauge moves, R-absorb and environment update, effective Hamiltonian)
+        and one batched solve."""
+        lib = L.load()
+        st = L.stream_handle()
+        rows = [j.rows() for j in jobs]
+        if self._ws is None:
+            self._ws = L.Workspace(torch.device(self.device))
+        if self._ws2 is None:
+            self._ws2 = L.Workspace(torch.device(self.device))
+
+        def ops(key):
+            tab = np.concatenate([r[key] for r in rows])
+            if tab.shape[0]:
+                wp, wb = self._ws2.args(lib.tn_grouped_ops_workspace_bytes(tab.shape[0]))
+                L.check(lib.tn_grouped_ops(ctypes.c_void_p(tab.ctypes.data), tab.shape[0], wp, wb, st), "grouped ops")
+            return tab
+
+        def gemm(key):
+            tab = np.concatenate([r[key] for r in rows])
+            if tab.shape[0]:
+                L.grouped_gemm(tab, precision=self.prec, ws=self._ws2)
+            return tab
+
+        keep = [ops("ops1")]
+        small = [r["qr"] for r in rows if not r["qr_big"]]
+        if small:
+            tab = np.concatenate(small)
+            tp = ctypes.c_void_p(tab.ctypes.data)
+            wp, wb = self._ws2.args(lib.tn_batched_qr_mixed_workspace_bytes(tp, tab.shape[0]))
+            L.check(lib.tn_batched_qr_mixed(tp, tab.shape[0], wp, wb, st), "batched qr")
+            keep.append(tab)
+        for j, r in zip(jobs, rows):
+            if r["qr_big"]:
+                j.big_qr(self._ws2)
+        keep += [gemm("gemm1"), ops("ops2"), gemm("gemm2"), ops("ops3")]
+        solves = np.concatenate([r["solve"] for r in rows])
+        return self._solve(jobs, solves, keep)
+
+    def _solve(self, jobs, solves, keep):
+        lib = L.load()
+        opts = L.LanczosOpts(float(jobs[0].para["eigs_tol"]), float(jobs[0].para["tau"]), 0.0, self.mixed_floor,
+                             self.krylov, 50, self.check_every, self.prec, 0, 0)
+        if len({(float(j.para["eigs_tol"]), float(j.para["tau"])) for j in jobs}) > 1:
+            raise ValueError("jobs of one batch share eigs_tol and tau")
+        table = ctypes.c_void_p(solves.ctypes.data)
+        need = lib.tn_batched_lanczos_workspace_bytes(table, len(jobs), ctypes.byref(opts))
+        wp, wb = self._ws.args(need + 1024)
+        res = (L.LanczosResult * len(jobs))()
+        st = lib.tn_batched_lanczos(table, len(jobs), ctypes.byref(opts), wp, wb, ctypes.cast(res, ctypes.c_void_p),
+                                    L.stream_handle())
+        if st not in (L.TN_OK, L.TN_ERR_NOCONV):
+            L.check(st, "batched lanczos")
+        finished = [job for i, job in enumerate(jobs) if job.solved(res[i])]
+        del keep
+        self.steps += 1
+        return finished
+
     def step(self):
         """One local update of every admitted job (one batched solve)."""
         jobs = list(self.active)
         if not jobs:
             return []
+        if self.grouped:
+            return self._grouped_step(jobs)
         keep, solves = [], (L.BatchSolve * len(jobs))()
         for i, (desc, kp, psi) in enumerate(self._prepare_all(jobs)):
             keep.append((kp, psi))

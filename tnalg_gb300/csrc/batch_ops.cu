@@ -1,0 +1,398 @@
+// Grouped building blocks and the batched gauge-move QR of the batched DMRG path.
+//
+// tn_grouped_ops: every item of a table in one launch, each item one of
+//   * a block operator of an enlarged block (the classify_and_update_env buckets summed,
+//     MPSClass.py:684-733), as tn_assemble_block;
+//   * slot combinations out[g] = sum c E[slot] (straddling pairs, gathered carried operators), as
+//     tn_combine_slots;
+//   * site operators on the physical bond (TensorBasicModule.py:414-421), as tn_apply_site_ops.
+// The environment stack of an item has general slot and row strides.
+//
+// tn_batched_qr_mixed: the gauge move of many jobs' site tensors at once (left2right_decompose_tensor
+// / right2left_decompose_tensor, TensorBasicModule.py:314-384), in the mixed precision of tn_qr_mixed:
+//   1. one CTA per matrix (m x n, n <= m, m n <= 32768): the input scaled by a power of two and
+//      rounded to FP32 in shared memory, Householder QR column by column (LAPACK geqr2 order), R
+//      written out (FP32-accurate, scaled back), Q formed in place (org2r order) and written as FP64
+//      over the input and as FP32 into scratch;
+//   2. E = Q^T Q - I in FP64 from the FP32 copy (every product of two FP32 values is exact in FP64);
+//   3. Q <- Q - Q E / 2 with the grouped split-TF32 GEMM (the product is ~1e-6 in size, so its
+//      ~1e-6 relative error is ~1e-12): Q orthonormal to ~1e-12, spanning col(A) to FP32 accuracy.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "grouped.cuh"
+
+namespace {
+
+constexpr int NT = 256;
+constexpr int CHUNK = 2048;  // output elements per block of tn_grouped_ops
+
+__device__ __forceinline__ int find_item(const int* prefix, int n, int t) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ double op_elem(const double* ops, int op, int64_t d, int64_t r, int64_t c) {
+  return op < 0 ? (r == c ? 1.0 : 0.0) : ops[(int64_t)op * d * d + r * d + c];
+}
+
+__global__ void grouped_ops_kernel(const tn_batch_op* items, int nitems, const int* prefix) {
+  const int t = blockIdx.x;
+  const int i = find_item(prefix, nitems, t);
+  const tn_batch_op it = items[i];
+  if (it.active && *it.active == 0) return;
+  const int64_t e0 = (int64_t)(t - prefix[i]) * CHUNK;
+  const int64_t e1 = min(it.total, e0 + CHUNK);
+  const int64_t chi = it.chi, d = it.d;
+  const tn_block_term* terms = (const tn_block_term*)it.terms;
+  for (int64_t idx = e0 + threadIdx.x; idx < e1; idx += blockDim.x) {
+    if (it.kind == TN_BOP_BLOCK_LEFT || it.kind == TN_BOP_BLOCK_RIGHT) {
+      const int64_t n = chi * d;
+      const int64_t row = idx / n, col = idx % n;
+      int64_t er, ec, orr, oc;
+      if (it.kind == TN_BOP_BLOCK_LEFT) {
+        er = row / d; orr = row % d; ec = col / d; oc = col % d;
+      } else {
+        orr = row / chi; er = row % chi; oc = col / chi; ec = col % chi;
+      }
+      double acc = 0.0;
+      for (int q = 0; q < it.nterms; ++q) {
+        const tn_block_term tt = terms[q];
+        const double o = op_elem(it.ops, tt.op, d, orr, oc);
+        if (o == 0.0) continue;
+        const double e = tt.slot < 0 ? (er == ec ? 1.0 : 0.0)
+                                     : it.src[(int64_t)tt.slot * it.s_slot + er * it.s_row + ec];
+        acc = fma(tt.coeff * o, e, acc);
+      }
+      it.out[idx] = acc;
+    } else if (it.kind == TN_BOP_COMBINE) {
+      const int64_t m = chi * chi;
+      const int64_t g = idx / m, e = idx % m, r = e / chi, c = e % chi;
+      double acc = 0.0;
+      for (int q = 0; q < it.nterms; ++q) {
+        const tn_block_term tt = terms[q];
+        if (tt.op != g) continue;
+        const double v = tt.slot < 0 ? (r == c ? 1.0 : 0.0) : it.src[(int64_t)tt.slot * it.s_slot + r * it.s_row + c];
+        acc = fma(tt.coeff, v, acc);
+      }
+      it.out[g * it.out_stride + e] = acc;
+    } else {  // TN_BOP_SITE_OPS: out[k][a, s', b] = sum_s ops[opidx[k]][s', s] src[a, s, b]
+      const int64_t chir = it.chir;
+      const int64_t per = chi * d * chir;
+      const int64_t k = idx / per, e = idx % per;
+      const int64_t a = e / (d * chir), sp = (e / chir) % d, b = e % chir;
+      const int op = ((const int32_t*)it.terms)[k];
+      double acc = 0.0;
+      for (int64_t s = 0; s < d; ++s) acc = fma(op_elem(it.ops, op, d, sp, s), it.src[(a * d + s) * chir + b], acc);
+      it.out[k * it.out_stride + e] = acc;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// batched mixed-precision QR
+
+constexpr int QR_NT = 256;
+constexpr int QR_MAX_ELEMS = 32768;  // m * n floats in shared memory (128 KB)
+
+struct QrbItem {
+  int32_t m, n;
+  double* a;
+  int64_t sAm, sAn;
+  double* r;
+  int64_t sRm, sRn;
+  float* qs;     // FP32 copy of Q, column-major (m x n)
+  double* e;     // n x n Gram correction
+  const int32_t* active;
+};
+
+__device__ __forceinline__ float block_sumf(float v, float* red) {
+  v = tn_warp_sumf(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = 0.f;
+  for (int w = 0; w < QR_NT / 32; ++w) t += red[w];
+  __syncthreads();
+  return t;
+}
+
+// one CTA per matrix; dynamic shared memory: A as column-major m x n floats (ld = m) + tau (n)
+__global__ void __launch_bounds__(QR_NT) qrb_householder_kernel(const QrbItem* items) {
+  extern __shared__ float sm[];
+  __shared__ float red[QR_NT / 32];
+  __shared__ float sv[2];
+  __shared__ int sexp;
+  const QrbItem it = items[blockIdx.x];
+  if (it.active && *it.active == 0) return;
+  const int m = it.m, n = it.n;
+  float* A = sm;             // A[r + c * m]
+  float* tau = sm + m * n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // scale: max |a| to [1, 2) by an exact power of two
+  double mx = 0.0;
+  for (int idx = threadIdx.x; idx < m * n; idx += QR_NT) {
+    const int r = idx % m, c = idx / m;
+    mx = fmax(mx, fabs(it.a[(int64_t)r * it.sAm + (int64_t)c * it.sAn]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  __shared__ double wmax[QR_NT / 32];
+  if (lane == 0) wmax[warp] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < QR_NT / 32; ++w) t = fmax(t, wmax[w]);
+    sexp = (t > 0.0 && isfinite(t)) ? ilogb(t) : 0;
+  }
+  __syncthreads();
+  const int ex = sexp;
+  for (int idx = threadIdx.x; idx < m * n; idx += QR_NT) {
+    const int r = idx % m, c = idx / m;
+    A[idx] = (float)ldexp(it.a[(int64_t)r * it.sAm + (int64_t)c * it.sAn], -ex);
+  }
+  __syncthreads();
+  // Householder QR: column j -> reflector v (v_j = 1 implicit, v below the diagonal stored in A),
+  // tau_j, beta_j on the diagonal
+  for (int j = 0; j < n; ++j) {
+    float ss = 0.f;
+    for (int r = j + 1 + threadIdx.x; r < m; r += QR_NT) ss = fmaf(A[r + j * m], A[r + j * m], ss);
+    ss = block_sumf(ss, red);
+    if (threadIdx.x == 0) {
+      const float alpha = A[j + j * m];
+      float t = 0.f, scale = 0.f, beta = alpha;
+      if (ss > 0.f) {
+        beta = -copysignf(sqrtf(fmaf(alpha, alpha, ss)), alpha);
+        t = (beta - alpha) / beta;
+        scale = 1.f / (alpha - beta);
+      }
+      tau[j] = t;
+      sv[0] = scale;
+      A[j + j * m] = beta;
+    }
+    __syncthreads();
+    const float scale = sv[0];
+    for (int r = j + 1 + threadIdx.x; r < m; r += QR_NT) A[r + j * m] *= scale;
+    __syncthreads();
+    const float tj = tau[j];
+    if (tj != 0.f) {
+      // columns c > j: w = A[j, c] + v . A[j+1:, c]; A[:, c] -= tau w v  (one warp per column)
+      for (int c = j + 1 + warp; c < n; c += QR_NT / 32) {
+        const float ajc = A[j + c * m];  // read by every lane before lane 0 rewrites it
+        float w = 0.f;
+        for (int r = j + 1 + lane; r < m; r += 32) w = fmaf(A[r + j * m], A[r + c * m], w);
+        w = tn_warp_sumf(w) + ajc;
+        const float tw = tj * w;
+        __syncwarp();
+        if (lane == 0) A[j + c * m] = ajc - tw;
+        for (int r = j + 1 + lane; r < m; r += 32) A[r + c * m] = fmaf(-tw, A[r + j * m], A[r + c * m]);
+      }
+    }
+    __syncthreads();
+  }
+  // R (upper n x n), scaled back
+  for (int idx = threadIdx.x; idx < n * n; idx += QR_NT) {
+    const int r = idx / n, c = idx % n;
+    it.r[(int64_t)r * it.sRm + (int64_t)c * it.sRn] = (r <= c) ? ldexp((double)A[r + c * m], ex) : 0.0;
+  }
+  __syncthreads();
+  // Q in place, backwards (org2r): column j of Q from reflector j applied to e_j, after the
+  // columns j+1.. have received reflector j
+  for (int j = n - 1; j >= 0; --j) {
+    const float tj = tau[j];
+    if (j < n - 1) {
+      for (int c = j + 1 + warp; c < n; c += QR_NT / 32) {
+        // w = v . Q[j:, c] with v_j = 1 (Q[j, c] is still 0 here: column c > j has no entries above
+        // its own diagonal yet)
+        const float ajc = A[j + c * m];
+        float w = 0.f;
+        for (int r = j + 1 + lane; r < m; r += 32) w = fmaf(A[r + j * m], A[r + c * m], w);
+        w = tn_warp_sumf(w) + ajc;
+        const float tw = tj * w;
+        __syncwarp();
+        if (lane == 0) A[j + c * m] = ajc - tw;
+        for (int r = j + 1 + lane; r < m; r += 32) A[r + c * m] = fmaf(-tw, A[r + j * m], A[r + c * m]);
+      }
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < m; r += QR_NT) {
+      if (r < j) A[r + j * m] = 0.f;
+      else if (r == j) A[r + j * m] = 1.f - tj;
+      else A[r + j * m] = -tj * A[r + j * m];
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < m * n; idx += QR_NT) {
+    const int r = idx % m, c = idx / m;
+    const float q = A[idx];
+    it.qs[idx] = q;
+    it.a[(int64_t)r * it.sAm + (int64_t)c * it.sAn] = (double)q;
+  }
+}
+
+// E = Q^T Q - I (n x n) from the FP32 copy; each product of two FP32 values is exact in FP64.
+// One block per (item, 32 x 32 tile of E); tiles below the diagonal are skipped and mirrored.
+__global__ void qrb_gram_kernel(const QrbItem* items, const int* prefix, int nitems) {
+  __shared__ float Qi[32][33], Qj[32][33];
+  const int t = blockIdx.x;
+  const int k = find_item(prefix, nitems, t);
+  const QrbItem it = items[k];
+  if (it.active && *it.active == 0) return;
+  const int nt = (it.n + 31) / 32;
+  const int local = t - prefix[k];
+  const int ti = local / nt, tj = local % nt;
+  if (tj < ti) return;
+  const int m = it.m, n = it.n;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads, 4 entries each
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int r0 = 0; r0 < m; r0 += 32) {
+    for (int q = threadIdx.x; q < 32 * 32; q += 256) {
+      const int rr = q & 31, cc = q >> 5;
+      const int r = r0 + rr;
+      Qi[cc][rr] = (r < m && ti * 32 + cc < n) ? it.qs[r + (int64_t)(ti * 32 + cc) * m] : 0.f;
+      Qj[cc][rr] = (r < m && tj * 32 + cc < n) ? it.qs[r + (int64_t)(tj * 32 + cc) * m] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < 32; ++rr) {
+      const double b = (double)Qj[tx][rr];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc[u] = fma((double)Qi[ty + 8 * u][rr], b, acc[u]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = ti * 32 + ty + 8 * u, j = tj * 32 + tx;
+    if (i < n && j < n) {
+      const double v = acc[u] - (i == j ? 1.0 : 0.0);
+      it.e[(int64_t)i * n + j] = v;
+      it.e[(int64_t)j * n + i] = v;
+    }
+  }
+}
+
+size_t al(size_t x, size_t a = 1024) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+extern "C" int tn_grouped_ops(const tn_batch_op* items, int count, void* ws, size_t ws_bytes, void* stream) {
+  if (count <= 0) return TN_OK;
+  if (!items) return tn_fail(TN_ERR_ARG, "grouped ops: null table");
+  cudaStream_t s = (cudaStream_t)stream;
+  std::vector<int> prefix(1, 0);
+  for (int i = 0; i < count; ++i) {
+    const tn_batch_op& it = items[i];
+    if (it.kind < TN_BOP_BLOCK_LEFT || it.kind > TN_BOP_SITE_OPS || it.total < 0 || (it.total > 0 && !it.out))
+      return tn_fail(TN_ERR_ARG, "grouped ops: bad item");
+    prefix.push_back(prefix.back() + (int)tn_cdiv(it.total, CHUNK));
+  }
+  const size_t tb = al(sizeof(tn_batch_op) * (size_t)count), pb = al(sizeof(int) * prefix.size());
+  if (!ws || ws_bytes < tb + pb + 1024) return tn_fail(TN_ERR_WORKSPACE, "grouped ops: workspace too small");
+  char* base = (char*)al((uintptr_t)ws);
+  TN_CUDA(cudaMemcpyAsync(base, items, sizeof(tn_batch_op) * (size_t)count, cudaMemcpyHostToDevice, s));
+  TN_CUDA(cudaMemcpyAsync(base + tb, prefix.data(), sizeof(int) * prefix.size(), cudaMemcpyHostToDevice, s));
+  if (prefix.back() > 0) {
+    grouped_ops_kernel<<<prefix.back(), NT, 0, s>>>((const tn_batch_op*)base, count, (const int*)(base + tb));
+    TN_CHECK_LAUNCH();
+  }
+  return TN_OK;
+}
+
+extern "C" size_t tn_grouped_ops_workspace_bytes(int count) {
+  return al(sizeof(tn_batch_op) * (size_t)std::max(count, 1)) + al(sizeof(int) * (size_t)(count + 1)) + 2048;
+}
+
+namespace {
+struct QrbPlan {
+  std::vector<QrbItem> items;
+  std::vector<int> gram_prefix;
+  std::vector<tn_grouped_gemm_problem> fix;
+  size_t bytes = 0, tab = 0, scratch = 0;
+  int max_smem = 0;
+};
+
+int qrb_plan(const tn_qr_item* in, int count, char* base, QrbPlan* P) {
+  size_t off = 0;
+  P->tab = off;
+  off += al(sizeof(QrbItem) * (size_t)count) + al(sizeof(int) * (size_t)(count + 1));
+  P->gram_prefix.assign(1, 0);
+  for (int i = 0; i < count; ++i) {
+    const tn_qr_item& q = in[i];
+    if (q.n < 1 || q.m < q.n || (int64_t)q.m * q.n > QR_MAX_ELEMS || !q.a || !q.r)
+      return tn_fail(TN_ERR_ARG, "batched qr: need 1 <= n <= m and m n <= 32768");
+    QrbItem it{};
+    it.m = q.m; it.n = q.n;
+    it.a = q.a; it.sAm = q.sAm; it.sAn = q.sAn;
+    it.r = q.r; it.sRm = q.sRm; it.sRn = q.sRn;
+    it.active = q.active;
+    it.qs = base ? (float*)(base + off) : nullptr;
+    off += al(sizeof(float) * (size_t)q.m * q.n);
+    it.e = base ? (double*)(base + off) : nullptr;
+    off += al(sizeof(double) * (size_t)q.n * q.n);
+    P->items.push_back(it);
+    const int nt = (q.n + 31) / 32;
+    P->gram_prefix.push_back(P->gram_prefix.back() + nt * nt);
+    P->max_smem = std::max(P->max_smem, (int)(sizeof(float) * ((size_t)q.m * q.n + q.n)));
+    // Q <- Q - 1/2 Q E: the operands are staged before the product runs, so C may alias A
+    tn_grouped_gemm_problem f{};
+    f.M = q.m; f.N = q.n; f.K = q.n; f.nred = 1; f.batch = 1;
+    f.A = q.a; f.sAm = q.sAm; f.sAk = q.sAn;
+    f.B = it.e; f.sBk = q.n; f.sBn = 1;
+    f.C = q.a; f.sCm = q.sAm; f.sCn = q.sAn;
+    f.alpha = -0.5; f.beta = 1.0; f.accumulate = 0; f.active = q.active;
+    P->fix.push_back(f);
+  }
+  P->scratch = off;
+  P->bytes = off + 2048;
+  return TN_OK;
+}
+}  // namespace
+
+size_t tn_grouped_gemm_workspace_bytes(int precision, const tn_grouped_gemm_problem* problems, int count);
+int tn_grouped_gemm(int precision, const tn_grouped_gemm_problem* problems, int count, void* ws, size_t ws_bytes,
+                    void* stream);
+
+extern "C" size_t tn_batched_qr_mixed_workspace_bytes(const tn_qr_item* items, int count) {
+  if (!items || count <= 0) return 4096;
+  QrbPlan P;
+  if (qrb_plan(items, count, nullptr, &P)) return 0;
+  // the correction GEMM's staging goes behind the plan's own scratch
+  return P.bytes + tn_grouped_gemm_workspace_bytes(TN_PREC_TF32X3, P.fix.data(), count) + 2048;
+}
+
+extern "C" int tn_batched_qr_mixed(const tn_qr_item* items, int count, void* ws, size_t ws_bytes, void* stream) {
+  if (count <= 0) return TN_OK;
+  if (!items) return tn_fail(TN_ERR_ARG, "batched qr: null table");
+  if (!tn_tf32x3_supported()) return tn_fail(TN_ERR_ARG, "batched qr: needs an sm_103 device (split-TF32 correction)");
+  cudaStream_t s = (cudaStream_t)stream;
+  QrbPlan M0;
+  int st = qrb_plan(items, count, nullptr, &M0);
+  if (st) return st;
+  const size_t gg = tn_grouped_gemm_workspace_bytes(TN_PREC_TF32X3, M0.fix.data(), count);
+  if (!ws || ws_bytes < M0.bytes + gg + 2048) return tn_fail(TN_ERR_WORKSPACE, "batched qr: workspace too small");
+  char* base = (char*)al((uintptr_t)ws);
+  QrbPlan P;
+  if ((st = qrb_plan(items, count, base, &P))) return st;
+  QrbItem* d_items = (QrbItem*)(base + P.tab);
+  int* d_gp = (int*)(base + P.tab + al(sizeof(QrbItem) * (size_t)count));
+  TN_CUDA(cudaMemcpyAsync(d_items, P.items.data(), sizeof(QrbItem) * (size_t)count, cudaMemcpyHostToDevice, s));
+  TN_CUDA(cudaMemcpyAsync(d_gp, P.gram_prefix.data(), sizeof(int) * P.gram_prefix.size(), cudaMemcpyHostToDevice, s));
+  if ((st = tn_set_smem_attr_once(TN_ATTR_BATCH_QR, (const void*)qrb_householder_kernel,
+                                  (int)(sizeof(float) * (QR_MAX_ELEMS + 512)))))
+    return st;
+  qrb_householder_kernel<<<count, QR_NT, P.max_smem, s>>>(d_items);
+  TN_CHECK_LAUNCH();
+  qrb_gram_kernel<<<P.gram_prefix.back(), 256, 0, s>>>(d_items, d_gp, count);
+  TN_CHECK_LAUNCH();
+  char* gws = base + al(P.bytes);
+  return tn_grouped_gemm(TN_PREC_TF32X3, P.fix.data(), count, gws, ws_bytes - (size_t)(gws - (char*)ws), stream);
+}

@@ -453,6 +453,7 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
       if (ng > 0) {
         // phase 1: Z (ng chil x d chir) = [SL_1; ...; SL_ng] (ng chil x chil) . x (chil x d chir)
         GgProblem p{};
+        p.nbatch = 1; p.n_mt = (int32_t)tn_cdiv(ng * cl, 128);
         p.M = (int32_t)(ng * cl); p.N = (int32_t)(dd * cr); p.nred = 1;
         p.n_kb = (int32_t)tn_cdiv(cl, 32); p.n_nt = (int32_t)tn_cdiv(dd * cr, 128);
         p.a = stage(L->st_static, L->pf_static, d.sl, ng * cl, cl, cl, 1);
@@ -464,6 +465,7 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
         L->pf_probs.push_back(L->pf_probs.back() + gg_tf32_tiles(p, 128));
         // phase 2: w += sum_g Z_g (chil d x chir) . SR_g^T
         GgProblem q{};
+        q.nbatch = 1; q.n_mt = (int32_t)tn_cdiv(cl * dd, 128);
         q.M = (int32_t)(cl * dd); q.N = (int32_t)cr; q.nred = (int32_t)ng;
         q.n_kb = (int32_t)tn_cdiv(cr, 32); q.n_nt = (int32_t)tn_cdiv(cr, 128);
         q.a = stage(L->st_iter2, L->pf_iter2, Z, cl * dd, cr, cr, 1, ng, n);
@@ -476,6 +478,7 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
       }
       if (d.wl) {
         GgProblem p{};
+        p.nbatch = 1; p.n_mt = (int32_t)tn_cdiv(cl * dd, 128);
         p.M = (int32_t)(cl * dd); p.N = (int32_t)cr; p.nred = 1;
         p.n_kb = (int32_t)tn_cdiv(cl * dd, 32); p.n_nt = (int32_t)tn_cdiv(cr, 128);
         p.a = stage(L->st_static, L->pf_static, d.wl, cl * dd, cl * dd, cl * dd, 1);
@@ -488,6 +491,7 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
       }
       if (d.wr) {
         GgProblem p{};
+        p.nbatch = 1; p.n_mt = (int32_t)tn_cdiv(cl, 128);
         p.M = (int32_t)cl; p.N = (int32_t)(dd * cr); p.nred = 1;
         p.n_kb = (int32_t)tn_cdiv(dd * cr, 32); p.n_nt = (int32_t)tn_cdiv(dd * cr, 128);
         p.a = stage(L->st_iter, L->pf_iter, J.x, cl, dd * cr, dd * cr, 1);
@@ -501,6 +505,7 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
     } else {
       if (ng > 0) {
         GgF64Problem f{};
+        f.nbatch = 1;
         f.M = (int32_t)(ng * cl); f.N = (int32_t)(dd * cr); f.K = (int32_t)cl; f.nred = 1;
         f.A = d.sl; f.sAm = cl; f.sAk = 1;
         f.B = J.x; f.sBk = dd * cr; f.sBn = 1;
@@ -508,6 +513,7 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
         L->f64.push_back(f);
         L->pf_f64.push_back(L->pf_f64.back() + gg_f64_tiles(f));
         GgF64Problem g{};
+        g.nbatch = 1;
         g.M = (int32_t)(cl * dd); g.N = (int32_t)cr; g.K = (int32_t)cr; g.nred = (int32_t)ng;
         g.A = Z; g.sAm = cr; g.sAk = 1; g.sAr = n;
         g.B = d.sr; g.sBk = 1; g.sBn = cr; g.sBr = cr * cr;
@@ -517,6 +523,7 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
       }
       if (d.wl) {
         GgF64Problem f{};
+        f.nbatch = 1;
         f.M = (int32_t)(cl * dd); f.N = (int32_t)cr; f.K = (int32_t)(cl * dd); f.nred = 1;
         f.A = d.wl; f.sAm = cl * dd; f.sAk = 1;
         f.B = J.x; f.sBk = cr; f.sBn = 1;
@@ -526,6 +533,7 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
       }
       if (d.wr) {
         GgF64Problem f{};
+        f.nbatch = 1;
         f.M = (int32_t)cl; f.N = (int32_t)(dd * cr); f.K = (int32_t)(dd * cr); f.nred = 1;
         f.A = J.x; f.sAm = dd * cr; f.sAk = 1;
         f.B = d.wr; f.sBk = 1; f.sBn = dd * cr;

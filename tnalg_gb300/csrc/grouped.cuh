@@ -19,10 +19,11 @@ struct GgStage {
 // added atomically when accumulate).
 struct GgProblem {
   int32_t M, N, n_kb, nred, n_nt, a_nrt, b_nrt, accumulate;
+  int32_t nbatch, n_mt;  // batch entries z (each its own staged A_z, B_z and output C + z sCb)
   const float* a;
   const float* b;
   double* C;
-  int64_t sCm, sCn;
+  int64_t sCm, sCn, sCb;
   double alpha, beta;
   const int32_t* active;
 };
@@ -37,7 +38,8 @@ struct GgF64Problem {
   double* C;
   int64_t sCm, sCn;
   double alpha, beta;
-  int32_t accumulate, pad;
+  int32_t accumulate, nbatch;
+  int64_t sAb, sBb, sCb;
   const int32_t* active;
 };
 

@@ -155,9 +155,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int p = find_item(prefix, nprobs, t);
     const GgProblem P = probs[p];
     const int local = t - prefix[p];
-    const int mt = local / P.n_nt, nt = local % P.n_nt;
+    const int per_z = P.n_mt * P.n_nt;
+    const int z = local / per_z;
+    const int mt = (local % per_z) / P.n_nt, nt = local % P.n_nt;
     const bool skip = P.active && *P.active == 0;
     const int nkb = skip ? 0 : P.n_kb * P.nred;
+    double* const Cz = P.C + (int64_t)z * P.sCb;
 
     if (warp == 0 && lane == 0) {
       const int b_rt = (nt * BN) / BM, b_half = (nt * BN) % BM;  // B rows of this tile in its 128-row tile
@@ -165,7 +168,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int s = issued % STAGES;
         const uint32_t round = issued / STAGES;
         if (round > 0 && !mbar_wait(&empty[s], (round - 1) & 1, err, 1)) { *abort_flag = 1; break; }
-        const int r = i / P.n_kb, kb = i % P.n_kb;
+        const int r = z * P.nred + i / P.n_kb, kb = i % P.n_kb;
         const float* a = P.a + ((size_t)(r * P.a_nrt + mt) * P.n_kb + kb) * PAIR_FLOATS;
         const float* b = P.b + ((size_t)(r * P.b_nrt + b_rt) * P.n_kb + kb) * PAIR_FLOATS;
         mbar_expect_tx(&full[s], cfg::STAGE_BYTES);
@@ -238,7 +241,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             for (int j = 0; j < 16; ++j) {
               const int col = nt * BN + c0 + j;
               if (col < P.N) {
-                double* c = P.C + (int64_t)row * P.sCm + (int64_t)col * P.sCn;
+                double* c = Cz + (int64_t)row * P.sCm + (int64_t)col * P.sCn;
                 const double v = P.alpha * (f32_to_f64(hi[j]) + f32_to_f64(lo[j]));
                 if (P.accumulate) atomicAdd(c, v);
                 else *c = (P.beta == 0.0) ? v : fma(P.beta, *c, v);
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int row = mt * BM + warp * 32 + lane;
       if (row < P.M)
         for (int col = nt * BN; col < min(P.N, nt * BN + BN); ++col) {
-          double* c = P.C + (int64_t)row * P.sCm + (int64_t)col * P.sCn;
+          double* c = Cz + (int64_t)row * P.sCm + (int64_t)col * P.sCn;
           *c = (P.beta == 0.0) ? 0.0 : P.beta * *c;
         }
     }
@@ -284,15 +287,16 @@ __global__ void __launch_bounds__(FNT) gg_f64_kernel(const GgF64Problem* probs, 
   const int p = find_item(prefix, nprobs, t);
   const GgF64Problem P = probs[p];
   if (P.active && *P.active == 0) return;
-  const int local = t - prefix[p];
-  const int n_nt = (P.N + FT - 1) / FT;
+  const int local0 = t - prefix[p];
+  const int n_nt = (P.N + FT - 1) / FT, n_mt = (P.M + FT - 1) / FT;
+  const int z = local0 / (n_mt * n_nt), local = local0 % (n_mt * n_nt);
   const int64_t m0 = (int64_t)(local / n_nt) * FT, n0 = (int64_t)(local % n_nt) * FT;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const bool a_kc = (P.sAk == 1), b_nc = (P.sBn == 1);
   double acc[4][4] = {};
   for (int r = 0; r < P.nred; ++r) {
-    const double* A = P.A + (int64_t)r * P.sAr;
-    const double* B = P.B + (int64_t)r * P.sBr;
+    const double* A = P.A + (int64_t)z * P.sAb + (int64_t)r * P.sAr;
+    const double* B = P.B + (int64_t)z * P.sBb + (int64_t)r * P.sBr;
     for (int64_t k0 = 0; k0 < P.K; k0 += FK) {
       for (int e = tid; e < FT * FK; e += FNT) {
         int mm, kk;
@@ -326,7 +330,7 @@ __global__ void __launch_bounds__(FNT) gg_f64_kernel(const GgF64Problem* probs, 
     for (int j = 0; j < 4; ++j) {
       const int64_t gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
       if (gm < P.M && gn < P.N) {
-        double* c = P.C + gm * P.sCm + gn * P.sCn;
+        double* c = P.C + (int64_t)z * P.sCb + gm * P.sCm + gn * P.sCn;
         const double v = P.alpha * acc[i][j];
         if (P.accumulate) atomicAdd(c, v);
         else *c = (P.beta == 0.0) ? v : fma(P.beta, *c, v);
@@ -355,7 +359,9 @@ void gg_stage_shape(GgStage* it, int64_t rows, int64_t K, int64_t nred) {
 
 int gg_stage_tiles(const GgStage& it) { return it.nred * it.n_rt * it.n_kb; }
 
-int gg_tf32_tiles(const GgProblem& p, int bn) { return (int)(tn_cdiv(p.M, BM) * tn_cdiv(p.N, bn)); }
+int gg_tf32_tiles(const GgProblem& p, int bn) {
+  return (int)(std::max(p.nbatch, 1) * tn_cdiv(p.M, BM) * tn_cdiv(p.N, bn));
+}
 
 int gg_launch_stage(const GgStage* dev_items, int nitems, const int* dev_prefix, int total_tiles, cudaStream_t s) {
   if (total_tiles <= 0) return TN_OK;
@@ -389,7 +395,7 @@ int gg_launch_tf32(const GgProblem* dev_probs, int nprobs, const int* dev_prefix
   return TN_OK;
 }
 
-int gg_f64_tiles(const GgF64Problem& p) { return (int)(tn_cdiv(p.M, FT) * tn_cdiv(p.N, FT)); }
+int gg_f64_tiles(const GgF64Problem& p) { return (int)(std::max(p.nbatch, 1) * tn_cdiv(p.M, FT) * tn_cdiv(p.N, FT)); }
 
 int gg_launch_f64(const GgF64Problem* dev_probs, int nprobs, const int* dev_prefix, int total_tiles, cudaStream_t s) {
   if (total_tiles <= 0) return TN_OK;
@@ -414,8 +420,8 @@ struct GroupPlan {
 };
 
 bool problem_ok(const tn_grouped_gemm_problem& q) {
-  return q.M >= 0 && q.N >= 0 && q.K >= 0 && q.nred >= 1 && (q.C || q.M * q.N == 0) &&
-         (q.K == 0 || (q.A && q.B));
+  return q.M >= 0 && q.N >= 0 && q.K >= 0 && q.nred >= 1 && q.batch >= 0 && (q.batch <= 1 || q.nred == 1) &&
+         (q.C || q.M * q.N == 0) && (q.K == 0 || (q.A && q.B));
 }
 
 int plan_group(int precision, const tn_grouped_gemm_problem* pr, int count, int bn, GroupPlan* g) {
@@ -430,6 +436,7 @@ int plan_group(int precision, const tn_grouped_gemm_problem* pr, int count, int 
       f.B = q.B; f.sBk = q.sBk; f.sBn = q.sBn; f.sBr = q.sBr;
       f.C = q.C; f.sCm = q.sCm; f.sCn = q.sCn;
       f.alpha = q.alpha; f.beta = q.beta; f.accumulate = q.accumulate; f.active = q.active;
+      f.nbatch = std::max(q.batch, 1); f.sAb = q.sAb; f.sBb = q.sBb; f.sCb = q.sCb;
       g->f64.push_back(f);
       g->f64_prefix.push_back(g->f64_prefix.back() + (q.M * q.N ? gg_f64_tiles(f) : 0));
     }
@@ -442,22 +449,27 @@ int plan_group(int precision, const tn_grouped_gemm_problem* pr, int count, int 
     const auto& q = pr[i];
     if (!problem_ok(q)) return tn_fail(TN_ERR_ARG, "grouped gemm: bad problem");
     GgProblem p{};
+    const int32_t nb = std::max(q.batch, 1);
     p.M = q.M; p.N = q.N;
     p.nred = q.nred;
+    p.nbatch = nb;
     p.n_kb = (int32_t)tn_cdiv(q.K, BK);
     p.n_nt = (int32_t)tn_cdiv(q.N, bn);
-    p.C = q.C; p.sCm = q.sCm; p.sCn = q.sCn;
+    p.n_mt = (int32_t)tn_cdiv(q.M, BM);
+    p.C = q.C; p.sCm = q.sCm; p.sCn = q.sCn; p.sCb = q.sCb;
     p.alpha = q.alpha; p.beta = q.beta; p.accumulate = q.accumulate; p.active = q.active;
     if (q.K > 0 && q.M > 0 && q.N > 0) {
+      // a batch is staged like a reduction over z (the two never combine: nred == 1 when batch > 1)
+      const int64_t nr = nb > 1 ? nb : q.nred;
       GgStage a{}, b{};
-      a.src = q.A; a.s_row = q.sAm; a.s_k = q.sAk; a.s_red = q.sAr; a.active = q.active;
-      gg_stage_shape(&a, q.M, q.K, q.nred);
+      a.src = q.A; a.s_row = q.sAm; a.s_k = q.sAk; a.s_red = nb > 1 ? q.sAb : q.sAr; a.active = q.active;
+      gg_stage_shape(&a, q.M, q.K, nr);
       a.dst = (float*)(uintptr_t)off;  // offset now, pointer once the workspace is known
-      off += gg_staged_floats(q.M, q.K, q.nred);
-      b.src = q.B; b.s_row = q.sBn; b.s_k = q.sBk; b.s_red = q.sBr; b.active = q.active;
-      gg_stage_shape(&b, q.N, q.K, q.nred);
+      off += gg_staged_floats(q.M, q.K, nr);
+      b.src = q.B; b.s_row = q.sBn; b.s_k = q.sBk; b.s_red = nb > 1 ? q.sBb : q.sBr; b.active = q.active;
+      gg_stage_shape(&b, q.N, q.K, nr);
       b.dst = (float*)(uintptr_t)off;
-      off += gg_staged_floats(q.N, q.K, q.nred);
+      off += gg_staged_floats(q.N, q.K, nr);
       p.a = a.dst; p.a_nrt = a.n_rt;
       p.b = b.dst; p.b_nrt = b.n_rt;
       g->stages.push_back(a);

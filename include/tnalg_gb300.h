@@ -214,6 +214,20 @@ int tn_singular_values(int64_t k, int64_t n, const double* x, int64_t sXr, int64
 size_t tn_singular_values_workspace_bytes(int64_t k, int64_t n);
 
 /*
+ * Thin SVD X = U diag(s) Vt of the k x n matrix X (general strides) by the same one-sided Jacobi,
+ * with the rotations accumulated: s (k values, unsorted, DEVICE), U (k x k, column i belongs to s[i],
+ * row-major with leading dimension ldu; may be NULL), Vt (k x n, row i = the rotated row i / s[i],
+ * zero for s[i] == 0; leading dimension ldvt; may be NULL). The decomposition behind truncation:
+ * keeping the largest chi values of s with their columns of U and rows of Vt gives the best rank-chi
+ * approximation (the truncated svd of decompose(..., way='svd'), TensorBasicModule.py:338-342).
+ * ws: 256-byte aligned DEVICE scratch of tn_svd_jacobi_workspace_bytes(k, n).
+ */
+int tn_svd_jacobi(int64_t k, int64_t n, const double* x, int64_t sXr, int64_t sXc, double* s_out, double* U,
+                  int64_t ldu, double* Vt, int64_t ldvt, double tol, int max_sweeps, void* ws, size_t ws_bytes,
+                  void* stream);
+size_t tn_svd_jacobi_workspace_bytes(int64_t k, int64_t n);
+
+/*
  * tn_singular_values without a workspace argument and without any device allocation. It has no
  * counterpart in the reference: it exists for hosts that cannot allocate device memory
  * themselves (a service that may only use buffers registered by its own allocator, or a process

@@ -222,6 +222,17 @@ class FakeLib:
                 return st
         return OK
 
+    def tn_dot(self, n, x, y, out, ws, wsb, stream):
+        n = int(n)
+        _view(out, 1)[0] = float(np.dot(_view(x, n), _view(y, n)))
+        return OK
+
+    def tn_scale(self, n, x, alpha, nrm2, stream):
+        n = int(n)
+        f = alpha / np.sqrt(_view(nrm2, 1)[0]) if _addr(nrm2) else alpha
+        _view(x, n)[:] *= f
+        return OK
+
     # -- grouped contractions ----------------------------------------------------------------
     def tn_grouped_gemm_workspace_bytes(self, prec, problems, count):
         return 0

@@ -206,7 +206,7 @@ def test_batched_qr_mixed_orthonormal_and_spanning(cuda_lib):
         keep += [A, R]
         refs.append(A.clone())
         items.append(_qr_item(A, m, n, (n, 1), R))
-    At = _rand(72, 48, seed=800)          # A (48 x 72)^T read through strides: Q written back the same way
+    At = _rand(48, 72, seed=800)          # A = At^T (72 x 48) read through strides; Q written back the same way
     Rt = torch.zeros(48, 48, dtype=torch.float64, device="cuda")
     keep += [At, Rt]
     refs.append(At.T.clone())

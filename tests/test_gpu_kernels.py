@@ -221,3 +221,23 @@ def test_errors_are_reported_not_raised(cuda_lib):
     A = _rand(8, 4, seed=1)
     st = lib.tn_qr(8, 4, L.ptr(A), 4, 1, None, 1, 1, None, 1, 1, None, 0, L.stream_handle())
     assert st == L.TN_ERR_WORKSPACE
+
+
+@pytest.mark.parametrize("k,n,chi", [(40, 60, 12), (96, 64, 30), (33, 33, 33)])
+def test_svd_jacobi_truncation_matches_numpy(cuda_lib, k, n, chi):
+    """tn_svd_jacobi with singular vectors: the rank-chi truncation U_r diag(s_r) Vt_r equals numpy's
+    (the best rank-chi approximation), U and V have orthonormal columns / rows, and the singular
+    values agree to 1e-13 of the largest."""
+    X = _rand(k, n, seed=k + n)
+    X[:, : n // 3] *= 1e-3   # spread the spectrum (distinct values, well separated at the cut)
+    U, s, Vt = L.svd_truncated(X, chi)
+    Xh = X.cpu().numpy()
+    u, sv, vt = np.linalg.svd(Xh, full_matrices=False)
+    r = min(chi, len(sv))
+    np.testing.assert_allclose(s.cpu().numpy(), sv[:r], atol=1e-13 * sv[0], rtol=1e-11)
+    approx = (U * s) @ Vt
+    ref = (u[:, :r] * sv[:r]) @ vt[:r]
+    assert np.max(np.abs(approx.cpu().numpy() - ref)) < 1e-11 * sv[0]
+    eye = np.eye(r)
+    assert np.max(np.abs((U.T @ U).cpu().numpy() - eye)) < 1e-12
+    assert np.max(np.abs((Vt @ Vt.T).cpu().numpy() - eye)) < 1e-12

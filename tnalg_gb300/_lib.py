@@ -129,6 +129,9 @@ _SIGS = {
     "tn_singular_values": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_singular_values_noalloc": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_dbl, c_int, c_vp]),
+    "tn_svd_jacobi": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_vp, c_i64, c_vp, c_i64, c_dbl, c_int, c_vp,
+                              c_sz, c_vp]),
+    "tn_svd_jacobi_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_singular_values_batched": (c_int, [c_int, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_batched_workspace_bytes": (c_sz, [c_int, c_vp]),
     "tn_grouped_gemm": (c_int, [c_int, c_vp, c_int, c_vp, c_sz, c_vp]),
@@ -291,6 +294,25 @@ def singular_values_batched(mats, ws=None, tol=1e-15, max_sweeps=60):
     else:
         check(st, "singular values")
     return [np.sort(o.cpu().numpy())[::-1] for o in outs]
+
+
+def svd_truncated(X, chi, ws=None, tol=1e-15, max_sweeps=60):
+    """Truncated SVD of a 2-D CUDA tensor X (k x n): (U (k x r), s (r,), Vt (r x n)) with the r =
+    min(chi, k) largest singular values in descending order, from tn_svd_jacobi."""
+    lib = load()
+    k, n = int(X.shape[0]), int(X.shape[1])
+    s = torch.empty(k, dtype=torch.float64, device=X.device)
+    U = torch.empty(k, k, dtype=torch.float64, device=X.device)
+    Vt = torch.empty(k, n, dtype=torch.float64, device=X.device)
+    ws = ws or Workspace(X.device)
+    buf = ws.get(lib.tn_svd_jacobi_workspace_bytes(k, n) + 256)
+    base = (buf.data_ptr() + 255) // 256 * 256
+    st = lib.tn_svd_jacobi(k, n, ptr(X), int(X.stride(0)), int(X.stride(1)), ptr(s), ptr(U), k, ptr(Vt), n, tol,
+                           max_sweeps, c_vp(base), c_sz(buf.numel() - (base - buf.data_ptr())), stream_handle())
+    if st != TN_ERR_NOCONV:
+        check(st, "svd")
+    order = torch.argsort(s, descending=True)[: min(int(chi), k)]
+    return U[:, order], s[order], Vt[order]
 
 
 def tf32x3_available():

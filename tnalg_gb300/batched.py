@@ -165,6 +165,18 @@ class ArenaJob(BatchJob):
         if b > 0:
             A.correct_orthogonal_center(b)
             A.correct_orthogonal_center(0)
+        # a random MPS centred by QR moves carries the product of all R factors' norms on its centre
+        # (~1e77 for 64 sites at chi = 128), beyond FP32's range for the split-TF32 absorb of the
+        # first gauge move; the state's norm is irrelevant to the solves (eigsh normalises its start
+        # vector), so the centre is normalised once here
+        c0 = dev.mps[0]
+        c0.div_(c0.abs().max().clamp_min(1e-300))   # first to O(1), so its squared norm cannot overflow
+        nrm2 = torch.empty(1, dtype=torch.float64, device=dev.device)
+        lib = L.load()
+        wp, wb = dev.ws.args(4096 + 64 * c0.numel())
+        L.check(lib.tn_dot(c0.numel(), L.ptr(c0), L.ptr(c0), L.ptr(nrm2), wp, wb, L.stream_handle()), "dot")
+        L.check(lib.tn_scale(c0.numel(), L.ptr(c0), 1.0, L.ptr(nrm2), L.stream_handle()), "scale")
+        dev.unit_norm = True
         dev.ensure_envs(0)
         dims = [int(x) for x in dev.virtual_dim]
         self.dims, self.d, self.model = dims, d, m

@@ -361,10 +361,14 @@ size_t tn_grouped_gemm_workspace_bytes(int precision, const tn_grouped_gemm_prob
 int tn_grouped_gemm(int precision, const tn_grouped_gemm_problem* problems, int count, void* ws, size_t ws_bytes,
                     void* stream);
 
+// Sizes only depend on the shapes: plans that are only measured are laid out at this placeholder
+// address (the correction GEMM's table needs non-null operand pointers to be planned).
+char* const kMeasureBase = (char*)(uintptr_t)(1 << 20);
+
 extern "C" size_t tn_batched_qr_mixed_workspace_bytes(const tn_qr_item* items, int count) {
   if (!items || count <= 0) return 4096;
   QrbPlan P;
-  if (qrb_plan(items, count, nullptr, &P)) return 0;
+  if (qrb_plan(items, count, kMeasureBase, &P)) return 0;
   // the correction GEMM's staging goes behind the plan's own scratch
   return P.bytes + tn_grouped_gemm_workspace_bytes(TN_PREC_TF32X3, P.fix.data(), count) + 2048;
 }
@@ -375,7 +379,7 @@ extern "C" int tn_batched_qr_mixed(const tn_qr_item* items, int count, void* ws,
   if (!tn_tf32x3_supported()) return tn_fail(TN_ERR_ARG, "batched qr: needs an sm_103 device (split-TF32 correction)");
   cudaStream_t s = (cudaStream_t)stream;
   QrbPlan M0;
-  int st = qrb_plan(items, count, nullptr, &M0);
+  int st = qrb_plan(items, count, kMeasureBase, &M0);
   if (st) return st;
   const size_t gg = tn_grouped_gemm_workspace_bytes(TN_PREC_TF32X3, M0.fix.data(), count);
   if (!ws || ws_bytes < M0.bytes + gg + 2048) return tn_fail(TN_ERR_WORKSPACE, "batched qr: workspace too small");

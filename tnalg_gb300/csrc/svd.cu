@@ -54,8 +54,9 @@ __device__ __forceinline__ int64_t rr_player(int64_t slot, int64_t r, int64_t kp
   return 1 + (slot - 1 + r) % (kp - 1);
 }
 
+// J: the accumulated rotations (kp x kp, row-major), rotated with X's rows when not null
 __global__ void jacobi_round(int64_t kp, int64_t n, int64_t r, double* X, double tol, const double* fro2,
-                             double null_rel2, int* rotated) {
+                             double null_rel2, int* rotated, double* J = nullptr) {
   const int64_t i = blockIdx.x;  // pair index 0..kp/2-1
   const int64_t p = rr_player(i, r, kp), q = rr_player(kp - 1 - i, r, kp);
   double* xp = X + p * n;
@@ -96,6 +97,47 @@ __global__ void jacobi_round(int64_t kp, int64_t n, int64_t r, double* X, double
     xp[t] = c * u - s * v;
     xq[t] = s * u + c * v;
   }
+  if (J) {
+    double* jp = J + p * kp;
+    double* jq = J + q * kp;
+    for (int64_t t = threadIdx.x; t < kp; t += blockDim.x) {
+      const double u = jp[t], v = jq[t];
+      jp[t] = c * u - s * v;
+      jq[t] = s * u + c * v;
+    }
+  }
+}
+
+__global__ void eye_kernel(int64_t kp, double* J) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < kp * kp;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    J[idx] = (idx / kp == idx % kp) ? 1.0 : 0.0;
+}
+
+// s[i] = ||X_i||, Vt[i] = X_i / s[i] (0 for a zero row), U[:, i] = J[i, :k]
+__global__ void svd_finish_kernel(int64_t k, int64_t kp, int64_t n, const double* X, const double* J, double* s_out,
+                                  double* U, int64_t ldu, double* Vt, int64_t ldvt) {
+  const int64_t i = blockIdx.x;
+  if (i >= k) return;
+  double a = 0.0;
+  for (int64_t t = threadIdx.x; t < n; t += blockDim.x) a = fma(X[i * n + t], X[i * n + t], a);
+  __shared__ double red[NT / 32];
+  __shared__ double sv;
+  a = tn_warp_sum(a);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < NT / 32; ++w) t += red[w];
+    sv = sqrt(t);
+    s_out[i] = sv;
+  }
+  __syncthreads();
+  const double inv = sv > 0.0 ? 1.0 / sv : 0.0;
+  if (Vt)
+    for (int64_t t = threadIdx.x; t < n; t += blockDim.x) Vt[i * ldvt + t] = X[i * n + t] * inv;
+  if (U)
+    for (int64_t r = threadIdx.x; r < k; r += blockDim.x) U[r * ldu + i] = J[i * kp + r];
 }
 
 __global__ void row_norms(int64_t k, int64_t n, const double* X, double* out) {
@@ -423,4 +465,51 @@ extern "C" int tn_singular_values_noalloc(int64_t k, int64_t n, const double* x,
   double* fro2 = (double*)base + 1;
   double* X = (double*)base + TN_SV_NOALLOC_FLAG_SLOTS;
   return jacobi_run(k, kp, n, x, sXr, sXc, s_out, tol, max_sweeps, X, flag, fro2, s);
+}
+
+// ---------------------------------------------------------------------------
+// Thin SVD with singular vectors (the same Jacobi, rotations accumulated).
+
+extern "C" size_t tn_svd_jacobi_workspace_bytes(int64_t k, int64_t n) {
+  const int64_t kp = k + (k & 1);
+  return 256 + (size_t)kp * n * sizeof(double) + 256 + (size_t)kp * kp * sizeof(double) + 512;
+}
+
+extern "C" int tn_svd_jacobi(int64_t k, int64_t n, const double* x, int64_t sXr, int64_t sXc, double* s_out,
+                             double* U, int64_t ldu, double* Vt, int64_t ldvt, double tol, int max_sweeps, void* ws,
+                             size_t ws_bytes, void* stream) {
+  if (k <= 0 || n <= 0 || !x || !s_out) return tn_fail(TN_ERR_ARG, "svd: bad args");
+  if ((U && ldu < k) || (Vt && ldvt < n)) return tn_fail(TN_ERR_ARG, "svd: leading dimension too small");
+  if (!ws || ws_bytes < tn_svd_jacobi_workspace_bytes(k, n) || ((uintptr_t)ws & 255))
+    return tn_fail(TN_ERR_WORKSPACE, "svd: workspace too small or not 256-byte aligned");
+  const int64_t kp = k + (k & 1);
+  cudaStream_t s = (cudaStream_t)stream;
+  int* flag = (int*)ws;
+  double* fro2 = (double*)((char*)ws + 8);
+  double* X = (double*)((char*)ws + 256);
+  double* J = (double*)((char*)X + ((size_t)kp * n * sizeof(double) + 255) / 256 * 256);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(kp * n, NT), 8LL * tn_sm_count()));
+  TN_CUDA(cudaMemsetAsync(fro2, 0, sizeof(double), s));
+  svd_copy_in<<<blocks, NT, 0, s>>>(k, kp, n, x, sXr, sXc, X, fro2);
+  TN_CHECK_LAUNCH();
+  eye_kernel<<<(int)std::max<int64_t>(1, std::min<int64_t>(tn_cdiv(kp * kp, NT), 8LL * tn_sm_count())), NT, 0, s>>>(kp, J);
+  TN_CHECK_LAUNCH();
+  const double nr2 = null_row_rel2(k, n);
+  int h = 0;
+  if (kp >= 2) {
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+      TN_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+      for (int64_t r = 0; r < kp - 1; ++r) {
+        jacobi_round<<<(unsigned)(kp / 2), NT, 0, s>>>(kp, n, r, X, tol, fro2, nr2, flag, J);
+        TN_CHECK_LAUNCH();
+      }
+      TN_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+      TN_CUDA(cudaStreamSynchronize(s));
+      if (!h) break;
+    }
+  }
+  svd_finish_kernel<<<(unsigned)k, NT, 0, s>>>(k, kp, n, X, J, s_out, U, ldu, Vt, ldvt);
+  TN_CHECK_LAUNCH();
+  if (h) return tn_fail(TN_ERR_NOCONV, "svd: Jacobi still rotating after max_sweeps");
+  return TN_OK;
 }

@@ -179,11 +179,12 @@ def run_ours(args, rank, world, local_rank):
 
     schedule = ramp + [args.chi]
     warm = max(args.warmup, len(schedule))
+    model = (para["index1"], para["index2"], para["coeff1"], para["coeff2"], para["eigs_tol"])
     for t in range(warm):
-        A.grow_bond_dimension(schedule[min(t, len(schedule) - 1)], seed=t)
+        A.grow_bond_dimension(schedule[min(t, len(schedule) - 1)], seed=t, method="expand", model=model)
         sweep()
     if A.virtual_dim.max() < min(args.chi, 2 ** (L_ // 2)):
-        A.grow_bond_dimension(args.chi, seed=warm)
+        A.grow_bond_dimension(args.chi, seed=warm, method="expand", model=model)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()

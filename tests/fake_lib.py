@@ -222,6 +222,28 @@ class FakeLib:
                 return st
         return OK
 
+    def tn_svd_jacobi_workspace_bytes(self, k, n):
+        return 0
+
+    def tn_svd_jacobi(self, k, n, x, sXr, sXc, s_out, U, ldu, Vt, ldvt, tol, sweeps, ws, wsb, stream):
+        self._count("tn_svd_jacobi")
+        k, n = int(k), int(n)
+        X = _strided(x, (k, n), (sXr, sXc)).copy()
+        u, sv, vt = np.linalg.svd(X, full_matrices=False)
+        r = len(sv)
+        s = np.zeros(k)
+        s[:r] = sv
+        _view(s_out, k)[:] = s
+        if _addr(U):
+            Um = np.zeros((k, k))
+            Um[:, :r] = u
+            _strided(U, (k, k), (int(ldu), 1))[...] = Um
+        if _addr(Vt):
+            Vm = np.zeros((k, n))
+            Vm[:r] = vt
+            _strided(Vt, (k, n), (int(ldvt), 1))[...] = Vm
+        return OK
+
     def tn_dot(self, n, x, y, out, ws, wsb, stream):
         n = int(n)
         _view(out, 1)[0] = float(np.dot(_view(x, n), _view(y, n)))

@@ -365,3 +365,39 @@ def test_methods_run_with_the_mps_device_current(monkeypatch):
     assert Stub("cuda:0").work() == "ran"   # already current: no switch
     assert Stub("cpu").work() == "ran"
     assert entered == [torch.device("cuda:1")]
+
+
+def test_bond_growth_by_expansion_keeps_the_state_and_uses_the_hamiltonian(fake_backend):
+    """DeviceMPS.expand_bonds (subspace expansion + truncated SVD): the grown MPS represents the same
+    state (energy and local magnetisations unchanged), every bond reaches min(chi, d^b, d^(L-b)), the
+    sites right of the centre are right-canonical again, and the enlarged bond spaces pay: one sweep
+    after growth ends well below one sweep at the old bond dimension."""
+    import torch
+    from tnalg_gb300 import DMRG_anyH, Parameters as pm
+    para = pm.generate_parameters_dmrg("chain")
+    para.update(l=10, chi=4, jxy=1.0, jz=0.8, hx=0.2, hz=0.1, sweep_time=2, dt_ob=1, break_tol=-1.0,
+                eigs_tol=1e-12, device="cpu")
+    para = pm.make_consistent_parameter_dmrg(para)
+    np.random.seed(4)
+    ob, A, _, _ = _quiet(DMRG_anyH.dmrg_finite_size, para)
+    model = (para["index1"], para["index2"], para["coeff1"], para["coeff2"], para["eigs_tol"])
+    A.correct_orthogonal_center(0)
+    e0 = A.observe_bond_energy(para["index2"], para["coeff2"]).sum()
+    mz0 = np.ravel(A.observe_magnetization(3))
+    import copy
+    B = copy.deepcopy(A)
+    A.grow_bond_dimension(16, seed=1, method="expand", model=model)
+    assert list(A.virtual_dim) == [1, 2, 4, 8, 16, 16, 16, 8, 4, 2, 1]
+    assert A.center == 0
+    e1 = A.observe_bond_energy(para["index2"], para["coeff2"]).sum()
+    assert abs(e1 - e0) < 1e-12 and np.max(np.abs(np.ravel(A.observe_magnetization(3)) - mz0)) < 1e-12
+    for n in range(1, 10):   # right of the centre: right-canonical
+        t = A.mps_device[n].reshape(A.mps_device[n].shape[0], -1)
+        assert torch.allclose(t @ t.T, torch.eye(t.shape[0], dtype=torch.float64), atol=1e-12)
+    def sweep(M):
+        for n in list(range(1, 10)) + list(range(8, -1, -1)):
+            M.update_tensor_eigs(n, para["index1"], para["index2"], para["coeff1"], para["coeff2"], para["tau"], True,
+                                 tol=para["eigs_tol"])
+        return (M.observe_bond_energy(para["index2"], para["coeff2"]).sum() -
+                para["hx"] * M.observe_magnetization(1).sum() - para["hz"] * M.observe_magnetization(3).sum())
+    assert sweep(A) < sweep(B) - 1e-5

@@ -48,7 +48,8 @@ def dmrg_finite_size(para=None):
         ts = time.time()
         if schedule:
             A.grow_bond_dimension(int(schedule[min(t, len(schedule) - 1)]), noise=para.get("chi_noise", 1e-3),
-                                  seed=t)
+                                  seed=t, method=para.get("chi_growth", "expand"),
+                                  model=(index1, index2, coeff1, coeff2, para["eigs_tol"]))
         A.refine_vectors = refine_sweep(para, t, info["convergence"])
         if_ob = ((t + 1) % para["dt_ob"] == 0) or t == (para["sweep_time"] - 1)
         if if_ob:

@@ -240,11 +240,25 @@ class MpsOpenBoundaryClass(MpsBasic):
             dev.orthogonality[l1] = 0
 
     @on_device
-    def grow_bond_dimension(self, chi_new, noise=1e-3, seed=0):
-        """Enlarge all bonds to chi_new (capped by d^b) with seeded noise and re-centre the MPS at
-        its previous centre (or 0). Not in the reference, whose chi is fixed; used by
-        para['chi_schedule']."""
+    def grow_bond_dimension(self, chi_new, noise=1e-3, seed=0, method="noise", model=None):
+        """Enlarge all bonds to chi_new (capped by d^b) and re-centre the MPS at its previous centre
+        (or 0). method 'expand': subspace expansion with a truncated SVD of the Hamiltonian's open
+        channels (DeviceMPS.expand_bonds; needs the run's coupling lists, model = (index1, index2,
+        coeff1, coeff2, tol)); 'noise': seeded Gaussian noise in the new entries. Not in the
+        reference, whose chi is fixed; used by para['chi_schedule']."""
         c = self.center if self.center >= 0 else 0
+        if method == "expand":
+            self._model(*model)
+            if self._dev.expand_bonds(chi_new, seed=seed):
+                self.lm = [np.zeros(0) for _ in range(self.length - 1)]
+                self._dev.fast_gauge = True
+                try:
+                    self.correct_orthogonal_center(c)
+                finally:
+                    self._dev.fast_gauge = False
+            return
+        if method != "noise":
+            raise ValueError("method must be 'expand' or 'noise'")
         if self._dev.grow_bonds(chi_new, noise=noise, seed=seed):
             self.lm = [np.zeros(0) for _ in range(self.length - 1)]
             # the grown state is re-optimised by the next sweep: its gauge moves may use the

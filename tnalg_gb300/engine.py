@@ -747,6 +747,107 @@ class DeviceMPS:
         self.er_from = max(self.er_from, self.length)
         return True
 
+    def expand_bonds(self, chi_new, seed=0, oversample=8):
+        """Grow every bond to min(chi_new, d^b, d^(L-b)) by subspace expansion and truncated SVD, in
+        one left-to-right pass of gauge moves: at bond (b, b+1), with the centre at b, the new bond
+        directions are the dominant left singular vectors of P_perp = (1 - Q Q^T) P, where Q spans
+        the centre tensor psi (its QR gauge move) and P = [T_0 | T_1 | ...] are the channels of the
+        Hamiltonian left of the bond applied to psi (T_0 = W_L psi with the block operator of site
+        b, T_k = the k-th operator left open at bond b+1 times psi: the products of an environment
+        update). P_perp is sketched by a seeded Gaussian matrix (chi_new - chi_b + oversample
+        columns, a randomised range finder), and its sketch is truncated by tn_svd_jacobi. The
+        site right of the bond receives zero rows for the new directions, so the state is
+        unchanged; the local solves of the next sweep then use the enlarged bond spaces. The
+        reference keeps chi fixed (TensorBasicModule.py:314-384); this is the bond ramp of a chi
+        schedule, and replaces growth by random noise. Returns True if a bond grew."""
+        Ln, d = self.length, self.d
+        cap = [1] + [min(chi_new, d ** min(b, 60), d ** min(Ln - b, 60)) for b in range(1, Ln)] + [1]
+        if all(int(c) <= int(v) for c, v in zip(cap, self.virtual_dim)):
+            return False
+        m = self.model
+        if m is None or m.compressed:
+            raise RuntimeError("expand_bonds needs the uncompressed coupling model of the run")
+        lib = L.load()
+        rng = np.random.default_rng(int(seed))
+        self.correct_orthogonal_center(0)
+        grew = False
+        for b in range(Ln - 1):
+            target = int(cap[b + 1])
+            A = self.mps[b]
+            cl, dd, cr = (int(x) for x in A.shape)
+            if target <= cr:
+                self.qr_left(b)
+                self.orthogonality[b] = -1
+                self.center = b + 1
+                continue
+            grew = True
+            self.ensure_envs(b)
+            mm = cl * dd
+            extra = min(target, mm) - min(mm, cr)
+            # the open channels at bond b+1 applied to psi: T[j] (mm x cr)
+            plan = m.memo(("lcp", b), lambda: m.left_carry_plan(b))
+            ns = 1 + len(plan)
+            T = torch.empty((ns, mm * cr), dtype=torch.float64, device=self.device)
+            W = torch.empty((mm, mm), dtype=torch.float64, device=self.device)
+            terms, nt = m.table_lazy(("wl", b), lambda: m.left_block_terms(b))
+            st = L.stream_handle()
+            L.check(lib.tn_assemble_block(0, cl, dd, L.ptr(self.EL[b]), L.ptr(m.ops), L.ptr(terms), nt, L.ptr(W), st),
+                    "assemble")
+            # the channels only choose directions: the working precision is enough
+            prec = self.precision if self.unit_norm else L.PREC_FP64
+            L.gemm(W, A, T[0], mm, cr, mm, (mm, 1), (cr, 1), (cr, 1), ws=self.ws, precision=prec)
+            for j, (kind, x) in enumerate(plan):
+                if kind == "carry":
+                    L.gemm(self.EL[b][x], A, T[1 + j], cl, dd * cr, cl, (cl, 1), (dd * cr, 1), (dd * cr, 1), ws=self.ws,
+                           precision=prec)
+                else:
+                    oi = m.opidx(("op", x), [x])
+                    L.check(lib.tn_apply_site_ops(cl, dd, cr, L.ptr(A), L.ptr(m.ops), L.ptr(oi), 1, L.ptr(T[1 + j]),
+                                                  mm * cr, st), "site op")
+            # Q R = psi (the plain gauge move), then the sketch Y = sum_j T_j G_j projected off range(Q)
+            k = min(mm, cr)
+            Q = torch.empty((mm, k), dtype=torch.float64, device=self.device)
+            R = torch.empty((k, cr), dtype=torch.float64, device=self.device)
+            self._qr(mm, cr, A, (cr, 1), Q, (k, 1), R, False)
+            s = min(extra + oversample, mm - k)
+            G = torch.tensor(rng.standard_normal((ns * cr, s)), dtype=torch.float64, device=self.device)
+            Y = torch.empty((mm, s), dtype=torch.float64, device=self.device)
+            L.gemm(T, G, Y, mm, s, cr, (cr, 1), (s, 1), (s, 1), nred=ns, rstrides=(mm * cr, cr * s), ws=self.ws,
+                   precision=prec)
+            QtY = torch.empty((k, s), dtype=torch.float64, device=self.device)
+            L.gemm(Q, Y, QtY, k, s, mm, (1, k), (s, 1), (s, 1), ws=self.ws)
+            L.gemm(Q, QtY, Y, mm, s, k, (k, 1), (s, 1), (s, 1), Cin=Y, alpha=-1.0, beta=1.0, ws=self.ws)
+            # truncated SVD of the sketch: its dominant left singular vectors (rows of Vt of Y^T)
+            Ut, sv, Vt = L.svd_truncated(Y.t(), extra, ws=self.ws2, tol=1e-10)
+            r = int(Vt.shape[0])
+            Vn = torch.empty((mm, r), dtype=torch.float64, device=self.device)
+            Vn.copy_(Vt.t())
+            # one more projection off range(Q) and an orthonormal basis of what is left
+            QtV = torch.empty((k, r), dtype=torch.float64, device=self.device)
+            L.gemm(Q, Vn, QtV, k, r, mm, (1, k), (r, 1), (r, 1), ws=self.ws)
+            L.gemm(Q, QtV, Vn, mm, r, k, (k, 1), (r, 1), (r, 1), Cin=Vn, alpha=-1.0, beta=1.0, ws=self.ws)
+            Vq = torch.empty((mm, r), dtype=torch.float64, device=self.device)
+            Rv = torch.empty((r, r), dtype=torch.float64, device=self.device)
+            self._qr(mm, r, Vn, (r, 1), Vq, (r, 1), Rv, False)
+            newk = k + r
+            Anew = torch.empty((cl, dd, newk), dtype=torch.float64, device=self.device)
+            Anew.view(mm, newk)[:, :k].copy_(Q)
+            Anew.view(mm, newk)[:, k:].copy_(Vq)
+            nxt = self.mps[b + 1]
+            c2, d2, r2 = (int(x) for x in nxt.shape)
+            new_next = torch.zeros((newk, d2, r2), dtype=torch.float64, device=self.device)
+            L.gemm(R, nxt, new_next, k, d2 * r2, cr, (cr, 1), (d2 * r2, 1), (d2 * r2, 1), ws=self.ws)
+            self.mps[b] = Anew
+            self.mps[b + 1] = new_next
+            self.virtual_dim[b + 1] = newk
+            self.orthogonality[b] = -1
+            self.center = b + 1
+            self.tensor_changed(b)
+            self.tensor_changed(b + 1)
+        self.orthogonality[Ln - 1] = 0
+        self.center = Ln - 1
+        return grew
+
     def move_center_for_solve(self, p):
         """Centre to p ahead of a local solve at p: a one-site move seeds site p in the working
         precision (the solve replaces it); longer moves go through correct_orthogonal_center."""

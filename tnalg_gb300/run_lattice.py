@@ -61,10 +61,12 @@ class _Timer:
             self.ms = 1000.0 * (time.perf_counter() - self.t)
 
 
-def run(para, precision, schedule, steps, device="cuda", seed=0, refine="off"):
+def run(para, precision, schedule, steps, device="cuda", seed=0, refine="off", growth="expand"):
     """Ramp over `schedule[:-1]` (one sweep per bond dimension), then `steps` timed sweeps at
     schedule[-1]. refine (split-TF32 path): 'final' refines the local solves of the last sweep to
-    the FP64 tolerance (DMRG_anyH.refine_sweep), 'all' those of every sweep, 'off' none."""
+    the FP64 tolerance (DMRG_anyH.refine_sweep), 'all' those of every sweep, 'off' none. growth: how
+    bonds grow between schedule entries ('expand': subspace expansion with a truncated SVD of the
+    Hamiltonian's open channels; 'noise': seeded noise)."""
     np.random.seed(seed)
     l = para["l"]
     A = MpsOpenBoundaryClass(l, para["d"], schedule[0], operators=para["op"], device=device, precision=precision)
@@ -82,10 +84,11 @@ def run(para, precision, schedule, steps, device="cuda", seed=0, refine="off"):
                                      para["tau"], True, tol=para["eigs_tol"])
         energies.append(float(e) / l)
 
+    model = (para["index1"], para["index2"], para["coeff1"], para["coeff2"], para["eigs_tol"])
     for t, chi in enumerate(schedule[:-1]):
-        A.grow_bond_dimension(int(chi), seed=t)
+        A.grow_bond_dimension(int(chi), seed=t, method=growth, model=model)
         sweep(t)
-    A.grow_bond_dimension(int(schedule[-1]), seed=len(schedule) - 1)
+    A.grow_bond_dimension(int(schedule[-1]), seed=len(schedule) - 1, method=growth, model=model)
     s0, m0 = A.stats["solves"], A.stats["matvecs"]
     with _Timer(device) as tm:
         for k in range(steps):
@@ -126,6 +129,7 @@ def main(argv=None):
     ap.add_argument("--refine", default="off", choices=["final", "all", "off"],
                     help="split-TF32 path: local solves refined to the FP64 tolerance in the last sweep (final), "
                          "in every sweep (all) or never (off)")
+    ap.add_argument("--growth", default="expand", choices=["expand", "noise"])
     a = ap.parse_args(argv)
     from . import _lib as L
     L.load()
@@ -133,11 +137,11 @@ def main(argv=None):
     schedule = [int(x) for x in a.ramp.split(",") if x] + [a.chi]
     out = {"workload": name, "sites": int(para["l"]), "two_body_rows": int(np.asarray(para["index2"]).shape[0]),
            "straddling_terms_max": straddle_max(para), "chi_schedule": schedule, "timed_sweeps": a.steps}
-    res = run(para, a.precision, schedule, a.steps, a.device, a.seed, refine=a.refine)
+    res = run(para, a.precision, schedule, a.steps, a.device, a.seed, refine=a.refine, growth=a.growth)
     eb = res.pop("eb_full")
     out.update(res)
     if a.compare_fp64 and a.precision != "fp64":
-        ref = run(para, "fp64", schedule, a.steps, a.device, a.seed)
+        ref = run(para, "fp64", schedule, a.steps, a.device, a.seed, growth=a.growth)
         eb64 = ref.pop("eb_full")
         out["fp64_path"] = ref
         out["speedup_vs_fp64"] = out["sweeps_per_s"] / ref["sweeps_per_s"]

@@ -151,6 +151,8 @@ class DMRGJob:
         for t in range(p["sweep_time"]):
             if schedule:
                 A.grow_bond_dimension(int(schedule[min(t, len(schedule) - 1)]), noise=p.get("chi_noise", 1e-3),
+                                      method=p.get("chi_growth", "expand"),
+                                      model=(p["index1"], p["index2"], p["coeff1"], p["coeff2"], p["eigs_tol"]),
                                       seed=t)
             order = list(range(p["ob_position"] + 1, l)) + list(range(l - 2, -1, -1)) + \
                 list(range(1, p["ob_position"]))

@@ -56,9 +56,18 @@ class BatchJob:
     # -- lifecycle --------------------------------------------------------------------
     def start(self, device, precision):
         p = self.para
-        np.random.seed(self.seed)
-        self.A = MpsOpenBoundaryClass(length=p["l"], d=p["d"], chi=p["chi"], operators=p["op"], device=device,
-                                      precision=precision)
+        # the job's own generator: the draws (and their order, TensorBasicModule.py:181-186) of
+        # np.random.seed(seed) followed by random_open_mps, without touching the global generator, so
+        # that jobs can be started from several host threads
+        rs = np.random.RandomState(self.seed)
+        l, d, chi = p["l"], p["d"], p["chi"]
+        tensors = [None] * l
+        tensors[0] = rs.randn(1, d, chi)
+        tensors[l - 1] = rs.randn(chi, d, 1)
+        for n in range(1, l - 1):
+            tensors[n] = rs.randn(chi, d, chi)
+        self.A = MpsOpenBoundaryClass(length=l, d=d, chi=chi, operators=p["op"], device=device, precision=precision,
+                                      tensors=tensors)
         self.A.correct_orthogonal_center(p["ob_position"])
         self.A._model(p["index1"], p["index2"], p["coeff1"], p["coeff2"], p["eigs_tol"])
         ob = p["ob_position"]
@@ -366,7 +375,7 @@ class BatchEngine:
     step for all admitted jobs, p50/p99 latency from arrival to result."""
 
     def __init__(self, device="cuda", precision="tf32x3", budget_bytes=None, max_active=1024, max_krylov=24,
-                 check_every=3, mixed_floor=2e-6, workers=8, streams=16, grouped=None):
+                 check_every=3, mixed_floor=2e-6, workers=8, streams=16, grouped=None, profile=False):
         self.device = device
         self.workers = max(1, int(workers))
         self.nstreams = max(1, int(streams))
@@ -390,6 +399,10 @@ class BatchEngine:
         self._ws2 = None
         self._t0 = None
         self.step_ms = []
+        self.times = {"admit": 0.0, "step": 0.0, "observe": 0.0, "tables": 0.0}
+        # device time of the grouped step's phases (CUDA events on the stream; profile=True)
+        self.profile = bool(profile)
+        self.phase_ms = {}
         # grouped path (job arenas, grouped launches for the whole local update) on the split-TF32
         # path; the FP64 path prepares every job with its own DeviceMPS calls
         self.grouped = self.prec == L.PREC_TF32X3 if grouped is None else bool(grouped)
@@ -407,20 +420,56 @@ class BatchEngine:
         return 1 << 62
 
     def _admit(self, now):
+        t_in = time.perf_counter()
+        self._admit_jobs(now)
+        self.times["admit"] += time.perf_counter() - t_in
+
+    def _admit_jobs(self, now):
         budget = self._budget()
-        while self.pending and self.pending[0].arrival <= now and len(self.active) < self.max_active:
+        admit = []
+        while self.pending and self.pending[0].arrival <= now and len(self.active) + len(admit) < self.max_active:
             fp = self.pending[0].footprint_bytes(self.krylov)
-            if self.active and self._used + fp > budget:
+            if (self.active or admit) and self._used + fp > budget:
                 break
             job = self.pending.pop(0)
             job.admitted = now
             if self.grouped and not isinstance(job, ArenaJob):
                 job.__class__ = ArenaJob
-            job.start(self.device, self.precision)
-            self.active.append(job)
+            admit.append(job)
             self._used += fp
+        self._on_workers(admit, lambda job: job.start(self.device, self.precision))
+        self.active += admit
         self.max_concurrent = max(self.max_concurrent, len(self.active))
         self.max_used = max(self.max_used, self._used)
+
+    def _on_workers(self, jobs, fn):
+        """fn(job) for every job: on a GPU from `workers` host threads, each job on the stream it keeps
+        for life (the library's calls release the GIL, so the jobs' small latency-bound kernels overlap);
+        every stream is synchronised before the call returns."""
+        cuda = str(self.device).startswith("cuda") and not L._host_test
+        if not cuda or self.workers == 1 or len(jobs) < 2:
+            for job in jobs:
+                fn(job)
+            return
+        self._ensure_streams()
+        main = torch.cuda.current_stream(self.device)
+        ready = torch.cuda.Event()
+        ready.record(main)
+
+        def run(job):
+            st = self._streams[job.job_id % self.nstreams]
+            st.wait_event(ready)
+            with torch.cuda.stream(st):
+                fn(job)
+            st.synchronize()
+        for _ in self._pool.map(run, jobs):
+            pass
+
+    def _ensure_streams(self):
+        if self._streams is None:
+            self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.nstreams)]
+            from concurrent.futures import ThreadPoolExecutor
+            self._pool = ThreadPoolExecutor(max_workers=self.workers)
 
     def _prepare_all(self, jobs):
         """Every job's gauge move, environment update and block assembly. On a GPU the jobs are
@@ -430,10 +479,7 @@ class BatchEngine:
         cuda = str(self.device).startswith("cuda") and not L._host_test
         if not cuda or self.workers == 1:
             return [job.prepare() for job in jobs]
-        if self._streams is None:
-            self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.nstreams)]
-            from concurrent.futures import ThreadPoolExecutor
-            self._pool = ThreadPoolExecutor(max_workers=self.workers)
+        self._ensure_streams()
         main = torch.cuda.current_stream(self.device)
         ready = torch.cuda.Event()
         ready.record(main)          # the previous step's solve wrote the site tensors
@@ -465,7 +511,17 @@ class BatchEngine:
         and one batched solve."""
         lib = L.load()
         st = L.stream_handle()
+        t_tab = time.perf_counter()
         rows = [j.rows() for j in jobs]
+        self.times["tables"] += time.perf_counter() - t_tab
+        marks = []
+
+        def mark(name):
+            if self.profile and not L._host_test:
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record()
+                marks.append((name, ev))
+        mark("start")
         if self._ws is None:
             self._ws = L.Workspace(torch.device(self.device))
         if self._ws2 is None:
@@ -485,6 +541,7 @@ class BatchEngine:
             return tab
 
         keep = [ops("ops1")]
+        mark("assemble_env_block")
         small = [r["qr"] for r in rows if not r["qr_big"]]
         if small:
             tab = np.concatenate(small)
@@ -495,9 +552,21 @@ class BatchEngine:
         for j, r in zip(jobs, rows):
             if r["qr_big"]:
                 j.big_qr(self._ws2)
-        keep += [gemm("gemm1"), ops("ops2"), gemm("gemm2"), ops("ops3")]
+        mark("qr")
+        keep += [gemm("gemm1"), ops("ops2")]
+        mark("absorb_and_transfer")
+        keep.append(gemm("gemm2"))
+        mark("env_close")
+        keep.append(ops("ops3"))
+        mark("heff_assembly")
         solves = np.concatenate([r["solve"] for r in rows])
-        return self._solve(jobs, solves, keep)
+        out = self._solve(jobs, solves, keep)
+        mark("lanczos")
+        if marks:
+            marks[-1][1].synchronize()
+            for (_, a), (name, b) in zip(marks[:-1], marks[1:]):
+                self.phase_ms[name] = self.phase_ms.get(name, 0.0) + a.elapsed_time(b)
+        return out
 
     def _solve(self, jobs, solves, keep):
         lib = L.load()
@@ -565,13 +634,16 @@ class BatchEngine:
                 continue
             ts = time.perf_counter()
             finished = self.step()
+            t1 = time.perf_counter()
+            self.step_ms.append(1000.0 * (t1 - ts))
+            self.times["step"] += t1 - ts
+            self._on_workers(finished, lambda job: job.observe())
             for job in finished:
-                job.observe()
                 job.finished = time.perf_counter() - t0
                 self.active.remove(job)
                 self._used -= job.footprint_bytes(self.krylov)
                 self.done.append(job)
-            self.step_ms.append(1000.0 * (time.perf_counter() - ts))
+            self.times["observe"] += time.perf_counter() - t1
             if progress:
                 progress(self)
         if str(self.device).startswith("cuda"):
@@ -587,7 +659,9 @@ class BatchEngine:
                 "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
                 "max_concurrent": self.max_concurrent, "steps": self.steps,
                 "step_ms_p50": float(np.percentile(self.step_ms, 50)) if self.step_ms else 0.0,
-                "matvecs_per_solve": (sum(j.matvecs for j in self.done) / solves) if solves else 0.0}
+                "matvecs_per_solve": (sum(j.matvecs for j in self.done) / solves) if solves else 0.0,
+                "host_s": {k: round(v, 3) for k, v in self.times.items()},
+                "device_ms_per_step": {k: round(v / max(self.steps, 1), 3) for k, v in self.phase_ms.items()}}
 
 
 def batch_jobs(njobs, seed=0, sweeps=8, precision="tf32x3", device="cuda", rate=None, lengths=(16, 64),
@@ -626,6 +700,7 @@ def main(argv=None):
                     help="how many of the jobs also run one at a time on the plain FP64 GPU path (0: none)")
     ap.add_argument("--baseline-precision", default="fp64")
     ap.add_argument("--device", default="cuda")
+    ap.add_argument("--profile", action="store_true", help="device time per phase of the grouped step (CUDA events)")
     a = ap.parse_args(argv)
     lengths = tuple(int(x) for x in a.lengths.split(","))
     chis = tuple(int(x) for x in a.chis.split(","))
@@ -638,7 +713,7 @@ def main(argv=None):
     for j in batch_jobs(4, seed=a.seed + 10 ** 6, sweeps=1, precision=a.precision, device=dev, **shape):
         warm.submit(j)
     warm.run()
-    eng = BatchEngine(dev, a.precision, max_active=a.max_active, max_krylov=a.krylov)
+    eng = BatchEngine(dev, a.precision, max_active=a.max_active, max_krylov=a.krylov, profile=a.profile)
     for j in batch_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev, rate=a.rate,
                         **shape):
         eng.submit(j)

@@ -323,3 +323,27 @@ def test_tf32x3_j1j2_lattice_matches_fp64_after_ten_sweeps(tf32):
     assert mixed["chi_max"] == fp64["chi_max"] == 64
     assert abs(mixed["e_per_site"] - fp64["e_per_site"]) <= 1e-8, (mixed["e_per_site"], fp64["e_per_site"])
     assert np.max(np.abs(mixed["eb_full"] - fp64["eb_full"])) < 1e-5
+
+
+@pytest.mark.parametrize("m,n,zero", [(1024, 512, "tail"), (512, 256, "every_third"), (256, 128, "tail")])
+def test_qr_mixed_exactly_zero_columns(tf32, m, n, zero):
+    """Gauge moves right after a bond grew by expansion factor matrices whose columns for the new
+    directions are exactly zero (the zero rows of the site right of the bond, transposed): Q must still
+    have orthonormal columns and Q R = A."""
+    lib = L.load()
+    A = _rand(m, n, seed=m + 3 * n)
+    if zero == "tail":
+        A[:, n // 2:] = 0.0
+    else:
+        A[:, ::3] = 0.0
+    Q = torch.empty((m, n), dtype=torch.float64, device="cuda")
+    R = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    for fn in ("tn_qr_mixed", "tn_qr"):
+        ws = L.Workspace(torch.device("cuda"))
+        wp, wb = ws.args(getattr(lib, fn + "_workspace_bytes")(m, n))
+        L.check(getattr(lib, fn)(m, n, L.ptr(A), n, 1, L.ptr(Q), n, 1, L.ptr(R), n, 1, wp, wb, L.stream_handle()))
+        L.check(lib.tn_check_device_status(L.stream_handle()))
+        eye = torch.eye(n, dtype=torch.float64, device="cuda")
+        assert torch.isfinite(Q).all() and torch.isfinite(R).all(), fn
+        assert torch.max(torch.abs(Q.T @ Q - eye)).item() < 1e-11, fn
+        assert torch.max(torch.abs(Q @ R - A)).item() < 1e-5 * torch.max(torch.abs(A)).item(), fn

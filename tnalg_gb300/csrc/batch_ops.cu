@@ -28,7 +28,7 @@
 namespace {
 
 constexpr int NT = 256;
-constexpr int CHUNK = 2048;  // output elements per block of tn_grouped_ops
+constexpr int CHUNK = 1024;  // work units per block of tn_grouped_ops
 
 __device__ __forceinline__ int find_item(const int* prefix, int n, int t) {
   int lo = 0, hi = n;
@@ -43,55 +43,91 @@ __device__ __forceinline__ double op_elem(const double* ops, int op, int64_t d, 
   return op < 0 ? (r == c ? 1.0 : 0.0) : ops[(int64_t)op * d * d + r * d + c];
 }
 
-__global__ void grouped_ops_kernel(const tn_batch_op* items, int nitems, const int* prefix) {
+// Work units of an item: a block operator is computed one (environment row, column) pair at a time
+// (its d x d block of outputs, d <= 4); the other kinds one output element at a time.
+__host__ __device__ __forceinline__ int64_t op_units(const tn_batch_op& it) {
+  return (it.kind == TN_BOP_BLOCK_LEFT || it.kind == TN_BOP_BLOCK_RIGHT) ? (int64_t)it.chi * it.chi : it.total;
+}
+
+constexpr int MAX_D = 4;
+
+__global__ void __launch_bounds__(NT) grouped_ops_kernel(const tn_batch_op* items, int nitems, const int* prefix) {
   const int t = blockIdx.x;
   const int i = find_item(prefix, nitems, t);
   const tn_batch_op it = items[i];
   if (it.active && *it.active == 0) return;
-  const int64_t e0 = (int64_t)(t - prefix[i]) * CHUNK;
-  const int64_t e1 = min(it.total, e0 + CHUNK);
-  const int64_t chi = it.chi, d = it.d;
+  const int64_t u0 = (int64_t)(t - prefix[i]) * CHUNK;
+  const int64_t u1 = min(op_units(it), u0 + CHUNK);
+  const int chi = it.chi, d = it.d;
   const tn_block_term* terms = (const tn_block_term*)it.terms;
-  for (int64_t idx = e0 + threadIdx.x; idx < e1; idx += blockDim.x) {
-    if (it.kind == TN_BOP_BLOCK_LEFT || it.kind == TN_BOP_BLOCK_RIGHT) {
-      const int64_t n = chi * d;
-      const int64_t row = idx / n, col = idx % n;
-      int64_t er, ec, orr, oc;
-      if (it.kind == TN_BOP_BLOCK_LEFT) {
-        er = row / d; orr = row % d; ec = col / d; oc = col % d;
-      } else {
-        orr = row / chi; er = row % chi; oc = col / chi; ec = col % chi;
-      }
-      double acc = 0.0;
+  if (it.kind == TN_BOP_BLOCK_LEFT || it.kind == TN_BOP_BLOCK_RIGHT) {
+    // unit (r, c) of the environment: W[(r s'), (c s)] (left) or W[(s' r), (s c)] (right) for all s', s
+    const int n = chi * d;
+    for (int64_t u = u0 + threadIdx.x; u < u1; u += blockDim.x) {
+      const int r = (int)(u / chi), c = (int)(u - (int64_t)r * chi);
+      double acc[MAX_D * MAX_D];
+#pragma unroll
+      for (int q = 0; q < MAX_D * MAX_D; ++q) acc[q] = 0.0;
       for (int q = 0; q < it.nterms; ++q) {
         const tn_block_term tt = terms[q];
-        const double o = op_elem(it.ops, tt.op, d, orr, oc);
-        if (o == 0.0) continue;
-        const double e = tt.slot < 0 ? (er == ec ? 1.0 : 0.0)
-                                     : it.src[(int64_t)tt.slot * it.s_slot + er * it.s_row + ec];
-        acc = fma(tt.coeff * o, e, acc);
+        const double e = tt.slot < 0 ? (r == c ? 1.0 : 0.0) : it.src[(int64_t)tt.slot * it.s_slot + (int64_t)r * it.s_row + c];
+        if (e == 0.0) continue;
+        const double ce = tt.coeff * e;
+        // fully unrolled over the MAX_D x MAX_D block so that acc stays in registers
+        if (tt.op < 0) {
+#pragma unroll
+          for (int x = 0; x < MAX_D; ++x)
+            if (x < d) acc[x * MAX_D + x] += ce;
+        } else {
+          const double* o = it.ops + (int64_t)tt.op * d * d;
+#pragma unroll
+          for (int x = 0; x < MAX_D; ++x)
+#pragma unroll
+            for (int y = 0; y < MAX_D; ++y)
+              if (x < d && y < d) acc[x * MAX_D + y] = fma(ce, o[x * d + y], acc[x * MAX_D + y]);
+        }
       }
-      it.out[idx] = acc;
-    } else if (it.kind == TN_BOP_COMBINE) {
-      const int64_t m = chi * chi;
-      const int64_t g = idx / m, e = idx % m, r = e / chi, c = e % chi;
+#pragma unroll
+      for (int x = 0; x < MAX_D; ++x)
+#pragma unroll
+        for (int y = 0; y < MAX_D; ++y)
+          if (x < d && y < d) {
+            const int64_t row = (it.kind == TN_BOP_BLOCK_LEFT) ? (int64_t)r * d + x : (int64_t)x * chi + r;
+            const int64_t col = (it.kind == TN_BOP_BLOCK_LEFT) ? (int64_t)c * d + y : (int64_t)y * chi + c;
+            it.out[row * n + col] = acc[x * MAX_D + y];
+          }
+    }
+  } else if (it.kind == TN_BOP_COMBINE) {
+    const int64_t m = (int64_t)chi * chi;
+    for (int64_t idx = u0 + threadIdx.x; idx < u1; idx += blockDim.x) {
+      const int g = (int)(idx / m);
+      const int e = (int)(idx - g * m);
+      const int r = e / chi, c = e - r * chi;
       double acc = 0.0;
       for (int q = 0; q < it.nterms; ++q) {
         const tn_block_term tt = terms[q];
         if (tt.op != g) continue;
-        const double v = tt.slot < 0 ? (r == c ? 1.0 : 0.0) : it.src[(int64_t)tt.slot * it.s_slot + r * it.s_row + c];
+        const double v = tt.slot < 0 ? (r == c ? 1.0 : 0.0) : it.src[(int64_t)tt.slot * it.s_slot + (int64_t)r * it.s_row + c];
         acc = fma(tt.coeff, v, acc);
       }
-      it.out[g * it.out_stride + e] = acc;
-    } else {  // TN_BOP_SITE_OPS: out[k][a, s', b] = sum_s ops[opidx[k]][s', s] src[a, s, b]
-      const int64_t chir = it.chir;
-      const int64_t per = chi * d * chir;
-      const int64_t k = idx / per, e = idx % per;
-      const int64_t a = e / (d * chir), sp = (e / chir) % d, b = e % chir;
+      it.out[(int64_t)g * it.out_stride + e] = acc;
+    }
+  } else {  // TN_BOP_SITE_OPS: out[k][a, s', b] = sum_s ops[opidx[k]][s', s] src[a, s, b]
+    const int chir = it.chir;
+    const int64_t per = (int64_t)chi * d * chir;
+    for (int64_t idx = u0 + threadIdx.x; idx < u1; idx += blockDim.x) {
+      const int k = (int)(idx / per);
+      const int64_t e = idx - k * per;
+      const int64_t a = e / ((int64_t)d * chir);
+      const int rem = (int)(e - a * d * chir);
+      const int sp = rem / chir, b = rem - sp * chir;
       const int op = ((const int32_t*)it.terms)[k];
       double acc = 0.0;
-      for (int64_t s = 0; s < d; ++s) acc = fma(op_elem(it.ops, op, d, sp, s), it.src[(a * d + s) * chir + b], acc);
-      it.out[k * it.out_stride + e] = acc;
+      for (int s2 = 0; s2 < d; ++s2) {
+        const double o = op < 0 ? (sp == s2 ? 1.0 : 0.0) : it.ops[(int64_t)op * d * d + sp * d + s2];
+        acc = fma(o, it.src[(a * d + s2) * chir + b], acc);
+      }
+      it.out[(int64_t)k * it.out_stride + e] = acc;
     }
   }
 }
@@ -293,7 +329,9 @@ extern "C" int tn_grouped_ops(const tn_batch_op* items, int count, void* ws, siz
     const tn_batch_op& it = items[i];
     if (it.kind < TN_BOP_BLOCK_LEFT || it.kind > TN_BOP_SITE_OPS || it.total < 0 || (it.total > 0 && !it.out))
       return tn_fail(TN_ERR_ARG, "grouped ops: bad item");
-    prefix.push_back(prefix.back() + (int)tn_cdiv(it.total, CHUNK));
+    if ((it.kind == TN_BOP_BLOCK_LEFT || it.kind == TN_BOP_BLOCK_RIGHT) && (it.d > MAX_D || it.d < 1))
+      return tn_fail(TN_ERR_ARG, "grouped ops: block operators need 1 <= d <= 4");
+    prefix.push_back(prefix.back() + (int)tn_cdiv(op_units(it), CHUNK));
   }
   const size_t tb = al(sizeof(tn_batch_op) * (size_t)count), pb = al(sizeof(int) * prefix.size());
   if (!ws || ws_bytes < tb + pb + 1024) return tn_fail(TN_ERR_WORKSPACE, "grouped ops: workspace too small");

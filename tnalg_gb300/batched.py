@@ -124,10 +124,12 @@ class BatchJob:
 
 
 def _rec(dtype, **kw):
-    r = np.zeros(1, dtype=dtype)
-    for k, v in kw.items():
-        r[k] = v
-    return r
+    """One record as a tuple in the dtype's field order (tables are built with one np.array call)."""
+    return tuple(kw.get(name, 0) for name in dtype.names)
+
+
+def _table(dtype, recs):
+    return np.array(recs, dtype=dtype) if recs else np.zeros(0, dtype=dtype)
 
 
 def _gemm(M, N, K, A, sA, B, sB, C, sC, *, batch=1, sAb=0, sBb=0, sCb=0, alpha=1.0, beta=0.0, accumulate=0,
@@ -326,9 +328,9 @@ class ArenaJob(BatchJob):
                                    nterms=nb, s_slot=pr * pr, s_row=pr, out_stride=pr * pr, active=act))
         solve = _rec(L.BATCH_SOLVE_DTYPE, chil=pl, d=d, chir=pr, wl=a["WL"], wr=a["WR"], nstr=ng,
                      sl=a["SL"] if ng else 0, sr=a["SR"] if ng else 0, psi_in=a["seed"], psi_out=a[("site", p)])
-        res = {key: (np.concatenate(v) if v else np.zeros(0, dtype=v_dtype(key))) for key, v in out.items() if key != "qr"}
-        res["qr"] = qr
-        res["solve"] = solve
+        res = {key: _table(v_dtype(key), v) for key, v in out.items() if key != "qr"}
+        res["qr"] = _table(L.QR_ITEM_DTYPE, [qr])
+        res["solve"] = _table(L.BATCH_SOLVE_DTYPE, [solve])
         res["qr_shape"] = (mm, nn, right, q)
         res["qr_big"] = mm * nn > QR_MAX_ELEMS
         return res
@@ -397,6 +399,7 @@ class BatchEngine:
         self._used = 0
         self._ws = None
         self._ws2 = None
+        self._observing = []
         self._t0 = None
         self.step_ms = []
         self.times = {"admit": 0.0, "step": 0.0, "observe": 0.0, "tables": 0.0}
@@ -465,11 +468,58 @@ class BatchEngine:
         for _ in self._pool.map(run, jobs):
             pass
 
+    def _observe_async(self, jobs):
+        """Observe finished jobs (bond energies, magnetisations: FP64 transfer products) on the
+        observer threads, each job on its own stream, while the engine steps the remaining jobs; a
+        job's device memory is released and its latency stamped when its observation is done."""
+        if not jobs:
+            return
+        cuda = str(self.device).startswith("cuda") and not L._host_test
+        if not cuda or self.workers == 1:
+            for job in jobs:
+                job.observe()
+                self._retire(job)
+            return
+        self._ensure_streams()
+        main = torch.cuda.current_stream(self.device)
+        ready = torch.cuda.Event()
+        ready.record(main)
+
+        def run(job):
+            st = self._streams[job.job_id % self.nstreams]
+            st.wait_event(ready)
+            with torch.cuda.stream(st):
+                job.observe()
+            st.synchronize()
+            return job
+        for job in jobs:
+            self._observing.append(self._obs_pool.submit(run, job))
+
+    def _collect_observed(self, block=False):
+        if not self._observing:
+            return
+        if block:
+            from concurrent.futures import FIRST_COMPLETED, wait
+            wait(self._observing, return_when=FIRST_COMPLETED)
+        still = []
+        for f in self._observing:
+            if f.done():
+                self._retire(f.result())   # an exception of the observation is raised here
+            else:
+                still.append(f)
+        self._observing = still
+
+    def _retire(self, job):
+        job.finished = time.perf_counter() - self._t0
+        self._used -= job.footprint_bytes(self.krylov)
+        self.done.append(job)
+
     def _ensure_streams(self):
         if self._streams is None:
             self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.nstreams)]
             from concurrent.futures import ThreadPoolExecutor
             self._pool = ThreadPoolExecutor(max_workers=self.workers)
+            self._obs_pool = ThreadPoolExecutor(max_workers=max(1, self.workers // 2))
 
     def _prepare_all(self, jobs):
         """Every job's gauge move, environment update and block assembly. On a GPU the jobs are
@@ -626,7 +676,10 @@ class BatchEngine:
     def run(self, progress=None):
         """Admit (by arrival time and memory), step, retire, until every submitted job is done."""
         self._t0 = t0 = time.perf_counter()
-        while self.pending or self.active:
+        while self.pending or self.active or self._observing:
+            if not self.active and not self.pending:
+                self._collect_observed(block=True)
+                continue
             now = time.perf_counter() - t0
             self._admit(now)
             if not self.active:
@@ -637,12 +690,10 @@ class BatchEngine:
             t1 = time.perf_counter()
             self.step_ms.append(1000.0 * (t1 - ts))
             self.times["step"] += t1 - ts
-            self._on_workers(finished, lambda job: job.observe())
             for job in finished:
-                job.finished = time.perf_counter() - t0
                 self.active.remove(job)
-                self._used -= job.footprint_bytes(self.krylov)
-                self.done.append(job)
+            self._observe_async(finished)
+            self._collect_observed(block=not self.active and not self.pending)
             self.times["observe"] += time.perf_counter() - t1
             if progress:
                 progress(self)

@@ -190,18 +190,21 @@ def test_batched_lanczos_with_straddling_pairs(cuda_lib, precision):
 
 def test_batched_qr_mixed_orthonormal_and_spanning(cuda_lib):
     """Many matrices of uneven shapes (2 x 2 up to 256 x 128 = the shared-memory limit, a transposed
-    view, a rank-deficient one, widely scaled entries) in one call: Q^T Q = I to 1e-12, Q R = A to
+    view, rank-deficient ones, widely scaled entries) in one call: Q^T Q = I to 1e-12, Q R = A to
     FP32 accuracy, R upper triangular, span(Q) = col(A)."""
     if not L.tf32x3_available():
         pytest.skip("needs an sm_103 device")
     lib = L.load()
     shapes = [(2, 2, 1.0), (8, 4, 1e-30), (64, 32, 1.0), (128, 64, 1e5), (256, 128, 1.0), (200, 100, 1.0),
-              (96, 96, 1.0)]
+              (96, 96, 1.0), (128, 128, 1.0)]
     keep, items, refs = [], [], []
     for i, (m, n, scale) in enumerate(shapes):
         A = _rand(m, n, seed=700 + i) * scale
         if i == 5:
             A[:, 50:] = A[:, :50] @ _rand(50, 50, seed=9)   # rank 50 of 100
+        if i == 7:
+            # columns 1e-21 below the rest: their FP32 squares are subnormal (no reflector from them)
+            A[:, 32:] = A[:, :32] @ _rand(32, 96, seed=10) + 1e-21 * _rand(128, 96, seed=11)
         R = torch.zeros(n, n, dtype=torch.float64, device="cuda")
         keep += [A, R]
         refs.append(A.clone())

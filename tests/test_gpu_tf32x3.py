@@ -199,12 +199,17 @@ def test_tf32x3_lanczos_fp64_refined_energy(tf32):
                                                  (1024, 512, 1e6, True), (512, 512, 1e8, False),
                                                  (1000, 300, 1e4, True), (256, 128, 1e6, False),
                                                  (64, 64, 1e3, False), (4, 2, 1.0, False), (96, 200, 1e3, False),
-                                                 (256, 128, 0.0, False)])
+                                                 (256, 128, 0.0, False), (512, 256, -1.0, False),
+                                                 (512, 256, -1.0, True), (128, 64, -1.0, True),
+                                                 (128, 128, -2.0, False), (512, 256, -2.0, True)])
 def test_qr_mixed_orthonormal_and_spanning(tf32, m, n, cond, transposed):
     """FP32 Householder + FP64 re-orthogonalisation: Q orthonormal to ~1e-12 at any conditioning,
     col(Q) = col(A) to FP32 accuracy, R accurate to FP32. n <= m <= 1024, n <= 512 run on the
     16-CTA cluster kernel; `transposed` reads A and writes Q through the column-major strides of a
-    right gauge move; cond = 0 makes the last 16 singular values exactly zero."""
+    right gauge move; cond = 0 makes the last 16 singular values exactly zero, cond = -1 all but the
+    first quarter (the centre tensor right after a bond grew by expansion: rank = the old bond), and
+    cond = -2 scales those to 1e-21: sub-columns whose squares are subnormal in FP32, which the
+    factorisation must take as zero instead of building a non-orthogonal reflector from them."""
     lib = L.load()
     k = min(m, n)
     g = torch.Generator(device="cpu").manual_seed(m + n)
@@ -214,7 +219,10 @@ def test_qr_mixed_orthonormal_and_spanning(tf32, m, n, cond, transposed):
         s = torch.logspace(0, -np.log10(cond), k, dtype=torch.float64)
     else:
         s = torch.ones(k, dtype=torch.float64)
-        s[-16:] = 0.0
+        if cond == 0:
+            s[-16:] = 0.0
+        else:
+            s[k // 4:] = 0.0 if cond == -1 else 1e-21
     A = ((U * s) @ V.T).cuda()
     R = torch.empty((k, n), dtype=torch.float64, device="cuda")
     ws = L.Workspace(torch.device("cuda"))

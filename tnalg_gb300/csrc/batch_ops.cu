@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(QR_NT) qrb_householder_kernel(const QrbItem* i
     if (threadIdx.x == 0) {
       const float alpha = A[j + j * m];
       float t = 0.f, scale = 0.f, beta = alpha;
-      if (ss > 0.f) {
+      if (ss > kHhTiny) {  // smaller sub-columns are taken as zero (see kHhTiny)
         beta = -copysignf(sqrtf(fmaf(alpha, alpha, ss)), alpha);
         t = (beta - alpha) / beta;
         scale = 1.f / (alpha - beta);

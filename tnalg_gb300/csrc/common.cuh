@@ -20,6 +20,13 @@ extern thread_local unsigned long long g_tn_thread_launches;
 constexpr int TN_DEVERR_RANGE = 16;
 constexpr int TN_DEVERR_QR_WAIT = 32;
 
+// FP32 Householder QR (inputs scaled by a power of two to max |a| ~ 1): a sub-column whose squared
+// norm is at most kHhTiny gets no reflector and is taken as zero. Below ~1e-19 the squares are
+// subnormal or flushed, the computed |x|^2 can be off by an O(1) factor, and a reflector built from
+// it is not orthogonal; with the threshold at 1e-24 the squares that matter are normal numbers, and
+// the entries dropped are below 1e-12 of the largest, under the FP32 accuracy of R.
+constexpr float kHhTiny = 1e-24f;
+
 // Per-device host state (device_state.cu). Device ordinals 0..TN_MAX_DEVICES-1.
 constexpr int TN_MAX_DEVICES = 64;
 int tn_current_device(int* dev);

@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(NTP) panel32(int64_t m, int64_t j0, int jb, fl
       for (int w = 0; w < NTP / 32; ++w) sigma += red[w][0];
       const float alpha = x[j];
       float tau = 0.f, beta = alpha, scale = 0.f;
-      if (sigma > 0.f) {
+      if (sigma > kHhTiny) {  // smaller sub-columns are taken as zero (see kHhTiny)
         const float nrm = sqrtf(alpha * alpha + sigma);
         beta = alpha >= 0.f ? -nrm : nrm;
         tau = (beta - alpha) / beta;

@@ -373,22 +373,18 @@ __device__ void factor_panel(Smem& sh, int slot, int m, int j0, int jb, int fr0)
         const float sig = __shfl_sync(0x0000ffffu, tot, 0);
         const float x1 = sh.prow[0];
         float beta = x1, tau = 0.f, scale = 0.f;
-        if (sig > 0.f) {
+        // a sub-column below kHhTiny in squared norm is taken as zero (no reflector): its squares
+        // would be subnormal or flushed, sig would misstate |x|^2 and the reflector built from it
+        // would not be orthogonal (input scaled to max |a| ~ 1, so the dropped entries are < 1e-12
+        // of the largest, below the FP32 accuracy of R)
+        if (sig > kHhTiny) {
           // hardware reciprocal square root and reciprocal (a few ulp, which the FP64
-          // re-orthogonalisation absorbs) on the critical path of every column; IEEE operations
-          // when the column is so small that the approximations would meet subnormal operands
+          // re-orthogonalisation absorbs) on the critical path of every column
           const float s2 = fmaf(x1, x1, sig);
-          if (s2 > 1e-30f) {
-            const float nrm = s2 * rsqrtf(s2);
-            beta = (x1 >= 0.f) ? -nrm : nrm;
-            tau = (beta - x1) * __fdividef(1.f, beta);
-            scale = __fdividef(1.f, x1 - beta);
-          } else {
-            const float nrm = sqrtf(s2);
-            beta = (x1 >= 0.f) ? -nrm : nrm;
-            tau = (beta - x1) / beta;
-            scale = 1.f / (x1 - beta);
-          }
+          const float nrm = s2 * rsqrtf(s2);
+          beta = (x1 >= 0.f) ? -nrm : nrm;
+          tau = (beta - x1) * __fdividef(1.f, beta);
+          scale = __fdividef(1.f, x1 - beta);
         }
         const float pc = fmaf(scale, tot, sh.prow[lane]);  // v_i^T (slot lane)
         const bool unfinished = lane >= 1 && lane <= BW - 1 - i && i + lane < jb;

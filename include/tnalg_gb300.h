@@ -368,6 +368,43 @@ int tn_batched_lanczos(const tn_batch_solve* jobs, int count, const tn_lanczos_o
                        size_t ws_bytes, tn_lanczos_result* results, void* stream);
 size_t tn_batched_lanczos_workspace_bytes(const tn_batch_solve* jobs, int count, const tn_lanczos_opts* opts);
 
+/* ---- one local update of many jobs ------------------------------------------------------ */
+/*
+ * The launch records of one local update (one step of the sweep loop of dmrg_finite_size,
+ * DMRG_anyH.py:43-64: the gauge move and environment update of correct_orthogonal_center,
+ * MPSClass.py:188-198, 202-325, then update_tensor_eigs, MPSClass.py:778-809) for every job of a
+ * batch, concatenated over the jobs. They run in this order on one stream:
+ *   ops1  block operator of the environment being extended (tn_grouped_ops)
+ *   qr    the gauge move of the site left behind, Q in place (tn_batched_qr_mixed; a matrix with
+ *         m n > 32768 goes through tn_qr_mixed and must have a dense layout and no active flag)
+ *   gemm1 R absorbed into the next site and the products of the environment update
+ *   ops2  site operators of the environment update
+ *   gemm2 the new environment slots
+ *   ops3  the effective Hamiltonian of the next site (WL, WR, straddling pairs)
+ *   solves the local solve of every job (tn_batched_lanczos with opts)
+ * gemm1 and gemm2 run in `precision` (TN_PREC_TF32X3 or TN_PREC_FP64). Every table is a HOST
+ * array; a count of 0 skips its phase. No counterpart in the reference, which runs one job's
+ * update at a time.
+ */
+typedef struct {
+  const tn_batch_op* ops1;
+  const tn_qr_item* qr;
+  const tn_grouped_gemm_problem* gemm1;
+  const tn_batch_op* ops2;
+  const tn_grouped_gemm_problem* gemm2;
+  const tn_batch_op* ops3;
+  const tn_batch_solve* solves;
+  int32_t n_ops1, n_qr, n_gemm1, n_ops2, n_gemm2, n_ops3, n_solves;
+  int32_t precision;
+} tn_batch_step_desc;
+
+/* One local update of every job: the phases above, then results[i] of solves[i]. ws: DEVICE
+ * scratch of tn_batched_step_workspace_bytes bytes (shared by the phases). Returns TN_ERR_NOCONV as
+ * tn_batched_lanczos does. */
+int tn_batched_step(const tn_batch_step_desc* desc, const tn_lanczos_opts* opts, void* ws, size_t ws_bytes,
+                    tn_lanczos_result* results, void* stream);
+size_t tn_batched_step_workspace_bytes(const tn_batch_step_desc* desc, const tn_lanczos_opts* opts);
+
 /* ---- profiling ----------------------------------------------------------------------- */
 /* CUDA-event timing of kernel classes on their launching stream (0 = effective-Hamiltonian
  * matvecs inside tn_lanczos). Off by default; reading synchronises the recorded events. */

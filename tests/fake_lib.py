@@ -222,6 +222,32 @@ class FakeLib:
                 return st
         return OK
 
+    def tn_batched_step_workspace_bytes(self, desc, opts):
+        return 4096
+
+    def tn_batched_step(self, desc, opts, ws, wsb, results, stream):
+        """The phases of tn_batched_step in their documented order through the functions above."""
+        self._count("tn_batched_step")
+        from tnalg_gb300 import _lib
+        d = _struct(desc)
+        if isinstance(d, ctypes.c_void_p) or isinstance(d, int):
+            d = ctypes.cast(d, ctypes.POINTER(_lib.BatchStepDesc))[0]
+        if d.n_ops1:
+            self.tn_grouped_ops(d.ops1, d.n_ops1, ws, wsb, stream)
+        if d.n_qr:
+            self.tn_batched_qr_mixed(d.qr, d.n_qr, ws, wsb, stream)
+        if d.n_gemm1:
+            self.tn_grouped_gemm(d.precision, d.gemm1, d.n_gemm1, ws, wsb, stream)
+        if d.n_ops2:
+            self.tn_grouped_ops(d.ops2, d.n_ops2, ws, wsb, stream)
+        if d.n_gemm2:
+            self.tn_grouped_gemm(d.precision, d.gemm2, d.n_gemm2, ws, wsb, stream)
+        if d.n_ops3:
+            self.tn_grouped_ops(d.ops3, d.n_ops3, ws, wsb, stream)
+        if d.n_solves:
+            return self.tn_batched_lanczos(d.solves, d.n_solves, opts, ws, wsb, results, stream)
+        return OK
+
     def tn_svd_jacobi_workspace_bytes(self, k, n):
         return 0
 

@@ -1,6 +1,8 @@
 """The batched engine (tnalg_gb300/batched.py) on the CPU through the test double of the C ABI:
 continuous batching of uneven jobs gives every job the result it gets alone and the result of the
 one-job scheduler; admission keeps to the slot limit and the memory budget."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -92,3 +94,30 @@ def test_grouped_path_matches_the_per_job_path():
         np.testing.assert_allclose(grouped[k]["eb_full"], per_job[k]["eb_full"], atol=1e-9)
         np.testing.assert_allclose(grouped[k]["mz"], per_job[k]["mz"], atol=1e-8)
         assert grouped[k]["solves"] == per_job[k]["solves"]
+
+
+def test_unconverged_solves_continue_in_the_next_step():
+    """A local solve of the grouped path that stops unconverged at its per-step cycle limit stays at
+    its site and continues from its Ritz vector in the next step (its gauge move and environment
+    update are not repeated); the job's sweeps and result are those of an undisturbed run."""
+    from tnalg_gb300 import _lib
+    _, ref = _run(_jobs(), grouped=True)
+    fake = fake_lib.install()
+    orig = fake.tn_batched_lanczos
+    calls = {"n": 0, "held": 0}
+
+    def flaky(jobs, count, opts, ws, wsb, results, stream):
+        st = orig(jobs, count, opts, ws, wsb, results, stream)
+        res = ctypes.cast(results, ctypes.POINTER(_lib.LanczosResult))
+        calls["n"] += 1
+        if calls["n"] % 3 == 0:      # every third batched call leaves its first job unconverged
+            res[0].converged = 0
+            calls["held"] += 1
+        return st
+    fake.tn_batched_lanczos = flaky
+    eng, got = _run(_jobs(), grouped=True)
+    assert calls["held"] > 0 and eng.steps > max(3 * 2 * (l - 1) for l, *_ in SPECS)
+    for k in ref:
+        assert got[k]["solves"] == ref[k]["solves"] == 3 * 2 * (SPECS[k][0] - 1)
+        assert got[k]["unconverged"] == 0
+        assert got[k]["e_per_site"] == pytest.approx(ref[k]["e_per_site"], abs=1e-11)

@@ -48,6 +48,17 @@ class BatchSolve(ctypes.Structure):
     _fields_ = [("site", SiteDesc), ("psi_in", c_vp), ("psi_out", c_vp)]
 
 
+class BatchStepDesc(ctypes.Structure):
+    """tn_batch_step_desc: the phase tables of one local update of many jobs (HOST arrays)."""
+    _fields_ = [("ops1", c_vp), ("qr", c_vp), ("gemm1", c_vp), ("ops2", c_vp), ("gemm2", c_vp), ("ops3", c_vp),
+                ("solves", c_vp), ("n_ops1", ctypes.c_int32), ("n_qr", ctypes.c_int32), ("n_gemm1", ctypes.c_int32),
+                ("n_ops2", ctypes.c_int32), ("n_gemm2", ctypes.c_int32), ("n_ops3", ctypes.c_int32),
+                ("n_solves", ctypes.c_int32), ("precision", ctypes.c_int32)]
+
+
+STEP_PHASES = ("ops1", "qr", "gemm1", "ops2", "gemm2", "ops3")
+
+
 class BatchOp(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("chi", ctypes.c_int32), ("d", ctypes.c_int32), ("chir", ctypes.c_int32),
                 ("nterms", ctypes.c_int32), ("reserved", ctypes.c_int32), ("src", c_vp), ("s_slot", c_i64),
@@ -142,6 +153,8 @@ _SIGS = {
     "tn_batched_qr_mixed_workspace_bytes": (c_sz, [c_vp, c_int]),
     "tn_batched_lanczos": (c_int, [c_vp, c_int, c_vp, c_vp, c_sz, c_vp, c_vp]),
     "tn_batched_lanczos_workspace_bytes": (c_sz, [c_vp, c_int, c_vp]),
+    "tn_batched_step": (c_int, [c_vp, c_vp, c_vp, c_sz, c_vp, c_vp]),
+    "tn_batched_step_workspace_bytes": (c_sz, [c_vp, c_vp]),
     "tn_profile_enable": (c_int, [c_int]),
     "tn_profile_reset": (c_int, []),
     "tn_profile_read": (c_int, [c_int, c_vp, c_vp, c_vp]),

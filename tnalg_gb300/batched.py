@@ -19,6 +19,7 @@ solver's arithmetic per job does not depend on the other jobs of the batch, so a
 the same alone and in any mix (tests/test_gpu_batched.py).
 """
 import ctypes
+import threading
 import time
 
 import numpy as np
@@ -41,6 +42,9 @@ class BatchJob:
         self.finished = None
         self.solves = 0
         self.matvecs = 0
+        self.unconverged = 0
+        self._cont = False
+        self._cycles = 0
         self.A = None
         self._order = None
         self._k = 0
@@ -133,10 +137,16 @@ def _table(dtype, recs):
 
 
 def _gemm(M, N, K, A, sA, B, sB, C, sC, *, batch=1, sAb=0, sBb=0, sCb=0, alpha=1.0, beta=0.0, accumulate=0,
-          active=0):
-    return _rec(L.GEMM_PROBLEM_DTYPE, M=M, N=N, K=K, nred=1, A=A, sAm=sA[0], sAk=sA[1], B=B, sBk=sB[0], sBn=sB[1],
-                C=C, sCm=sC[0], sCn=sC[1], alpha=alpha, beta=beta, accumulate=accumulate, batch=batch, sAb=sAb,
-                sBb=sBb, sCb=sCb, active=active)
+          active=0, nred=1, sAr=0, sBr=0):
+    return _rec(L.GEMM_PROBLEM_DTYPE, M=M, N=N, K=K, nred=nred, A=A, sAm=sA[0], sAk=sA[1], sAr=sAr, B=B, sBk=sB[0],
+                sBn=sB[1], sBr=sBr, C=C, sCm=sC[0], sCn=sC[1], alpha=alpha, beta=beta, accumulate=accumulate,
+                batch=batch, sAb=sAb, sBb=sBb, sCb=sCb, active=active)
+
+
+def _density(M_ptr, X_ptr, cl, d, cr, out):
+    """out[s', s] = sum_{a,b} M[a, s', b] X[a, s, b] (tn_pair_contract's local density) as one
+    product with a reduction over the left bond."""
+    return _gemm(d, d, cr, M_ptr, (cr, 1), X_ptr, (1, cr), out, (d, 1), nred=cl, sAr=d * cr, sBr=d * cr)
 
 
 def _op(kind, chi, d, src, out, total, *, terms=0, nterms=0, ops=0, s_slot=0, s_row=0, chir=0, out_stride=0,
@@ -148,6 +158,35 @@ def _op(kind, chi, d, src, out, total, *, terms=0, nterms=0, ops=0, s_slot=0, s_
 QR_MAX_ELEMS = 32768   # m n of one matrix of tn_batched_qr_mixed
 
 
+_EYE = {}
+
+
+def _eye_term(device):
+    """Device term list of one identity term (slot -1, group 0, coefficient 1) for BOP_COMBINE."""
+    key = str(device)
+    hit = _EYE.get(key)
+    if hit is None:
+        hit = _EYE[key] = L.terms_tensor([(-1, 0, 1.0)], device)[0]
+    return hit
+
+
+def _adm_step():
+    return {"ops_pre": [], "qr": [], "f64": [], "ops_post": [], "gemm1": [], "ops2": [], "gemm2": []}
+
+
+def _adm_tables(step, R):
+    """Tables of one admission step; QR items given as (location, m, n, sAm, sAn) with the R factor
+    at R (tn_batched_step runs those above tn_batched_qr_mixed's limit through tn_qr_mixed)."""
+    out = {k: _table(v_dtype(k), v) for k, v in step.items() if k != "qr"}
+    recs = []
+    for (loc, mm, nn, sam, san) in step["qr"]:
+        t, o = loc
+        recs.append(_rec(L.QR_ITEM_DTYPE, m=mm, n=nn, a=t.data_ptr() + 8 * o, sAm=sam, sAn=san, r=R, sRm=nn, sRn=1,
+                         active=0))
+    out["qr"] = _table(L.QR_ITEM_DTYPE, recs)
+    return out
+
+
 class ArenaJob(BatchJob):
     """A job of the grouped path. Its MPS, both environment stacks of every bond and its scratch live
     in one device arena allocated at admission, so every pointer of every local update is fixed and
@@ -157,40 +196,142 @@ class ArenaJob(BatchJob):
     plans of engine.Model, block assembly), in the grouped kernels."""
 
     def start(self, device, precision):
-        super().start(device, precision)
-        if self.para["ob_position"] != 0:
+        """Host side of admission (run on the engine's worker threads): the job's random MPS (the
+        draws of BatchJob.start, uploaded as drawn), its coupling model, the arena at the final bond
+        dimensions, the staging of the batched canonicalisation and its launch records. The device
+        side (BatchEngine._admit_device) then centres every admitted job at site 0 in grouped
+        launches: a left-to-right pass of gauge moves followed by a right-to-left pass that also
+        builds every right environment (the centring of MPSClass.py:188-198 and the environment
+        builds of MPSClass.py:202-325, for all jobs at once)."""
+        p = self.para
+        if p["ob_position"] != 0:
             raise ValueError("the grouped path starts its sweeps at site 0 (ob_position = 0)")
-        A = self.A
+        t0 = time.perf_counter()
+        rs = np.random.RandomState(self.seed)
+        Ln, d, chi = p["l"], p["d"], p["chi"]
+        tensors = [None] * Ln
+        tensors[0] = rs.randn(1, d, chi)
+        tensors[Ln - 1] = rs.randn(chi, d, 1)
+        for n in range(1, Ln - 1):
+            tensors[n] = rs.randn(chi, d, chi)
+        t1 = time.perf_counter()
+        self.A = A = MpsOpenBoundaryClass(length=Ln, d=d, chi=chi, operators=p["op"], device=device,
+                                          precision=precision, tensors=tensors)
+        t2 = time.perf_counter()
+        A._model(p["index1"], p["index2"], p["coeff1"], p["coeff2"], p["eigs_tol"])
+        t3 = time.perf_counter()
+        self._order = list(range(1, Ln)) + list(range(Ln - 2, -1, -1))
+        self._k = 0
+        self._t = 0
         dev = A._dev
         m = dev.model
         if m.compressed:
             raise ValueError("the grouped path runs uncompressed coupling models")
-        Ln, d = A.length, A.phys_dim
-        # a random MPS is centred by QR moves from the right end, which leave the bonds near the left
-        # end wider than d^b; moving the centre right past them and back gives every bond its final
-        # dimension min(chi, d^b, d^(L-b)) now (a reduced QR truncates nothing: the state is
-        # unchanged), so the arena's shapes stay fixed for the whole run
-        b = 0
-        while b < Ln - 1 and int(dev.virtual_dim[b + 1]) > d ** (b + 1):
-            b += 1
-        if b > 0:
-            A.correct_orthogonal_center(b)
-            A.correct_orthogonal_center(0)
-        # a random MPS centred by QR moves carries the product of all R factors' norms on its centre
-        # (~1e77 for 64 sites at chi = 128), beyond FP32's range for the split-TF32 absorb of the
-        # first gauge move; the state's norm is irrelevant to the solves (eigsh normalises its start
-        # vector), so the centre is normalised once here
-        c0 = dev.mps[0]
-        c0.div_(c0.abs().max().clamp_min(1e-300))   # first to O(1), so its squared norm cannot overflow
-        nrm2 = torch.empty(1, dtype=torch.float64, device=dev.device)
-        lib = L.load()
-        wp, wb = dev.ws.args(4096 + 64 * c0.numel())
-        L.check(lib.tn_dot(c0.numel(), L.ptr(c0), L.ptr(c0), L.ptr(nrm2), wp, wb, L.stream_handle()), "dot")
-        L.check(lib.tn_scale(c0.numel(), L.ptr(c0), 1.0, L.ptr(nrm2), L.stream_handle()), "scale")
-        dev.unit_norm = True
-        dev.ensure_envs(0)
-        dims = [int(x) for x in dev.virtual_dim]
+        rb = [int(x) for x in dev.virtual_dim]          # bonds of the random tensors
+        # left bonds after the left-to-right pass (a reduced QR keeps min(rows, columns)), then the
+        # final bonds after the right-to-left pass: min(chi, d^b, d^(L-b))
+        lA = [1] * Ln
+        for t in range(Ln - 1):
+            lA[t + 1] = min(lA[t] * d, rb[t + 1])
+        dims = [1] * (Ln + 1)
+        for n in range(Ln - 1, 0, -1):
+            dims[n] = min(lA[n], d * dims[n + 1])
         self.dims, self.d, self.model = dims, d, m
+        self._alloc_arena(dev, dims)
+        # staging: the left-to-right pass writes site t+1 (lA[t+1] x d x rb[t+2]) into slot t+1, R
+        # factors go to R; the random tensors themselves hold the site 0 gauge move and, in the
+        # right-to-left pass, the absorbed sites that are not final yet
+        soff, slots = 0, [None] * Ln
+        for t in range(1, Ln):
+            slots[t] = soff
+            soff += (lA[t] * d * rb[t + 1] + 31) // 32 * 32
+        r_off = soff
+        soff += max(rb) ** 2
+        self.stage = torch.empty(soff, dtype=torch.float64, device=dev.device)
+        self._rand = dev.mps
+        sbase = self.stage.data_ptr()
+        self._ld = (lA, rb)
+        self._eye = _eye_term(dev.device)
+        act = self.active.data_ptr()
+        arena = self.arena
+
+        def loc_site(n):
+            return (arena, self.lay[("site", n)][0])
+
+        def loc_slot(t):
+            return (self._rand[0], 0) if t == 0 else (self.stage, slots[t])
+
+        def loc_rand(n):
+            return (self._rand[n], 0)
+
+        def ptr(loc):
+            t, o = loc
+            return t.data_ptr() + 8 * o
+        R = sbase + 8 * r_off
+        tall_b = [False] * Ln
+        for n in range(1, Ln):
+            tall_b[n] = d * dims[n + 1] >= lA[n]
+        steps = []
+        # left-to-right pass: site t (lA[t] d x rb[t+1]) = Q R (or, when it has fewer rows than
+        # columns, = I M: the identity is an isometry and M moves on), site t+1 <- R . site t+1,
+        # scaled by 1/sqrt(d rb[t+2]) so that the norm of the moving centre stays O(1) (a Gaussian
+        # site multiplies it by ~sqrt(d rb[t+2])); the state's norm is irrelevant to the solves
+        for t in range(Ln - 1):
+            st = _adm_step()
+            mm, nn = lA[t] * d, rb[t + 1]
+            src = loc_slot(t)
+            tall = mm >= nn
+            if tall:
+                st["qr"].append((src, mm, nn, nn, 1))
+                X, ldx, k = R, nn, nn
+            else:
+                X, ldx, k = ptr(src), nn, mm
+            ncol = d * rb[t + 2]
+            dst = loc_site(Ln - 1) if (t + 1 == Ln - 1 and tall_b[Ln - 1]) else loc_slot(t + 1)
+            st["f64"].append(_gemm(k, ncol, nn, X, (ldx, 1), ptr(loc_rand(t + 1)), (ncol, 1), ptr(dst), (ncol, 1),
+                                   alpha=1.0 / np.sqrt(ncol), active=act))
+            if not tall:
+                st["ops_post"].append(self._identity(mm, ptr(src), act))
+            steps.append(st)
+        # right-to-left pass: site n (lA[n] x d dims[n+1]) = L Q^T (QR of its transpose) or = M I;
+        # Q^T (or I) is the final right-canonical site n, site n-1 <- site n-1 . L, and ER[n] is
+        # built from ER[n+1] and site n with the records of a left-moving local update
+        for n in range(Ln - 1, 0, -1):
+            st = _adm_step()
+            r = dims[n + 1]
+            if n == Ln - 1:
+                cur = loc_site(n) if tall_b[n] else loc_slot(n)
+            else:
+                cur = loc_site(n) if tall_b[n] else loc_rand(n)
+            prev = loc_slot(n - 1)
+            dst = loc_site(0) if n - 1 == 0 else (loc_site(n - 1) if tall_b[n - 1] else loc_rand(n - 1))
+            rows = lA[n - 1] * d
+            if tall_b[n]:
+                st["qr"].append((cur, d * r, lA[n], 1, d * r))
+                st["f64"].append(_gemm(rows, lA[n], lA[n], ptr(prev), (lA[n], 1), R, (1, lA[n]), ptr(dst),
+                                       (lA[n], 1), active=act))
+            else:
+                st["ops_pre"].append(self._identity(d * r, ptr(loc_site(n)), act))
+                st["f64"].append(_gemm(rows, d * r, lA[n], ptr(prev), (lA[n], 1), ptr(cur), (d * r, 1), ptr(dst),
+                                       (d * r, 1), active=act))
+            e_ops1, e_g1, e_ops2, e_g2 = self._env_right_rows(n)
+            st["ops_pre"] += e_ops1
+            st["gemm1"] += e_g1
+            st["ops2"] += e_ops2
+            st["gemm2"] += e_g2
+            steps.append(st)
+        self._adm = [_adm_tables(s, R) for s in steps]
+        self._rows = {}
+        self.admit_parts = {"draws": t1 - t0, "upload": t2 - t1, "model": t3 - t2,
+                            "arena_and_tables": time.perf_counter() - t3}
+
+    def _identity(self, k, out, act):
+        """A record writing the k x k identity to out (a slot combination of one identity term)."""
+        return _op(L.BOP_COMBINE, k, self.d, out, out, k * k, terms=self._eye.data_ptr(), nterms=1, out_stride=k * k,
+                   active=act)
+
+    def _alloc_arena(self, dev, dims):
+        m, d, Ln = self.model, self.d, len(dims) - 1
         nl = [m.n_left(b) for b in range(Ln + 1)]
         nr = [m.n_right(b) for b in range(Ln + 1)]
         cmax = max(dims)
@@ -216,33 +357,79 @@ class ArenaJob(BatchJob):
         take("T", carry_max * d * cmax * cmax)
         take("SL", max(ngmax, 1) * cmax * cmax)
         take("SR", max(ngmax, 1) * cmax * cmax)
+        # zeros: the boundary environments EL[0] and ER[L] (no block Hamiltonian, no open operator)
         self.arena = torch.zeros(off, dtype=torch.float64, device=dev.device)
         self.active = torch.ones(1, dtype=torch.int32, device=dev.device)
         self.lay = lay
         base = self.arena.data_ptr()
         self.addr = {k: base + 8 * o for k, (o, _) in lay.items()}
-        for n in range(Ln):
-            self.view(("site", n)).copy_(dev.mps[n].reshape(-1))
-        self.view(("EL", 0)).copy_(dev.EL[0].reshape(-1))
-        for b in range(1, Ln + 1):
-            self.view(("ER", b)).copy_(dev.ER[b].reshape(-1))
-        # the one-job state is no longer needed (observables use the arena's site tensors)
+
+    def finish_admission(self):
+        """After the device side of admission: the job's DeviceMPS views the arena, centred at site 0
+        (right-canonical sites 1..L-1; the centre carries an O(1) norm, which the first solve
+        normalises)."""
+        dev = self.A._dev
+        Ln, d, dims = len(self.dims) - 1, self.d, self.dims
         dev.mps = [self.view(("site", n)).view(dims[n], d, dims[n + 1]) for n in range(Ln)]
+        dev.virtual_dim = np.array(dims)
+        dev.center = 0
+        dev.orthogonality = np.ones(Ln)
+        dev.orthogonality[0] = 0
         dev.EL = [None] * (Ln + 1)
         dev.ER = [None] * (Ln + 1)
         dev.el_upto, dev.er_from = -1, Ln + 1
-        self._rows = {}
+        dev.unit_norm = False
+        self._rand = self.stage = self._adm = None
+
+    def _env_right_rows(self, q):
+        """Records of ER[q] from ER[q+1] and the right-canonical site q (cl x d x cr): the block
+        operator Wenv of ER[q+1] with site q's terms, the products T[s] of every open operator with
+        site q, and ER[q][s] = B . T[s]^T (transfer_right of TensorBasicModule.py:575-619 for every
+        carried operator, the classify_and_update_env buckets of MPSClass.py:633-733)."""
+        m, d, dims, a = self.model, self.d, self.dims, self.addr
+        act = self.active.data_ptr()
+        ops = m.ops.data_ptr()
+        cl, cr = dims[q], dims[q + 1]
+        n_q = cl * d * cr
+        site_q = a[("site", q)]
+        plan = m.memo(("rcp", q), lambda: m.right_carry_plan(q))
+        terms, nt = m.table_lazy(("wrf", q), lambda: m.right_block_terms(q, with_site=True))
+        ops1 = [_op(L.BOP_BLOCK_RIGHT, cr, d, a[("ER", q + 1)], a["Wenv"], (d * cr) ** 2, terms=terms.data_ptr(),
+                    nterms=nt, ops=ops, s_slot=cr * cr, s_row=cr, active=act)]
+        # T0 = B (cl x d cr) . Wenv^T
+        gemm1 = [_gemm(cl, d * cr, d * cr, site_q, (d * cr, 1), a["Wenv"], (1, d * cr), a["T"], (d * cr, 1),
+                       active=act)]
+        ops2 = []
+        for j, (kind, x) in enumerate(plan):
+            tj = a["T"] + 8 * (1 + j) * n_q
+            if kind == "carry":   # T[1+j] = B (cl d x cr) . ER[q+1][slot]^T
+                gemm1.append(_gemm(cl * d, cr, cr, site_q, (cr, 1), a[("ER", q + 1)] + 8 * x * cr * cr, (1, cr), tj,
+                                   (cr, 1), active=act))
+            else:
+                oi = m.opidx(("op", x), [x])
+                ops2.append(_op(L.BOP_SITE_OPS, cl, d, site_q, tj, n_q, terms=oi.data_ptr(), nterms=1, ops=ops,
+                                chir=cr, out_stride=n_q, active=act))
+        ns = 1 + len(plan)
+        # ER[q][s] = B (cl x d cr) . T[s]^T
+        gemm2 = [_gemm(cl, cl, d * cr, site_q, (d * cr, 1), a["T"], (1, d * cr), a[("ER", q)], (cl, 1), batch=ns,
+                       sAb=0, sBb=n_q, sCb=cl * cl, active=act)]
+        return ops1, gemm1, ops2, gemm2
 
     def view(self, key):
         o, n = self.lay[key]
         return self.arena[o:o + n]
 
     def rows(self):
-        """Launch records of this step's local update (built once per (site, direction))."""
+        """Launch records of this step's local update (built once per (site, direction)); a job
+        whose last local solve stopped unconverged at its cycle limit gets only that solve's
+        record, restarted from its current Ritz vector (the effective Hamiltonian in the arena is
+        unchanged until the job's next gauge move)."""
         k = self._k
         hit = self._rows.get(k)
         if hit is None:
             hit = self._rows[k] = self._build(k)
+        if self._cont:
+            return hit["cont"]
         return hit
 
     def _build(self, k):
@@ -256,9 +443,11 @@ class ArenaJob(BatchJob):
         n_q = cl * d * cr
         site_q = a[("site", q)]
         out = {"ops1": [], "qr": [], "gemm1": [], "ops2": [], "gemm2": [], "ops3": []}
+        # a gauge move above tn_batched_qr_mixed's limit runs through tn_qr_mixed, unmasked
         if right:
             mm, nn = cl * d, cr
-            qr = _rec(L.QR_ITEM_DTYPE, m=mm, n=nn, a=site_q, sAm=cr, sAn=1, r=a["R"], sRm=nn, sRn=1, active=act)
+            qr = _rec(L.QR_ITEM_DTYPE, m=mm, n=nn, a=site_q, sAm=cr, sAn=1, r=a["R"], sRm=nn, sRn=1,
+                      active=act if mm * nn <= QR_MAX_ELEMS else 0)
             # seed = R (cr x cr) . site[p] (cr x d dims[p+1])
             nxt = d * dims[p + 1]
             out["gemm1"].append(_gemm(cr, nxt, cr, a["R"], (cr, 1), a[("site", p)], (nxt, 1), a["seed"], (nxt, 1),
@@ -285,31 +474,17 @@ class ArenaJob(BatchJob):
                                       batch=ns, sAb=0, sBb=n_q, sCb=cr * cr, active=act))
         else:
             mm, nn = d * cr, cl
-            qr = _rec(L.QR_ITEM_DTYPE, m=mm, n=nn, a=site_q, sAm=1, sAn=d * cr, r=a["R"], sRm=nn, sRn=1, active=act)
+            qr = _rec(L.QR_ITEM_DTYPE, m=mm, n=nn, a=site_q, sAm=1, sAn=d * cr, r=a["R"], sRm=nn, sRn=1,
+                      active=act if mm * nn <= QR_MAX_ELEMS else 0)
             # seed = site[p] (dims[p] d x cl) . R^T
             prv = dims[p] * d
             out["gemm1"].append(_gemm(prv, cl, cl, a[("site", p)], (cl, 1), a["R"], (1, cl), a["seed"], (cl, 1),
                                       active=act))
-            plan = m.memo(("rcp", q), lambda: m.right_carry_plan(q))
-            terms, nt = m.table_lazy(("wrf", q), lambda: m.right_block_terms(q, with_site=True))
-            out["ops1"].append(_op(L.BOP_BLOCK_RIGHT, cr, d, a[("ER", q + 1)], a["Wenv"], (d * cr) ** 2,
-                                   terms=terms.data_ptr(), nterms=nt, ops=ops, s_slot=cr * cr, s_row=cr, active=act))
-            # T0 = B (cl x d cr) . Wenv^T
-            out["gemm1"].append(_gemm(cl, d * cr, d * cr, site_q, (d * cr, 1), a["Wenv"], (1, d * cr), a["T"],
-                                      (d * cr, 1), active=act))
-            for j, (kind, x) in enumerate(plan):
-                tj = a["T"] + 8 * (1 + j) * n_q
-                if kind == "carry":   # T[1+j] = B (cl d x cr) . ER[q+1][slot]^T
-                    out["gemm1"].append(_gemm(cl * d, cr, cr, site_q, (cr, 1), a[("ER", q + 1)] + 8 * x * cr * cr,
-                                              (1, cr), tj, (cr, 1), active=act))
-                else:
-                    oi = m.opidx(("op", x), [x])
-                    out["ops2"].append(_op(L.BOP_SITE_OPS, cl, d, site_q, tj, n_q, terms=oi.data_ptr(), nterms=1,
-                                           ops=ops, chir=cr, out_stride=n_q, active=act))
-            ns = 1 + len(plan)
-            # ER[q][s] = B (cl x d cr) . T[s]^T
-            out["gemm2"].append(_gemm(cl, cl, d * cr, site_q, (d * cr, 1), a["T"], (1, d * cr), a[("ER", q)], (cl, 1),
-                                      batch=ns, sAb=0, sBb=n_q, sCb=cl * cl, active=act))
+            e_ops1, e_g1, e_ops2, e_g2 = self._env_right_rows(q)
+            out["ops1"] += e_ops1
+            out["gemm1"] += e_g1
+            out["ops2"] += e_ops2
+            out["gemm2"] += e_g2
         # effective Hamiltonian of site p
         pl, pr = dims[p], dims[p + 1]
         t, nt = m.table_lazy(("wl", p), lambda: m.left_block_terms(p))
@@ -328,48 +503,154 @@ class ArenaJob(BatchJob):
                                    nterms=nb, s_slot=pr * pr, s_row=pr, out_stride=pr * pr, active=act))
         solve = _rec(L.BATCH_SOLVE_DTYPE, chil=pl, d=d, chir=pr, wl=a["WL"], wr=a["WR"], nstr=ng,
                      sl=a["SL"] if ng else 0, sr=a["SR"] if ng else 0, psi_in=a["seed"], psi_out=a[("site", p)])
-        res = {key: _table(v_dtype(key), v) for key, v in out.items() if key != "qr"}
-        res["qr"] = _table(L.QR_ITEM_DTYPE, [qr])
-        res["solve"] = _table(L.BATCH_SOLVE_DTYPE, [solve])
-        res["qr_shape"] = (mm, nn, right, q)
-        res["qr_big"] = mm * nn > QR_MAX_ELEMS
+        # raw record bytes: a step joins every job's bytes per phase (b"".join is far cheaper than
+        # concatenating hundreds of small structured arrays)
+        res = {key: _table(v_dtype(key), v).tobytes() for key, v in out.items() if key != "qr"}
+        res["qr"] = _table(L.QR_ITEM_DTYPE, [qr]).tobytes()
+        res["solve"] = _table(L.BATCH_SOLVE_DTYPE, [solve]).tobytes()
+        cont = _rec(L.BATCH_SOLVE_DTYPE, chil=pl, d=d, chir=pr, wl=a["WL"], wr=a["WR"], nstr=ng,
+                    sl=a["SL"] if ng else 0, sr=a["SR"] if ng else 0, psi_in=a[("site", p)], psi_out=a[("site", p)])
+        res["cont"] = dict({key: b"" for key in res if key != "solve"},
+                           solve=_table(L.BATCH_SOLVE_DTYPE, [cont]).tobytes())
         return res
 
-    def big_qr(self, ws):
-        """A gauge move whose site tensor exceeds the batched QR's shared memory (m n > 32768, e.g.
-        chi > 128 at d = 2): tn_qr_mixed into a scratch Q, copied back in place."""
-        mm, nn, right, q = self.rows()["qr_shape"]
-        lib = L.load()
-        cl, cr = self.dims[q], self.dims[q + 1]
-        site = self.view(("site", q))
-        Qt = torch.empty(mm * nn, dtype=torch.float64, device=site.device)
-        R = self.view("R")
-        wp, wb = ws.args(lib.tn_qr_mixed_workspace_bytes(mm, nn))
-        if right:
-            L.check(lib.tn_qr_mixed(mm, nn, L.ptr(site), nn, 1, L.ptr(Qt), nn, 1, L.ptr(R), nn, 1, wp, wb,
-                                    L.stream_handle()), "qr_mixed")
-            site.copy_(Qt)
-        else:
-            L.check(lib.tn_qr_mixed(mm, nn, L.ptr(site), 1, mm, L.ptr(Qt), 1, mm, L.ptr(R), nn, 1, wp, wb,
-                                    L.stream_handle()), "qr_mixed")
-            site.copy_(Qt)
-
-    def solved(self, res):
-        done = super().solved(res)
-        return done
+    def solved(self, res, max_cycles=None):
+        """Book the local solve (the arena holds the state: no DeviceMPS bookkeeping); True when
+        the job's last sweep is done. An unconverged solve continues in the next step (its restart
+        cycles so far counted against max_cycles) instead of holding back the whole batch."""
+        self.matvecs += res.matvecs
+        self._cycles += res.restarts + 1
+        if not res.converged and max_cycles is not None and self._cycles < max_cycles:
+            self._cont = True
+            return False
+        self._cont = False
+        self._cycles = 0
+        self.solves += 1
+        if not res.converged:
+            self.unconverged += 1
+        self._k += 1
+        if self._k == len(self._order):
+            self._k = 0
+            self._t += 1
+            return self._t >= self.para["sweep_time"]
+        return False
 
     def observe(self):
-        dev = self.A._dev
-        dev.center = self._order[self._k - 1] if self._k > 0 else 0
-        if self._k == 0:
-            dev.center = self._order[-1]
-        dev.unit_norm = True
-        super().observe()
+        raise RuntimeError("jobs of the grouped path are observed in groups (BatchEngine._observe_group)")
+
+    def observe_plan(self):
+        """Records of the FP64 observation of the final state, in stages of grouped launches
+        (gemm1 -> ops2 -> gemm2 of tn_batched_step): the expectation values of engine._Observer
+        (observe_magnetization and observe_bond_energy, MPSClass.py:911-934) for a state centred
+        at site 0 (every later site right-canonical), so every term is contracted left to right
+        from an identity. Stage q: X = E_q M_q (E_q the identity transfer to bond q) and, for
+        every operator string open at bond q, X' = V M_q (gemm1); the first operator of the
+        strings that start at q applied to X (ops2); the local densities of site q (one-site,
+        and of every string that closes at q), E_{q+1} = M_q^T X and the strings carried to bond
+        q+1, V <- M_q^T X' or M_q^T (op X) (gemm2). Returns (stages, G): G holds the d x d densities
+        of the sites, then those of the two-body terms, in index2 order."""
+        if self._k != 0 or self._t < 1:
+            raise RuntimeError("observe_plan needs the state at the end of a sweep (centre at site 0)")
+        p = self.para
+        Ln, d, dims, m = len(self.dims) - 1, self.d, self.dims, self.model
+        dev = self.A._dev.device
+        idx = np.asarray(p["index2"]).reshape(-1, 4).astype(int)
+        groups = {}
+        for k, (i, j, a, b) in enumerate(idx):
+            if i == j:
+                raise ValueError("a two-body term needs two sites")
+            if i > j:
+                i, j, a, b = j, i, b, a
+            groups.setdefault((int(i), int(a)), []).append((int(j), int(b), k))
+        gl = sorted(groups.items())
+        jmax = {g: max(j for j, _, _ in lst) for g, lst in gl}
+        closing = {}
+        for g, lst in gl:
+            for j, b, k in lst:
+                closing.setdefault((g, j), []).append(k)
+        cmax = max(dims)
+        nV, nX = cmax * cmax, cmax * d * cmax
+        # slots for the strings open at one time (a string holds its slot from its first site to
+        # its last)
+        live, need = 0, 0
+        for q in range(Ln):
+            live += sum(1 for (i, a) in groups if i == q)
+            need = max(need, live)
+            live -= sum(1 for g in groups if jmax[g] == q)
+        nslot = max(need, 1)
+        G = torch.zeros((Ln + len(idx)) * d * d, dtype=torch.float64, device=dev)
+        scratch = torch.empty(nV + nX + nslot * (nV + 2 * nX), dtype=torch.float64, device=dev)
+        base = scratch.data_ptr()
+        E, X0 = base, base + 8 * nV
+        sl = [base + 8 * (nV + nX + t * (nV + 2 * nX)) for t in range(nslot)]
+        ops = m.ops.data_ptr()
+        gbase = G.data_ptr()
+        free = list(range(nslot))[::-1]
+        slot_of = {}
+        stages = []
+        for q in range(Ln):
+            cl, cr = dims[q], dims[q + 1]
+            nq = cl * d * cr
+            M = self.addr[("site", q)]
+            g1, o2, g2 = [], [], []
+            X = M if q == 0 else X0
+            if q > 0:
+                g1.append(_gemm(cl, d * cr, cl, E, (cl, 1), M, (d * cr, 1), X, (d * cr, 1)))
+            g2.append(_density(M, X, cl, d, cr, gbase + 8 * q * d * d))
+            for g in [g for g in slot_of if g[0] < q]:      # strings carried into bond q
+                V = sl[slot_of[g]]
+                Xp = V + 8 * nV
+                g1.append(_gemm(cl, d * cr, cl, V, (cl, 1), M, (d * cr, 1), Xp, (d * cr, 1)))
+                for k in closing.get((g, q), []):
+                    g2.append(_density(M, Xp, cl, d, cr, gbase + 8 * (Ln + k) * d * d))
+                if jmax[g] > q:
+                    g2.append(_gemm(cr, cr, cl * d, M, (1, cr), Xp, (cr, 1), V, (cr, 1)))
+            for g in [g for g in groups if g[0] == q]:      # strings that start at q
+                t = free.pop()
+                slot_of[g] = t
+                V = sl[t]
+                Y = V + 8 * (nV + nX)
+                oi = m.opidx(("op", g[1]), [g[1]])
+                o2.append(_op(L.BOP_SITE_OPS, cl, d, X, Y, nq, terms=oi.data_ptr(), nterms=1, ops=ops, chir=cr,
+                              out_stride=nq))
+                g2.append(_gemm(cr, cr, cl * d, M, (1, cr), Y, (cr, 1), V, (cr, 1)))
+            if q < Ln - 1:
+                g2.append(_gemm(cr, cr, cl * d, M, (1, cr), X, (cr, 1), E, (cr, 1)))
+            for g in [g for g in list(slot_of) if jmax[g] == q]:
+                free.append(slot_of.pop(g))
+            stages.append({"gemm1": _table(L.GEMM_PROBLEM_DTYPE, g1), "ops2": _table(L.BATCH_OP_DTYPE, o2),
+                           "gemm2": _table(L.GEMM_PROBLEM_DTYPE, g2)})
+        self._obs_keep = scratch
+        return stages, G
+
+    def finish_observe(self, g):
+        """The results of observe() from the host copy of observe_plan's densities."""
+        p, A = self.para, self.A
+        Ln, d = len(self.dims) - 1, self.d
+        idx = np.asarray(p["index2"]).reshape(-1, 4).astype(int)
+        c2 = np.ravel(np.asarray(p["coeff2"], dtype=float))
+        opsn = self.model.ops_np
+        dens = np.asarray(g).reshape(-1, d, d)
+        mx = np.array([np.sum(opsn[1] * dens[q]) for q in range(Ln)])
+        mz = np.array([np.sum(opsn[3] * dens[q]) for q in range(Ln)])
+        closing = [b if i < j else a for (i, j, a, b) in idx]
+        v2 = np.array([np.sum(opsn[closing[k]] * dens[Ln + k]) for k in range(len(idx))])
+        eb = c2 * v2
+        e = float((np.sum(eb) - p["hx"] * np.sum(mx) - p["hz"] * np.sum(mz)) / p["l"])
+        self.result = {"e_per_site": e, "eb_full": np.ravel(eb), "mx": mx, "mz": mz, "sweeps": self._t,
+                       "solves": self.solves, "matvecs": self.matvecs, "unconverged": self.unconverged}
+        self.A = None
         self.arena = None
+        self._obs_keep = None
 
 
 def v_dtype(key):
-    return L.GEMM_PROBLEM_DTYPE if key.startswith("gemm") else L.BATCH_OP_DTYPE
+    return L.GEMM_PROBLEM_DTYPE if key.startswith("gemm") or key == "f64" else L.BATCH_OP_DTYPE
+
+
+_DTYPE_OF = {"qr": L.QR_ITEM_DTYPE, "solve": L.BATCH_SOLVE_DTYPE, "ops1": L.BATCH_OP_DTYPE,
+             "ops2": L.BATCH_OP_DTYPE, "ops3": L.BATCH_OP_DTYPE, "gemm1": L.GEMM_PROBLEM_DTYPE,
+             "gemm2": L.GEMM_PROBLEM_DTYPE}
 
 
 class BatchEngine:
@@ -377,7 +658,8 @@ class BatchEngine:
     step for all admitted jobs, p50/p99 latency from arrival to result."""
 
     def __init__(self, device="cuda", precision="tf32x3", budget_bytes=None, max_active=1024, max_krylov=24,
-                 check_every=3, mixed_floor=2e-6, workers=8, streams=16, grouped=None, profile=False):
+                 check_every=3, mixed_floor=2e-6, workers=8, streams=16, grouped=None, profile=False, max_restarts=1,
+                 max_cycles=51):
         self.device = device
         self.workers = max(1, int(workers))
         self.nstreams = max(1, int(streams))
@@ -388,6 +670,13 @@ class BatchEngine:
         self.budget = budget_bytes
         self.max_active = int(max_active)
         self.krylov = int(max_krylov)
+        # restart cycles of a batched solve: all jobs of a step wait for the slowest, so a solve of
+        # the grouped path runs at most max_restarts + 1 cycles per step and, if unconverged,
+        # continues from its Ritz vector in the next step (its site does not advance) until
+        # max_cycles cycles in all; then it keeps its best Ritz vector (reported unconverged) and
+        # the sweep goes on, as eigsh's maxiter would
+        self.max_restarts = int(max_restarts)
+        self.max_cycles = int(max_cycles)
         self.check_every = int(check_every)
         self.mixed_floor = float(mixed_floor)
         self.pending = []
@@ -398,8 +687,8 @@ class BatchEngine:
         self.max_used = 0
         self._used = 0
         self._ws = None
-        self._ws2 = None
         self._observing = []
+        self._tls = threading.local()   # the observer threads' workspaces and streams
         self._t0 = None
         self.step_ms = []
         self.times = {"admit": 0.0, "step": 0.0, "observe": 0.0, "tables": 0.0}
@@ -441,6 +730,8 @@ class BatchEngine:
             admit.append(job)
             self._used += fp
         self._on_workers(admit, lambda job: job.start(self.device, self.precision))
+        if self.grouped and admit:
+            self._admit_device(admit)
         self.active += admit
         self.max_concurrent = max(self.max_concurrent, len(self.active))
         self.max_used = max(self.max_used, self._used)
@@ -476,8 +767,12 @@ class BatchEngine:
             return
         cuda = str(self.device).startswith("cuda") and not L._host_test
         if not cuda or self.workers == 1:
+            if self.grouped:
+                self._observe_group(jobs)
+            else:
+                for job in jobs:
+                    job.observe()
             for job in jobs:
-                job.observe()
                 self._retire(job)
             return
         self._ensure_streams()
@@ -486,14 +781,53 @@ class BatchEngine:
         ready.record(main)
 
         def run(job):
+            t_in = time.perf_counter()
             st = self._streams[job.job_id % self.nstreams]
             st.wait_event(ready)
             with torch.cuda.stream(st):
                 job.observe()
             st.synchronize()
+            job.observe_s = time.perf_counter() - t_in
             return job
+        now = time.perf_counter() - self._t0
+        for job in jobs:
+            job.solved_at = now
+        if self.grouped:
+            self._observing.append(self._obs_pool.submit(self._observe_group, jobs, ready))
+            return
         for job in jobs:
             self._observing.append(self._obs_pool.submit(run, job))
+
+    def _observe_group(self, jobs, ready=None):
+        """The final observation of jobs of the grouped path that finished together: stage q of
+        every job's observe_plan in one tn_batched_step call (FP64), on a stream and workspace of
+        the observer thread; returns the jobs."""
+        t_in = time.perf_counter()
+        cuda = str(self.device).startswith("cuda") and not L._host_test
+        tls = self._tls
+        if getattr(tls, "ws", None) is None:
+            tls.ws = L.Workspace(torch.device(self.device))
+            tls.stream = torch.cuda.Stream(device=self.device) if cuda else None
+        if cuda:
+            if ready is not None:
+                tls.stream.wait_event(ready)
+            ctx = torch.cuda.stream(tls.stream)
+        else:
+            import contextlib
+            ctx = contextlib.nullcontext()
+        with ctx:
+            plans = [j.observe_plan() for j in jobs]
+            nst = max(len(st) for st, _ in plans)
+            for q in range(nst):
+                tabs = [st[q] for st, _ in plans if q < len(st)]
+                self._step_call({"gemm1": self._cat(tabs, "gemm1"), "ops2": self._cat(tabs, "ops2"),
+                                 "gemm2": self._cat(tabs, "gemm2")}, L.PREC_FP64, ws=tls.ws)
+            host = [G.cpu().numpy() for _, G in plans]
+        dt = time.perf_counter() - t_in
+        for j, g in zip(jobs, host):
+            j.finish_observe(g)
+            j.observe_s = dt
+        return jobs
 
     def _collect_observed(self, block=False):
         if not self._observing:
@@ -504,7 +838,9 @@ class BatchEngine:
         still = []
         for f in self._observing:
             if f.done():
-                self._retire(f.result())   # an exception of the observation is raised here
+                r = f.result()   # an exception of the observation is raised here
+                for job in (r if isinstance(r, list) else [r]):
+                    self._retire(job)
             else:
                 still.append(f)
         self._observing = still
@@ -519,7 +855,7 @@ class BatchEngine:
             self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.nstreams)]
             from concurrent.futures import ThreadPoolExecutor
             self._pool = ThreadPoolExecutor(max_workers=self.workers)
-            self._obs_pool = ThreadPoolExecutor(max_workers=max(1, self.workers // 2))
+            self._obs_pool = ThreadPoolExecutor(max_workers=self.workers)
 
     def _prepare_all(self, jobs):
         """Every job's gauge move, environment update and block assembly. On a GPU the jobs are
@@ -555,85 +891,100 @@ class BatchEngine:
                 results[i] = r
         return results
 
-    def _grouped_step(self, jobs):
-        """One local update of every job of the grouped path: ~a dozen grouped launches for all
-        jobs (block assembly, gauge moves, R-absorb and environment update, effective Hamiltonian)
-        and one batched solve."""
+    def _ensure_ws(self):
+        if self._ws is None:
+            self._ws = L.Workspace(torch.device(self.device))
+
+    def _opts(self, jobs):
+        if jobs and len({(float(j.para["eigs_tol"]), float(j.para["tau"])) for j in jobs}) > 1:
+            raise ValueError("jobs of one batch share eigs_tol and tau")
+        tol, tau = (float(jobs[0].para["eigs_tol"]), float(jobs[0].para["tau"])) if jobs else (1e-12, 1e-4)
+        return L.LanczosOpts(tol, tau, 0.0, self.mixed_floor, self.krylov, self.max_restarts, self.check_every,
+                             self.prec, 0, 0)
+
+    def _step_call(self, phases, precision, solves=None, jobs=None, ws=None):
+        """One tn_batched_step call: the given phase tables (concatenated over jobs, in the order of
+        L.STEP_PHASES), then the batched solve of `solves` if given. Returns the solve results."""
         lib = L.load()
-        st = L.stream_handle()
+        d = L.BatchStepDesc()
+        for key in L.STEP_PHASES:
+            tab = phases.get(key)
+            if tab is not None and tab.shape[0]:
+                setattr(d, key, tab.ctypes.data)
+                setattr(d, "n_" + key, tab.shape[0])
+        d.precision = precision
+        opts = self._opts(jobs)
+        res = None
+        if solves is not None and solves.shape[0]:
+            d.solves = solves.ctypes.data
+            d.n_solves = solves.shape[0]
+            res = (L.LanczosResult * solves.shape[0])()
+        need = lib.tn_batched_step_workspace_bytes(ctypes.byref(d), ctypes.byref(opts))
+        wp, wb = (ws or self._ws).args(need)
+        st = lib.tn_batched_step(ctypes.byref(d), ctypes.byref(opts), wp, wb,
+                                 ctypes.cast(res, ctypes.c_void_p) if res is not None else None, L.stream_handle())
+        if st not in (L.TN_OK, L.TN_ERR_NOCONV):
+            L.check(st, "batched step")
+        return res
+
+    @staticmethod
+    def _cat(tabs, key):
+        """The records under `key` of every table, as one array (tables hold arrays or raw bytes)."""
+        parts = [r[key] for r in tabs]
+        if parts and isinstance(parts[0], bytes):
+            return np.frombuffer(b"".join(parts), dtype=_DTYPE_OF[key])
+        return np.concatenate(parts)
+
+    def _admit_device(self, jobs):
+        """Device side of admission for the jobs just started: step s of every job's centring
+        (ArenaJob.start) in one set of grouped launches, then the jobs' DeviceMPS views of their
+        arenas."""
+        self._ensure_ws()
+        nsteps = max(len(j._adm) for j in jobs)
+        for s_ in range(nsteps):
+            tabs = [j._adm[s_] for j in jobs if s_ < len(j._adm)]
+            # gauge move and FP64 absorb (and the identity sites), then the environment update
+            self._step_call({"ops1": self._cat(tabs, "ops_pre"), "qr": self._cat(tabs, "qr"),
+                             "gemm1": self._cat(tabs, "f64"), "ops2": self._cat(tabs, "ops_post")}, L.PREC_FP64)
+            self._step_call({"gemm1": self._cat(tabs, "gemm1"), "ops2": self._cat(tabs, "ops2"),
+                             "gemm2": self._cat(tabs, "gemm2")}, self.prec)
+        if str(self.device).startswith("cuda") and not L._host_test:
+            # the staging buffers are released below
+            torch.cuda.current_stream(self.device).synchronize()
+        for j in jobs:
+            j.finish_admission()
+
+    def _grouped_step(self, jobs):
+        """One local update of every job of the grouped path: one tn_batched_step call (block
+        assembly, gauge moves, R-absorb and environment update, effective Hamiltonian, batched
+        solve). With profile=True the phases are issued one call each, between CUDA events."""
         t_tab = time.perf_counter()
         rows = [j.rows() for j in jobs]
+        phases = {key: self._cat(rows, key) for key in L.STEP_PHASES}
+        solves = self._cat(rows, "solve")
         self.times["tables"] += time.perf_counter() - t_tab
-        marks = []
+        self._ensure_ws()
+        if not (self.profile and not L._host_test):
+            res = self._step_call(phases, self.prec, solves, jobs)
+        else:
+            marks = []
 
-        def mark(name):
-            if self.profile and not L._host_test:
+            def mark(name):
                 ev = torch.cuda.Event(enable_timing=True)
                 ev.record()
                 marks.append((name, ev))
-        mark("start")
-        if self._ws is None:
-            self._ws = L.Workspace(torch.device(self.device))
-        if self._ws2 is None:
-            self._ws2 = L.Workspace(torch.device(self.device))
-
-        def ops(key):
-            tab = np.concatenate([r[key] for r in rows])
-            if tab.shape[0]:
-                wp, wb = self._ws2.args(lib.tn_grouped_ops_workspace_bytes(tab.shape[0]))
-                L.check(lib.tn_grouped_ops(ctypes.c_void_p(tab.ctypes.data), tab.shape[0], wp, wb, st), "grouped ops")
-            return tab
-
-        def gemm(key):
-            tab = np.concatenate([r[key] for r in rows])
-            if tab.shape[0]:
-                L.grouped_gemm(tab, precision=self.prec, ws=self._ws2)
-            return tab
-
-        keep = [ops("ops1")]
-        mark("assemble_env_block")
-        small = [r["qr"] for r in rows if not r["qr_big"]]
-        if small:
-            tab = np.concatenate(small)
-            tp = ctypes.c_void_p(tab.ctypes.data)
-            wp, wb = self._ws2.args(lib.tn_batched_qr_mixed_workspace_bytes(tp, tab.shape[0]))
-            L.check(lib.tn_batched_qr_mixed(tp, tab.shape[0], wp, wb, st), "batched qr")
-            keep.append(tab)
-        for j, r in zip(jobs, rows):
-            if r["qr_big"]:
-                j.big_qr(self._ws2)
-        mark("qr")
-        keep += [gemm("gemm1"), ops("ops2")]
-        mark("absorb_and_transfer")
-        keep.append(gemm("gemm2"))
-        mark("env_close")
-        keep.append(ops("ops3"))
-        mark("heff_assembly")
-        solves = np.concatenate([r["solve"] for r in rows])
-        out = self._solve(jobs, solves, keep)
-        mark("lanczos")
-        if marks:
+            mark("start")
+            names = {"ops1": "assemble_env_block", "qr": "qr", "gemm1": "absorb_and_transfer", "ops2": "site_ops",
+                     "gemm2": "env_close", "ops3": "heff_assembly"}
+            for key in L.STEP_PHASES:
+                self._step_call({key: phases[key]}, self.prec)
+                mark(names[key])
+            res = self._step_call({}, self.prec, solves, jobs)
+            mark("lanczos")
             marks[-1][1].synchronize()
             for (_, a), (name, b) in zip(marks[:-1], marks[1:]):
                 self.phase_ms[name] = self.phase_ms.get(name, 0.0) + a.elapsed_time(b)
-        return out
-
-    def _solve(self, jobs, solves, keep):
-        lib = L.load()
-        opts = L.LanczosOpts(float(jobs[0].para["eigs_tol"]), float(jobs[0].para["tau"]), 0.0, self.mixed_floor,
-                             self.krylov, 50, self.check_every, self.prec, 0, 0)
-        if len({(float(j.para["eigs_tol"]), float(j.para["tau"])) for j in jobs}) > 1:
-            raise ValueError("jobs of one batch share eigs_tol and tau")
-        table = ctypes.c_void_p(solves.ctypes.data)
-        need = lib.tn_batched_lanczos_workspace_bytes(table, len(jobs), ctypes.byref(opts))
-        wp, wb = self._ws.args(need + 1024)
-        res = (L.LanczosResult * len(jobs))()
-        st = lib.tn_batched_lanczos(table, len(jobs), ctypes.byref(opts), wp, wb, ctypes.cast(res, ctypes.c_void_p),
-                                    L.stream_handle())
-        if st not in (L.TN_OK, L.TN_ERR_NOCONV):
-            L.check(st, "batched lanczos")
-        finished = [job for i, job in enumerate(jobs) if job.solved(res[i])]
-        del keep
+        finished = [job for i, job in enumerate(jobs) if job.solved(res[i], self.max_cycles)]
         self.steps += 1
         return finished
 
@@ -652,7 +1003,7 @@ class BatchEngine:
             solves[i].psi_out = psi.data_ptr()
         lib = L.load()
         opts = L.LanczosOpts(float(jobs[0].para["eigs_tol"]), float(jobs[0].para["tau"]), 0.0, self.mixed_floor,
-                             self.krylov, 50, self.check_every, self.prec, 0, 0)
+                             self.krylov, self.max_restarts, self.check_every, self.prec, 0, 0)
         if len({(float(j.para["eigs_tol"]), float(j.para["tau"])) for j in jobs}) > 1:
             raise ValueError("jobs of one batch share eigs_tol and tau")
         table = ctypes.cast(solves, ctypes.c_void_p)
@@ -705,13 +1056,23 @@ class BatchEngine:
         lat = np.array([j.finished - j.arrival for j in self.done]) if self.done else np.zeros(1)
         span = max((j.finished for j in self.done), default=0.0)
         solves = sum(j.solves for j in self.done)
+        obs = [getattr(j, "observe_s", 0.0) for j in self.done]
+        parts = {}
+        for j in self.done:
+            for key, v in (getattr(j, "admit_parts", None) or {}).items():
+                parts[key] = parts.get(key, 0.0) + v
+        lag = [j.finished - getattr(j, "solved_at", j.finished) for j in self.done]
         return {"jobs": len(self.done), "solves": solves, "wall_s": span,
+                "observe_s_p50": float(np.percentile(obs, 50)) if obs else 0.0,
+                "retire_lag_s_p50": float(np.percentile(lag, 50)) if lag else 0.0,
+                "retire_lag_s_max": float(max(lag)) if lag else 0.0,
                 "solves_per_s": solves / span if span > 0 else 0.0,
                 "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
                 "max_concurrent": self.max_concurrent, "steps": self.steps,
                 "step_ms_p50": float(np.percentile(self.step_ms, 50)) if self.step_ms else 0.0,
                 "matvecs_per_solve": (sum(j.matvecs for j in self.done) / solves) if solves else 0.0,
                 "host_s": {k: round(v, 3) for k, v in self.times.items()},
+                "admit_thread_s": {k: round(v, 3) for k, v in parts.items()},
                 "device_ms_per_step": {k: round(v / max(self.steps, 1), 3) for k, v in self.phase_ms.items()}}
 
 
@@ -747,11 +1108,14 @@ def main(argv=None):
     ap.add_argument("--ladder-rungs", default="8,48")
     ap.add_argument("--max-active", type=int, default=1024)
     ap.add_argument("--krylov", type=int, default=24)
+    ap.add_argument("--restarts", type=int, default=1, help="restart cycles of a batched local solve per step")
+    ap.add_argument("--max-cycles", type=int, default=51, help="restart cycles of a local solve in all")
     ap.add_argument("--baseline-jobs", type=int, default=12,
                     help="how many of the jobs also run one at a time on the plain FP64 GPU path (0: none)")
     ap.add_argument("--baseline-precision", default="fp64")
     ap.add_argument("--device", default="cuda")
     ap.add_argument("--profile", action="store_true", help="device time per phase of the grouped step (CUDA events)")
+    ap.add_argument("--warmup-jobs", type=int, default=4, help="jobs of the untimed warm-up run (0: none)")
     a = ap.parse_args(argv)
     lengths = tuple(int(x) for x in a.lengths.split(","))
     chis = tuple(int(x) for x in a.chis.split(","))
@@ -760,18 +1124,21 @@ def main(argv=None):
     L.load()
     dev = a.device
     # warm-up (first launches, tensor-core attributes, QR graphs)
-    warm = BatchEngine(dev, a.precision, max_krylov=a.krylov)
-    for j in batch_jobs(4, seed=a.seed + 10 ** 6, sweeps=1, precision=a.precision, device=dev, **shape):
-        warm.submit(j)
-    warm.run()
-    eng = BatchEngine(dev, a.precision, max_active=a.max_active, max_krylov=a.krylov, profile=a.profile)
+    if a.warmup_jobs > 0:
+        warm = BatchEngine(dev, a.precision, max_krylov=a.krylov)
+        for j in batch_jobs(a.warmup_jobs, seed=a.seed + 10 ** 6, sweeps=1, precision=a.precision, device=dev,
+                            **shape):
+            warm.submit(j)
+        warm.run()
+    eng = BatchEngine(dev, a.precision, max_active=a.max_active, max_krylov=a.krylov, profile=a.profile,
+                      max_restarts=a.restarts, max_cycles=a.max_cycles)
     for j in batch_jobs(a.jobs, seed=a.seed, sweeps=a.sweeps, precision=a.precision, device=dev, rate=a.rate,
                         **shape):
         eng.submit(j)
     eng.run()
     out = eng.summary()
     out.update({"precision": a.precision, "sweeps": a.sweeps, "rate_per_s": a.rate, "lengths": list(lengths),
-                "chis": list(chis), "ladder_fraction": a.ladders, "krylov": a.krylov,
+                "chis": list(chis), "ladder_fraction": a.ladders, "krylov": a.krylov, "restarts": a.restarts, "max_cycles": a.max_cycles,
                 "unconverged_solves": int(sum(j.result["unconverged"] for j in eng.done))})
     if a.baseline_jobs > 0:
         # the first jobs of the same stream, one at a time on the single-job path

@@ -20,6 +20,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "common.cuh"
@@ -363,8 +364,15 @@ int qrb_plan(const tn_qr_item* in, int count, char* base, QrbPlan* P) {
   P->tab = off;
   off += al(sizeof(QrbItem) * (size_t)count) + al(sizeof(int) * (size_t)(count + 1));
   P->gram_prefix.assign(1, 0);
-  for (int i = 0; i < count; ++i) {
-    const tn_qr_item& q = in[i];
+  // largest factorisations first (m n^2 work each, one CTA per matrix): the long ones start in the
+  // first wave and the short ones fill the SMs behind them
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return (int64_t)in[x].m * in[x].n * in[x].n > (int64_t)in[y].m * in[y].n * in[y].n;
+  });
+  for (int oi = 0; oi < count; ++oi) {
+    const tn_qr_item& q = in[order[oi]];
     if (q.n < 1 || q.m < q.n || (int64_t)q.m * q.n > QR_MAX_ELEMS || !q.a || !q.r)
       return tn_fail(TN_ERR_ARG, "batched qr: need 1 <= n <= m and m n <= 32768");
     QrbItem it{};

@@ -100,40 +100,137 @@ __global__ void bl_init_kernel(BjJob* jobs, int njobs, const int* prefix) {
   reduce_partial(J, c, kMaxM + 1, acc, J.nrm2);
 }
 
-// h[i] = V[i] . w for i < k: grid (chunks, k)
-__global__ void bl_multidot_kernel(BjJob* jobs, int njobs, const int* prefix, int which) {
+constexpr int EPT = CH / NT;  // vector elements per thread
+
+// h[i] = V[i] . x for i < k over the block's chunk (x: this thread's EPT elements, at e0 + tid +
+// q NT), reduced over the block, then, by the last block of the job, over the chunks in chunk order
+// (deterministic). One block computes all k dots of its chunk: the w chunk is read once and the k
+// basis chunks stream through with EPT independent loads per thread in flight.
+__device__ void chunk_dots(BjJob& J, int c, int k, const double (&x)[EPT], int64_t e0, double* out) {
+  __shared__ double red[NT / 32][kMaxM + 1];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t nrem = J.n - e0;
+#pragma unroll 2
+  for (int i = 0; i < k; ++i) {
+    const double* v = J.V + (int64_t)i * J.n + e0;
+    double acc = 0.0;
+#pragma unroll
+    for (int q = 0; q < EPT; ++q) {
+      const int idx = threadIdx.x + q * NT;
+      if (idx < nrem) acc = fma(v[idx], x[q], acc);
+    }
+    acc = tn_warp_sum(acc);
+    if (lane == 0) red[wid][i] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x < k) {
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) t += red[w][threadIdx.x];
+    J.part[(int64_t)threadIdx.x * J.nchunks + c] = t;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(J.tickets + kMaxM, 1u) == (unsigned)J.nchunks - 1);
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    // warp w sums dots w, w + 8, ...: its lanes stride over the chunks, then a warp sum
+    for (int i = wid; i < k; i += NT / 32) {
+      const volatile double* pp = J.part + (int64_t)i * J.nchunks;
+      double t = 0.0;
+      for (int q = lane; q < J.nchunks; q += 32) t += pp[q];
+      t = tn_warp_sum(t);
+      if (lane == 0) out[i] = t;
+    }
+    if (threadIdx.x == 0) J.tickets[kMaxM] = 0u;
+  }
+}
+
+__device__ __forceinline__ void load_chunk(const BjJob& J, int64_t e0, double (&x)[EPT]) {
+  const int64_t nrem = J.n - e0;
+#pragma unroll
+  for (int q = 0; q < EPT; ++q) {
+    const int idx = threadIdx.x + q * NT;
+    x[q] = idx < nrem ? J.w[e0 + idx] : 0.0;
+  }
+}
+
+// x -= sum_{i<k} h[i] V[i] on this thread's elements (EPT independent chains)
+__device__ __forceinline__ void chunk_axpy(const BjJob& J, int64_t e0, int k, const double* hs, double (&x)[EPT]) {
+  const int64_t nrem = J.n - e0;
+#pragma unroll 4
+  for (int i = 0; i < k; ++i) {
+    const double* v = J.V + (int64_t)i * J.n + e0;
+    const double h = hs[i];
+#pragma unroll
+    for (int q = 0; q < EPT; ++q) {
+      const int idx = threadIdx.x + q * NT;
+      if (idx < nrem) x[q] = fma(-h, v[idx], x[q]);
+    }
+  }
+}
+
+__device__ __forceinline__ void store_chunk(const BjJob& J, int64_t e0, const double (&x)[EPT]) {
+  const int64_t nrem = J.n - e0;
+#pragma unroll
+  for (int q = 0; q < EPT; ++q) {
+    const int idx = threadIdx.x + q * NT;
+    if (idx < nrem) J.w[e0 + idx] = x[q];
+  }
+}
+
+// pass 1 of the Gram-Schmidt: h1 = V[0..k) . w
+__global__ void __launch_bounds__(NT) bl_dots_kernel(BjJob* jobs, int njobs, const int* prefix, int k) {
   const int t = blockIdx.x;
   const int j = find_job(prefix, njobs, t);
   BjJob J = jobs[j];
   if (!J.active) return;
-  const int c = t - prefix[j], i = blockIdx.y;
+  const int c = t - prefix[j];
   const int64_t e0 = (int64_t)c * CH;
-  const double* v = J.V + (int64_t)i * J.n;
-  double acc = 0.0;
-  for (int64_t e = e0 + threadIdx.x; e < min(J.n, e0 + CH); e += NT) acc = fma(v[e], J.w[e], acc);
-  reduce_partial(J, c, i, acc, (which ? J.h2 : J.h1) + i);
+  double x[EPT];
+  load_chunk(J, e0, x);
+  chunk_dots(J, c, k, x, e0, J.h1);
 }
 
-// w -= sum_{i<k} h[i] V[i]; with_norm: ||w||^2 into nrm2
-__global__ void bl_multiaxpy_kernel(BjJob* jobs, int njobs, const int* prefix, int k, int which, int with_norm) {
+// w -= sum h1[i] V[i] (pass 1), then h2 = V[0..k) . w (pass 2's projections) in the same block
+__global__ void __launch_bounds__(NT) bl_axpy_dots_kernel(BjJob* jobs, int njobs, const int* prefix, int k) {
   const int t = blockIdx.x;
   const int j = find_job(prefix, njobs, t);
   BjJob J = jobs[j];
   if (!J.active) return;
   const int c = t - prefix[j];
   __shared__ double hs[kMaxM + 1];
-  const double* h = which ? J.h2 : J.h1;
-  for (int i = threadIdx.x; i < k; i += NT) hs[i] = h[i];
+  for (int i = threadIdx.x; i < k; i += NT) hs[i] = J.h1[i];
   __syncthreads();
   const int64_t e0 = (int64_t)c * CH;
+  double x[EPT];
+  load_chunk(J, e0, x);
+  chunk_axpy(J, e0, k, hs, x);
+  store_chunk(J, e0, x);
+  chunk_dots(J, c, k, x, e0, J.h2);
+}
+
+// w -= sum h2[i] V[i] (pass 2) and ||w||^2 into nrm2
+__global__ void __launch_bounds__(NT) bl_axpy_norm_kernel(BjJob* jobs, int njobs, const int* prefix, int k) {
+  const int t = blockIdx.x;
+  const int j = find_job(prefix, njobs, t);
+  BjJob J = jobs[j];
+  if (!J.active) return;
+  const int c = t - prefix[j];
+  __shared__ double hs[kMaxM + 1];
+  for (int i = threadIdx.x; i < k; i += NT) hs[i] = J.h2[i];
+  __syncthreads();
+  const int64_t e0 = (int64_t)c * CH;
+  double x[EPT];
+  load_chunk(J, e0, x);
+  chunk_axpy(J, e0, k, hs, x);
+  store_chunk(J, e0, x);
   double acc = 0.0;
-  for (int64_t e = e0 + threadIdx.x; e < min(J.n, e0 + CH); e += NT) {
-    double x = J.w[e];
-    for (int i = 0; i < k; ++i) x = fma(-hs[i], J.V[(int64_t)i * J.n + e], x);
-    J.w[e] = x;
-    acc = fma(x, x, acc);
-  }
-  if (with_norm) reduce_partial(J, c, kMaxM + 1, acc, J.nrm2);
+#pragma unroll
+  for (int q = 0; q < EPT; ++q) acc = fma(x[q], x[q], acc);
+  reduce_partial(J, c, kMaxM + 1, acc, J.nrm2);
 }
 
 // V[k] = w / ||w||, x = V[k], w = 0; alpha[k-1] = h1 + h2, beta[k-1] = ||w|| (k >= 1; k == 0 is
@@ -189,38 +286,65 @@ __device__ int sturm_count(const double* a, const double* b, int m, double x) {
   return cnt;
 }
 
-// (T - lam I) z = z0 by Gaussian elimination with partial pivoting (one thread)
-__device__ void tri_solve(const double* a, const double* b, int m, double lam, double* z, double* d0, double* d1,
-                          double* d2, double* sub) {
+// LU factorisation of the tridiagonal T - lam I with partial pivoting (one thread): U has the
+// diagonal d0 (stored as reciprocals rp) and two superdiagonals d1, d2; row i's multiplier is f[i]
+// and sw[i] says whether rows i and i+1 were swapped. Factored once per eigenvector, solved twice.
+// lam is an eigenvalue to working accuracy, so a pivot may vanish: it is replaced by 1e-18 of the
+// matrix scale tn (inverse iteration then magnifies the eigenvector by ~1e18 / tn, and the
+// normalisation stays in range; a pivot of 1e-300 would overflow the norm).
+__device__ void tri_factor(const double* a, const double* b, int m, double lam, double tn, double* rp, double* d1,
+                           double* d2, double* f, unsigned char* sw) {
+  const double tiny = 1e-18 * fmax(tn, 1e-280);
+  double p0 = a[0] - lam, p1 = (m > 1) ? b[0] : 0.0, p2 = 0.0;   // working row i
   for (int i = 0; i < m; ++i) {
-    d0[i] = a[i] - lam;
-    d1[i] = (i + 1 < m) ? b[i] : 0.0;
-    d2[i] = 0.0;
-    sub[i] = (i > 0) ? b[i - 1] : 0.0;
-  }
-  for (int i = 0; i < m - 1; ++i) {
-    if (fabs(sub[i + 1]) > fabs(d0[i])) {
-      double t;
-      t = d0[i]; d0[i] = sub[i + 1]; sub[i + 1] = t;
-      t = d1[i]; d1[i] = d0[i + 1]; d0[i + 1] = t;
-      t = d2[i]; d2[i] = d1[i + 1]; d1[i + 1] = t;
-      t = z[i]; z[i] = z[i + 1]; z[i + 1] = t;
+    if (i + 1 < m) {
+      // next row (below the diagonal b[i], then a[i+1] - lam, then b[i+1])
+      double n0 = b[i], n1 = a[i + 1] - lam, n2 = (i + 2 < m) ? b[i + 1] : 0.0;
+      const bool swp = fabs(n0) > fabs(p0);
+      if (swp) {
+        double t;
+        t = p0; p0 = n0; n0 = t;
+        t = p1; p1 = n1; n1 = t;
+        t = p2; p2 = n2; n2 = t;
+      }
+      double piv = p0;
+      if (fabs(piv) < tiny) piv = (piv < 0.0) ? -tiny : tiny;
+      const double r = 1.0 / piv;
+      const double fi = n0 * r;
+      rp[i] = r;
+      d1[i] = p1;
+      d2[i] = p2;
+      f[i] = fi;
+      sw[i] = swp ? 1 : 0;
+      p0 = n1 - fi * p1;
+      p1 = n2 - fi * p2;
+      p2 = 0.0;
+    } else {
+      double piv = p0;
+      if (fabs(piv) < tiny) piv = (piv < 0.0) ? -tiny : tiny;
+      rp[i] = 1.0 / piv;
+      d1[i] = 0.0;
+      d2[i] = 0.0;
     }
-    double piv = d0[i];
-    if (fabs(piv) < 1e-300) piv = 1e-300;
-    const double f = sub[i + 1] / piv;
-    d0[i + 1] -= f * d1[i];
-    d1[i + 1] -= f * d2[i];
-    z[i + 1] -= f * z[i];
-    sub[i + 1] = 0.0;
+  }
+}
+
+// z <- (T - lam I)^{-1} z with the factorisation of tri_factor (multiplications only)
+__device__ void tri_apply(int m, const double* rp, const double* d1, const double* d2, const double* f,
+                          const unsigned char* sw, double* z) {
+  for (int i = 0; i + 1 < m; ++i) {
+    if (sw[i]) {
+      const double t = z[i];
+      z[i] = z[i + 1];
+      z[i + 1] = t;
+    }
+    z[i + 1] = fma(-f[i], z[i], z[i + 1]);
   }
   for (int i = m - 1; i >= 0; --i) {
     double v = z[i];
-    if (i + 1 < m) v -= d1[i] * z[i + 1];
-    if (i + 2 < m) v -= d2[i] * z[i + 2];
-    double piv = d0[i];
-    if (fabs(piv) < 1e-300) piv = 1e-300;
-    z[i] = v / piv;
+    if (i + 1 < m) v = fma(-d1[i], z[i + 1], v);
+    if (i + 2 < m) v = fma(-d2[i], z[i + 2], v);
+    z[i] = v * rp[i];
   }
 }
 
@@ -235,7 +359,8 @@ __global__ void bl_tridiag_kernel(BjJob* jobs, int njobs, int k, TriOpts o) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int wl = threadIdx.x >> 5;
   __shared__ double sa[4][kMaxM], sb[4][kMaxM], sz[4][kMaxM];
-  __shared__ double w0[4][kMaxM], w1[4][kMaxM], w2[4][kMaxM], w3[4][kMaxM];
+  __shared__ double w0[4][kMaxM], w1[4][kMaxM], w2[4][kMaxM], wf[4][kMaxM];
+  __shared__ unsigned char wsw[4][kMaxM];
   __shared__ double lohi[4][2];
   if (warp >= njobs) return;
   BjJob& J = jobs[warp];
@@ -286,12 +411,14 @@ __global__ void bl_tridiag_kernel(BjJob* jobs, int njobs, int k, TriOpts o) {
     hi = nhi;
   }
   const double lam = 0.5 * (lo + hi);
-  // eigenvector by inverse iteration (three solves from a generic start), one lane
-  double* z = sz[wl];
   if (lane == 0) {
+    // eigenvector of the leading mm x mm block by inverse iteration (one factorisation, two
+    // solves from a generic start); its last component gives the residual |beta_mm s_mm|
+    double* z = sz[wl];
+    tri_factor(a, b, mm, lam, tn, w0[wl], w1[wl], w2[wl], wf[wl], wsw[wl]);
     for (int i = 0; i < mm; ++i) z[i] = 1.0 + 1e-3 * i;
-    for (int rep = 0; rep < 3; ++rep) {
-      tri_solve(a, b, mm, lam, z, w0[wl], w1[wl], w2[wl], w3[wl]);
+    for (int rep = 0; rep < 2; ++rep) {
+      tri_apply(mm, w0[wl], w1[wl], w2[wl], wf[wl], wsw[wl], z);
       double nrm = 0.0;
       for (int i = 0; i < mm; ++i) nrm = fma(z[i], z[i], nrm);
       nrm = sqrt(nrm);
@@ -299,7 +426,7 @@ __global__ void bl_tridiag_kernel(BjJob* jobs, int njobs, int k, TriOpts o) {
       const double inv = 1.0 / nrm;
       for (int i = 0; i < mm; ++i) z[i] *= inv;
     }
-    double resid = brk ? 0.0 : fabs(b[mm - 1] * z[mm - 1]);
+    const double resid = brk ? 0.0 : fabs(b[mm - 1] * z[mm - 1]);
     double tol;
     if (o.tau > 0.0) tol = o.eigs_tol / o.tau * fabs(1.0 - o.tau * lam);
     else tol = o.eigs_tol * fmax(1.0, fabs(lam));
@@ -310,8 +437,9 @@ __global__ void bl_tridiag_kernel(BjJob* jobs, int njobs, int k, TriOpts o) {
     J.resid = resid;
     J.tol = tol;
     J.brk = brk ? 1 : 0;
-    for (int i = 0; i < k; ++i) J.s[i] = (i < mm) ? z[i] : 0.0;
     J.combine = conv ? 1 : ((k >= o.m) ? 2 : 0);
+    if (J.combine)
+      for (int i = 0; i < k; ++i) J.s[i] = (i < mm) ? z[i] : 0.0;
   }
 }
 
@@ -657,13 +785,12 @@ extern "C" int tn_batched_lanczos(const tn_batch_solve* in, int count, const tn_
       if (!L.f64b.empty() && (st = gg_launch_f64(d_f2, (int)L.f64b.size(), d_pf2, L.pf_f64b.back(), s))) return st;
     }
     const int nc = k + 1;
-    bl_multidot_kernel<<<dim3(chunks, nc), NT, 0, s>>>(d_jobs, njobs, d_cpf, 0);
+    // classical Gram-Schmidt twice against V[0..nc): dots, update + second dots, update + norm
+    bl_dots_kernel<<<chunks, NT, 0, s>>>(d_jobs, njobs, d_cpf, nc);
     TN_CHECK_LAUNCH();
-    bl_multiaxpy_kernel<<<chunks, NT, 0, s>>>(d_jobs, njobs, d_cpf, nc, 0, 0);
+    bl_axpy_dots_kernel<<<chunks, NT, 0, s>>>(d_jobs, njobs, d_cpf, nc);
     TN_CHECK_LAUNCH();
-    bl_multidot_kernel<<<dim3(chunks, nc), NT, 0, s>>>(d_jobs, njobs, d_cpf, 1);
-    TN_CHECK_LAUNCH();
-    bl_multiaxpy_kernel<<<chunks, NT, 0, s>>>(d_jobs, njobs, d_cpf, nc, 1, 1);
+    bl_axpy_norm_kernel<<<chunks, NT, 0, s>>>(d_jobs, njobs, d_cpf, nc);
     TN_CHECK_LAUNCH();
     bl_finish_kernel<<<chunks, NT, 0, s>>>(d_jobs, njobs, d_cpf, nc);
     TN_CHECK_LAUNCH();

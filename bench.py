@@ -19,8 +19,10 @@ sweeps at chi=512, mixed against FP64; config4_batched = 512 uneven XXZ chains a
 (tnalg_gb300.batched) against the same jobs one at a time on the FP64 path; config5_serving = a
 Poisson stream of chain and ladder requests at several rates. `summary` (the last key) gathers
 the figures the metric is quoted on.
-`--impl reference` times the same local update of the reference's algorithm (oracle/) on a seeded
-random state whose site is converged first, on the host cores.
+`--impl reference` times the reference's algorithm (oracle/) on the host cores, on a seeded random
+state whose interior site is converged first: W untimed and K timed steps, one step = one local
+update of the sweep (eigsh + centre move), so `ms_per_step` is the measured time of one step and
+`value` = 1 / (2(N-1) x ms_per_step) sweeps/s.
 """
 import argparse
 import contextlib
@@ -283,16 +285,20 @@ def cpu_info():
     return {"nproc": os.cpu_count(), "threads": threads, "cpu": model, "blas": blas.strip()}
 
 
-def cpu_sample(length, chi, eigs_tol, nsolves, mps=None, seed=0):
+def cpu_sample(length, chi, eigs_tol, steps, warmup=0, mps=None, seed=0):
     """The reference's local update timed on the host cores (oracle/: numpy + scipy ARPACK, the
-    reference's algorithm and bookkeeping) at an interior site of the N-site chain at `chi`:
-      (b) eigsh at a converged site: the site is solved once untimed, then re-solved `nsolves`
-          times from its own eigenvector (ARPACK still builds its ncv = 20 vectors first);
-      (a) one move of the orthogonality centre with the rebuild of the site's operator buckets
-          (the QR move and the transfers of every carried term the move invalidated).
-    A converged sweep costs 2(N-1) x (a + b): both parts measured here, nothing assumed. `mps`: the
-    host tensors of a converged state (the benchmark's own, after its timed sweeps); without it a
-    seeded random MPS, whose site the untimed first solve converges."""
+    reference's algorithm and bookkeeping) on the two interior sites mid, mid + 1 of the N-site
+    chain at `chi`. One step is one local update of a sweep, as update_tensor_eigs and the gauge
+    move that follows it run in DMRG_anyH.py:43-64:
+      eigsh at the current centre site (started from its own tensor; ARPACK builds at least its
+      ncv = 20 vectors), then the move of the orthogonality centre to the other site with the
+      rebuild of that site's operator buckets (the QR move and the transfers of every carried term
+      the move invalidated).
+    The centre goes back and forth across the bond (mid, mid + 1), so every step is a genuine
+    interior local update; `warmup` steps run untimed, then `steps` are timed one by one. A sweep
+    is 2(N-1) local updates, so sweeps/s = 1 / (2(N-1) x mean step time): measured, nothing
+    assumed. `mps`: the host tensors of a converged state (the benchmark's own, after its timed
+    sweeps); without it a seeded random MPS, whose site an untimed first solve converges."""
     from oracle import dmrg_oracle as O
     para = chain_para(length, chi, eigs_tol, "fp64", "cpu")
     if mps is None:
@@ -307,29 +313,39 @@ def cpu_sample(length, chi, eigs_tol, nsolves, mps=None, seed=0):
     A.site_buckets(mid, one, two)
     A.update_tensor_eigs(mid, one, two, 1e-4, eigs_tol)
     t_setup = time.time() - t0
-    times, mvs = [], []
-    for _ in range(max(1, nsolves)):
+    site = [mid]
+
+    def local_update():
+        p = site[0]
         mv0 = A.n_matvec
         t = time.time()
-        A.update_tensor_eigs(mid, one, two, 1e-4, eigs_tol)
-        times.append(time.time() - t)
-        mvs.append(A.n_matvec - mv0)
-    t = time.time()
-    A.correct_orthogonal_center(mid + 1)
-    A.site_buckets(mid + 1, one, two)
-    t_move = time.time() - t
-    per_solve = float(np.mean(times)) + t_move
-    sweeps_per_s = 1.0 / (per_solve * 2 * (length - 1))
+        A.update_tensor_eigs(p, one, two, 1e-4, eigs_tol)
+        t_solve = time.time() - t
+        q = mid + 1 if p == mid else mid
+        t = time.time()
+        A.correct_orthogonal_center(q)
+        A.site_buckets(q, one, two)
+        site[0] = q
+        return t_solve, time.time() - t, A.n_matvec - mv0
+
+    for _ in range(max(0, warmup)):
+        local_update()
+    rows = [local_update() for _ in range(max(1, steps))]
+    solve_s = float(np.mean([r[0] for r in rows]))
+    move_s = float(np.mean([r[1] for r in rows]))
+    per_step = solve_s + move_s
+    sweeps_per_s = 1.0 / (per_step * 2 * (length - 1))
     info = cpu_info()
     return {"value": sweeps_per_s, "unit": UNIT, "cores": info["threads"], "kind": "port",
-            "cpu": info, "solve_s": float(np.mean(times)), "move_s": t_move, "matvecs_per_solve": float(np.mean(mvs)),
+            "cpu": info, "steps": len(rows), "warmup": max(0, warmup), "ms_per_step": 1000.0 * per_step,
+            "solve_s": solve_s, "move_s": move_s, "matvecs_per_solve": float(np.mean([r[2] for r in rows])),
             "sample": "oracle (numpy/scipy ARPACK restatement of the reference) on %d host threads, N=%d chain at "
-                      "chi=%d, %s state: %d eigsh solve(s) at converged interior site %d (%.2f s each, %.0f matvecs) "
-                      "+ one centre move with its operator rebuild (%.2f s), measured; sweeps/s = 1 / (2(N-1) x "
-                      "%.2f s); %.0f s untimed setup" % (
+                      "chi=%d, %s state: %d timed local updates (after %d untimed) back and forth across interior "
+                      "bond (%d, %d): eigsh solve %.2f s (%.0f matvecs) + centre move with its operator rebuild "
+                      "%.2f s per update, measured; sweeps/s = 1 / (2(N-1) x %.2f s); %.0f s untimed setup" % (
                           info["threads"], length, chi, "converged (the GPU run's)" if mps is not None else
-                          "seeded random", len(times), mid, float(np.mean(times)), float(np.mean(mvs)), t_move,
-                          per_solve, t_setup)}
+                          "seeded random", len(rows), max(0, warmup), mid, mid + 1, solve_s,
+                          float(np.mean([r[2] for r in rows])), move_s, per_step, t_setup)}
 
 
 def config1_leg(device):
@@ -453,11 +469,15 @@ def summarise(line):
 def run_reference(args, rank):
     if rank != 0:
         return None
-    s = cpu_sample(args.length, args.chi, args.eigs_tol, max(1, args.cpu_solves))
+    s = cpu_sample(args.length, args.chi, args.eigs_tol, max(1, args.steps), warmup=args.warmup)
+    # one step = one measured local update of the sweep (a bounded sample of it): ms_per_step is the
+    # time of that step, value the sweeps/s it gives (a sweep is 2(N-1) local updates)
     line = {"metric": METRIC, "value": s["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / s["value"], "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": s["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
+            "step": "one local update of the sweep (eigsh at a converged interior site + the centre move with its "
+                    "operator rebuild); sweeps/s = 1 / (2(N-1) x ms_per_step)",
             "config": {"workload": "N=%d spin-1/2 Heisenberg open chain, J=1, chi=%d, one-site DMRG sweep"
                                    % (args.length, args.chi), "global_batch": 1, "seq_len": args.length,
                        "parallelism": "replicas"},

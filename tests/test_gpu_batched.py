@@ -348,3 +348,60 @@ def test_grouped_engine_matches_the_per_job_engine(cuda_lib):
     for k in res[False]:
         assert abs(res[True][k]["e_per_site"] - res[False][k]["e_per_site"]) < 1e-8, k
         assert res[True][k]["solves"] == res[False][k]["solves"]
+
+
+def test_batched_step_large_gauge_moves_side_by_side(cuda_lib):
+    """Gauge moves above tn_batched_qr_mixed's shared-memory limit (chi = 256 and 512 sites, left and
+    right moves, i.e. row-major and column-major layouts) in one tn_batched_step call run on side
+    streams next to each other, small ones in the same call on the batched kernel: every Q and R
+    equals tn_qr_mixed's on the same matrix, called alone."""
+    if not L.tf32x3_available():
+        pytest.skip("needs an sm_103 device")
+    import ctypes
+    lib = L.load()
+    shapes = [(1024, 512, False), (512, 256, True), (1024, 512, True), (512, 256, False), (768, 384, False),
+              (1024, 512, False), (512, 256, False), (1000, 500, True), (512, 512, False), (64, 32, False)]
+    items, keep, ref = [], [], []
+    for i, (m, n, colmajor) in enumerate(shapes):
+        A = _rand(m, n, seed=900 + i) * (10.0 ** (i % 4 - 2))
+        if i == 2:
+            A[:, n // 4:] = A[:, :n // 4] @ _rand(n // 4, n - n // 4, seed=13)   # rank n/4 (a grown bond)
+        store = A.T.contiguous() if colmajor else A.clone()   # column-major A: element (r, c) at store[c, r]
+        sA = (1, m) if colmajor else (n, 1)
+        R = torch.zeros(n, n, dtype=torch.float64, device="cuda")
+        keep += [store, R]
+        # the same move alone through tn_qr_mixed
+        Qr = torch.empty_like(store)
+        Rr = torch.zeros(n, n, dtype=torch.float64, device="cuda")
+        ws = L.Workspace(torch.device("cuda"))
+        wp, wb = ws.args(lib.tn_qr_mixed_workspace_bytes(m, n))
+        L.check(lib.tn_qr_mixed(m, n, L.ptr(store), sA[0], sA[1], L.ptr(Qr), sA[0], sA[1], L.ptr(Rr), n, 1, wp, wb,
+                                L.stream_handle()))
+        ref.append((Qr, Rr, ws))
+        r = np.zeros(1, dtype=L.QR_ITEM_DTYPE)
+        r["m"], r["n"], r["a"], r["sAm"], r["sAn"] = m, n, store.data_ptr(), sA[0], sA[1]
+        r["r"], r["sRm"], r["sRn"] = R.data_ptr(), n, 1
+        items.append(r)
+    torch.cuda.synchronize()
+    tab = np.concatenate(items)
+    d = L.BatchStepDesc()
+    d.qr = tab.ctypes.data
+    d.n_qr = len(items)
+    d.precision = L.PREC_TF32X3
+    opts = L.LanczosOpts(1e-12, 1e-4, 0.0, 2e-6, 24, 1, 3, L.PREC_TF32X3, 0, 0)
+    need = lib.tn_batched_step_workspace_bytes(ctypes.byref(d), ctypes.byref(opts))
+    wsb = L.Workspace(torch.device("cuda"))
+    wp, wb = wsb.args(need)
+    L.check(lib.tn_batched_step(ctypes.byref(d), ctypes.byref(opts), wp, wb, None, L.stream_handle()))
+    L.check(lib.tn_check_device_status(L.stream_handle()))
+    torch.cuda.synchronize()
+    for i, (m, n, colmajor) in enumerate(shapes):
+        store, R = keep[2 * i], keep[2 * i + 1]
+        Qr, Rr, _ = ref[i]
+        if m * n > 32768:
+            # the same kernels on the same input: the same results
+            assert torch.max(torch.abs(store - Qr)).item() <= 1e-14, i
+            assert torch.max(torch.abs(R - Rr)).item() <= 1e-14 * max(1.0, torch.max(torch.abs(Rr)).item()), i
+        Q = store.T if colmajor else store
+        eye = torch.eye(n, dtype=torch.float64, device="cuda")
+        assert torch.max(torch.abs(Q.T @ Q - eye)).item() < 1e-11, i

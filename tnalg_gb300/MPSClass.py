@@ -249,13 +249,15 @@ class MpsOpenBoundaryClass(MpsBasic):
         c = self.center if self.center >= 0 else 0
         if method == "expand":
             self._model(*model)
-            if self._dev.expand_bonds(chi_new, seed=seed):
-                self.lm = [np.zeros(0) for _ in range(self.length - 1)]
-                self._dev.fast_gauge = True
-                try:
+            # the expansion's gauge moves, like the re-centring after it, may use the
+            # mixed-precision QR: the grown state is re-optimised by the next sweep
+            self._dev.fast_gauge = True
+            try:
+                if self._dev.expand_bonds(chi_new, seed=seed):
+                    self.lm = [np.zeros(0) for _ in range(self.length - 1)]
                     self.correct_orthogonal_center(c)
-                finally:
-                    self._dev.fast_gauge = False
+            finally:
+                self._dev.fast_gauge = False
             return
         if method != "noise":
             raise ValueError("method must be 'expand' or 'noise'")

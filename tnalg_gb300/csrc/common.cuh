@@ -19,6 +19,8 @@ extern thread_local unsigned long long g_tn_thread_launches;
 // TN_DEVERR_QR_WAIT a cluster-QR panel wait that timed out.
 constexpr int TN_DEVERR_RANGE = 16;
 constexpr int TN_DEVERR_QR_WAIT = 32;
+// TN_DEVERR_SVD_WAIT: a grid barrier of the single-launch Jacobi SVD that timed out.
+constexpr int TN_DEVERR_SVD_WAIT = 64;
 
 // FP32 Householder QR (inputs scaled by a power of two to max |a| ~ 1): a sub-column whose squared
 // norm is at most kHhTiny gets no reflector and is taken as zero. Below ~1e-19 the squares are

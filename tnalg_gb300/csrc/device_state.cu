@@ -105,6 +105,7 @@ int tn_error_status(int h, cudaStream_t s) {
   if (h == TN_DEVERR_RANGE)
     return tn_fail(TN_ERR_NUMERIC, "tf32x3 gemm: an operand lies outside the FP32 range (|x| >= 3.4e38)");
   if (h == TN_DEVERR_QR_WAIT) return tn_fail(TN_ERR_TIMEOUT, "qr32 cluster: a bounded panel wait gave up");
+  if (h == TN_DEVERR_SVD_WAIT) return tn_fail(TN_ERR_TIMEOUT, "svd: a bounded grid barrier gave up");
   return tn_fail(TN_ERR_TIMEOUT, "tf32x3 gemm: a bounded pipeline wait gave up");
 }
 

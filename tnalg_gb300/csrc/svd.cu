@@ -54,10 +54,10 @@ __device__ __forceinline__ int64_t rr_player(int64_t slot, int64_t r, int64_t kp
   return 1 + (slot - 1 + r) % (kp - 1);
 }
 
-// J: the accumulated rotations (kp x kp, row-major), rotated with X's rows when not null
-__global__ void jacobi_round(int64_t kp, int64_t n, int64_t r, double* X, double tol, const double* fro2,
-                             double null_rel2, int* rotated, double* J = nullptr) {
-  const int64_t i = blockIdx.x;  // pair index 0..kp/2-1
+// Pair i of round r, by the whole block: J, the accumulated rotations (kp x kp, row-major), is
+// rotated with X's rows when not null.
+__device__ __forceinline__ void jacobi_pair(int64_t kp, int64_t n, int64_t i, int64_t r, double* X, double tol,
+                                            const double* fro2, double null_rel2, int* rotated, double* J) {
   const int64_t p = rr_player(i, r, kp), q = rr_player(kp - 1 - i, r, kp);
   double* xp = X + p * n;
   double* xq = X + q * n;
@@ -91,6 +91,8 @@ __global__ void jacobi_round(int64_t kp, int64_t n, int64_t r, double* X, double
   }
   __syncthreads();
   const double c = cs[0], s = cs[1];
+  // every thread has read cs: the next pair of this block may overwrite it
+  __syncthreads();
   if (s == 0.0) return;
   for (int64_t t = threadIdx.x; t < n; t += blockDim.x) {
     const double u = xp[t], v = xq[t];
@@ -105,6 +107,77 @@ __global__ void jacobi_round(int64_t kp, int64_t n, int64_t r, double* X, double
       jp[t] = c * u - s * v;
       jq[t] = s * u + c * v;
     }
+  }
+}
+
+__global__ void jacobi_round(int64_t kp, int64_t n, int64_t r, double* X, double tol, const double* fro2,
+                             double null_rel2, int* rotated, double* J = nullptr) {
+  jacobi_pair(kp, n, blockIdx.x, r, X, tol, fro2, null_rel2, rotated, J);
+}
+
+constexpr long long kBarrierCycles = 4000000000LL;  // ~2 s at 2 GHz
+
+// Grid-wide barrier of a cooperative launch (every block is resident): an arrival count and a
+// generation word in global memory (bar[0], bar[1]). The last block to arrive resets the count and
+// advances the generation; the others wait for it, for at most kBarrierCycles. Returns false in
+// every thread of a block whose wait gave up.
+__device__ bool grid_barrier(unsigned int* bar, unsigned int nblocks) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = bar + 1;
+    const unsigned int g = *gen;
+    __threadfence();
+    int good = 1;
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*gen == g) {
+        if (clock64() - t0 > kBarrierCycles) {
+          good = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Every sweep of the one-sided Jacobi in ONE launch: block i takes pair i of every round, and a
+// grid barrier separates the rounds (the round-robin schedule of jacobi_round, the same pair
+// arithmetic, so the result equals the one-launch-per-round loop bit for bit). The "rotated" flag
+// of sweep w is flags[w % 3]; block 0 clears flags[(w + 1) % 3] as sweep w starts, which no block
+// reads or writes during sweeps w - 1 and w. After each sweep every block reads its flag behind
+// the sweep's last barrier and stops when it is clear. out[0] = sweeps run, out[1] = 1 if the last
+// sweep still rotated. bar: 2 words, zero at launch. A barrier that gives up records
+// TN_DEVERR_SVD_WAIT in *err and ends the block.
+__global__ void __launch_bounds__(NT) jacobi_sweeps_kernel(int64_t kp, int64_t n, double* X, double tol,
+                                                           const double* fro2, double null_rel2, int* flags, double* J,
+                                                           int max_sweeps, unsigned int* bar, int* out, int* err) {
+  const unsigned int nb = gridDim.x;
+  int sweeps = 0, still = 0;
+  for (int w = 0; w < max_sweeps; ++w) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) flags[(w + 1) % 3] = 0;
+    for (int64_t r = 0; r < kp - 1; ++r) {
+      jacobi_pair(kp, n, blockIdx.x, r, X, tol, fro2, null_rel2, flags + (w % 3), J);
+      if (!grid_barrier(bar, nb)) {
+        if (threadIdx.x == 0) atomicExch(err, TN_DEVERR_SVD_WAIT);
+        return;
+      }
+    }
+    ++sweeps;
+    still = *(volatile int*)(flags + (w % 3));
+    if (!still) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    out[0] = sweeps;
+    out[1] = still;
   }
 }
 
@@ -475,6 +548,32 @@ extern "C" size_t tn_svd_jacobi_workspace_bytes(int64_t k, int64_t n) {
   return 256 + (size_t)kp * n * sizeof(double) + 256 + (size_t)kp * kp * sizeof(double) + 512;
 }
 
+namespace {
+
+// Can jacobi_sweeps_kernel run kp/2 blocks co-resident on the current device? (once per device)
+bool jacobi_coop_fits(int64_t kp) {
+  static std::mutex mu;
+  static int per_sm[TN_MAX_DEVICES] = {0};   // resident blocks per SM, -1: no cooperative launch
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= TN_MAX_DEVICES) return false;
+  int b;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!per_sm[dev]) {
+      int coop = 0, nb = 0;
+      if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, jacobi_sweeps_kernel, NT, 0) != cudaSuccess || nb <= 0)
+        nb = -1;
+      cudaGetLastError();
+      per_sm[dev] = nb;
+    }
+    b = per_sm[dev];
+  }
+  return b > 0 && kp / 2 <= (int64_t)b * tn_sm_count();
+}
+
+}  // namespace
+
 extern "C" int tn_svd_jacobi(int64_t k, int64_t n, const double* x, int64_t sXr, int64_t sXc, double* s_out,
                              double* U, int64_t ldu, double* Vt, int64_t ldvt, double tol, int max_sweeps, void* ws,
                              size_t ws_bytes, void* stream) {
@@ -496,6 +595,33 @@ extern "C" int tn_svd_jacobi(int64_t k, int64_t n, const double* x, int64_t sXr,
   TN_CHECK_LAUNCH();
   const double nr2 = null_row_rel2(k, n);
   int h = 0;
+  if (kp >= 2 && max_sweeps > 0 && jacobi_coop_fits(kp)) {
+    // all sweeps in one cooperative launch; flags, barrier and result words in the header bytes
+    // of the workspace (flag at 0, fro2 at 8): flags[3] at 16, bar[2] at 32, out[2] at 40
+    int* flags = (int*)((char*)ws + 16);
+    unsigned int* bar = (unsigned int*)((char*)ws + 32);
+    int* out = (int*)((char*)ws + 40);
+    int* err = nullptr;
+    int st = tn_error_word(s, &err);
+    if (st) return st;
+    TN_CUDA(cudaMemsetAsync(flags, 0, 32, s));
+    int64_t a_kp = kp, a_n = n;
+    double a_tol = tol, a_nr2 = nr2;
+    int a_max = max_sweeps;
+    void* args[] = {&a_kp, &a_n, &X, &a_tol, &fro2, &a_nr2, &flags, &J, &a_max, &bar, &out, &err};
+    TN_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_sweeps_kernel, dim3((unsigned)(kp / 2)), dim3(NT), args,
+                                        0, s));
+    TN_CHECK_LAUNCH();
+    svd_finish_kernel<<<(unsigned)k, NT, 0, s>>>(k, kp, n, X, J, s_out, U, ldu, Vt, ldvt);
+    TN_CHECK_LAUNCH();
+    int hv[2] = {0, 0}, herr = 0;
+    TN_CUDA(cudaMemcpyAsync(hv, out, sizeof(hv), cudaMemcpyDeviceToHost, s));
+    TN_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TN_CUDA(cudaStreamSynchronize(s));
+    if (herr) return tn_error_status(herr, s);
+    if (hv[1]) return tn_fail(TN_ERR_NOCONV, "svd: Jacobi still rotating after max_sweeps");
+    return TN_OK;
+  }
   if (kp >= 2) {
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
       TN_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));

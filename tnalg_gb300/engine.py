@@ -634,11 +634,12 @@ class DeviceMPS:
             self.er_from = b
 
     # -- gauge -------------------------------------------------------------------
-    def _qr(self, mm, nn, A, sA, Q, sQ, R, seed_only):
+    def _qr(self, mm, nn, A, sA, Q, sQ, R, seed_only, exact=False):
         """tn_qr, or tn_qr_mixed on the mixed-precision path for a seeding move (R only seeds the
-        next local solve) or while fast_gauge is set; Q stays orthonormal to ~1e-12 either way."""
+        next local solve) or while fast_gauge is set; Q stays orthonormal to ~1e-12 either way.
+        exact: always tn_qr (a Q whose span must equal col(A) to FP64 accuracy)."""
         lib, st = L.load(), L.stream_handle()
-        if (self.mixed_qr and (seed_only or self.fast_gauge) and self.precision == L.PREC_TF32X3
+        if (not exact and self.mixed_qr and (seed_only or self.fast_gauge) and self.precision == L.PREC_TF32X3
                 and min(mm, nn) >= 64):
             self.stats["qr_mixed"] += 1
             wp, wb = self.ws2.args(lib.tn_qr_mixed_workspace_bytes(mm, nn))
@@ -817,8 +818,11 @@ class DeviceMPS:
             QtY = torch.empty((k, s), dtype=torch.float64, device=self.device)
             L.gemm(Q, Y, QtY, k, s, mm, (1, k), (s, 1), (s, 1), ws=self.ws)
             L.gemm(Q, QtY, Y, mm, s, k, (k, 1), (s, 1), (s, 1), Cin=Y, alpha=-1.0, beta=1.0, ws=self.ws)
-            # truncated SVD of the sketch: its dominant left singular vectors (rows of Vt of Y^T)
-            Ut, sv, Vt = L.svd_truncated(Y.t(), extra, ws=self.ws2, tol=1e-10)
+            # truncated SVD of the sketch: its dominant left singular vectors (rows of Vt of Y^T). The
+            # directions only need ranking, and they are projected and re-orthonormalised in FP64
+            # below, so the Jacobi stops once the rows are orthogonal to 1e-7 (the singular values
+            # are then accurate to ~1e-14 relative)
+            Ut, sv, Vt = L.svd_truncated(Y.t(), extra, ws=self.ws2, tol=1e-7)
             r = int(Vt.shape[0])
             Vn = torch.empty((mm, r), dtype=torch.float64, device=self.device)
             Vn.copy_(Vt.t())
@@ -828,7 +832,8 @@ class DeviceMPS:
             L.gemm(Q, QtV, Vn, mm, r, k, (k, 1), (r, 1), (r, 1), Cin=Vn, alpha=-1.0, beta=1.0, ws=self.ws)
             Vq = torch.empty((mm, r), dtype=torch.float64, device=self.device)
             Rv = torch.empty((r, r), dtype=torch.float64, device=self.device)
-            self._qr(mm, r, Vn, (r, 1), Vq, (r, 1), Rv, False)
+            # FP64: the new directions must stay orthogonal to range(Q) to FP64 accuracy
+            self._qr(mm, r, Vn, (r, 1), Vq, (r, 1), Rv, False, exact=True)
             newk = k + r
             Anew = torch.empty((cl, dd, newk), dtype=torch.float64, device=self.device)
             Anew.view(mm, newk)[:, :k].copy_(Q)

@@ -121,3 +121,26 @@ def test_unconverged_solves_continue_in_the_next_step():
         assert got[k]["solves"] == ref[k]["solves"] == 3 * 2 * (SPECS[k][0] - 1)
         assert got[k]["unconverged"] == 0
         assert got[k]["e_per_site"] == pytest.approx(ref[k]["e_per_site"], abs=1e-11)
+
+
+def test_prepared_admission_joins_in_groups_and_keeps_each_result():
+    """Admission with the host side prepared ahead on worker threads (the grouped path): jobs are
+    prepared while admitted ones step, join in groups of at least admit_chunk (fewer when nothing
+    else is being prepared), and every job's result equals the one it gets with admission done all
+    at once (prefetch = 0)."""
+    def jobs():
+        out = _jobs()
+        for k in range(3):
+            para = serving.chain_job_para(7 + k, 4, jz=0.3 * k, hz=0.1, sweeps=2, device="cpu")
+            out.append(batched.BatchJob(len(out), para, seed=300 + k, arrival=0.0))
+        return out
+    _, ref = _run(jobs(), grouped=True, prefetch=0)
+    eng, res = _run(jobs(), grouped=True, prefetch=3, admit_chunk=2, workers=2)
+    assert sorted(res) == sorted(ref)
+    assert eng.max_concurrent <= len(SPECS) + 3
+    for k in ref:
+        assert res[k]["e_per_site"] == pytest.approx(ref[k]["e_per_site"], abs=1e-13), k
+        np.testing.assert_allclose(res[k]["mz"], ref[k]["mz"], atol=1e-12)
+        assert res[k]["solves"] == ref[k]["solves"]
+    assert all(j.admitted is not None for j in eng.done)
+    assert not eng._prep

@@ -659,8 +659,16 @@ class BatchEngine:
 
     def __init__(self, device="cuda", precision="tf32x3", budget_bytes=None, max_active=1024, max_krylov=24,
                  check_every=3, mixed_floor=2e-6, workers=8, streams=16, grouped=None, profile=False, max_restarts=1,
-                 max_cycles=51):
+                 max_cycles=51, prefetch=128, admit_chunk=128):
         self.device = device
+        # host side of admission ahead of time (grouped path on a GPU): up to `prefetch` arrived jobs
+        # are prepared on the worker threads (random MPS, upload, coupling model, arena and launch
+        # records) while the engine steps the admitted ones; prepared jobs join the batch in groups
+        # of at least `admit_chunk` (fewer when no other arrived job is still being prepared, or when
+        # nothing runs), so the GPU is not idle while a large group is prepared on the host
+        self.prefetch = max(0, int(prefetch))
+        self.admit_chunk = max(1, int(admit_chunk))
+        self._prep = {}
         self.workers = max(1, int(workers))
         self.nstreams = max(1, int(streams))
         self._streams = None
@@ -716,7 +724,66 @@ class BatchEngine:
         self._admit_jobs(now)
         self.times["admit"] += time.perf_counter() - t_in
 
+    def _prefetching(self):
+        return self.prefetch > 0 and self.grouped and self.workers > 1
+
+    def _start_prepared(self, job):
+        """job.start on a worker thread, on the stream the job keeps for life (synchronised before
+        the job can be admitted)."""
+        st = self._streams[job.job_id % self.nstreams]
+        if st is None:
+            job.start(self.device, self.precision)
+            return job
+        with torch.cuda.stream(st):
+            job.start(self.device, self.precision)
+        st.synchronize()
+        return job
+
+    def _admit_prefetched(self, now):
+        """Admission with the host side prepared ahead (see __init__): reserve memory and start the
+        preparation of arrived jobs, then admit the prepared ones (device side for all of them in
+        one group)."""
+        self._ensure_streams()
+        budget = self._budget()
+        for job in self.pending:
+            if len(self._prep) >= self.prefetch or job.arrival > now:
+                break
+            if job.job_id in self._prep:
+                continue
+            if len(self.active) + len(self._prep) >= self.max_active:
+                break
+            fp = job.footprint_bytes(self.krylov)
+            if (self.active or self._prep) and self._used + fp > budget:
+                break
+            self._used += fp
+            job.__class__ = ArenaJob
+            self._prep[job.job_id] = self._pool.submit(self._start_prepared, job)
+        if not self._prep:
+            return
+        ready = [j for j in self.pending if j.job_id in self._prep and self._prep[j.job_id].done()]
+        waiting = len(self._prep) - len(ready)
+        if not self.active and waiting > 0 and len(ready) < self.admit_chunk:
+            # nothing to step: wait for a first group (admit_chunk jobs, or every job being prepared)
+            from concurrent.futures import FIRST_COMPLETED, wait
+            while waiting > 0 and len(ready) < self.admit_chunk:
+                wait([f for f in self._prep.values() if not f.done()], return_when=FIRST_COMPLETED)
+                ready = [j for j in self.pending if j.job_id in self._prep and self._prep[j.job_id].done()]
+                waiting = len(self._prep) - len(ready)
+        if not ready or (len(ready) < self.admit_chunk and waiting > 0 and self.active):
+            return
+        for job in ready:
+            self._prep.pop(job.job_id).result()   # an exception of the preparation is raised here
+            self.pending.remove(job)
+            job.admitted = now
+        self._admit_device(ready)
+        self.active += ready
+        self.max_concurrent = max(self.max_concurrent, len(self.active))
+        self.max_used = max(self.max_used, self._used)
+
     def _admit_jobs(self, now):
+        if self._prefetching():
+            self._admit_prefetched(now)
+            return
         budget = self._budget()
         admit = []
         while self.pending and self.pending[0].arrival <= now and len(self.active) + len(admit) < self.max_active:
@@ -852,7 +919,8 @@ class BatchEngine:
 
     def _ensure_streams(self):
         if self._streams is None:
-            self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.nstreams)]
+            cuda = str(self.device).startswith("cuda") and not L._host_test
+            self._streams = [torch.cuda.Stream(device=self.device) if cuda else None for _ in range(self.nstreams)]
             from concurrent.futures import ThreadPoolExecutor
             self._pool = ThreadPoolExecutor(max_workers=self.workers)
             self._obs_pool = ThreadPoolExecutor(max_workers=self.workers)
@@ -1034,7 +1102,8 @@ class BatchEngine:
             now = time.perf_counter() - t0
             self._admit(now)
             if not self.active:
-                time.sleep(max(0.0, min(self.pending[0].arrival - now, 0.01)))
+                if self.pending and self.pending[0].arrival > now:
+                    time.sleep(max(0.0, min(self.pending[0].arrival - now, 0.01)))
                 continue
             ts = time.perf_counter()
             finished = self.step()
@@ -1113,6 +1182,9 @@ def main(argv=None):
     ap.add_argument("--baseline-jobs", type=int, default=12,
                     help="how many of the jobs also run one at a time on the plain FP64 GPU path (0: none)")
     ap.add_argument("--baseline-precision", default="fp64")
+    ap.add_argument("--baseline-seconds", type=float, default=0.0,
+                    help="cap on the sequential pass (0: none): it stops inside a job once the cap is reached and "
+                         "its solves/s counts the local updates run so far")
     ap.add_argument("--device", default="cuda")
     ap.add_argument("--profile", action="store_true", help="device time per phase of the grouped step (CUDA events)")
     ap.add_argument("--warmup-jobs", type=int, default=4, help="jobs of the untimed warm-up run (0: none)")
@@ -1149,26 +1221,41 @@ def main(argv=None):
             s = serving.Scheduler(dev, max_active=1)
             s.submit(serving.DMRGJob(0, j.para, j.seed))
             s.run()
-        wall, solves, lat = 0.0, 0, []
+        wall, solves, lat, finished = 0.0, 0, [], []
+        cap = a.baseline_seconds if a.baseline_seconds > 0 else float("inf")
         for j in seq:
+            if wall >= cap:
+                break
             j.para["dt_ob"] = int(a.sweeps)
             j.arrival = 0.0
-            s = serving.Scheduler(dev, max_active=1)
-            s.submit(j)
             t0 = time.perf_counter()
-            s.run()
+            # one job at a time, one local update per call (the single-job path of serving.Scheduler),
+            # stopping inside the job once the pass has used its time cap
+            j.start(dev)
+            done_j = False
+            while not done_j:
+                done_j = j.advance()
+                if not done_j and wall + (time.perf_counter() - t0) >= cap:
+                    break
             if str(dev).startswith("cuda"):
                 torch.cuda.synchronize()
-            wall += time.perf_counter() - t0
+            dt = time.perf_counter() - t0
+            wall += dt
             solves += j.solves
-            lat.append(time.perf_counter() - t0)
+            if done_j:
+                lat.append(dt)
+                finished.append(j)
+            else:
+                j.A = None
+                j._steps = None
         done = {j.job_id: j for j in eng.done}
-        de = [abs(done[j.job_id].result["e_per_site"] - j.result["e_per_site"]) for j in seq]
-        out["sequential"] = {"precision": a.baseline_precision, "jobs": len(seq), "solves": solves, "wall_s": wall,
-                             "solves_per_s": solves / wall, "latency_per_job_p50_s": float(np.percentile(lat, 50)),
-                             "latency_per_job_p99_s": float(np.percentile(lat, 99))}
+        de = [abs(done[j.job_id].result["e_per_site"] - j.result["e_per_site"]) for j in finished]
+        out["sequential"] = {"precision": a.baseline_precision, "jobs": len(finished), "solves": solves,
+                             "wall_s": wall, "solves_per_s": solves / wall, "capped": bool(wall >= cap),
+                             "latency_per_job_p50_s": float(np.percentile(lat, 50)) if lat else None,
+                             "latency_per_job_p99_s": float(np.percentile(lat, 99)) if lat else None}
         out["speedup_vs_sequential"] = out["solves_per_s"] / (solves / wall)
-        out["max_abs_de_per_site_vs_sequential"] = float(max(de))
+        out["max_abs_de_per_site_vs_sequential"] = float(max(de)) if de else None
     print(json.dumps(out), flush=True)
 
 

@@ -160,6 +160,50 @@ __device__ __forceinline__ float block_sumf(float v, float* red) {
   return t;
 }
 
+// Columns c > j of A (column-major, ld m) <- H_j A: w = A[j, c] + v . A[j+1:, c] (v_j = 1, v below
+// the diagonal in column j), A[:, c] -= tau w v. Warp `warp` takes columns j + 1 + warp + 8 i, four
+// at a time so that four independent load / FMA / shuffle chains overlap; each column's arithmetic
+// (per-lane partial sums in row order, then the warp sum) is that of one column at a time.
+__device__ __forceinline__ void apply_reflector_cols(float* A, int m, int n, int j, float tj, int warp, int lane) {
+  constexpr int NWARP = QR_NT / 32, G = 4;
+  for (int c0 = j + 1 + warp; c0 < n; c0 += G * NWARP) {
+    float ajc[G], w[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int c = c0 + g * NWARP;
+      ajc[g] = (c < n) ? A[j + c * m] : 0.f;  // read by every lane before lane 0 rewrites it
+      w[g] = 0.f;
+    }
+    for (int r = j + 1 + lane; r < m; r += 32) {
+      const float v = A[r + j * m];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const int c = c0 + g * NWARP;
+        if (c < n) w[g] = fmaf(v, A[r + c * m], w[g]);
+      }
+    }
+    float tw[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) tw[g] = tj * (tn_warp_sumf(w[g]) + ajc[g]);
+    __syncwarp();
+    if (lane == 0) {
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const int c = c0 + g * NWARP;
+        if (c < n) A[j + c * m] = ajc[g] - tw[g];
+      }
+    }
+    for (int r = j + 1 + lane; r < m; r += 32) {
+      const float v = A[r + j * m];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const int c = c0 + g * NWARP;
+        if (c < n) A[r + c * m] = fmaf(-tw[g], v, A[r + c * m]);
+      }
+    }
+  }
+}
+
 // one CTA per matrix; dynamic shared memory: A as column-major m x n floats (ld = m) + tau (n)
 __global__ void __launch_bounds__(QR_NT) qrb_householder_kernel(const QrbItem* items) {
   extern __shared__ float sm[];
@@ -218,19 +262,7 @@ __global__ void __launch_bounds__(QR_NT) qrb_householder_kernel(const QrbItem* i
     for (int r = j + 1 + threadIdx.x; r < m; r += QR_NT) A[r + j * m] *= scale;
     __syncthreads();
     const float tj = tau[j];
-    if (tj != 0.f) {
-      // columns c > j: w = A[j, c] + v . A[j+1:, c]; A[:, c] -= tau w v  (one warp per column)
-      for (int c = j + 1 + warp; c < n; c += QR_NT / 32) {
-        const float ajc = A[j + c * m];  // read by every lane before lane 0 rewrites it
-        float w = 0.f;
-        for (int r = j + 1 + lane; r < m; r += 32) w = fmaf(A[r + j * m], A[r + c * m], w);
-        w = tn_warp_sumf(w) + ajc;
-        const float tw = tj * w;
-        __syncwarp();
-        if (lane == 0) A[j + c * m] = ajc - tw;
-        for (int r = j + 1 + lane; r < m; r += 32) A[r + c * m] = fmaf(-tw, A[r + j * m], A[r + c * m]);
-      }
-    }
+    if (tj != 0.f) apply_reflector_cols(A, m, n, j, tj, warp, lane);
     __syncthreads();
   }
   // R (upper n x n), scaled back
@@ -243,20 +275,9 @@ __global__ void __launch_bounds__(QR_NT) qrb_householder_kernel(const QrbItem* i
   // columns j+1.. have received reflector j
   for (int j = n - 1; j >= 0; --j) {
     const float tj = tau[j];
-    if (j < n - 1) {
-      for (int c = j + 1 + warp; c < n; c += QR_NT / 32) {
-        // w = v . Q[j:, c] with v_j = 1 (Q[j, c] is still 0 here: column c > j has no entries above
-        // its own diagonal yet)
-        const float ajc = A[j + c * m];
-        float w = 0.f;
-        for (int r = j + 1 + lane; r < m; r += 32) w = fmaf(A[r + j * m], A[r + c * m], w);
-        w = tn_warp_sumf(w) + ajc;
-        const float tw = tj * w;
-        __syncwarp();
-        if (lane == 0) A[j + c * m] = ajc - tw;
-        for (int r = j + 1 + lane; r < m; r += 32) A[r + c * m] = fmaf(-tw, A[r + j * m], A[r + c * m]);
-      }
-    }
+    // w = v . Q[j:, c] with v_j = 1 (Q[j, c] is still 0 here: column c > j has no entries above its
+    // own diagonal yet)
+    if (j < n - 1) apply_reflector_cols(A, m, n, j, tj, warp, lane);
     __syncthreads();
     for (int r = threadIdx.x; r < m; r += QR_NT) {
       if (r < j) A[r + j * m] = 0.f;
@@ -273,7 +294,22 @@ __global__ void __launch_bounds__(QR_NT) qrb_householder_kernel(const QrbItem* i
   }
 }
 
-// E = Q^T Q - I (n x n) from the FP32 copy; each product of two FP32 values is exact in FP64.
+// a * b added to the double-float (hi, lo): TwoProduct by FMA and TwoSum (Ogita, Rump and Oishi's
+// Dot2); the _rn intrinsics are never contracted into FMAs, which would break both transformations
+__device__ __forceinline__ void qrb_dot2_step(float a, float b, float& hi, float& lo) {
+  const float h = __fmul_rn(a, b);
+  const float r = fmaf(a, b, -h);
+  const float t = __fadd_rn(hi, h);
+  const float z = __fsub_rn(t, hi);
+  const float q = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(h, z));
+  hi = t;
+  lo = __fadd_rn(lo, __fadd_rn(q, r));
+}
+
+// E = Q^T Q - I (n x n) from the FP32 copy. Every product of two FP32 values is exact as a pair of
+// floats; the 32 products of a shared-memory stage are summed in double-float on the FP32 pipe and
+// each stage's sum is added in FP64 (one FP64 add per 32 products: GB300's FP64 pipe issues ~64
+// times fewer lanes per clock than its FP32 pipe).
 // One block per (item, 32 x 32 tile of E); tiles below the diagonal are skipped and mirrored.
 __global__ void qrb_gram_kernel(const QrbItem* items, const int* prefix, int nitems) {
   __shared__ float Qi[32][33], Qj[32][33];
@@ -296,12 +332,15 @@ __global__ void qrb_gram_kernel(const QrbItem* items, const int* prefix, int nit
       Qj[cc][rr] = (r < m && tj * 32 + cc < n) ? it.qs[r + (int64_t)(tj * 32 + cc) * m] : 0.f;
     }
     __syncthreads();
+    float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 4
     for (int rr = 0; rr < 32; ++rr) {
-      const double b = (double)Qj[tx][rr];
+      const float b = Qj[tx][rr];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) acc[u] = fma((double)Qi[ty + 8 * u][rr], b, acc[u]);
+      for (int u = 0; u < 4; ++u) qrb_dot2_step(Qi[ty + 8 * u][rr], b, hi[u], lo[u]);
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] += (double)hi[u] + (double)lo[u];
     __syncthreads();
   }
 #pragma unroll

@@ -102,26 +102,51 @@ __global__ void bl_init_kernel(BjJob* jobs, int njobs, const int* prefix) {
 
 constexpr int EPT = CH / NT;  // vector elements per thread
 
+// Sum over the 32 lanes of G = 8 values at once: on return lane L holds the sum over the warp of
+// v[L & 7] (3 halving exchanges, then 2 on the single value left: 9 shuffles instead of 40).
+__device__ __forceinline__ double warp_transpose_sum8(double (&v)[8], int lane) {
+#pragma unroll
+  for (int half = 4; half >= 1; half >>= 1) {
+    const bool upper = (lane & half) != 0;
+#pragma unroll
+    for (int i = 0; i < half; ++i) {
+      const double send = upper ? v[i] : v[i + half];
+      const double keep = upper ? v[i + half] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, half);
+    }
+  }
+  double t = v[0];
+  t += __shfl_xor_sync(0xffffffffu, t, 8);
+  t += __shfl_xor_sync(0xffffffffu, t, 16);
+  return t;
+}
+
 // h[i] = V[i] . x for i < k over the block's chunk (x: this thread's EPT elements, at e0 + tid +
 // q NT), reduced over the block, then, by the last block of the job, over the chunks in chunk order
-// (deterministic). One block computes all k dots of its chunk: the w chunk is read once and the k
-// basis chunks stream through with EPT independent loads per thread in flight.
+// (deterministic). One block computes all k dots of its chunk: the w chunk is read once and the
+// basis chunks stream through eight at a time (8 EPT independent loads per thread in flight), the
+// eight partial dots of a group reduced over the warp together.
 __device__ void chunk_dots(BjJob& J, int c, int k, const double (&x)[EPT], int64_t e0, double* out) {
-  __shared__ double red[NT / 32][kMaxM + 1];
+  __shared__ double red[NT / 32][kMaxM + 8];
   __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t nrem = J.n - e0;
-#pragma unroll 2
-  for (int i = 0; i < k; ++i) {
-    const double* v = J.V + (int64_t)i * J.n + e0;
-    double acc = 0.0;
+  for (int i0 = 0; i0 < k; i0 += 8) {
+    double acc[8];
 #pragma unroll
-    for (int q = 0; q < EPT; ++q) {
-      const int idx = threadIdx.x + q * NT;
-      if (idx < nrem) acc = fma(v[idx], x[q], acc);
+    for (int g = 0; g < 8; ++g) {
+      acc[g] = 0.0;
+      if (i0 + g < k) {
+        const double* v = J.V + (int64_t)(i0 + g) * J.n + e0;
+#pragma unroll
+        for (int q = 0; q < EPT; ++q) {
+          const int idx = threadIdx.x + q * NT;
+          if (idx < nrem) acc[g] = fma(v[idx], x[q], acc[g]);
+        }
+      }
     }
-    acc = tn_warp_sum(acc);
-    if (lane == 0) red[wid][i] = acc;
+    const double t = warp_transpose_sum8(acc, lane);
+    if (lane < 8) red[wid][i0 + lane] = t;
   }
   __syncthreads();
   if (threadIdx.x < k) {
@@ -160,7 +185,7 @@ __device__ __forceinline__ void load_chunk(const BjJob& J, int64_t e0, double (&
 // x -= sum_{i<k} h[i] V[i] on this thread's elements (EPT independent chains)
 __device__ __forceinline__ void chunk_axpy(const BjJob& J, int64_t e0, int k, const double* hs, double (&x)[EPT]) {
   const int64_t nrem = J.n - e0;
-#pragma unroll 4
+#pragma unroll 8
   for (int i = 0; i < k; ++i) {
     const double* v = J.V + (int64_t)i * J.n + e0;
     const double h = hs[i];

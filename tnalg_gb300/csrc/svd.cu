@@ -12,8 +12,14 @@
 // A pair is left alone when its off-diagonal is below tol relative to the rows, or when one
 // of its rows is numerically null (squared norm below (4 eps)^2 max(k, n) ||X||_F^2): rounding
 // noise keeps such rows from ever becoming orthogonal, and their norms are noise-level singular
-// values either way (LAPACK's are accurate to ~eps ||X|| too). A sweep that still rotated after
-// max_sweeps makes the call return TN_ERR_NOCONV (the values are written all the same).
+// values either way (LAPACK's are accurate to ~eps ||X|| too). A row that is small but above the
+// null level (squared norm below (64 eps)^2 k n ||X||_F^2, e.g. a direction left over from the
+// cancellation of two large rows) still rotates, but its rotations do not count as "rotated": its
+// dot products carry the rounding of the large rows it came from (relative error up to
+// eps ||X|| / ||row||), so they may never fall below tol, and would otherwise keep every sweep
+// going until max_sweeps. Its singular value is then accurate to ~eps ||X||, LAPACK's accuracy.
+// A sweep that still rotated after max_sweeps makes the call return TN_ERR_NOCONV (the values are
+// written all the same).
 #include <math.h>
 
 #include <vector>
@@ -80,12 +86,14 @@ __device__ __forceinline__ void jacobi_pair(int64_t kp, int64_t n, int64_t i, in
     double A = 0, B = 0, G = 0;
     for (int w = 0; w < NT / 32; ++w) { A += red[0][w]; B += red[1][w]; G += red[2][w]; }
     double c = 1.0, s = 0.0;
-    if (G != 0.0 && fabs(G) > tol * sqrt(A * B) && fmin(A, B) > null_rel2 * (*fro2)) {
+    const double f2 = *fro2;
+    if (G != 0.0 && fabs(G) > tol * sqrt(A * B) && fmin(A, B) > null_rel2 * f2) {
       const double zeta = (B - A) / (2.0 * G);
       const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
       c = 1.0 / sqrt(1.0 + t * t);
       s = c * t;
-      if (s != 0.0) *rotated = 1;
+      // rows below the "small" level rotate without holding up convergence (see the top)
+      if (s != 0.0 && fmin(A, B) > null_rel2 * 256.0 * (double)min(kp, n) * f2) *rotated = 1;
     }
     cs[0] = c; cs[1] = s;
   }
@@ -356,12 +364,14 @@ __global__ void svb_round(const SvItem<T>* items, int64_t r, T tol, int* rotated
       G += red[2][w];
     }
     T c = 1, sn = 0;
-    if (G != (T)0 && fabs(G) > tol * sqrt(A * B) && (double)fmin(A, B) > it.null_rel2 * (*it.fro2)) {
+    const double f2 = *it.fro2;
+    if (G != (T)0 && fabs(G) > tol * sqrt(A * B) && (double)fmin(A, B) > it.null_rel2 * f2) {
       const T zeta = (B - A) / (2 * G);
       const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
       c = (T)1 / sqrt((T)1 + tt * tt);
       sn = c * tt;
-      if (sn != (T)0) *rotated = 1;
+      // rows below the "small" level rotate without holding up convergence (see the top)
+      if (sn != (T)0 && (double)fmin(A, B) > it.null_rel2 * 256.0 * (double)min(it.kp, it.n) * f2) *rotated = 1;
     }
     cs[0] = c;
     cs[1] = sn;

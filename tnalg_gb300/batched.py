@@ -321,7 +321,9 @@ class ArenaJob(BatchJob):
             st["gemm2"] += e_g2
             steps.append(st)
         self._adm = [_adm_tables(s, R) for s in steps]
-        self._rows = {}
+        # the launch records of every (site, direction) of a sweep, built here on the admitting
+        # thread rather than on the engine's thread during the first sweep
+        self._rows = {k: self._build(k) for k in range(len(self._order))}
         self.admit_parts = {"draws": t1 - t0, "upload": t2 - t1, "model": t3 - t2,
                             "arena_and_tables": time.perf_counter() - t3}
 

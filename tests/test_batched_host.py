@@ -144,3 +144,25 @@ def test_prepared_admission_joins_in_groups_and_keeps_each_result():
         assert res[k]["solves"] == ref[k]["solves"]
     assert all(j.admitted is not None for j in eng.done)
     assert not eng._prep
+
+
+def test_large_jobs_run_alone_beside_the_batch():
+    """Jobs with chi >= alone_chi run the single-job path on worker threads beside the grouped
+    batch: each gets the result of the one-job scheduler (same draws, same kernels), the batched
+    jobs keep theirs, and every job is reported once with its latency."""
+    _, ref = _run(_jobs(), grouped=True, alone_chi=0)
+    eng, res = _run(_jobs(), grouped=True, alone_chi=6, alone_workers=2)
+    assert sorted(res) == sorted(ref) and len(eng.done) == len(SPECS)
+    big = [k for k, s in enumerate(SPECS) if s[1] >= 6]
+    assert big and not isinstance(next(j for j in eng.done if j.job_id == big[0]), batched.ArenaJob)
+    for k, (l, chi, jz, hz) in enumerate(SPECS):
+        if k in big:
+            j = _jobs("serial")[k]
+            s = serving.Scheduler("cpu", max_active=1)
+            s.submit(j)
+            s.run()
+            assert res[k]["e_per_site"] == pytest.approx(j.result["e_per_site"], abs=1e-12), k
+            np.testing.assert_allclose(res[k]["mz"], j.result["mz"], atol=1e-10)
+        else:
+            assert res[k]["e_per_site"] == pytest.approx(ref[k]["e_per_site"], abs=1e-13), k
+    assert all(j.finished is not None and j.finished >= j.arrival for j in eng.done)

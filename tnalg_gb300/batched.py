@@ -21,6 +21,7 @@ the same alone and in any mix (tests/test_gpu_batched.py).
 import ctypes
 import threading
 import time
+from contextlib import nullcontext as _nullcontext
 
 import numpy as np
 import torch
@@ -661,8 +662,18 @@ class BatchEngine:
 
     def __init__(self, device="cuda", precision="tf32x3", budget_bytes=None, max_active=1024, max_krylov=24,
                  check_every=3, mixed_floor=2e-6, workers=8, streams=16, grouped=None, profile=False, max_restarts=1,
-                 max_cycles=51, prefetch=128, admit_chunk=128):
+                 max_cycles=51, prefetch=128, admit_chunk=128, alone_chi=256, alone_workers=4):
         self.device = device
+        # jobs with chi >= alone_chi run the single-job path (tn_lanczos, tn_qr_mixed on one 16-CTA
+        # cluster, the split-TF32 GEMMs at full size) on their own worker thread and stream, up to
+        # alone_workers at a time, beside the grouped batch: a chi = 512 local update already fills
+        # the GPU's tensor and memory pipes on its own, while in the lockstep batch every small job
+        # would wait for it (and its grouped block operators and FP64 absorbs cost more than the
+        # single-job path's incremental updates). 0 disables the split.
+        self.alone_chi = int(alone_chi)
+        self.alone_workers = max(1, int(alone_workers))
+        self._alone = {}
+        self._alone_pool = None
         # host side of admission ahead of time (grouped path on a GPU): up to `prefetch` arrived jobs
         # are prepared on the worker threads (random MPS, upload, coupling model, arena and launch
         # records) while the engine steps the admitted ones; prepared jobs join the batch in groups
@@ -723,8 +734,73 @@ class BatchEngine:
 
     def _admit(self, now):
         t_in = time.perf_counter()
+        self._admit_alone(now)
         self._admit_jobs(now)
         self.times["admit"] += time.perf_counter() - t_in
+
+    def _is_alone(self, job):
+        return self.alone_chi > 0 and self.grouped and int(job.para["chi"]) >= self.alone_chi
+
+    def _admit_alone(self, now):
+        """Arrived jobs with chi >= alone_chi start on the single-job path (a worker thread each, at
+        most alone_workers at a time) while their device memory fits the budget."""
+        if self.alone_chi <= 0 or not self.grouped:
+            return
+        budget = None
+        for job in [j for j in self.pending if j.arrival <= now and self._is_alone(j)]:
+            if len(self._alone) >= self.alone_workers:
+                break
+            fp = job.footprint_bytes(self.krylov)
+            if budget is None:
+                budget = self._budget()
+            if (self.active or self._alone or self._prep) and self._used + fp > budget:
+                break
+            self._used += fp
+            self.pending.remove(job)
+            job.admitted = now
+            if self._alone_pool is None:
+                from concurrent.futures import ThreadPoolExecutor
+                self._alone_pool = ThreadPoolExecutor(max_workers=self.alone_workers)
+            self._alone[job.job_id] = (job, self._alone_pool.submit(self._run_alone, job))
+            self.max_concurrent = max(self.max_concurrent, len(self.active) + len(self._alone))
+            self.max_used = max(self.max_used, self._used)
+
+    def _run_alone(self, job):
+        """Every sweep of one job on the single-job path (the sweep loop of dmrg_finite_size,
+        DMRG_anyH.py:43-64, through MpsOpenBoundaryClass), on its own stream, then its observation."""
+        cuda = str(self.device).startswith("cuda") and not L._host_test
+        st = torch.cuda.Stream(device=self.device) if cuda else None
+        ctx = torch.cuda.stream(st) if cuda else _nullcontext()
+        with ctx:
+            job.start(self.device, self.precision)
+            A, p = job.A, job.para
+            for _ in range(p["sweep_time"]):
+                for k, n in enumerate(job._order):
+                    if k == len(job._order) - 1:
+                        A.refine_next_solve()
+                    A.update_tensor_eigs(n, p["index1"], p["index2"], p["coeff1"], p["coeff2"], p["tau"],
+                                         p["is_real"], tol=p["eigs_tol"])
+                    job.solves += 1
+            job.matvecs = int(A.stats["matvecs"])
+            job.unconverged = int(A.stats["unconverged"])
+            job.solved_at = time.perf_counter() - self._t0
+            job.observe()
+        if st is not None:
+            st.synchronize()
+        job.observe_s = 0.0
+        return job
+
+    def _collect_alone(self, block=False):
+        if not self._alone:
+            return
+        if block:
+            from concurrent.futures import FIRST_COMPLETED, wait
+            wait([f for _, f in self._alone.values()], return_when=FIRST_COMPLETED)
+        for jid, (job, fut) in list(self._alone.items()):
+            if fut.done():
+                fut.result()   # an exception of the job is raised here
+                del self._alone[jid]
+                self._retire(job)
 
     def _prefetching(self):
         return self.prefetch > 0 and self.grouped and self.workers > 1
@@ -750,7 +826,7 @@ class BatchEngine:
         for job in self.pending:
             if len(self._prep) >= self.prefetch or job.arrival > now:
                 break
-            if job.job_id in self._prep:
+            if job.job_id in self._prep or self._is_alone(job):
                 continue
             if len(self.active) + len(self._prep) >= self.max_active:
                 break
@@ -788,11 +864,15 @@ class BatchEngine:
             return
         budget = self._budget()
         admit = []
-        while self.pending and self.pending[0].arrival <= now and len(self.active) + len(admit) < self.max_active:
-            fp = self.pending[0].footprint_bytes(self.krylov)
+        while len(self.active) + len(admit) < self.max_active:
+            # the first arrived job that runs in the batch (large jobs are started by _admit_alone)
+            job = next((j for j in self.pending if j.arrival <= now and not self._is_alone(j)), None)
+            if job is None:
+                break
+            fp = job.footprint_bytes(self.krylov)
             if (self.active or admit) and self._used + fp > budget:
                 break
-            job = self.pending.pop(0)
+            self.pending.remove(job)
             job.admitted = now
             if self.grouped and not isinstance(job, ArenaJob):
                 job.__class__ = ArenaJob
@@ -1097,15 +1177,22 @@ class BatchEngine:
     def run(self, progress=None):
         """Admit (by arrival time and memory), step, retire, until every submitted job is done."""
         self._t0 = t0 = time.perf_counter()
-        while self.pending or self.active or self._observing:
+        while self.pending or self.active or self._observing or self._alone:
+            self._collect_alone()
             if not self.active and not self.pending:
-                self._collect_observed(block=True)
+                if self._observing:
+                    self._collect_observed(block=True)
+                else:
+                    self._collect_alone(block=True)
                 continue
             now = time.perf_counter() - t0
             self._admit(now)
             if not self.active:
                 if self.pending and self.pending[0].arrival > now:
                     time.sleep(max(0.0, min(self.pending[0].arrival - now, 0.01)))
+                elif self._alone and (not self.pending or self._is_alone(self.pending[0])):
+                    # only large jobs left to run or to start: wait for one of them
+                    self._collect_alone(block=True)
                 continue
             ts = time.perf_counter()
             finished = self.step()

@@ -28,6 +28,7 @@ import torch
 
 from . import _lib as L
 from .MPSClass import MpsOpenBoundaryClass
+from .serving import pow2_scaled
 
 
 class BatchJob:
@@ -72,7 +73,7 @@ class BatchJob:
         for n in range(1, l - 1):
             tensors[n] = rs.randn(chi, d, chi)
         self.A = MpsOpenBoundaryClass(length=l, d=d, chi=chi, operators=p["op"], device=device, precision=precision,
-                                      tensors=tensors)
+                                      tensors=pow2_scaled(tensors))
         self.A.correct_orthogonal_center(p["ob_position"])
         self.A._model(p["index1"], p["index2"], p["coeff1"], p["coeff2"], p["eigs_tol"])
         ob = p["ob_position"]
@@ -322,9 +323,9 @@ class ArenaJob(BatchJob):
             st["gemm2"] += e_g2
             steps.append(st)
         self._adm = [_adm_tables(s, R) for s in steps]
-        # the launch records of every (site, direction) of a sweep, built here on the admitting
-        # thread rather than on the engine's thread during the first sweep
-        self._rows = {k: self._build(k) for k in range(len(self._order))}
+        # the launch records of each (site, direction) are built when first needed, on the engine's
+        # thread (built here, on the admitting threads, they cost ~10x more host time under the GIL)
+        self._rows = {}
         self.admit_parts = {"draws": t1 - t0, "upload": t2 - t1, "model": t3 - t2,
                             "arena_and_tables": time.perf_counter() - t3}
 
@@ -662,7 +663,7 @@ class BatchEngine:
 
     def __init__(self, device="cuda", precision="tf32x3", budget_bytes=None, max_active=1024, max_krylov=24,
                  check_every=3, mixed_floor=2e-6, workers=8, streams=16, grouped=None, profile=False, max_restarts=1,
-                 max_cycles=51, prefetch=128, admit_chunk=128, alone_chi=256, alone_workers=4):
+                 max_cycles=51, prefetch=128, admit_chunk=32, alone_chi=256, alone_workers=4):
         self.device = device
         # jobs with chi >= alone_chi run the single-job path (tn_lanczos, tn_qr_mixed on one 16-CTA
         # cluster, the split-TF32 GEMMs at full size) on their own worker thread and stream, up to

@@ -98,6 +98,19 @@ def estimate_device_bytes(para, krylov=40):
     return int(8 * (mps + env + scratch))
 
 
+def pow2_scaled(tensors):
+    """The random tensors of a job, each scaled by the power of two nearest 1 / sqrt(its size). A
+    Gaussian site multiplies the norm of the state by ~sqrt(size), so centring a long chain at large
+    chi would carry ~724^N on the centre (chi = 512) and overflow FP64 beyond ~100 sites; a
+    power-of-two scaling is exact, leaves every QR factor Q bit for bit as it was and only rescales
+    the state, which the first local solve normalises."""
+    out = []
+    for t in tensors:
+        e = int(np.round(0.5 * np.log2(max(t.size, 1))))
+        out.append(np.ldexp(t, -e))
+    return out
+
+
 class DMRGJob:
     """One DMRG run advanced one local update at a time (`advance`)."""
 
@@ -127,10 +140,12 @@ class DMRGJob:
         if str(device).startswith("cuda"):
             self.stream = torch.cuda.Stream(device=device)
         with self._on_stream():
+            from .MPSClass import random_open_mps
             np.random.seed(self.seed)
             p = self.para
+            tensors = pow2_scaled(random_open_mps(p["l"], p["d"], p["chi"]))
             self.A = Mob(length=p["l"], d=p["d"], chi=p["chi"], operators=p["op"], device=p.get("device", device),
-                         precision=p.get("precision", "fp64"))
+                         precision=p.get("precision", "fp64"), tensors=tensors)
             self.A.correct_orthogonal_center(p["ob_position"])
         self._steps = self._run()
 

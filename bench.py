@@ -385,7 +385,7 @@ def config1_leg(device):
     return out
 
 
-LEGS_BUDGET_S = 840   # the child legs together (normally ~10 minutes)
+LEGS_BUDGET_S = 960   # the child legs together (normally ~10-12 minutes)
 CHAIN_ARGS = ["chain", "--length", "100", "--chi", "512", "--ramp", "64,256", "--steps", "6"]
 LATTICE_ARGS = ["j1j2", "--width", "6", "--height", "6", "--chi", "512", "--ramp", "", "--steps", "10"]
 BATCH_ARGS = ["--jobs", "512", "--lengths", "16,64", "--chis", "32,64,128", "--sweeps", "8", "--baseline-jobs", "8"]

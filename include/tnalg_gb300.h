@@ -228,6 +228,16 @@ int tn_svd_jacobi(int64_t k, int64_t n, const double* x, int64_t sXr, int64_t sX
 size_t tn_svd_jacobi_workspace_bytes(int64_t k, int64_t n);
 
 /*
+ * Self-test of the library's bounded device waits: a 2-block kernel waits at a grid barrier that
+ * can never complete (it expects a third block); every block gives up after its wait limit (~2 s)
+ * and records the timeout in the error word of `stream`, which this call reads and clears. Returns
+ * TN_ERR_TIMEOUT when the bounded wait worked; the context stays usable. ws: 256-byte aligned DEVICE
+ * scratch of at least 256 bytes. Synchronises stream. Diagnostic only; no counterpart in the
+ * reference.
+ */
+int tn_selftest_wait_timeout(void* ws, size_t ws_bytes, void* stream);
+
+/*
  * tn_singular_values without a workspace argument and without any device allocation. It has no
  * counterpart in the reference: it exists for hosts that cannot allocate device memory
  * themselves (a service that may only use buffers registered by its own allocator, or a process

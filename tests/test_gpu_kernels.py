@@ -241,3 +241,21 @@ def test_svd_jacobi_truncation_matches_numpy(cuda_lib, k, n, chi):
     eye = np.eye(r)
     assert np.max(np.abs((U.T @ U).cpu().numpy() - eye)) < 1e-12
     assert np.max(np.abs((Vt @ Vt.T).cpu().numpy() - eye)) < 1e-12
+
+
+def test_bounded_wait_gives_up_and_the_context_stays_usable(cuda_lib):
+    """A device wait that can never be satisfied (a grid barrier expecting one block more than
+    launched) gives up after its limit and reports TN_ERR_TIMEOUT through the stream's error word;
+    the next calls on the same stream run normally (a Jacobi SVD through the same barrier code)."""
+    lib = L.load()
+    ws = L.Workspace(_dev())
+    buf = ws.get(4096)
+    base = (buf.data_ptr() + 255) // 256 * 256
+    st = lib.tn_selftest_wait_timeout(base, 1024, L.stream_handle())
+    assert st == L.TN_ERR_TIMEOUT, lib.tn_last_error()
+    assert b"gave up" in lib.tn_last_error()
+    L.check(lib.tn_check_device_status(L.stream_handle()))   # the error word was read and cleared
+    X = _rand(40, 64, seed=5)
+    U, s, Vt = L.svd_truncated(X, 40, tol=1e-15)
+    ref = np.linalg.svd(X.cpu().numpy(), compute_uv=False)
+    np.testing.assert_allclose(np.sort(s.cpu().numpy())[::-1], ref, atol=1e-13 * ref[0], rtol=1e-11)

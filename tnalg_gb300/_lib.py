@@ -143,6 +143,7 @@ _SIGS = {
     "tn_svd_jacobi": (c_int, [c_i64, c_i64, c_vp, c_i64, c_i64, c_vp, c_vp, c_i64, c_vp, c_i64, c_dbl, c_int, c_vp,
                               c_sz, c_vp]),
     "tn_svd_jacobi_workspace_bytes": (c_sz, [c_i64, c_i64]),
+    "tn_selftest_wait_timeout": (c_int, [c_vp, c_sz, c_vp]),
     "tn_singular_values_batched": (c_int, [c_int, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_batched_workspace_bytes": (c_sz, [c_int, c_vp]),
     "tn_grouped_gemm": (c_int, [c_int, c_vp, c_int, c_vp, c_sz, c_vp]),

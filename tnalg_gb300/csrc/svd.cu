@@ -157,6 +157,13 @@ __device__ bool grid_barrier(unsigned int* bar, unsigned int nblocks) {
   return ok != 0;
 }
 
+// Self-test of the bounded barrier: every block waits at a barrier that expects one block more
+// than the grid holds, so no block can pass; each gives up after kBarrierCycles and records
+// TN_DEVERR_SVD_WAIT. No copies are in flight and no other resource is held, so the blocks just end.
+__global__ void barrier_timeout_selftest_kernel(unsigned int* bar, int* err) {
+  if (!grid_barrier(bar, gridDim.x + 1u) && threadIdx.x == 0) atomicExch(err, TN_DEVERR_SVD_WAIT);
+}
+
 // Every sweep of the one-sided Jacobi in ONE launch: block i takes pair i of every round, and a
 // grid barrier separates the rounds (the round-robin schedule of jacobi_round, the same pair
 // arithmetic, so the result equals the one-launch-per-round loop bit for bit). The "rotated" flag
@@ -552,6 +559,19 @@ extern "C" int tn_singular_values_noalloc(int64_t k, int64_t n, const double* x,
 
 // ---------------------------------------------------------------------------
 // Thin SVD with singular vectors (the same Jacobi, rotations accumulated).
+
+extern "C" int tn_selftest_wait_timeout(void* ws, size_t ws_bytes, void* stream) {
+  if (!ws || ws_bytes < 256 || ((uintptr_t)ws & 255)) return tn_fail(TN_ERR_WORKSPACE, "selftest: workspace");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int* bar = (unsigned int*)ws;
+  int* err = nullptr;
+  int st = tn_error_word(s, &err);
+  if (st) return st;
+  TN_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned int), s));
+  barrier_timeout_selftest_kernel<<<2, NT, 0, s>>>(bar, err);
+  TN_CHECK_LAUNCH();
+  return tn_error_check(s);
+}
 
 extern "C" size_t tn_svd_jacobi_workspace_bytes(int64_t k, int64_t n) {
   const int64_t kp = k + (k & 1);

@@ -302,6 +302,17 @@ int tn_grouped_gemm(int precision, const tn_grouped_gemm_problem* problems, int 
                     void* stream);
 size_t tn_grouped_gemm_workspace_bytes(int precision, const tn_grouped_gemm_problem* problems, int count);
 
+/*
+ * Output tile width (64 or 128 columns; 0 restores the default, 128) of the split-TF32 grouped GEMMs
+ * that the CALLING HOST THREAD issues from now on (tn_grouped_gemm, tn_batched_lanczos,
+ * tn_batched_step, tn_batched_qr_mixed). The setting is thread-local, so engines on different
+ * threads tune independently; the results do not depend on it (the same products are summed in
+ * the same order). Picked by tnalg_gb300/tuner.py from a measured table. No counterpart in the
+ * reference.
+ */
+int tn_set_grouped_tile(int tile_n);
+int tn_get_grouped_tile(void);
+
 /* ---- grouped building blocks and the batched gauge move --------------------------------- */
 enum { TN_BOP_BLOCK_LEFT = 0, TN_BOP_BLOCK_RIGHT = 1, TN_BOP_COMBINE = 2, TN_BOP_SITE_OPS = 3 };
 

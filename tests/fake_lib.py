@@ -57,6 +57,16 @@ class FakeLib:
     def __init__(self):
         self.err = b""
         self.calls = {}
+        self.tile_n = 0
+
+    def tn_set_grouped_tile(self, tile_n):
+        if tile_n not in (0, 64, 128):
+            return ERR_ARG
+        self.tile_n = int(tile_n)
+        return OK
+
+    def tn_get_grouped_tile(self):
+        return self.tile_n or 128
 
     def _count(self, name):
         self.calls[name] = self.calls.get(name, 0) + 1

@@ -144,6 +144,8 @@ _SIGS = {
                               c_sz, c_vp]),
     "tn_svd_jacobi_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "tn_selftest_wait_timeout": (c_int, [c_vp, c_sz, c_vp]),
+    "tn_set_grouped_tile": (c_int, [c_int]),
+    "tn_get_grouped_tile": (c_int, []),
     "tn_singular_values_batched": (c_int, [c_int, c_vp, c_dbl, c_int, c_vp, c_sz, c_vp]),
     "tn_singular_values_batched_workspace_bytes": (c_sz, [c_int, c_vp]),
     "tn_grouped_gemm": (c_int, [c_int, c_vp, c_int, c_vp, c_sz, c_vp]),

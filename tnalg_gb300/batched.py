@@ -671,6 +671,11 @@ class BatchEngine:
         # the GPU's tensor and memory pipes on its own, while in the lockstep batch every small job
         # would wait for it (and its grouped block operators and FP64 absorbs cost more than the
         # single-job path's incremental updates). 0 disables the split.
+        # output tile width of the grouped split-TF32 GEMMs per step, from the tuner's measured table
+        # (tnalg_gb300/tuner.py; the library default where the table has no class)
+        from .tuner import Choice
+        self.tiles = Choice()
+        self.tile_widths = {}
         self.alone_chi = int(alone_chi)
         self.alone_workers = max(1, int(alone_workers))
         self._alone = {}
@@ -1115,6 +1120,10 @@ class BatchEngine:
         solves = self._cat(rows, "solve")
         self.times["tables"] += time.perf_counter() - t_tab
         self._ensure_ws()
+        if self.prec == L.PREC_TF32X3:
+            w = self.tiles.width(max(int(j.para["chi"]) for j in jobs), len(jobs))
+            L.check(L.load().tn_set_grouped_tile(w), "tile width")
+            self.tile_widths[w] = self.tile_widths.get(w, 0) + 1
         if not (self.profile and not L._host_test):
             res = self._step_call(phases, self.prec, solves, jobs)
         else:
@@ -1232,7 +1241,8 @@ class BatchEngine:
                 "matvecs_per_solve": (sum(j.matvecs for j in self.done) / solves) if solves else 0.0,
                 "host_s": {k: round(v, 3) for k, v in self.times.items()},
                 "admit_thread_s": {k: round(v, 3) for k, v in parts.items()},
-                "device_ms_per_step": {k: round(v / max(self.steps, 1), 3) for k, v in self.phase_ms.items()}}
+                "device_ms_per_step": {k: round(v / max(self.steps, 1), 3) for k, v in self.phase_ms.items()},
+                "tile_width_steps": {str(k): v for k, v in sorted(self.tile_widths.items())}}
 
 
 def batch_jobs(njobs, seed=0, sweeps=8, precision="tf32x3", device="cuda", rate=None, lengths=(16, 64),

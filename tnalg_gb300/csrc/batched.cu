@@ -533,6 +533,7 @@ struct Layout {
   std::vector<int> pf_probs, pf_probs2;
   std::vector<GgF64Problem> f64, f64b;
   std::vector<int> pf_f64, pf_f64b;
+  int bn = 128;  // split-TF32 tile width (gg_tile_n of the calling thread)
   BjJob* d_jobs = nullptr;
   unsigned int* tickets = nullptr;
   size_t tickets_bytes = 0;
@@ -544,6 +545,8 @@ struct Layout {
 int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* base, Layout* L) {
   const bool mixed = o->precision == TN_PREC_TF32X3;
   const int m = std::max(2, std::min<int>(o->max_krylov, kMaxM));
+  const int bn = gg_tile_n();
+  L->bn = bn;
   size_t off = 256;
   auto take = [&](size_t bytes) -> char* {
     char* p = base ? base + off : nullptr;
@@ -608,52 +611,52 @@ int layout(const tn_batch_solve* in, int count, const tn_lanczos_opts* o, char* 
         GgProblem p{};
         p.nbatch = 1; p.n_mt = (int32_t)tn_cdiv(ng * cl, 128);
         p.M = (int32_t)(ng * cl); p.N = (int32_t)(dd * cr); p.nred = 1;
-        p.n_kb = (int32_t)tn_cdiv(cl, 32); p.n_nt = (int32_t)tn_cdiv(dd * cr, 128);
+        p.n_kb = (int32_t)tn_cdiv(cl, 32); p.n_nt = (int32_t)tn_cdiv(dd * cr, bn);
         p.a = stage(L->st_static, L->pf_static, d.sl, ng * cl, cl, cl, 1);
         p.a_nrt = (int32_t)tn_cdiv(ng * cl, 128);
         p.b = stage(L->st_iter, L->pf_iter, J.x, dd * cr, cl, 1, dd * cr);  // B^T rows (s b), k = a
         p.b_nrt = (int32_t)tn_cdiv(dd * cr, 128);
         p.C = Z; p.sCm = dd * cr; p.sCn = 1; p.alpha = 1.0; p.beta = 0.0; p.accumulate = 0; p.active = active;
         L->probs.push_back(p);
-        L->pf_probs.push_back(L->pf_probs.back() + gg_tf32_tiles(p, 128));
+        L->pf_probs.push_back(L->pf_probs.back() + gg_tf32_tiles(p, bn));
         // phase 2: w += sum_g Z_g (chil d x chir) . SR_g^T
         GgProblem q{};
         q.nbatch = 1; q.n_mt = (int32_t)tn_cdiv(cl * dd, 128);
         q.M = (int32_t)(cl * dd); q.N = (int32_t)cr; q.nred = (int32_t)ng;
-        q.n_kb = (int32_t)tn_cdiv(cr, 32); q.n_nt = (int32_t)tn_cdiv(cr, 128);
+        q.n_kb = (int32_t)tn_cdiv(cr, 32); q.n_nt = (int32_t)tn_cdiv(cr, bn);
         q.a = stage(L->st_iter2, L->pf_iter2, Z, cl * dd, cr, cr, 1, ng, n);
         q.a_nrt = (int32_t)tn_cdiv(cl * dd, 128);
         q.b = stage(L->st_static, L->pf_static, d.sr, cr, cr, cr, 1, ng, cr * cr);  // B^T rows b = SR_g rows
         q.b_nrt = (int32_t)tn_cdiv(cr, 128);
         q.C = J.w; q.sCm = cr; q.sCn = 1; q.alpha = 1.0; q.accumulate = 1; q.active = active;
         L->probs2.push_back(q);
-        L->pf_probs2.push_back(L->pf_probs2.back() + gg_tf32_tiles(q, 128));
+        L->pf_probs2.push_back(L->pf_probs2.back() + gg_tf32_tiles(q, bn));
       }
       if (d.wl) {
         GgProblem p{};
         p.nbatch = 1; p.n_mt = (int32_t)tn_cdiv(cl * dd, 128);
         p.M = (int32_t)(cl * dd); p.N = (int32_t)cr; p.nred = 1;
-        p.n_kb = (int32_t)tn_cdiv(cl * dd, 32); p.n_nt = (int32_t)tn_cdiv(cr, 128);
+        p.n_kb = (int32_t)tn_cdiv(cl * dd, 32); p.n_nt = (int32_t)tn_cdiv(cr, bn);
         p.a = stage(L->st_static, L->pf_static, d.wl, cl * dd, cl * dd, cl * dd, 1);
         p.a_nrt = (int32_t)tn_cdiv(cl * dd, 128);
         p.b = stage(L->st_iter, L->pf_iter, J.x, cr, cl * dd, 1, cr);  // B^T rows b, k = (a s)
         p.b_nrt = (int32_t)tn_cdiv(cr, 128);
         p.C = J.w; p.sCm = cr; p.sCn = 1; p.alpha = 1.0; p.accumulate = 1; p.active = active;
         L->probs.push_back(p);
-        L->pf_probs.push_back(L->pf_probs.back() + gg_tf32_tiles(p, 128));
+        L->pf_probs.push_back(L->pf_probs.back() + gg_tf32_tiles(p, bn));
       }
       if (d.wr) {
         GgProblem p{};
         p.nbatch = 1; p.n_mt = (int32_t)tn_cdiv(cl, 128);
         p.M = (int32_t)cl; p.N = (int32_t)(dd * cr); p.nred = 1;
-        p.n_kb = (int32_t)tn_cdiv(dd * cr, 32); p.n_nt = (int32_t)tn_cdiv(dd * cr, 128);
+        p.n_kb = (int32_t)tn_cdiv(dd * cr, 32); p.n_nt = (int32_t)tn_cdiv(dd * cr, bn);
         p.a = stage(L->st_iter, L->pf_iter, J.x, cl, dd * cr, dd * cr, 1);
         p.a_nrt = (int32_t)tn_cdiv(cl, 128);
         p.b = stage(L->st_static, L->pf_static, d.wr, dd * cr, dd * cr, dd * cr, 1);  // B^T = WR rows
         p.b_nrt = (int32_t)tn_cdiv(dd * cr, 128);
         p.C = J.w; p.sCm = dd * cr; p.sCn = 1; p.alpha = 1.0; p.accumulate = 1; p.active = active;
         L->probs.push_back(p);
-        L->pf_probs.push_back(L->pf_probs.back() + gg_tf32_tiles(p, 128));
+        L->pf_probs.push_back(L->pf_probs.back() + gg_tf32_tiles(p, bn));
       }
     } else {
       if (ng > 0) {
@@ -800,10 +803,10 @@ extern "C" int tn_batched_lanczos(const tn_batch_solve* in, int count, const tn_
     // w = H x
     if (mixed) {
       if ((st = gg_launch_stage(d_sit, (int)L.st_iter.size(), d_pit, L.pf_iter.back(), s))) return st;
-      if ((st = gg_launch_tf32(d_pr, (int)L.probs.size(), d_ppr, L.pf_probs.back(), 128, 0, s))) return st;
+      if ((st = gg_launch_tf32(d_pr, (int)L.probs.size(), d_ppr, L.pf_probs.back(), L.bn, 0, s))) return st;
       if (!L.probs2.empty()) {
         if ((st = gg_launch_stage(d_sit2, (int)L.st_iter2.size(), d_pit2, L.pf_iter2.back(), s))) return st;
-        if ((st = gg_launch_tf32(d_pr2, (int)L.probs2.size(), d_ppr2, L.pf_probs2.back(), 128, 0, s))) return st;
+        if ((st = gg_launch_tf32(d_pr2, (int)L.probs2.size(), d_ppr2, L.pf_probs2.back(), L.bn, 0, s))) return st;
       }
     } else {
       if ((st = gg_launch_f64(d_f, (int)L.f64.size(), d_pf, L.pf_f64.back(), s))) return st;

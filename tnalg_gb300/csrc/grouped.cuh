@@ -54,3 +54,6 @@ int gg_launch_tf32(const GgProblem* dev_probs, int nprobs, const int* dev_prefix
                    cudaStream_t s);
 int gg_launch_f64(const GgF64Problem* dev_probs, int nprobs, const int* dev_prefix, int total_tiles, cudaStream_t s);
 bool tn_tf32x3_supported();
+// output tile width (64 or 128 columns) of the split-TF32 grouped GEMMs issued by the calling host
+// thread: tn_set_grouped_tile, 128 unless set
+int gg_tile_n();

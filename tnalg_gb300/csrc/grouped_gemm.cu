@@ -492,9 +492,22 @@ size_t tables_bytes(const GroupPlan& g) {
          al(g.f64.size() * sizeof(GgF64Problem) + 64) + al(g.f64_prefix.size() * sizeof(int) + 64);
 }
 
-int pick_bn(int precision) { return precision == TN_PREC_TF32X3 ? 128 : 64; }
+int pick_bn(int precision) { return precision == TN_PREC_TF32X3 ? gg_tile_n() : 64; }
+
+// the split-TF32 tile width chosen for the calls of this host thread (0: the default, 128)
+thread_local int t_tile_n = 0;
 
 }  // namespace
+
+int gg_tile_n() { return t_tile_n ? t_tile_n : 128; }
+
+extern "C" int tn_set_grouped_tile(int tile_n) {
+  if (tile_n != 0 && tile_n != 64 && tile_n != 128) return tn_fail(TN_ERR_ARG, "grouped tile width must be 0, 64 or 128");
+  t_tile_n = tile_n;
+  return TN_OK;
+}
+
+extern "C" int tn_get_grouped_tile(void) { return gg_tile_n(); }
 
 extern "C" size_t tn_grouped_gemm_workspace_bytes(int precision, const tn_grouped_gemm_problem* problems, int count) {
   if (!problems || count <= 0) return 1024;

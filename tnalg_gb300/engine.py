@@ -821,10 +821,10 @@ class DeviceMPS:
             # truncated SVD of the sketch: its dominant left singular vectors (rows of Vt of Y^T). The
             # directions only need ranking, and they are projected and re-orthonormalised in FP64
             # below, so the Jacobi stops once the rows are orthogonal to 1e-7 (the singular values
-            # are then accurate to ~1e-14 relative) or after 12 sweeps (a sketch with more columns
-            # than independent channels keeps a few noise rows rotating; the ranking of the leading
-            # directions is settled long before)
-            Ut, sv, Vt = L.svd_truncated(Y.t(), extra, ws=self.ws2, tol=1e-7, max_sweeps=12)
+            # are then accurate to ~1e-14 relative) or after 6 sweeps (a sketch with more columns
+            # than independent channels keeps a few noise rows rotating; the oversampled sketch only
+            # drops its 8 weakest directions, and their ranking is settled long before)
+            Ut, sv, Vt = L.svd_truncated(Y.t(), extra, ws=self.ws2, tol=1e-7, max_sweeps=6)
             r = int(Vt.shape[0])
             Vn = torch.empty((mm, r), dtype=torch.float64, device=self.device)
             Vn.copy_(Vt.t())

@@ -327,8 +327,11 @@ def svd_truncated(X, chi, ws=None, tol=1e-15, max_sweeps=60):
                            max_sweeps, c_vp(base), c_sz(buf.numel() - (base - buf.data_ptr())), stream_handle())
     if st != TN_ERR_NOCONV:
         check(st, "svd")
-    order = torch.argsort(s, descending=True)[: min(int(chi), k)]
-    return U[:, order], s[order], Vt[order]
+    # the k values are ordered on the host (the call has synchronised the stream already); a device
+    # sort would load torch's sorting kernels on first use, which took seconds in a fresh process
+    order = np.argsort(-s.cpu().numpy(), kind="stable")[: min(int(chi), k)]
+    idx = torch.as_tensor(order, dtype=torch.long, device=X.device)
+    return U[:, idx], s[idx], Vt[idx]
 
 
 def tf32x3_available():

@@ -207,3 +207,27 @@ def test_requests_submitted_while_running(workers):
         assert j.arrival > 0 and j.finished >= j.admitted >= j.arrival
     arrivals = [j.arrival for j in sorted(done, key=lambda j: j.job_id)]
     assert arrivals == sorted(arrivals)
+
+
+def test_power_of_two_scaling_of_the_random_start_changes_nothing():
+    """The job engines scale their random tensors by powers of two (so that centring a long chain at
+    large chi cannot overflow FP64); the scaling is exact, so a job's result is the one
+    dmrg_finite_size gives from the unscaled draws of the same seed."""
+    import contextlib
+    import io
+    from tnalg_gb300 import DMRG_anyH, MPSClass
+    t = MPSClass.random_open_mps(6, 2, 4)
+    for a, b in zip(t, serving.pow2_scaled(t)):
+        e = np.log2(np.abs(a[a != 0]) / np.abs(b[a != 0]))
+        assert np.all(e == np.round(e)) and np.ptp(e) == 0      # one exact power of two per tensor
+    para = serving.chain_job_para(10, 6, jz=0.7, hz=0.2, sweeps=3, device="cpu")
+    para["break_tol"] = -1.0
+    job = serving.DMRGJob(0, dict(para), seed=42)
+    s = serving.Scheduler("cpu", max_active=1)
+    s.submit(job)
+    s.run()
+    np.random.seed(42)
+    with contextlib.redirect_stdout(io.StringIO()):
+        ob, _, _, _ = DMRG_anyH.dmrg_finite_size(dict(para))
+    assert job.result["e_per_site"] == pytest.approx(ob["e_per_site"], abs=1e-12)
+    np.testing.assert_allclose(job.result["mz"], np.ravel(ob["mz"]), atol=1e-10)

@@ -12,11 +12,11 @@ Prints ONE JSON line. `value` = sweeps/s (inputs resident in HBM), `e2e` = sweep
 dmrg_finite_size() job from host inputs (ramp included, final MPS copied back to the host),
 `cpu_baseline` = the reference's local update (oracle/: numpy + scipy ARPACK) measured on the host
 cores on the converged state of the timed sweeps. At one GPU the workload legs follow (child
-processes, one shared time budget; a failure is reported in the line): config1 = N=12, chi=16,
-10 sweeps in full on the CPU port and the GPU path; config2_chain = N=100, chi 64 -> 256 -> 512 over
-8 sweeps, mixed against the plain FP64 GPU path; config3_j1j2 = J1-J2 6x6 in snake order, 10
-sweeps at chi=512, mixed against FP64; config4_batched = 512 uneven XXZ chains advanced together
-(tnalg_gb300.batched) against the same jobs one at a time on the FP64 path; config5_serving = a
+processes, one shared time budget; a failure is reported in the line): chain_n12_chi16 = N=12, chi=16,
+10 sweeps in full on the CPU port and the GPU path; chain_n100_chi512 = N=100, chi 64 -> 256 -> 512
+over 8 sweeps, mixed against the plain FP64 GPU path; j1j2_6x6_chi512 = J1-J2 6x6 in snake order, 10
+sweeps at chi=512, mixed against FP64; batched_512_xxz = 512 uneven XXZ chains advanced together
+(tnalg_gb300.batched) against the same jobs one at a time on the FP64 path; serving_stream = a
 Poisson stream of chain and ladder requests at several rates. `summary` (the last key) gathers
 the figures the metric is quoted on.
 `--impl reference` times the reference's algorithm (oracle/) on the host cores, on a seeded random
@@ -58,7 +58,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-solves", type=int, default=2)
     p.add_argument("--no-legs", action="store_true",
-                   help="skip the workload legs (configs 1-5: N=12 in full, N=100 and J1-J2 6x6 mixed vs FP64, "
+                   help="skip the workload legs (N=12 chain in full, N=100 chain and J1-J2 6x6 mixed vs FP64, "
                         "batched jobs, serving)")
     return p.parse_args()
 
@@ -348,8 +348,8 @@ def cpu_sample(length, chi, eigs_tol, steps, warmup=0, mps=None, seed=0):
                           float(np.mean([r[2] for r in rows])), move_s, per_step, t_setup)}
 
 
-def config1_leg(device):
-    """BASELINE config 1 in full: N=12 Heisenberg chain, chi=16, seed 0, 10 sweeps (break_tol=-1),
+def small_chain_leg(device):
+    """The N=12 Heisenberg chain in full: chi=16, seed 0, 10 sweeps (break_tol=-1),
     eigs_tol 1e-12, on the oracle (the reference's numpy/scipy path, host cores) and on the GPU
     path (dmrg_finite_size, FP64 and split TF32); sweeps/s, solves/s and the energy against exact
     diagonalisation."""
@@ -434,14 +434,14 @@ def _pick(d, keys):
 def summarise(line):
     """The figures the metric is quoted on, gathered in one compact object (last key of the line)."""
     out = {}
-    c1 = line.get("config1")
+    c1 = line.get("chain_n12_chi16")
     if isinstance(c1, dict) and "cpu_port" in c1:
-        out["config1_n12_chi16"] = {"cpu_port_sweeps_per_s": c1["cpu_port"]["sweeps_per_s"],
+        out["chain_n12_chi16"] = {"cpu_port_sweeps_per_s": c1["cpu_port"]["sweeps_per_s"],
                                     "gpu_fp64_sweeps_per_s": c1.get("gpu_fp64", {}).get("sweeps_per_s"),
                                     "gpu_tf32x3_sweeps_per_s": c1.get("gpu_tf32x3", {}).get("sweeps_per_s"),
                                     "abs_de_per_site_vs_ed": {k: c1[k]["abs_de_per_site_vs_ed"] for k in
                                                               ("cpu_port", "gpu_fp64", "gpu_tf32x3") if k in c1}}
-    for key, name in (("config2_chain", "config2_n100_chi512_8sweeps"), ("config3_j1j2", "config3_j1j2_6x6_chi512_10sweeps")):
+    for key, name in (("chain_n100_chi512", "chain_n100_chi512_8sweeps"), ("j1j2_6x6_chi512", "j1j2_6x6_chi512_10sweeps")):
         c = line.get(key)
         if isinstance(c, dict) and "fp64_path" in c:
             out[name] = {"speedup_vs_fp64": c["speedup_vs_fp64"], "abs_de_per_site_vs_fp64": c["abs_de_per_site_vs_fp64"],
@@ -451,16 +451,16 @@ def summarise(line):
                          "fp64_matvecs_per_solve": c["fp64_path"]["matvecs_per_solve"]}
         elif isinstance(c, dict):
             out[name] = _pick(c, ["error", "skipped"])
-    c4 = line.get("config4_batched")
+    c4 = line.get("batched_512_xxz")
     if isinstance(c4, dict):
-        out["config4_batched_512"] = _pick(c4, ["solves_per_s", "speedup_vs_sequential", "latency_p50_s",
+        out["batched_512_xxz_chains"] = _pick(c4, ["solves_per_s", "speedup_vs_sequential", "latency_p50_s",
                                                 "latency_p99_s", "max_abs_de_per_site_vs_sequential", "jobs",
                                                 "unconverged_solves", "error", "skipped"])
         if "sequential" in c4:
-            out["config4_batched_512"]["sequential_fp64_solves_per_s"] = c4["sequential"]["solves_per_s"]
-    c5 = line.get("config5_serving")
+            out["batched_512_xxz_chains"]["sequential_fp64_solves_per_s"] = c4["sequential"]["solves_per_s"]
+    c5 = line.get("serving_stream")
     if isinstance(c5, list):
-        out["config5_serving"] = [_pick(r, ["rate_per_s", "solves_per_s", "latency_p50_s", "latency_p99_s",
+        out["serving_poisson_stream"] = [_pick(r, ["rate_per_s", "solves_per_s", "latency_p50_s", "latency_p99_s",
                                             "speedup_vs_sequential", "max_abs_de_per_site_vs_sequential",
                                             "max_concurrent", "error", "skipped"]) for r in c5]
     return out
@@ -567,15 +567,15 @@ def main():
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
         try:
-            line["config1"] = config1_leg("cuda:%d" % local_rank)
+            line["chain_n12_chi16"] = small_chain_leg("cuda:%d" % local_rank)
         except Exception as e:
-            line["config1"] = {"error": repr(e)[:300]}
+            line["chain_n12_chi16"] = {"error": repr(e)[:300]}
         # the child legs share one time budget, so a stuck leg cannot hold back the line
         end = time.time() + LEGS_BUDGET_S
         prec = res["precision"]
-        line["config2_chain"] = run_lattice_leg(CHAIN_ARGS, prec, min(200.0, end - time.time()))
-        line["config3_j1j2"] = run_lattice_leg(LATTICE_ARGS, prec, min(330.0, end - time.time()))
-        line["config4_batched"] = run_batch_leg(BATCH_ARGS, prec, min(240.0, end - time.time()))
+        line["chain_n100_chi512"] = run_lattice_leg(CHAIN_ARGS, prec, min(200.0, end - time.time()))
+        line["j1j2_6x6_chi512"] = run_lattice_leg(LATTICE_ARGS, prec, min(330.0, end - time.time()))
+        line["batched_512_xxz"] = run_batch_leg(BATCH_ARGS, prec, min(240.0, end - time.time()))
         serving = []
         for k, rate in enumerate(SERVING_RATES):
             # the sequential FP64 pass runs once, on the first jobs of the stream, capped at 40 s
@@ -590,7 +590,7 @@ def main():
             for r in serving[1:]:
                 if "solves_per_s" in r:
                     r["speedup_vs_sequential"] = r["solves_per_s"] / seq
-        line["config5_serving"] = serving
+        line["serving_stream"] = serving
     if rank == 0:
         line["summary"] = summarise(line)
     if rank == 0:

@@ -296,16 +296,16 @@ def test_bench_summary_gathers_the_metric_figures():
     leg = {"speedup_vs_fp64": 12.0, "abs_de_per_site_vs_fp64": 3e-10, "max_abs_d_term_energy_vs_fp64": 2e-5,
            "sweeps_per_s": 3.0, "matvecs_per_solve": 3.5,
            "fp64_path": {"sweeps_per_s": 0.25, "matvecs_per_solve": 7.0}}
-    line = {"config2_chain": leg, "config3_j1j2": {"error": "exit 1: x"},
-            "config4_batched": {"solves_per_s": 9000.0, "speedup_vs_sequential": 30.0, "latency_p99_s": 20.0,
+    line = {"chain_n100_chi512": leg, "j1j2_6x6_chi512": {"error": "exit 1: x"},
+            "batched_512_xxz": {"solves_per_s": 9000.0, "speedup_vs_sequential": 30.0, "latency_p99_s": 20.0,
                                 "sequential": {"solves_per_s": 300.0}},
-            "config5_serving": [{"rate_per_s": 10.0, "solves_per_s": 500.0, "latency_p99_s": 3.0, "noise": 1}]}
+            "serving_stream": [{"rate_per_s": 10.0, "solves_per_s": 500.0, "latency_p99_s": 3.0, "noise": 1}]}
     out = bench.summarise(line)
-    assert out["config2_n100_chi512_8sweeps"]["speedup_vs_fp64"] == 12.0
-    assert out["config2_n100_chi512_8sweeps"]["fp64_matvecs_per_solve"] == 7.0
-    assert out["config3_j1j2_6x6_chi512_10sweeps"] == {"error": "exit 1: x"}
-    assert out["config4_batched_512"]["sequential_fp64_solves_per_s"] == 300.0
-    assert out["config5_serving"] == [{"rate_per_s": 10.0, "solves_per_s": 500.0, "latency_p99_s": 3.0}]
+    assert out["chain_n100_chi512_8sweeps"]["speedup_vs_fp64"] == 12.0
+    assert out["chain_n100_chi512_8sweeps"]["fp64_matvecs_per_solve"] == 7.0
+    assert out["j1j2_6x6_chi512_10sweeps"] == {"error": "exit 1: x"}
+    assert out["batched_512_xxz_chains"]["sequential_fp64_solves_per_s"] == 300.0
+    assert out["serving_poisson_stream"] == [{"rate_per_s": 10.0, "solves_per_s": 500.0, "latency_p99_s": 3.0}]
 
 
 def test_chi_schedule_grows_bonds_and_reaches_the_direct_energy(fake_backend):

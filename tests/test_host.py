@@ -401,3 +401,20 @@ def test_bond_growth_by_expansion_keeps_the_state_and_uses_the_hamiltonian(fake_
         return (M.observe_bond_energy(para["index2"], para["coeff2"]).sum() -
                 para["hx"] * M.observe_magnetization(1).sum() - para["hz"] * M.observe_magnetization(3).sum())
     assert sweep(A) < sweep(B) - 1e-5
+
+
+def test_reference_arm_times_measured_local_updates():
+    """bench.py --impl reference: W untimed and K timed local updates of the oracle (the reference's
+    algorithm) on the host; ms_per_step is one measured step and value the sweeps/s it gives."""
+    import argparse
+    import bench
+    s = bench.cpu_sample(10, 8, 1e-10, 3, warmup=1)
+    assert s["kind"] == "port" and s["steps"] == 3 and s["warmup"] == 1 and s["matvecs_per_solve"] > 0
+    assert s["value"] == pytest.approx(1.0 / (2 * 9 * s["ms_per_step"] / 1000.0), rel=1e-12)
+    assert s["ms_per_step"] == pytest.approx(1000.0 * (s["solve_s"] + s["move_s"]), rel=1e-12)
+    args = argparse.Namespace(length=10, chi=8, eigs_tol=1e-10, steps=2, warmup=1, gpus=1)
+    line = bench.run_reference(args, 0)
+    assert line["impl"] == "reference" and line["steps"] == 2 and line["warmup"] == 1
+    assert line["value"] == line["cpu_baseline"]["value"] == line["e2e"]["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["higher_is_better"]
+    assert bench.run_reference(args, 1) is None      # other ranks do no work

@@ -1185,7 +1185,15 @@ class BatchEngine:
         return finished
 
     def run(self, progress=None):
-        """Admit (by arrival time and memory), step, retire, until every submitted job is done."""
+        """Admit (by arrival time and memory), step, retire, until every submitted job is done. The
+        engine's device is current on the calling thread meanwhile (every library call works on the
+        current device and stream; worker threads enter their jobs' streams, which carry the device)."""
+        if str(self.device).startswith("cuda") and not L._host_test:
+            with torch.cuda.device(torch.device(self.device)):
+                return self._run(progress)
+        return self._run(progress)
+
+    def _run(self, progress=None):
         self._t0 = t0 = time.perf_counter()
         while self.pending or self.active or self._observing or self._alone:
             self._collect_alone()

@@ -166,3 +166,27 @@ def test_large_jobs_run_alone_beside_the_batch():
         else:
             assert res[k]["e_per_site"] == pytest.approx(ref[k]["e_per_site"], abs=1e-13), k
     assert all(j.finished is not None and j.finished >= j.arrival for j in eng.done)
+
+
+def test_poisson_stream_with_prepared_admission_and_large_jobs_alone():
+    """The serving configuration of the engine at once: arrivals spread in time, the host side of
+    admission prepared ahead (small groups), large jobs on the single-job path beside the batch. Every
+    job finishes once, after it arrived, with the result it gets when it runs alone."""
+    def stream():
+        out = []
+        for k, (l, chi, jz, hz) in enumerate(SPECS):
+            para = serving.chain_job_para(l, chi, jz=jz, hz=hz, sweeps=2, device="cpu")
+            out.append(batched.BatchJob(k, para, seed=500 + k, arrival=0.004 * k))
+        return out
+    alone = {}
+    for j in stream():
+        j.arrival = 0.0
+        _, r = _run([j], grouped=True, alone_chi=6, prefetch=0)
+        alone.update(r)
+    eng, res = _run(stream(), grouped=True, alone_chi=6, alone_workers=2, prefetch=2, admit_chunk=2, workers=2)
+    assert sorted(res) == sorted(alone) and len(eng.done) == len(SPECS)
+    for j in eng.done:
+        assert j.finished >= j.arrival
+        assert res[j.job_id]["e_per_site"] == pytest.approx(alone[j.job_id]["e_per_site"], abs=1e-13), j.job_id
+    summ = eng.summary()
+    assert summ["jobs"] == len(SPECS) and summ["latency_p99_s"] >= summ["latency_p50_s"] > 0
